@@ -1,0 +1,40 @@
+/*
+ * Additive entry points of the GB300 build. None of them has a counterpart in RobotecGPULidar's C API;
+ * existing callers never need them, and every reference call keeps its meaning without them.
+ */
+#pragma once
+
+#include <rgl/api/core.h>
+
+/*
+ * Makes a Gaussian noise node reproducible. The reference seeds its noise from std::random_device
+ * (src/graph/NodesCore.hpp:536,563,590), so two runs never agree; this build draws each normal from
+ * Philox4x32-10 keyed by (seed, noise kind, point or ray index, frame) and advances `frame` by one on
+ * every graph run. Without this call a node gets a random seed, as in the reference.
+ * Applies to nodes created by rgl_node_gaussian_noise_angular_ray / _angular_hitpoint / _distance.
+ */
+RGL_API rgl_status_t rgl_gb300_node_gaussian_noise_set_seed(rgl_node_t node, uint64_t seed, uint64_t frame);
+
+/*
+ * Sets the beam-divergence sub-ray pattern of a raytrace node: one primary ray plus `layers` rings of
+ * `vertices` rays each (sample index 1 + layer * vertices + vertex, ring l scaled by 1 - l/layers).
+ * The default, 3 x 19 (58 samples per beam), is the reference's fixed pattern
+ * (src/gpu/MultiReturn.hpp:19-21); e.g. 1 x 4 gives 5 samples per beam. At most 63 extra rays.
+ * Only used when a beam divergence is configured.
+ */
+RGL_API rgl_status_t rgl_gb300_node_raytrace_configure_beam_samples(rgl_node_t node, int32_t layers, int32_t vertices);
+
+/* Enables CUDA-event timing of graph runs (whole run and traversal kernel). */
+RGL_API rgl_status_t rgl_gb300_configure_timing(bool enable);
+
+/* Device time of the last completed run of the node's graph, in milliseconds (timing enabled). */
+RGL_API rgl_status_t rgl_gb300_graph_get_timing(rgl_node_t node, float* out_run_ms, float* out_trace_ms);
+
+/* Waits until the last run of the node's graph completed (rgl_graph_get_result_* also wait). */
+RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node);
+
+/* Number of CUDA kernels this library launched since it was loaded. */
+RGL_API rgl_status_t rgl_gb300_get_kernel_launch_count(uint64_t* out_count);
+
+/* SM count and compute capability (major * 10 + minor) of the device in use. */
+RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_compute_capability);

@@ -1,0 +1,1030 @@
+// C API of libRobotecGPULidar.so (declarations: include/rgl/api/core.h and
+// include/rgl/api/extensions/gb300.h).
+//
+// Error handling follows reference src/api/apiCommon.hpp:55-139 and apiCommon.cpp:18-91: every call
+// runs inside safeCall(), which maps exceptions to status codes, stores the last error string and
+// latches RGL_INVALID_STATE after an unrecoverable error. Argument checks produce the reference's
+// message "RGL API Error: Invalid argument, condition unsatisfied: <expression>"; unknown handles
+// produce "RGL API Error: Object does not exist: <Type> <pointer>".
+#include <cstring>
+#include <functional>
+#include <optional>
+#include <random>
+#include <set>
+#include <unordered_map>
+
+#include <rgl/api/core.h>
+#include <rgl/api/extensions/gb300.h>
+#include <rgl/api/extensions/tape.h>
+
+#include "graph.hpp"
+#include "scene.hpp"
+
+using namespace rgl;
+
+namespace {
+
+rgl_status_t lastStatus = RGL_SUCCESS;
+std::optional<std::string> lastMessage;
+
+const char* lastErrorString()
+{
+	if (lastMessage) {
+		return lastMessage->c_str();
+	}
+	switch (lastStatus) {
+		case RGL_SUCCESS: return "operation successful";
+		case RGL_INVALID_ARGUMENT: return "invalid argument";
+		case RGL_INTERNAL_EXCEPTION: return "unhandled internal exception";
+		case RGL_INVALID_STATE: return "invalid state - unrecoverable error occurred";
+		case RGL_NOT_IMPLEMENTED: return "operation not (yet) implemented";
+		case RGL_LOGGING_ERROR: return "logging error";
+		case RGL_INVALID_FILE_PATH: return "invalid file path";
+		case RGL_TAPE_ERROR: return "tape error";
+		case RGL_UDP_ERROR: return "UDP error";
+		case RGL_ROS2_ERROR: return "ROS2 error";
+		default: return "???";
+	}
+}
+
+bool recoverable(rgl_status_t s)
+{
+	static const std::set<rgl_status_t> ok = {RGL_INVALID_ARGUMENT,  RGL_INVALID_API_OBJECT, RGL_INVALID_PIPELINE,
+	                                          RGL_INVALID_FILE_PATH, RGL_NOT_IMPLEMENTED,    RGL_TAPE_ERROR,
+	                                          RGL_UDP_ERROR,         RGL_ROS2_ERROR};
+	return s == RGL_SUCCESS || ok.count(s) != 0;
+}
+
+rgl_status_t updateState(rgl_status_t s, std::optional<std::string> msg = std::nullopt)
+{
+	lastMessage = std::move(msg);
+	lastStatus = s;
+	if (s != RGL_SUCCESS) {
+		if (recoverable(s)) {
+			logMessage(LogLevel::Error, format("Recoverable error (code=%d): %s", (int) s, lastErrorString()));
+		} else {
+			logMessage(LogLevel::Critical, format("Unrecoverable error (code=%d): %s", (int) s, lastErrorString()));
+		}
+	}
+	return s;
+}
+
+template<class Fn>
+rgl_status_t safeCall(Fn&& fn)
+{
+	static bool initTried = false;
+	if (!initTried) {
+		initTried = true;
+		try {
+			ensureCudaInitialized();
+		}
+		catch (std::exception& e) {
+			return updateState(RGL_INITIALIZATION_ERROR, std::string(e.what()));
+		}
+	}
+	if (!recoverable(lastStatus)) {
+		return updateState(RGL_INVALID_STATE);
+	}
+	try {
+		fn();
+	}
+	catch (InvalidAPIObject& e) {
+		return updateState(RGL_INVALID_API_OBJECT, std::string(e.what()));
+	}
+	catch (InvalidPipeline& e) {
+		return updateState(RGL_INVALID_PIPELINE, std::string(e.what()));
+	}
+	catch (NotImplemented& e) {
+		return updateState(RGL_NOT_IMPLEMENTED, std::string(e.what()));
+	}
+	catch (std::invalid_argument& e) {
+		return updateState(RGL_INVALID_ARGUMENT, std::string(e.what()));
+	}
+	catch (std::exception& e) {
+		return updateState(RGL_INTERNAL_EXCEPTION, std::string(e.what()));
+	}
+	catch (...) {
+		return updateState(RGL_INTERNAL_EXCEPTION, std::string("exceptional exception"));
+	}
+	return updateState(RGL_SUCCESS);
+}
+
+#define CHECK_ARG(expr)                                                                                                        \
+	do {                                                                                                                       \
+		if (!(expr)) {                                                                                                         \
+			throw std::invalid_argument("RGL API Error: Invalid argument, condition unsatisfied: " #expr);                    \
+		}                                                                                                                      \
+	} while (0)
+
+// Handle registry (reference src/APIObject.hpp:35-110): raw handle -> owning shared_ptr.
+template<class T>
+struct Registry
+{
+	static std::unordered_map<T*, std::shared_ptr<T>>& map()
+	{
+		static std::unordered_map<T*, std::shared_ptr<T>> m;
+		return m;
+	}
+	static T* add(const std::shared_ptr<T>& p)
+	{
+		map()[p.get()] = p;
+		return p.get();
+	}
+	static std::shared_ptr<T> get(T* raw, const char* typeName)
+	{
+		auto it = map().find(raw);
+		if (it == map().end()) {
+			throw InvalidAPIObject(format("RGL API Error: Object does not exist: %s %p", typeName, (void*) raw));
+		}
+		return it->second;
+	}
+	static void release(T* raw, const char* typeName)
+	{
+		get(raw, typeName);
+		map().erase(raw);
+	}
+	static bool contains(T* raw) { return map().count(raw) != 0; }
+};
+
+using Nodes = Registry<Node>;
+using Meshes = Registry<Mesh>;
+using Entities = Registry<Entity>;
+using Textures = Registry<Texture>;
+
+std::shared_ptr<Node> getNode(rgl_node_t n) { return Nodes::get(n, "Node"); }
+
+template<class T>
+std::shared_ptr<T> getNodeAs(rgl_node_t n, const char* typeName)
+{
+	auto node = getNode(n);
+	auto t = std::dynamic_pointer_cast<T>(node);
+	if (!t) {
+		throw InvalidAPIObject(format("RGL API Error: Node type mismatch: expected %s, got %s", typeName, node->name()));
+	}
+	return t;
+}
+
+// Create-or-modify idiom (reference apiCommon.hpp:108-139).
+template<class T, class Setter>
+void createOrUpdateNode(rgl_node_t* handle, const char* typeName, Setter&& set)
+{
+	std::shared_ptr<T> node;
+	if (*handle == nullptr) {
+		node = std::make_shared<T>();
+	} else {
+		node = getNodeAs<T>(*handle, typeName);
+	}
+	if (node->ctx) {
+		node->ctx->synchronize();
+	}
+	set(*node);
+	node->dirty = true;
+	if (*handle == nullptr) {
+		*handle = Nodes::add(node);
+	}
+}
+
+Mat34 toMat(const rgl_mat3x4f& m)
+{
+	Mat34 r;
+	std::memcpy(r.m, m.value, sizeof(r.m));
+	return r;
+}
+
+void releaseGraph(const std::shared_ptr<Node>& node)
+{
+	if (node->ctx) {
+		node->ctx->detachAndDestroy();
+	}
+	for (auto& n : node->disconnectConnectedNodes()) {
+		Nodes::map().erase(n.get());
+	}
+}
+
+[[noreturn]] void notImplemented(const char* what)
+{
+	throw NotImplemented(format("%s is not implemented by this GB300 build", what));
+}
+
+// Default noise seed, as random as the reference's std::random_device seeding.
+uint64_t randomSeed()
+{
+	std::random_device rd;
+	return ((uint64_t) rd() << 32) ^ (uint64_t) rd();
+}
+
+} // namespace
+
+// ================================================================ general
+
+RGL_API rgl_status_t rgl_get_version_info(int32_t* out_major, int32_t* out_minor, int32_t* out_patch)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_major != nullptr);
+		CHECK_ARG(out_minor != nullptr);
+		CHECK_ARG(out_patch != nullptr);
+		*out_major = RGL_VERSION_MAJOR;
+		*out_minor = RGL_VERSION_MINOR;
+		*out_patch = RGL_VERSION_PATCH;
+	});
+}
+
+RGL_API rgl_status_t rgl_get_extension_info(rgl_extension_t extension, int32_t* out_available)
+{
+	return safeCall([&]() {
+		CHECK_ARG(0 <= extension && extension < RGL_EXTENSION_COUNT);
+		CHECK_ARG(out_available != nullptr);
+		*out_available = 0; // PCL, ROS2, UDP and weather extensions are not part of this build
+	});
+}
+
+RGL_API rgl_status_t rgl_configure_logging(rgl_log_level_t log_level, const char* log_file_path, bool use_stdout)
+{
+	return safeCall([&]() {
+		CHECK_ARG(0 <= log_level && log_level <= 6);
+		logConfigure((int) log_level, log_file_path, use_stdout);
+	});
+}
+
+RGL_API void rgl_get_last_error_string(const char** out_error_string)
+{
+	if (out_error_string == nullptr) {
+		return;
+	}
+	*out_error_string = lastErrorString();
+}
+
+RGL_API rgl_status_t rgl_cleanup(void)
+{
+	return safeCall([&]() {
+		while (!Nodes::map().empty()) {
+			auto node = Nodes::map().begin()->second;
+			releaseGraph(node);
+		}
+		for (auto& c : std::vector<std::shared_ptr<GraphRunCtx>>(GraphRunCtx::instances())) {
+			c->detachAndDestroy();
+		}
+		Scene::defaultScene().clear();
+		Entities::map().clear();
+		Meshes::map().clear();
+		Textures::map().clear();
+	});
+}
+
+// ================================================================ mesh
+
+RGL_API rgl_status_t rgl_mesh_create(rgl_mesh_t* out_mesh, const rgl_vec3f* vertices, int32_t vertex_count,
+                                     const rgl_vec3i* indices, int32_t index_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_mesh != nullptr);
+		CHECK_ARG(vertices != nullptr);
+		CHECK_ARG(vertex_count > 0);
+		CHECK_ARG(indices != nullptr);
+		CHECK_ARG(index_count > 0);
+		GraphRunCtx::synchronizeAll();
+		*out_mesh = Meshes::add(std::make_shared<Mesh>(vertices, vertex_count, indices, index_count));
+	});
+}
+
+RGL_API rgl_status_t rgl_mesh_set_texture_coords(rgl_mesh_t mesh, const rgl_vec2f* uvs, int32_t uv_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(mesh != nullptr);
+		CHECK_ARG(uvs != nullptr);
+		CHECK_ARG(uv_count > 0);
+		notImplemented("rgl_mesh_set_texture_coords");
+	});
+}
+
+RGL_API rgl_status_t rgl_mesh_set_bone_weights(rgl_mesh_t mesh, const rgl_bone_weights_t* bone_weights, int32_t bone_weights_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(mesh != nullptr);
+		CHECK_ARG(bone_weights != nullptr);
+		CHECK_ARG(bone_weights_count > 0);
+		notImplemented("rgl_mesh_set_bone_weights");
+	});
+}
+
+RGL_API rgl_status_t rgl_mesh_set_restposes(rgl_mesh_t mesh, const rgl_mat3x4f* restposes, int32_t bones_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(mesh != nullptr);
+		CHECK_ARG(restposes != nullptr);
+		CHECK_ARG(bones_count > 0);
+		notImplemented("rgl_mesh_set_restposes");
+	});
+}
+
+RGL_API rgl_status_t rgl_mesh_destroy(rgl_mesh_t mesh)
+{
+	return safeCall([&]() {
+		CHECK_ARG(mesh != nullptr);
+		GraphRunCtx::synchronizeAll();
+		Meshes::release(mesh, "Mesh");
+	});
+}
+
+RGL_API rgl_status_t rgl_mesh_is_alive(rgl_mesh_t mesh, bool* out_alive)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_alive != nullptr);
+		*out_alive = Meshes::contains(mesh);
+	});
+}
+
+// ================================================================ entity
+
+RGL_API rgl_status_t rgl_entity_create(rgl_entity_t* out_entity, rgl_scene_t scene, rgl_mesh_t mesh)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_entity != nullptr);
+		CHECK_ARG(mesh != nullptr);
+		CHECK_ARG(scene == nullptr);
+		GraphRunCtx::synchronizeAll();
+		auto m = Meshes::get(mesh, "Mesh");
+		Scene& sc = Scene::defaultScene();
+		auto e = std::make_shared<Entity>(m, &sc);
+		sc.addEntity(e);
+		*out_entity = Entities::add(e);
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_destroy(rgl_entity_t entity)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		GraphRunCtx::synchronizeAll();
+		auto e = Entities::get(entity, "Entity");
+		e->scene->removeEntity(e.get());
+		Entities::release(entity, "Entity");
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_set_transform(rgl_entity_t entity, const rgl_mat3x4f* transform)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		CHECK_ARG(transform != nullptr);
+		GraphRunCtx::synchronizeAll();
+		Entities::get(entity, "Entity")->setTransform(toMat(*transform));
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_set_pose_world(rgl_entity_t entity, const rgl_mat3x4f* pose, int32_t bones_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		CHECK_ARG(pose != nullptr);
+		CHECK_ARG(bones_count > 0);
+		notImplemented("rgl_entity_set_pose_world (skeletal animation)");
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_set_id(rgl_entity_t entity, int32_t id)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		CHECK_ARG(id != RGL_ENTITY_INVALID_ID);
+		GraphRunCtx::synchronizeAll();
+		Entities::get(entity, "Entity")->setId(id);
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_set_intensity_texture(rgl_entity_t entity, rgl_texture_t texture)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		CHECK_ARG(texture != nullptr);
+		notImplemented("rgl_entity_set_intensity_texture");
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_set_laser_retro(rgl_entity_t entity, float retro)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		Entities::get(entity, "Entity")->laserRetro = retro;
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_apply_external_animation(rgl_entity_t entity, const rgl_vec3f* vertices, int32_t vertex_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(entity != nullptr);
+		CHECK_ARG(vertices != nullptr);
+		CHECK_ARG(vertex_count > 0);
+		notImplemented("rgl_entity_apply_external_animation");
+	});
+}
+
+RGL_API rgl_status_t rgl_entity_is_alive(rgl_entity_t entity, bool* out_alive)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_alive != nullptr);
+		*out_alive = Entities::contains(entity);
+	});
+}
+
+// ================================================================ texture
+
+RGL_API rgl_status_t rgl_texture_create(rgl_texture_t* out_texture, const void* texels, int32_t width, int32_t height)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_texture != nullptr);
+		CHECK_ARG(texels != nullptr);
+		CHECK_ARG(width > 0);
+		CHECK_ARG(height > 0);
+		notImplemented("rgl_texture_create");
+	});
+}
+
+RGL_API rgl_status_t rgl_texture_destroy(rgl_texture_t texture)
+{
+	return safeCall([&]() {
+		CHECK_ARG(texture != nullptr);
+		Textures::release(texture, "Texture");
+	});
+}
+
+RGL_API rgl_status_t rgl_texture_is_alive(rgl_texture_t texture, bool* out_alive)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_alive != nullptr);
+		*out_alive = Textures::contains(texture);
+	});
+}
+
+// ================================================================ scene
+
+RGL_API rgl_status_t rgl_scene_set_time(rgl_scene_t scene, uint64_t nanoseconds)
+{
+	return safeCall([&]() {
+		CHECK_ARG(scene == nullptr);
+		GraphRunCtx::synchronizeAll();
+		Scene::defaultScene().timeNs = nanoseconds;
+		Scene::defaultScene().timeSet = true;
+	});
+}
+
+// ================================================================ graph
+
+RGL_API rgl_status_t rgl_graph_run(rgl_node_t raw_node)
+{
+	return safeCall([&]() {
+		CHECK_ARG(raw_node != nullptr);
+		auto node = getNode(raw_node);
+		if (!node->ctx) {
+			GraphRunCtx::createAndAttach(node);
+		}
+		node->ctx->run();
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_destroy(rgl_node_t raw_node)
+{
+	return safeCall([&]() {
+		CHECK_ARG(raw_node != nullptr);
+		releaseGraph(getNode(raw_node));
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_get_result_size(rgl_node_t node, rgl_field_t field, int32_t* out_count, int32_t* out_size_of)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto pn = getNodeAs<PointsNode>(node, "IPointsNode");
+		if (pn->dirty || !pn->ctx) {
+			throw InvalidPipeline(format("Cannot get results from %s; it hasn't been run yet, or the run has failed", pn->name()));
+		}
+		pn->ctx->synchronize();
+		int32_t count = (int32_t) pn->pointCountHost();
+		int32_t size = (int32_t) pn->fieldPointSize(field);
+		if (out_count != nullptr) {
+			*out_count = count;
+		}
+		if (out_size_of != nullptr) {
+			*out_size_of = size;
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_get_result_data(rgl_node_t node, rgl_field_t field, void* dst)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(dst != nullptr);
+		auto pn = getNodeAs<PointsNode>(node, "IPointsNode");
+		if (!pn->hasField(field)) {
+			throw InvalidPipeline(format("node %s does not provide field %s", pn->name(), fieldName(field)));
+		}
+		if (pn->dirty || !pn->ctx) {
+			throw InvalidPipeline(format("Cannot get results from %s; it hasn't been run yet, or the run has failed", pn->name()));
+		}
+		pn->ctx->synchronize();
+		size_t count = pn->pointCountHost();
+		size_t bytes = count * pn->fieldPointSize(field);
+		if (bytes == 0) {
+			return;
+		}
+		const void* src = pn->fieldDev(field);
+		RGL_CHECK_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_node_add_child(rgl_node_t parent, rgl_node_t child)
+{
+	return safeCall([&]() {
+		CHECK_ARG(parent != nullptr);
+		CHECK_ARG(child != nullptr);
+		CHECK_ARG(parent != child);
+		getNode(parent)->addChild(getNode(child));
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_node_remove_child(rgl_node_t parent, rgl_node_t child)
+{
+	return safeCall([&]() {
+		CHECK_ARG(parent != nullptr);
+		CHECK_ARG(child != nullptr);
+		getNode(parent)->removeChild(getNode(child));
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_node_set_priority(rgl_node_t node, int32_t priority)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto n = getNode(node);
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setPriority(priority);
+	});
+}
+
+RGL_API rgl_status_t rgl_graph_node_get_priority(rgl_node_t node, int32_t* out_priority)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(out_priority != nullptr);
+		*out_priority = getNode(node)->priority;
+	});
+}
+
+// ================================================================ ray nodes
+
+RGL_API rgl_status_t rgl_node_rays_from_mat3x4f(rgl_node_t* node, const rgl_mat3x4f* rays, int32_t ray_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(rays != nullptr);
+		CHECK_ARG(ray_count > 0);
+		createOrUpdateNode<FromMat3x4fRaysNode>(node, "FromMat3x4fRaysNode",
+		                                        [&](FromMat3x4fRaysNode& n) { n.setParameters(rays, (size_t) ray_count); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_rays_set_ring_ids(rgl_node_t* node, const int32_t* ring_ids, int32_t ring_ids_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(ring_ids != nullptr);
+		CHECK_ARG(ring_ids_count > 0);
+		notImplemented("rgl_node_rays_set_ring_ids");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_rays_set_range(rgl_node_t* node, const rgl_vec2f* ranges, int32_t ranges_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(ranges != nullptr);
+		CHECK_ARG(ranges_count > 0);
+		createOrUpdateNode<SetRangeRaysNode>(node, "SetRangeRaysNode",
+		                                     [&](SetRangeRaysNode& n) { n.setParameters(ranges, (size_t) ranges_count); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_rays_set_time_offsets(rgl_node_t* node, const float* offsets, int32_t offsets_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(offsets != nullptr);
+		CHECK_ARG(offsets_count > 0);
+		notImplemented("rgl_node_rays_set_time_offsets");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_rays_transform(rgl_node_t* node, const rgl_mat3x4f* transform)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(transform != nullptr);
+		Mat34 tf = toMat(*transform);
+		createOrUpdateNode<TransformRaysNode>(node, "TransformRaysNode", [&](TransformRaysNode& n) { n.setParameters(tf); });
+	});
+}
+
+// ================================================================ point nodes
+
+RGL_API rgl_status_t rgl_node_points_transform(rgl_node_t* node, const rgl_mat3x4f* transform)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(transform != nullptr);
+		Mat34 tf = toMat(*transform);
+		createOrUpdateNode<TransformPointsNode>(node, "TransformPointsNode", [&](TransformPointsNode& n) { n.setParameters(tf); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace(rgl_node_t* node, rgl_scene_t scene)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(scene == nullptr);
+		createOrUpdateNode<RaytraceNode>(node, "RaytraceNode", [&](RaytraceNode& n) { n.scene = &Scene::defaultScene(); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_velocity(rgl_node_t node, const rgl_vec3f* linear_velocity,
+                                                          const rgl_vec3f* angular_velocity)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(linear_velocity != nullptr);
+		CHECK_ARG(angular_velocity != nullptr);
+		getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		// Velocity only feeds velocity/distortion fields, which this build does not compute; the
+		// configuration is accepted and has no effect on the computed fields.
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_distortion(rgl_node_t node, bool enable)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (enable) {
+			notImplemented("velocity distortion");
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_non_hits(rgl_node_t node, float nearDistance, float farDistance)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setNonHits(nearDistance, farDistance);
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_mask(rgl_node_t node, const int8_t* rays_mask, int32_t rays_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(rays_mask != nullptr);
+		CHECK_ARG(rays_count > 0);
+		notImplemented("rgl_node_raytrace_configure_mask");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_beam_divergence(rgl_node_t node, float horizontal_beam_divergence,
+                                                                 float vertical_beam_divergence)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG((horizontal_beam_divergence > 0.0f && vertical_beam_divergence > 0.0f) ||
+		          (horizontal_beam_divergence == 0.0f && vertical_beam_divergence == 0.0f));
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setBeamDivergence(horizontal_beam_divergence, vertical_beam_divergence);
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_default_intensity(rgl_node_t node, float default_intensity)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(default_intensity >= 0.0f);
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setDefaultIntensity(default_intensity);
+	});
+}
+
+RGL_API rgl_status_t rgl_node_raytrace_configure_return_mode(rgl_node_t node, rgl_return_mode_t return_mode)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(return_mode != RGL_RETURN_UNKNOWN);
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setReturnMode((int32_t) return_mode);
+		n->dirty = true;
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_format(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(fields != nullptr);
+		CHECK_ARG(field_count > 0);
+		std::vector<rgl_field_t> f(fields, fields + field_count);
+		createOrUpdateNode<FormatPointsNode>(node, "FormatPointsNode", [&](FormatPointsNode& n) { n.setParameters(f); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_yield(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(fields != nullptr);
+		CHECK_ARG(field_count > 0);
+		std::vector<rgl_field_t> f(fields, fields + field_count);
+		createOrUpdateNode<YieldPointsNode>(node, "YieldPointsNode", [&](YieldPointsNode& n) { n.setParameters(f); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_compact_by_field(rgl_node_t* node, rgl_field_t field)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(field == RGL_FIELD_IS_HIT_I32 || field == RGL_FIELD_IS_GROUND_I32);
+		createOrUpdateNode<CompactByFieldPointsNode>(node, "CompactByFieldPointsNode",
+		                                             [&](CompactByFieldPointsNode& n) { n.setParameters(field); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_spatial_merge(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(fields != nullptr);
+		CHECK_ARG(field_count > 0);
+		notImplemented("rgl_node_points_spatial_merge");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_temporal_merge(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(fields != nullptr);
+		CHECK_ARG(field_count > 0);
+		notImplemented("rgl_node_points_temporal_merge");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_from_array(rgl_node_t* node, const void* points, int32_t points_count, const rgl_field_t* fields,
+                                                int32_t field_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(points != nullptr);
+		CHECK_ARG(points_count > 0);
+		CHECK_ARG(fields != nullptr);
+		CHECK_ARG(field_count > 0);
+		std::vector<rgl_field_t> f(fields, fields + field_count);
+		createOrUpdateNode<FromArrayPointsNode>(node, "FromArrayPointsNode",
+		                                        [&](FromArrayPointsNode& n) { n.setParameters(points, (size_t) points_count, f); });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_radar_postprocess(rgl_node_t* node, const rgl_radar_scope_t* radar_scopes,
+                                                       int32_t radar_scopes_count, float ray_azimuth_step, float ray_elevation_step,
+                                                       float frequency, float power_transmitted, float cumulative_device_gain,
+                                                       float received_noise_mean, float received_noise_st_dev)
+{
+	return safeCall([&]() {
+		CHECK_ARG(radar_scopes != nullptr);
+		CHECK_ARG(radar_scopes_count > 0);
+		notImplemented("rgl_node_points_radar_postprocess");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_radar_track_objects(rgl_node_t* node, float object_distance_threshold,
+                                                         float object_azimuth_threshold, float object_elevation_threshold,
+                                                         float object_radial_speed_threshold, float max_matching_distance,
+                                                         float max_prediction_time_frame, float movement_sensitivity)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		notImplemented("rgl_node_points_radar_track_objects");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_radar_set_classes(rgl_node_t node, const int32_t* entity_ids,
+                                                       const rgl_radar_object_class_t* object_classes, int32_t count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		notImplemented("rgl_node_points_radar_set_classes");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_points_filter_ground(rgl_node_t* node, const rgl_vec3f* sensor_up_vector, float ground_angle_threshold)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(ground_angle_threshold >= 0);
+		notImplemented("rgl_node_points_filter_ground");
+	});
+}
+
+RGL_API rgl_status_t rgl_node_gaussian_noise_angular_ray(rgl_node_t* node, float mean, float st_dev, rgl_axis_t rotation_axis)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(st_dev >= 0);
+		CHECK_ARG((rotation_axis == RGL_AXIS_X) || (rotation_axis == RGL_AXIS_Y) || (rotation_axis == RGL_AXIS_Z));
+		bool created = *node == nullptr;
+		createOrUpdateNode<GaussianNoiseAngularRaysNode>(node, "GaussianNoiseAngularRaysNode", [&](GaussianNoiseAngularRaysNode& n) {
+			n.setParameters(mean, st_dev, rotation_axis);
+			if (created) {
+				n.setSeed(randomSeed(), 0);
+			}
+		});
+	});
+}
+
+RGL_API rgl_status_t rgl_node_gaussian_noise_angular_hitpoint(rgl_node_t* node, float mean, float st_dev, rgl_axis_t rotation_axis)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(st_dev >= 0);
+		CHECK_ARG((rotation_axis == RGL_AXIS_X) || (rotation_axis == RGL_AXIS_Y) || (rotation_axis == RGL_AXIS_Z));
+		bool created = *node == nullptr;
+		createOrUpdateNode<GaussianNoiseAngularHitpointNode>(node, "GaussianNoiseAngularHitpointNode",
+		                                                     [&](GaussianNoiseAngularHitpointNode& n) {
+			                                                     n.setParameters(mean, st_dev, rotation_axis);
+			                                                     if (created) {
+				                                                     n.setSeed(randomSeed(), 0);
+			                                                     }
+		                                                     });
+	});
+}
+
+RGL_API rgl_status_t rgl_node_gaussian_noise_distance(rgl_node_t* node, float mean, float st_dev_base, float st_dev_rise_per_meter)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(st_dev_base >= 0);
+		CHECK_ARG(st_dev_rise_per_meter >= 0);
+		bool created = *node == nullptr;
+		createOrUpdateNode<GaussianNoiseDistanceNode>(node, "GaussianNoiseDistanceNode", [&](GaussianNoiseDistanceNode& n) {
+			n.setParameters(mean, st_dev_base, st_dev_rise_per_meter);
+			if (created) {
+				n.setSeed(randomSeed(), 0);
+			}
+		});
+	});
+}
+
+RGL_API rgl_status_t rgl_node_is_alive(rgl_node_t node, bool* out_alive)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_alive != nullptr);
+		*out_alive = Nodes::contains(node);
+	});
+}
+
+// ================================================================ tape extension (not part of this build)
+
+RGL_API rgl_status_t rgl_tape_record_begin(const char* path)
+{
+	return safeCall([&]() {
+		CHECK_ARG(path != nullptr);
+		CHECK_ARG(path[0] != '\0');
+		notImplemented("rgl_tape_record_begin");
+	});
+}
+
+RGL_API rgl_status_t rgl_tape_record_end() { return safeCall([&]() { notImplemented("rgl_tape_record_end"); }); }
+
+RGL_API rgl_status_t rgl_tape_record_is_active(bool* is_active)
+{
+	return safeCall([&]() {
+		CHECK_ARG(is_active != nullptr);
+		*is_active = false;
+	});
+}
+
+RGL_API rgl_status_t rgl_tape_play(const char* path)
+{
+	return safeCall([&]() {
+		CHECK_ARG(path != nullptr);
+		CHECK_ARG(path[0] != '\0');
+		notImplemented("rgl_tape_play");
+	});
+}
+
+// ================================================================ GB300 extensions
+
+RGL_API rgl_status_t rgl_gb300_node_gaussian_noise_set_seed(rgl_node_t node, uint64_t seed, uint64_t frame)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto n = getNode(node);
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		if (auto a = std::dynamic_pointer_cast<GaussianNoiseAngularRaysNode>(n)) {
+			a->setSeed(seed, frame);
+		} else if (auto b = std::dynamic_pointer_cast<GaussianNoiseAngularHitpointNode>(n)) {
+			b->setSeed(seed, frame);
+		} else if (auto c = std::dynamic_pointer_cast<GaussianNoiseDistanceNode>(n)) {
+			c->setSeed(seed, frame);
+		} else {
+			throw InvalidAPIObject(format("RGL API Error: Node type mismatch: expected a Gaussian noise node, got %s", n->name()));
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_node_raytrace_configure_beam_samples(rgl_node_t node, int32_t layers, int32_t vertices)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		CHECK_ARG(layers > 0);
+		CHECK_ARG(vertices > 0);
+		CHECK_ARG(1 + layers * vertices <= kMaxBeamSamples);
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setBeamSamples(layers, vertices);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_configure_timing(bool enable)
+{
+	return safeCall([&]() {
+		GraphRunCtx::synchronizeAll();
+		setTimingEnabled(enable);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_graph_get_timing(rgl_node_t node, float* out_run_ms, float* out_trace_ms)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto n = getNode(node);
+		if (!n->ctx) {
+			throw InvalidPipeline(format("%s has not been run", n->name()));
+		}
+		n->ctx->synchronize();
+		if (out_run_ms) {
+			*out_run_ms = n->ctx->lastRunMs;
+		}
+		if (out_trace_ms) {
+			*out_trace_ms = n->ctx->lastTraceMs;
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto n = getNode(node);
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_get_kernel_launch_count(uint64_t* out_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_count != nullptr);
+		*out_count = launchCount();
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_cc)
+{
+	return safeCall([&]() {
+		int dev = 0;
+		RGL_CHECK_CUDA(cudaGetDevice(&dev));
+		cudaDeviceProp p{};
+		RGL_CHECK_CUDA(cudaGetDeviceProperties(&p, dev));
+		if (out_sm_count) {
+			*out_sm_count = p.multiProcessorCount;
+		}
+		if (out_cc) {
+			*out_cc = p.major * 10 + p.minor;
+		}
+	});
+}

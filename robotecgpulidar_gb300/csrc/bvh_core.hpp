@@ -1,0 +1,309 @@
+// Per-item steps of the on-device BVH builder, as host/device functions (the CUDA kernels in bvh.cu
+// are thin wrappers; the test-suite's CPU harness runs the same functions serially).
+//
+// Build = Morton codes (30 bit) -> radix sort -> LBVH (Karras, "Maximizing Parallelism in the
+// Construction of BVHs, Octrees, and k-d Trees", HPG 2012) -> bottom-up bounds -> top-down collapse
+// into 8-wide nodes (children chosen by repeatedly opening the child of largest surface area) with
+// 8-bit child boxes rounded outward and verified in float.  It replaces OptiX's GAS/IAS builds at
+// reference src/scene/GASBuilder.hpp:31-100 and src/scene/Scene.cpp:131-190.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+#include "device_types.hpp"
+#include "trace_core.hpp"
+
+namespace rgl {
+
+struct Box
+{
+	float lox, loy, loz, hix, hiy, hiz;
+};
+
+RGL_HD Box emptyBox() { return Box{FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX}; }
+RGL_HD Box unite(const Box& a, const Box& b)
+{
+	return Box{a.lox < b.lox ? a.lox : b.lox, a.loy < b.loy ? a.loy : b.loy, a.loz < b.loz ? a.loz : b.loz,
+	           a.hix > b.hix ? a.hix : b.hix, a.hiy > b.hiy ? a.hiy : b.hiy, a.hiz > b.hiz ? a.hiz : b.hiz};
+}
+RGL_HD float halfArea(const Box& b)
+{
+	float dx = b.hix - b.lox, dy = b.hiy - b.loy, dz = b.hiz - b.loz;
+	return dx * dy + dy * dz + dz * dx;
+}
+RGL_HD Box binBox(const BinNode& n) { return Box{n.lox, n.loy, n.loz, n.hix, n.hiy, n.hiz}; }
+
+RGL_HD uint32_t expandBits10(uint32_t v)
+{
+	v = (v * 0x00010001u) & 0xFF0000FFu;
+	v = (v * 0x00000101u) & 0x0F00F00Fu;
+	v = (v * 0x00000011u) & 0xC30C30C3u;
+	v = (v * 0x00000005u) & 0x49249249u;
+	return v;
+}
+
+// 30-bit Morton code of point c inside [lo, lo + 1/invExt].
+RGL_HD uint32_t morton30(float cx, float cy, float cz, const Box& cb)
+{
+	float ex = cb.hix - cb.lox, ey = cb.hiy - cb.loy, ez = cb.hiz - cb.loz;
+	float fx = ex > 0.0f ? (cx - cb.lox) / ex : 0.0f;
+	float fy = ey > 0.0f ? (cy - cb.loy) / ey : 0.0f;
+	float fz = ez > 0.0f ? (cz - cb.loz) / ez : 0.0f;
+	auto q = [](float f) -> uint32_t {
+		float s = f * 1024.0f;
+		s = s < 0.0f ? 0.0f : (s > 1023.0f ? 1023.0f : s);
+		return (uint32_t) s;
+	};
+	return (expandBits10(q(fx)) << 2) | (expandBits10(q(fy)) << 1) | expandBits10(q(fz));
+}
+
+RGL_HD int clz32(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+	return __clz((int) x);
+#else
+	return x == 0 ? 32 : __builtin_clz(x);
+#endif
+}
+
+// Common-prefix length of sorted keys i and j, with the index as tie-break for equal keys.
+RGL_HD int lbvhDelta(const uint32_t* codes, int n, int i, int j)
+{
+	if (j < 0 || j >= n) {
+		return -1;
+	}
+	uint32_t a = codes[i], b = codes[j];
+	if (a == b) {
+		return 32 + clz32((uint32_t) i ^ (uint32_t) j);
+	}
+	return clz32(a ^ b);
+}
+
+// Internal node i of the LBVH over n >= 2 sorted keys. Children: >= 0 internal node, < 0 leaf ~k
+// (k = sorted position). Also returns the covered sorted range [first, last].
+RGL_HD void lbvhInternal(int i, const uint32_t* codes, int n, int32_t& left, int32_t& right, int32_t& first, int32_t& last)
+{
+	int d = (lbvhDelta(codes, n, i, i + 1) - lbvhDelta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+	int dmin = lbvhDelta(codes, n, i, i - d);
+	int lmax = 2;
+	while (lbvhDelta(codes, n, i, i + lmax * d) > dmin) {
+		lmax *= 2;
+	}
+	int l = 0;
+	for (int t = lmax / 2; t >= 1; t /= 2) {
+		if (lbvhDelta(codes, n, i, i + (l + t) * d) > dmin) {
+			l += t;
+		}
+	}
+	int j = i + l * d;
+	int dnode = lbvhDelta(codes, n, i, j);
+	int s = 0;
+	int div = 2;
+	int t;
+	do {
+		t = (l + div - 1) / div;
+		if (lbvhDelta(codes, n, i, i + (s + t) * d) > dnode) {
+			s += t;
+		}
+		div *= 2;
+	} while (t > 1);
+	int gamma = i + s * d + (d < 0 ? -1 : 0);
+	int lo = i < j ? i : j;
+	int hi = i < j ? j : i;
+	left = (lo == gamma) ? ~gamma : gamma;
+	right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+	first = lo;
+	last = hi;
+}
+
+// Smallest power of two 2^(e-127) with 255 * 2^(e-127) >= ext, as the biased exponent byte e.
+RGL_HD uint8_t quantExponent(float ext)
+{
+	double s = (double) ext / 255.0;
+	int e = 1; // 2^-126
+	double p = 1.1754943508222875e-38;
+	while (p < s && e < 254) {
+		p *= 2.0;
+		++e;
+	}
+	return (uint8_t) e;
+}
+
+RGL_HD void quantizeAxis(float p, float scale, float clo, float chi, uint8_t& qlo, uint8_t& qhi)
+{
+	double flo = ((double) clo - (double) p) / (double) scale;
+	double fhi = ((double) chi - (double) p) / (double) scale;
+	int lo = (int) flo; // flo >= 0
+	if ((double) lo > flo) {
+		--lo;
+	}
+	int hi = (int) fhi;
+	if ((double) hi < fhi) {
+		++hi;
+	}
+	lo = lo < 0 ? 0 : (lo > 255 ? 255 : lo);
+	hi = hi < 0 ? 0 : (hi > 255 ? 255 : hi);
+	// Verify with the exact float expression the traversal evaluates.
+	while (lo > 0 && fadd(p, (float) lo * scale) > clo) {
+		--lo;
+	}
+	while (hi < 255 && fadd(p, (float) hi * scale) < chi) {
+		++hi;
+	}
+	qlo = (uint8_t) lo;
+	qhi = (uint8_t) hi;
+}
+
+// Atomic counters used by the collapse step: device atomics on the GPU, plain adds on the host.
+RGL_HD uint32_t atomicAddU32(uint32_t* p, uint32_t v)
+{
+#if defined(__CUDA_ARCH__)
+	return atomicAdd(p, v);
+#else
+	uint32_t old = *p;
+	*p = old + v;
+	return old;
+#endif
+}
+
+struct CollapseInputs
+{
+	const BinNode* bin;        // n-1 internal nodes with bounds (n >= 2)
+	const int32_t* rangeFirst; // per internal node
+	const int32_t* rangeLast;
+	const int32_t* sortedIds;  // sorted position -> original triangle
+	const float4* triLo;       // per original triangle
+	const float4* triHi;
+	const float* vertices;     // 3 floats per vertex
+	const int32_t* indices;    // 3 ints per triangle
+};
+
+struct CollapseOutputs
+{
+	WideNode* wide;
+	TriRecord* tris;
+	uint32_t* wideCounter;
+	uint32_t* triCounter;
+	int2* queueOut;
+	uint32_t* queueOutCount;
+};
+
+RGL_HD int binCount(const CollapseInputs& in, int32_t c) { return c < 0 ? 1 : (in.rangeLast[c] - in.rangeFirst[c] + 1); }
+
+RGL_HD Box childBounds(const CollapseInputs& in, int32_t c)
+{
+	if (c >= 0) {
+		return binBox(in.bin[c]);
+	}
+	int tid = in.sortedIds[~c];
+	float4 lo = in.triLo[tid], hi = in.triHi[tid];
+	return Box{lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+}
+
+// Builds wide node `wideIdx` from the binary subtree rooted at `binRoot` (leaf ~k allowed).
+RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs& in, const CollapseOutputs& out)
+{
+	int32_t ch[kWideArity];
+	int n = 0;
+	if (binRoot < 0) {
+		ch[n++] = binRoot;
+	} else {
+		ch[n++] = in.bin[binRoot].left;
+		ch[n++] = in.bin[binRoot].right;
+	}
+	while (n < kWideArity) {
+		int bestK = -1;
+		float bestA = -1.0f;
+		for (int k = 0; k < n; ++k) {
+			int32_t c = ch[k];
+			if (c >= 0 && binCount(in, c) > kLeafMaxTris) {
+				float a = halfArea(binBox(in.bin[c]));
+				if (a > bestA) {
+					bestA = a;
+					bestK = k;
+				}
+			}
+		}
+		if (bestK < 0) {
+			break;
+		}
+		int32_t c = ch[bestK];
+		ch[bestK] = in.bin[c].left;
+		ch[n++] = in.bin[c].right;
+	}
+
+	Box cb[kWideArity];
+	Box nb = emptyBox();
+	uint32_t nInternal = 0, nLeafTris = 0;
+	for (int k = 0; k < n; ++k) {
+		cb[k] = childBounds(in, ch[k]);
+		nb = unite(nb, cb[k]);
+		int cnt = binCount(in, ch[k]);
+		if (ch[k] >= 0 && cnt > kLeafMaxTris) {
+			++nInternal;
+		} else {
+			nLeafTris += (uint32_t) cnt;
+		}
+	}
+	uint32_t childBase = nInternal ? atomicAddU32(out.wideCounter, nInternal) : 0;
+	uint32_t triBase = nLeafTris ? atomicAddU32(out.triCounter, nLeafTris) : 0;
+	uint32_t qBase = nInternal ? atomicAddU32(out.queueOutCount, nInternal) : 0;
+
+	WideNode w;
+	w.px = nb.lox;
+	w.py = nb.loy;
+	w.pz = nb.loz;
+	w.ex = quantExponent(nb.hix - nb.lox);
+	w.ey = quantExponent(nb.hiy - nb.loy);
+	w.ez = quantExponent(nb.hiz - nb.loz);
+	w.imask = 0;
+	w.childBase = childBase;
+	w.triBase = triBase;
+	float sx = exp2Byte(w.ex), sy = exp2Byte(w.ey), sz = exp2Byte(w.ez);
+	for (int k = 0; k < kWideArity; ++k) {
+		w.meta[k] = 0;
+		w.qlox[k] = w.qloy[k] = w.qloz[k] = 255;
+		w.qhix[k] = w.qhiy[k] = w.qhiz[k] = 0;
+	}
+	uint32_t rank = 0, triOff = 0;
+	for (int k = 0; k < n; ++k) {
+		quantizeAxis(w.px, sx, cb[k].lox, cb[k].hix, w.qlox[k], w.qhix[k]);
+		quantizeAxis(w.py, sy, cb[k].loy, cb[k].hiy, w.qloy[k], w.qhiy[k]);
+		quantizeAxis(w.pz, sz, cb[k].loz, cb[k].hiz, w.qloz[k], w.qhiz[k]);
+		int32_t c = ch[k];
+		int cnt = binCount(in, c);
+		if (c >= 0 && cnt > kLeafMaxTris) {
+			w.imask |= (uint8_t) (1u << k);
+			out.queueOut[qBase + rank] = make_int2(c, (int) (childBase + rank));
+			++rank;
+		} else {
+			int firstPos = c < 0 ? ~c : in.rangeFirst[c];
+			w.meta[k] = (uint8_t) ((cnt << 5) | (int) triOff);
+			for (int m = 0; m < cnt; ++m) {
+				int tid = in.sortedIds[firstPos + m];
+				const int32_t* ix = in.indices + 3 * (size_t) tid;
+				const float* a = in.vertices + 3 * (size_t) ix[0];
+				const float* b = in.vertices + 3 * (size_t) ix[1];
+				const float* cc = in.vertices + 3 * (size_t) ix[2];
+				TriRecord tr;
+				tr.v0x = a[0];
+				tr.v0y = a[1];
+				tr.v0z = a[2];
+				tr.primId = tid;
+				tr.v1x = b[0];
+				tr.v1y = b[1];
+				tr.v1z = b[2];
+				tr.pad1 = 0;
+				tr.v2x = cc[0];
+				tr.v2y = cc[1];
+				tr.v2z = cc[2];
+				tr.pad2 = 0;
+				out.tris[triBase + triOff + m] = tr;
+			}
+			triOff += (uint32_t) cnt;
+		}
+	}
+	out.wide[wideIdx] = w;
+}
+
+} // namespace rgl

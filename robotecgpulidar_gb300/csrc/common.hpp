@@ -1,0 +1,114 @@
+// Host-side utilities of the C API layer: exception types mapped to rgl_status_t, field table,
+// device buffers and a minimal logger.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <rgl/api/core.h>
+
+namespace rgl {
+
+// Exceptions and the status each maps to (reference src/api/apiCommon.hpp:55-106).
+struct InvalidAPIArgument : std::invalid_argument
+{
+	using std::invalid_argument::invalid_argument; // RGL_INVALID_ARGUMENT
+};
+struct InvalidAPIObject : std::runtime_error
+{
+	using std::runtime_error::runtime_error; // RGL_INVALID_API_OBJECT
+};
+struct InvalidPipeline : std::runtime_error
+{
+	using std::runtime_error::runtime_error; // RGL_INVALID_PIPELINE
+};
+struct NotImplemented : std::runtime_error
+{
+	using std::runtime_error::runtime_error; // RGL_NOT_IMPLEMENTED
+};
+
+std::string format(const char* fmt, ...) __attribute__((format(printf, 1, 2)));
+
+#define RGL_CHECK_CUDA(expr)                                                                                                   \
+	do {                                                                                                                       \
+		cudaError_t err_ = (expr);                                                                                             \
+		if (err_ != cudaSuccess) {                                                                                             \
+			throw std::runtime_error(::rgl::format("CUDA error: %s (%s) at %s:%d", cudaGetErrorString(err_), #expr, __FILE__, \
+			                                       __LINE__));                                                                 \
+		}                                                                                                                      \
+	} while (0)
+
+// ---- fields (reference src/RGLFields.hpp:108-201)
+size_t fieldSize(rgl_field_t f);   // throws InvalidAPIArgument for unknown fields
+bool isDummy(rgl_field_t f);       // paddings
+const char* fieldName(rgl_field_t f);
+size_t pointSize(const std::vector<rgl_field_t>& fields);
+
+// ---- logging (reference src/Logger.cpp:17-59, reduced to level / file / stdout)
+enum class LogLevel : int
+{
+	Trace = 0,
+	Debug = 1,
+	Info = 2,
+	Warn = 3,
+	Error = 4,
+	Critical = 5,
+	Off = 6
+};
+void logConfigure(int level, const char* filePath, bool useStdout);
+void logMessage(LogLevel level, const std::string& msg);
+
+// ---- device memory
+
+// Grow-only device allocation owned by a node or scene.
+class DeviceBuffer
+{
+public:
+	DeviceBuffer() = default;
+	DeviceBuffer(const DeviceBuffer&) = delete;
+	DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+	~DeviceBuffer();
+	void* ensure(size_t bytes);
+	void* get() const { return ptr_; }
+	size_t capacity() const { return cap_; }
+	void release();
+
+	template<class T>
+	T* as() const
+	{
+		return static_cast<T*>(ptr_);
+	}
+
+private:
+	void* ptr_ = nullptr;
+	size_t cap_ = 0;
+};
+
+// Grow-only pinned host allocation.
+class PinnedBuffer
+{
+public:
+	PinnedBuffer() = default;
+	PinnedBuffer(const PinnedBuffer&) = delete;
+	PinnedBuffer& operator=(const PinnedBuffer&) = delete;
+	~PinnedBuffer();
+	void* ensure(size_t bytes);
+	void* get() const { return ptr_; }
+
+private:
+	void* ptr_ = nullptr;
+	size_t cap_ = 0;
+};
+
+// Library-wide CUDA state: device selected lazily on the first API call.
+void ensureCudaInitialized();
+
+} // namespace rgl

@@ -1,0 +1,846 @@
+#include "graph.hpp"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <functional>
+
+#include "scene.hpp"
+
+using rgl::format;
+using rgl::InvalidPipeline;
+using rgl::Mat34;
+
+namespace {
+bool gTiming = false;
+}
+bool timingEnabled() { return gTiming; }
+void setTimingEnabled(bool on) { gTiming = on; }
+
+// ================================================================ Node links
+// (reference src/graph/Node.cpp:23-215)
+
+template<class T>
+std::shared_ptr<T> Node::exactlyOneInput(const char* ifaceName)
+{
+	std::vector<std::shared_ptr<T>> typed;
+	for (auto& in : inputs) {
+		if (auto t = std::dynamic_pointer_cast<T>(in)) {
+			typed.push_back(t);
+		}
+	}
+	if (typed.size() != 1) {
+		std::string names;
+		for (size_t i = 0; i < inputs.size(); ++i) {
+			names += (i ? ", " : "") + std::string(inputs[i]->name());
+		}
+		throw InvalidPipeline(format("looked for %s, but found [%s]", ifaceName, names.c_str()));
+	}
+	return typed[0];
+}
+
+void Node::addChild(const Ptr& child)
+{
+	if (child == nullptr) {
+		throw InvalidPipeline(format("attempted to set an empty child for %s", name()));
+	}
+	if (std::find(outputs.begin(), outputs.end(), child) != outputs.end()) {
+		throw InvalidPipeline(format("attempted to add child %s to parent %s twice", child->name(), name()));
+	}
+	if (ctx) {
+		ctx->detachAndDestroy();
+	}
+	if (child->ctx) {
+		child->ctx->detachAndDestroy();
+	}
+	outputs.push_back(child);
+	child->inputs.push_back(shared_from_this());
+	std::stable_sort(outputs.begin(), outputs.end(), [](const Ptr& a, const Ptr& b) { return a->priority > b->priority; });
+	int32_t maxChild = outputs.front()->priority;
+	if (maxChild > priority) {
+		setPriority(maxChild);
+	}
+	dirty = true;
+	child->dirty = true;
+}
+
+void Node::removeChild(const Ptr& child)
+{
+	if (child == nullptr) {
+		throw InvalidPipeline(format("attempted to remove an empty child for %s", name()));
+	}
+	auto it = std::find(outputs.begin(), outputs.end(), child);
+	if (it == outputs.end()) {
+		throw InvalidPipeline(format("attempted to remove child %s from %s,but it was not found", child->name(), name()));
+	}
+	auto self = shared_from_this();
+	auto jt = std::find(child->inputs.begin(), child->inputs.end(), self);
+	if (jt == child->inputs.end()) {
+		throw InvalidPipeline(format("attempted to remove parent %s from %s,but it was not found", name(), child->name()));
+	}
+	if (ctx) {
+		ctx->detachAndDestroy();
+	}
+	outputs.erase(it);
+	child->inputs.erase(jt);
+	dirty = true;
+	child->dirty = true;
+}
+
+void Node::setPriority(int32_t p)
+{
+	if (p == priority) {
+		return;
+	}
+	if (!outputs.empty() && outputs.front()->priority > p) {
+		throw InvalidPipeline(format("cannot set priority of node %s to %d, because it's children %s has higher priority %d", name(),
+		                             (int) p, outputs.front()->name(), (int) outputs.front()->priority));
+	}
+	priority = p;
+	for (auto& in : inputs) {
+		std::stable_sort(in->outputs.begin(), in->outputs.end(), [](const Ptr& a, const Ptr& b) { return a->priority > b->priority; });
+		if (in->priority < p) {
+			in->setPriority(p);
+		}
+	}
+	if (ctx) {
+		ctx->invalidateOrder();
+	}
+}
+
+std::set<Node::Ptr> Node::connectedComponent()
+{
+	if (ctx) {
+		return ctx->nodes;
+	}
+	std::set<Ptr> visited;
+	std::function<void(const Ptr&)> rec = [&](const Ptr& cur) {
+		visited.insert(cur);
+		for (auto& o : cur->outputs) {
+			if (!visited.count(o)) {
+				rec(o);
+			}
+		}
+		for (auto& i : cur->inputs) {
+			if (!visited.count(i)) {
+				rec(i);
+			}
+		}
+	};
+	rec(shared_from_this());
+	return visited;
+}
+
+std::set<Node::Ptr> Node::disconnectConnectedNodes()
+{
+	auto nodes = connectedComponent();
+	for (auto& n : nodes) {
+		n->inputs.clear();
+		n->outputs.clear();
+		n->ctx.reset();
+		n->dirty = true;
+	}
+	return nodes;
+}
+
+// ================================================================ rays nodes
+
+void RaysNodeSingleInput::validateImpl() { input = exactlyOneInput<RaysNode>("IRaysNode"); }
+
+void FromMat3x4fRaysNode::setParameters(const rgl_mat3x4f* r, size_t n)
+{
+	RGL_CHECK_CUDA(cudaMemcpy(rays.ensure(sizeof(rgl_mat3x4f) * n), r, sizeof(rgl_mat3x4f) * n, cudaMemcpyHostToDevice));
+	count = n;
+}
+
+void FromMat3x4fRaysNode::validateImpl()
+{
+	if (!inputs.empty()) {
+		throw InvalidPipeline(format("inputs for node %s are not allowed", name()));
+	}
+}
+
+void TransformRaysNode::enqueueImpl(cudaStream_t s)
+{
+	size_t n = rayCount();
+	auto* o = static_cast<Mat34*>(out.ensure(sizeof(Mat34) * std::max<size_t>(1, n)));
+	rgl::launchTransformRays(input->raysDev(), o, (int) n, transform, s);
+}
+
+void SetRangeRaysNode::setParameters(const rgl_vec2f* r, size_t n)
+{
+	for (size_t i = 0; i < n; ++i) {
+		float mn = r[i].value[0], mx = r[i].value[1];
+		if (std::isnan(mn) || std::isnan(mx)) {
+			throw rgl::InvalidAPIArgument("range must be a number");
+		}
+		if (mn > mx) {
+			throw rgl::InvalidAPIArgument("minimum range must be lower or equal to maximum range");
+		}
+		if (mn < 0.0f) {
+			throw rgl::InvalidAPIArgument("minimum range must not be negative");
+		}
+	}
+	RGL_CHECK_CUDA(cudaMemcpy(ranges.ensure(sizeof(rgl_vec2f) * n), r, sizeof(rgl_vec2f) * n, cudaMemcpyHostToDevice));
+	count = n;
+}
+
+void SetRangeRaysNode::validateImpl()
+{
+	RaysNodeSingleInput::validateImpl();
+	if (!(count == 1 || count == input->rayCount())) {
+		throw InvalidPipeline(format("ranges doesn't match number of rays. RangesCount(%zu) should be one or equal to RayCount(%zu)",
+		                             count, input->rayCount()));
+	}
+}
+
+void GaussianNoiseAngularRaysNode::setParameters(float m, float sd, rgl_axis_t a)
+{
+	mean = m;
+	stDev = sd;
+	axis = a;
+}
+
+static rgl::NoiseParams makeNoise(uint64_t seed, uint64_t frame, uint32_t kind, float mean, float sd, float rise, int axis,
+                                  const Mat34& lookAt)
+{
+	rgl::NoiseParams np{};
+	np.seedLo = (uint32_t) seed;
+	np.seedHi = (uint32_t) (seed >> 32);
+	np.frameLo = (uint32_t) frame;
+	np.frameHi = (uint32_t) (frame >> 32);
+	np.kind = kind;
+	np.mean = mean;
+	np.stDev = sd;
+	np.stDevRise = rise;
+	np.axis = axis;
+	np.lookAt = lookAt;
+	np.lookAtInv = rgl::inverse(lookAt);
+	return np;
+}
+
+void GaussianNoiseAngularRaysNode::enqueueImpl(cudaStream_t s)
+{
+	size_t n = rayCount();
+	auto* o = static_cast<Mat34*>(out.ensure(sizeof(Mat34) * std::max<size_t>(1, n)));
+	Mat34 lookAt = rgl::inverse(input->cumulativeRayTransform());
+	rgl::launchNoiseAngularRay(input->raysDev(), o, (int) n, makeNoise(seed, frame, 1, mean, stDev, 0.0f, axis, lookAt), s);
+	++frame;
+}
+
+// ================================================================ points nodes
+
+size_t PointsNode::pointCountHost()
+{
+	const int32_t* dc = deviceCount();
+	if (dc == nullptr) {
+		return capacity();
+	}
+	int32_t c = 0;
+	RGL_CHECK_CUDA(cudaMemcpy(&c, dc, sizeof(c), cudaMemcpyDeviceToHost));
+	return (size_t) c;
+}
+
+void PointsNodeSingleInput::validateImpl()
+{
+	input = exactlyOneInput<PointsNode>("IPointsNode");
+	for (auto f : requiredFields()) {
+		if (!input->hasField(f) && !rgl::isDummy(f)) {
+			throw InvalidPipeline(format("%s requires %s to be present", name(), rgl::fieldName(f)));
+		}
+	}
+}
+
+// ---- RaytraceNode
+
+static bool raytraceSupports(rgl_field_t f)
+{
+	switch (f) {
+		case RGL_FIELD_XYZ_VEC3_F32:
+		case RGL_FIELD_DISTANCE_F32:
+		case RGL_FIELD_IS_HIT_I32:
+		case RGL_FIELD_ENTITY_ID_I32:
+		case RGL_FIELD_RETURN_TYPE_U8:
+		case RGL_FIELD_INTENSITY_F32:
+		case RGL_FIELD_INTENSITY_U8:
+		case RGL_FIELD_RAY_IDX_U32:
+		case RGL_FIELD_NORMAL_VEC3_F32:
+		case RGL_FIELD_INCIDENT_ANGLE_F32: return true;
+		default: return false;
+	}
+}
+
+std::set<rgl_field_t> RaytraceNode::findFieldsToCompute()
+{
+	// XYZ plus every field required by point nodes reachable downstream (reference RaytraceNode.cpp:165-191).
+	std::set<rgl_field_t> out{RGL_FIELD_XYZ_VEC3_F32};
+	std::set<Node*> seen;
+	std::function<void(Node*)> dfs = [&](Node* cur) {
+		for (auto& o : cur->outputs) {
+			auto pn = std::dynamic_pointer_cast<PointsNode>(o);
+			if (!pn || seen.count(o.get())) {
+				continue;
+			}
+			seen.insert(o.get());
+			for (auto f : pn->requiredFields()) {
+				if (!rgl::isDummy(f)) {
+					out.insert(f);
+				}
+			}
+			dfs(o.get());
+		}
+	};
+	dfs(this);
+	return out;
+}
+
+int RaytraceNode::sampleCount() const
+{
+	bool div = (hDivergence / 2.0f) > 0.0f && (vDivergence / 2.0f) > 0.0f;
+	return div ? 1 + sampleLayers * sampleVertices : 1;
+}
+
+void RaytraceNode::validateImpl()
+{
+	fields = findFieldsToCompute();
+	for (auto f : fields) {
+		if (!raytraceSupports(f)) {
+			throw rgl::NotImplemented(format("RaytraceNode cannot compute field %s in this implementation", rgl::fieldName(f)));
+		}
+	}
+	rays = exactlyOneInput<RaysNode>("IRaysNode");
+	if (sampleCount() > rgl::kMaxBeamSamples) {
+		throw rgl::InvalidAPIArgument(format("beam sample pattern of %d rays exceeds %d", sampleCount(), rgl::kMaxBeamSamples));
+	}
+	// Sub-ray table (reference optixPrograms.cu:75-86,230-248), evaluated on the host in float with the
+	// reference's operation order so every consumer sees identical sub-ray poses.
+	int ns = sampleCount();
+	if (ns != uploadedSamples || hDivergence != uploadedH || vDivergence != uploadedV) {
+		std::vector<Mat34> table(ns, Mat34::identity());
+		if (ns > 1) {
+			const float hHalf = hDivergence / 2.0f, vHalf = vDivergence / 2.0f;
+			const float step = 2.0f * static_cast<float>(M_PI) / (float) sampleVertices;
+			int k = 1;
+			for (int l = 0; l < sampleLayers; ++l) {
+				for (int v = 0; v < sampleVertices; ++v) {
+					volatile float frac = 1.0f - (float) l / (float) sampleLayers;
+					volatile float a = (float) v * step;
+					float hAngle = (hHalf * frac) * cosf(a);
+					float vAngle = (vHalf * frac) * sinf(a);
+					table[k++] = rgl::beamSampleRotation(hAngle, vAngle);
+				}
+			}
+		}
+		RGL_CHECK_CUDA(cudaMemcpy(sampleTable.ensure(sizeof(Mat34) * ns), table.data(), sizeof(Mat34) * ns, cudaMemcpyHostToDevice));
+		uploadedSamples = ns;
+		uploadedH = hDivergence;
+		uploadedV = vDivergence;
+	}
+	if (defaultRange.get() == nullptr) {
+		const float r[2] = {0.0f, FLT_MAX};
+		RGL_CHECK_CUDA(cudaMemcpy(defaultRange.ensure(sizeof(r)), r, sizeof(r), cudaMemcpyHostToDevice));
+	}
+	if (errorFlag.get() == nullptr) {
+		RGL_CHECK_CUDA(cudaMemset(errorFlag.ensure(sizeof(int32_t)), 0, sizeof(int32_t)));
+	}
+	if (scene == nullptr) {
+		scene = &Scene::defaultScene();
+	}
+}
+
+const void* RaytraceNode::fieldDev(rgl_field_t f)
+{
+	auto it = outputs.find(f);
+	if (it == outputs.end() || !fields.count(f)) {
+		throw InvalidPipeline(format("RaytraceNode does not provide field %s", rgl::fieldName(f)));
+	}
+	return it->second.get();
+}
+
+void RaytraceNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t n = rays->rayCount();
+	const size_t cap = std::max<size_t>(1, (size_t) returnCount() * n);
+	for (auto f : fields) {
+		outputs[f].ensure(rgl::fieldSize(f) * cap);
+	}
+	for (auto it = outputs.begin(); it != outputs.end();) {
+		it = fields.count(it->first) ? std::next(it) : outputs.erase(it);
+	}
+	scene->prepare(s);
+
+	rgl::TraceParams p{};
+	p.rays = rays->raysDev();
+	p.ranges = rays->rangesDev() ? rays->rangesDev() : defaultRange.as<float>();
+	p.nRanges = rays->rangesDev() ? (int32_t) rays->rangesCount() : 1;
+	p.nRays = (int32_t) n;
+	p.nSamples = sampleCount();
+	p.returnMode = mode;
+	p.returnCount = returnCount();
+	p.nearNonHitDistance = nearDistance;
+	p.farNonHitDistance = farDistance;
+	p.defaultIntensity = defaultIntensity;
+	bool strongestSelected = false;
+	for (int r = 0; r < p.returnCount; ++r) {
+		uint32_t t = (((uint32_t) mode) >> (8 * r)) & 0xffu;
+		strongestSelected = strongestSelected || t == RGL_RETURN_TYPE_STRONGEST || t == RGL_RETURN_TYPE_SECOND_STRONGEST;
+	}
+	p.needIntensity = (fields.count(RGL_FIELD_INTENSITY_F32) || fields.count(RGL_FIELD_INTENSITY_U8) || strongestSelected) ? 1 : 0;
+	p.errorFlag = errorFlag.as<int32_t>();
+	p.scene = scene->view();
+	auto ptr = [&](rgl_field_t f) -> void* { return fields.count(f) ? outputs[f].get() : nullptr; };
+	p.out.xyz = static_cast<float*>(ptr(RGL_FIELD_XYZ_VEC3_F32));
+	p.out.distance = static_cast<float*>(ptr(RGL_FIELD_DISTANCE_F32));
+	p.out.isHit = static_cast<int32_t*>(ptr(RGL_FIELD_IS_HIT_I32));
+	p.out.entityId = static_cast<int32_t*>(ptr(RGL_FIELD_ENTITY_ID_I32));
+	p.out.returnType = static_cast<uint8_t*>(ptr(RGL_FIELD_RETURN_TYPE_U8));
+	p.out.intensityF32 = static_cast<float*>(ptr(RGL_FIELD_INTENSITY_F32));
+	p.out.rayIdx = static_cast<uint32_t*>(ptr(RGL_FIELD_RAY_IDX_U32));
+	p.out.intensityU8 = static_cast<uint8_t*>(ptr(RGL_FIELD_INTENSITY_U8));
+	p.out.normal = static_cast<float*>(ptr(RGL_FIELD_NORMAL_VEC3_F32));
+	p.out.incidentAngle = static_cast<float*>(ptr(RGL_FIELD_INCIDENT_ANGLE_F32));
+	p.out.laserRetro = nullptr;
+	if (timingEnabled()) {
+		if (!evStart) {
+			RGL_CHECK_CUDA(cudaEventCreate(&evStart));
+			RGL_CHECK_CUDA(cudaEventCreate(&evStop));
+		}
+		RGL_CHECK_CUDA(cudaEventRecord(evStart, s));
+	}
+	rgl::launchTrace(p, sampleTable.as<Mat34>(), s);
+	RGL_CHECK_CUDA(cudaGetLastError());
+	if (timingEnabled()) {
+		RGL_CHECK_CUDA(cudaEventRecord(evStop, s));
+	}
+}
+
+void RaytraceNode::checkErrors()
+{
+	if (errorFlag.get() == nullptr) {
+		return;
+	}
+	int32_t e = 0;
+	RGL_CHECK_CUDA(cudaMemcpy(&e, errorFlag.get(), sizeof(e), cudaMemcpyDeviceToHost));
+	if (e != 0) {
+		RGL_CHECK_CUDA(cudaMemset(errorFlag.get(), 0, sizeof(int32_t)));
+		throw std::runtime_error("RaytraceNode: traversal stack overflow on the device (scene BVH too deep)");
+	}
+	if (scene) {
+		scene->checkDeviceErrors();
+	}
+}
+
+// ---- YieldPointsNode
+
+void YieldPointsNode::setParameters(const std::vector<rgl_field_t>& f)
+{
+	if (std::find(f.begin(), f.end(), RGL_FIELD_DYNAMIC_FORMAT) != f.end()) {
+		throw rgl::InvalidAPIArgument("cannot yield field 'RGL_FIELD_DYNAMIC_FORMAT'");
+	}
+	for (auto x : f) {
+		(void) rgl::fieldSize(x);
+	}
+	fields = f;
+}
+
+bool YieldPointsNode::hasField(rgl_field_t f) const { return std::find(fields.begin(), fields.end(), f) != fields.end(); }
+
+// ---- FormatPointsNode
+
+void FormatPointsNode::setParameters(const std::vector<rgl_field_t>& f)
+{
+	if (std::find(f.begin(), f.end(), RGL_FIELD_DYNAMIC_FORMAT) != f.end()) {
+		throw rgl::InvalidAPIArgument("cannot format field 'RGL_FIELD_DYNAMIC_FORMAT'");
+	}
+	for (auto x : f) {
+		(void) rgl::fieldSize(x);
+	}
+	fields = f;
+}
+
+bool FormatPointsNode::hasField(rgl_field_t f) const
+{
+	return f == RGL_FIELD_DYNAMIC_FORMAT || std::find(fields.begin(), fields.end(), f) != fields.end();
+}
+
+size_t FormatPointsNode::fieldPointSize(rgl_field_t f) const
+{
+	return f == RGL_FIELD_DYNAMIC_FORMAT ? rgl::pointSize(fields) : rgl::fieldSize(f);
+}
+
+const void* FormatPointsNode::fieldDev(rgl_field_t f)
+{
+	if (f == RGL_FIELD_DYNAMIC_FORMAT) {
+		return out.get();
+	}
+	return input->fieldDev(f);
+}
+
+void FormatPointsNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t ps = rgl::pointSize(fields);
+	const size_t cap = input->capacity();
+	out.ensure(std::max<size_t>(1, ps * cap));
+	if (fields.size() > (size_t) rgl::kMaxFieldCopies) {
+		throw rgl::InvalidAPIArgument(format("format of %zu fields exceeds %d", fields.size(), rgl::kMaxFieldCopies));
+	}
+	rgl::FieldCopies fc{};
+	int off = 0;
+	for (auto f : fields) {
+		rgl::FieldCopy c{};
+		c.src = rgl::isDummy(f) ? nullptr : input->fieldDev(f);
+		c.size = (int32_t) rgl::fieldSize(f);
+		c.offset = off;
+		off += c.size;
+		fc.f[fc.count++] = c;
+	}
+	rgl::launchFormat(fc, (int) ps, (int) cap, input->deviceCount(), out.as<uint8_t>(), s);
+}
+
+// ---- CompactByFieldPointsNode
+
+void CompactByFieldPointsNode::validateImpl()
+{
+	PointsNodeSingleInput::validateImpl();
+	// Fields needed downstream are compacted eagerly in the run's single compaction kernel.
+	eager.clear();
+	std::set<Node*> seen;
+	std::function<void(Node*)> dfs = [&](Node* cur) {
+		for (auto& o : cur->outputs) {
+			auto pn = std::dynamic_pointer_cast<PointsNode>(o);
+			if (!pn || seen.count(o.get())) {
+				continue;
+			}
+			seen.insert(o.get());
+			for (auto f : pn->requiredFields()) {
+				if (!rgl::isDummy(f) && input->hasField(f)) {
+					eager.insert(f);
+				}
+			}
+			dfs(o.get());
+		}
+	};
+	dfs(this);
+	if (count.get() == nullptr) {
+		count.ensure(sizeof(int32_t));
+		RGL_CHECK_CUDA(cudaMemset(count.get(), 0, sizeof(int32_t)));
+	}
+	if (errorFlag.get() == nullptr) {
+		RGL_CHECK_CUDA(cudaMemset(errorFlag.ensure(sizeof(int32_t)), 0, sizeof(int32_t)));
+	}
+}
+
+void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cudaStream_t s)
+{
+	const size_t cap = input->capacity();
+	rgl::FieldCopies fc{};
+	for (auto f : which) {
+		if (fc.count == rgl::kMaxFieldCopies) {
+			throw rgl::InvalidAPIArgument(format("compaction of more than %d fields", rgl::kMaxFieldCopies));
+		}
+		rgl::FieldCopy c{};
+		c.size = (int32_t) rgl::fieldSize(f);
+		c.src = input->fieldDev(f);
+		c.dst = outputs[f].ensure(std::max<size_t>(1, c.size * cap));
+		fc.f[fc.count++] = c;
+	}
+	scratch.ensure(rgl::compactScratchBytes((int) cap));
+	rgl::launchCompact(static_cast<const int32_t*>(input->fieldDev(field)), (int) cap, input->deviceCount(), fc, count.as<int32_t>(),
+	                   scratch.get(), errorFlag.as<int32_t>(), s);
+}
+
+void CompactByFieldPointsNode::enqueueImpl(cudaStream_t s)
+{
+	lastStream = s;
+	lazyDone.clear();
+	compact(std::vector<rgl_field_t>(eager.begin(), eager.end()), s);
+}
+
+const void* CompactByFieldPointsNode::fieldDev(rgl_field_t f)
+{
+	if (eager.count(f) || lazyDone.count(f)) {
+		return outputs[f].get();
+	}
+	if (!input->hasField(f)) {
+		throw InvalidPipeline(format("CompactByFieldPointsNode: input does not provide field %s", rgl::fieldName(f)));
+	}
+	// A field nobody downstream declared: compact it now on the graph's stream and wait for it.
+	compact({f}, lastStream);
+	RGL_CHECK_CUDA(cudaStreamSynchronize(lastStream));
+	lazyDone.insert(f);
+	return outputs[f].get();
+}
+
+void CompactByFieldPointsNode::checkErrors()
+{
+	if (errorFlag.get() == nullptr) {
+		return;
+	}
+	int32_t e = 0;
+	RGL_CHECK_CUDA(cudaMemcpy(&e, errorFlag.get(), sizeof(e), cudaMemcpyDeviceToHost));
+	if (e != 0) {
+		RGL_CHECK_CUDA(cudaMemset(errorFlag.get(), 0, sizeof(int32_t)));
+		throw std::runtime_error("CompactByFieldPointsNode: decoupled look-back did not complete on the device");
+	}
+}
+
+// ---- TransformPointsNode
+
+void TransformPointsNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t cap = input->capacity();
+	out.ensure(std::max<size_t>(1, 12 * cap));
+	rgl::launchTransformPoints(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), out.as<float>(), (int) cap,
+	                           input->deviceCount(), transform, s);
+}
+
+const void* TransformPointsNode::fieldDev(rgl_field_t f)
+{
+	return f == RGL_FIELD_XYZ_VEC3_F32 ? out.get() : input->fieldDev(f);
+}
+
+// ---- Gaussian noise on points
+
+void GaussianNoiseAngularHitpointNode::setParameters(float m, float sd, rgl_axis_t a)
+{
+	mean = m;
+	stDev = sd;
+	axis = a;
+}
+
+void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t cap = input->capacity();
+	withDistance = input->hasField(RGL_FIELD_DISTANCE_F32);
+	outXyz.ensure(std::max<size_t>(1, 12 * cap));
+	if (withDistance) {
+		outDist.ensure(std::max<size_t>(1, 4 * cap));
+	}
+	rgl::NoiseParams np = makeNoise(seed, frame, 2, mean, stDev, 0.0f, axis, input->lookAtOriginTransform());
+	rgl::launchNoiseAngularHitpoint(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), outXyz.as<float>(),
+	                                withDistance ? outDist.as<float>() : nullptr, (int) cap, input->deviceCount(), np, s);
+	++frame;
+}
+
+const void* GaussianNoiseAngularHitpointNode::fieldDev(rgl_field_t f)
+{
+	if (f == RGL_FIELD_XYZ_VEC3_F32) {
+		return outXyz.get();
+	}
+	if (f == RGL_FIELD_DISTANCE_F32 && withDistance) {
+		return outDist.get();
+	}
+	return input->fieldDev(f);
+}
+
+void GaussianNoiseDistanceNode::setParameters(float m, float b, float r)
+{
+	mean = m;
+	base = b;
+	rise = r;
+}
+
+void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t cap = input->capacity();
+	outXyz.ensure(std::max<size_t>(1, 12 * cap));
+	outDist.ensure(std::max<size_t>(1, 4 * cap));
+	rgl::NoiseParams np = makeNoise(seed, frame, 3, mean, base, rise, 0, input->lookAtOriginTransform());
+	rgl::launchNoiseDistance(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)),
+	                         static_cast<const float*>(input->fieldDev(RGL_FIELD_DISTANCE_F32)), outXyz.as<float>(),
+	                         outDist.as<float>(), (int) cap, input->deviceCount(), np, s);
+	++frame;
+}
+
+const void* GaussianNoiseDistanceNode::fieldDev(rgl_field_t f)
+{
+	if (f == RGL_FIELD_XYZ_VEC3_F32) {
+		return outXyz.get();
+	}
+	if (f == RGL_FIELD_DISTANCE_F32) {
+		return outDist.get();
+	}
+	return input->fieldDev(f);
+}
+
+// ---- FromArrayPointsNode (reference src/graph/FromArrayPointsNode.cpp:18-46)
+
+void FromArrayPointsNode::setParameters(const void* points, size_t n, const std::vector<rgl_field_t>& fields)
+{
+	if (std::find(fields.begin(), fields.end(), RGL_FIELD_DYNAMIC_FORMAT) != fields.end()) {
+		throw rgl::InvalidAPIArgument("cannot create point cloud from field 'RGL_FIELD_DYNAMIC_FORMAT'");
+	}
+	if (fields.size() > (size_t) rgl::kMaxFieldCopies) {
+		throw rgl::InvalidAPIArgument(format("more than %d fields", rgl::kMaxFieldCopies));
+	}
+	const size_t ps = rgl::pointSize(fields);
+	data.clear();
+	count = n;
+	rgl::DeviceBuffer staging;
+	RGL_CHECK_CUDA(cudaMemcpy(staging.ensure(ps * n), points, ps * n, cudaMemcpyHostToDevice));
+	rgl::FieldCopies fc{};
+	int off = 0;
+	for (auto f : fields) {
+		rgl::FieldCopy c{};
+		c.size = (int32_t) rgl::fieldSize(f);
+		c.offset = off;
+		off += c.size;
+		if (!rgl::isDummy(f) && !data.count(f)) {
+			c.dst = data[f].ensure(std::max<size_t>(1, c.size * n));
+		}
+		fc.f[fc.count++] = c;
+	}
+	rgl::launchAosToSoa(staging.as<uint8_t>(), (int) ps, (int) n, fc, nullptr);
+	RGL_CHECK_CUDA(cudaDeviceSynchronize());
+}
+
+void FromArrayPointsNode::validateImpl()
+{
+	if (!inputs.empty()) {
+		throw InvalidPipeline(format("inputs for node %s are not allowed", name()));
+	}
+}
+
+const void* FromArrayPointsNode::fieldDev(rgl_field_t f)
+{
+	auto it = data.find(f);
+	if (it == data.end()) {
+		throw InvalidPipeline(format("FromArrayPointsNode does not provide field %s", rgl::fieldName(f)));
+	}
+	return it->second.get();
+}
+
+// ================================================================ GraphRunCtx
+// (reference src/graph/GraphRunCtx.cpp:23-211)
+
+std::vector<std::shared_ptr<GraphRunCtx>>& GraphRunCtx::instances()
+{
+	static std::vector<std::shared_ptr<GraphRunCtx>> v;
+	return v;
+}
+
+GraphRunCtx::GraphRunCtx()
+{
+	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+	RGL_CHECK_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+	RGL_CHECK_CUDA(cudaEventCreate(&runStart));
+	RGL_CHECK_CUDA(cudaEventCreate(&runStop));
+}
+
+GraphRunCtx::~GraphRunCtx()
+{
+	cudaEventDestroy(done);
+	cudaEventDestroy(runStart);
+	cudaEventDestroy(runStop);
+	cudaStreamDestroy(stream_);
+}
+
+std::shared_ptr<GraphRunCtx> GraphRunCtx::createAndAttach(const Node::Ptr& node)
+{
+	auto ctx = std::shared_ptr<GraphRunCtx>(new GraphRunCtx());
+	ctx->nodes = node->connectedComponent();
+	for (auto& n : ctx->nodes) {
+		if (n->ctx) {
+			throw std::logic_error(format("attempted to replace existing graphRunCtx in node %s when creating for %s", n->name(),
+			                              node->name()));
+		}
+		n->ctx = ctx;
+		n->dirty = true;
+	}
+	instances().push_back(ctx);
+	return ctx;
+}
+
+std::vector<Node::Ptr> GraphRunCtx::findExecutionOrder(std::set<Node::Ptr> nodes)
+{
+	std::vector<Node::Ptr> reverseOrder;
+	std::function<void(const Node::Ptr&)> dfs = [&](const Node::Ptr& cur) {
+		nodes.erase(cur);
+		for (auto it = cur->outputs.rbegin(); it != cur->outputs.rend(); ++it) {
+			if (nodes.count(*it)) {
+				dfs(*it);
+			}
+		}
+		reverseOrder.push_back(cur);
+	};
+	std::vector<Node::Ptr> entries;
+	for (auto& n : nodes) {
+		if (n->inputs.empty()) {
+			entries.push_back(n);
+		}
+	}
+	std::stable_sort(entries.begin(), entries.end(), [](const Node::Ptr& a, const Node::Ptr& b) { return a->priority < b->priority; });
+	for (auto& e : entries) {
+		if (nodes.count(e)) {
+			dfs(e);
+		}
+	}
+	if (!nodes.empty()) {
+		throw std::logic_error("bug: detected unreachable nodes");
+	}
+	return {reverseOrder.rbegin(), reverseOrder.rend()};
+}
+
+void GraphRunCtx::run()
+{
+	synchronize();
+	if (order.empty()) {
+		order = findExecutionOrder(nodes);
+	}
+	for (auto& n : order) {
+		n->validateImpl();
+		n->dirty = false;
+	}
+	running = true;
+	if (timingEnabled()) {
+		RGL_CHECK_CUDA(cudaEventRecord(runStart, stream_));
+	}
+	for (auto& n : order) {
+		n->enqueueImpl(stream_);
+	}
+	if (timingEnabled()) {
+		RGL_CHECK_CUDA(cudaEventRecord(runStop, stream_));
+	}
+	RGL_CHECK_CUDA(cudaEventRecord(done, stream_));
+}
+
+void GraphRunCtx::synchronize()
+{
+	if (!running) {
+		return;
+	}
+	running = false;
+	RGL_CHECK_CUDA(cudaEventSynchronize(done));
+	RGL_CHECK_CUDA(cudaGetLastError());
+	if (timingEnabled()) {
+		cudaEventElapsedTime(&lastRunMs, runStart, runStop);
+		for (auto& n : order) {
+			if (auto rt = std::dynamic_pointer_cast<RaytraceNode>(n); rt && rt->evStart) {
+				cudaEventElapsedTime(&lastTraceMs, rt->evStart, rt->evStop);
+			}
+		}
+	}
+	for (auto& n : order) {
+		n->checkErrors();
+	}
+}
+
+void GraphRunCtx::detachAndDestroy()
+{
+	auto self = shared_from_this();
+	synchronize();
+	for (auto& n : nodes) {
+		n->ctx.reset();
+		n->dirty = true;
+	}
+	auto& v = instances();
+	v.erase(std::remove(v.begin(), v.end(), self), v.end());
+}
+
+void GraphRunCtx::synchronizeAll()
+{
+	for (auto& c : instances()) {
+		c->synchronize();
+	}
+}

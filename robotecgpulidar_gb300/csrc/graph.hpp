@@ -1,0 +1,379 @@
+// Graph runtime behind rgl_node_t (reference src/graph/Node.hpp:57-214, Interfaces.hpp:24-145,
+// GraphRunCtx.cpp:23-211, NodesCore.hpp).
+//
+// Nodes keep RGL's semantics: create-or-modify parameters, DAG links with priorities, a per-graph
+// CUDA stream, validation on the client thread at rgl_graph_run, results readable from any node of
+// the graph after the run. Differences in mechanism (not in results):
+//  * runs are enqueued by the calling thread (no per-run host thread);
+//  * compaction keeps its point count on the device; downstream kernels read it from there and the
+//    host reads it only when a result size is requested;
+//  * formatted output stays on the device until rgl_graph_get_result_data copies it.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <optional>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+#include "kernels.hpp"
+
+struct GraphRunCtx;
+struct Scene;
+
+struct Node : std::enable_shared_from_this<Node>
+{
+	using Ptr = std::shared_ptr<Node>;
+	virtual ~Node() = default;
+	virtual const char* name() const = 0;
+
+	void addChild(const Ptr& child);
+	void removeChild(const Ptr& child);
+	void setPriority(int32_t p);
+	std::set<Ptr> connectedComponent();
+	std::set<Ptr> disconnectConnectedNodes();
+
+	virtual void validateImpl() = 0;
+	virtual void enqueueImpl(cudaStream_t s) = 0;
+	// Called after the graph's stream completed; throws if a kernel of this node raised its error flag.
+	virtual void checkErrors() {}
+	// Host-side parameters changed: the node must re-upload or re-plan at the next run.
+	void markDirty() { dirty = true; }
+
+	template<class T>
+	std::shared_ptr<T> exactlyOneInput(const char* ifaceName);
+
+	std::vector<Ptr> inputs, outputs;
+	int32_t priority = 0;
+	bool dirty = true;
+	std::shared_ptr<GraphRunCtx> ctx;
+};
+
+// ---------------------------------------------------------------- rays
+
+struct RaysNode : virtual Node
+{
+	virtual size_t rayCount() const = 0;
+	virtual const rgl::Mat34* raysDev() const = 0;
+	virtual const float* rangesDev() const { return nullptr; } // 2 floats per entry
+	virtual size_t rangesCount() const { return 0; }
+	virtual rgl::Mat34 cumulativeRayTransform() const { return rgl::Mat34::identity(); }
+};
+
+struct RaysNodeSingleInput : RaysNode
+{
+	void validateImpl() override;
+	size_t rayCount() const override { return input->rayCount(); }
+	const rgl::Mat34* raysDev() const override { return input->raysDev(); }
+	const float* rangesDev() const override { return input->rangesDev(); }
+	size_t rangesCount() const override { return input->rangesCount(); }
+	rgl::Mat34 cumulativeRayTransform() const override { return input->cumulativeRayTransform(); }
+
+protected:
+	std::shared_ptr<RaysNode> input;
+};
+
+struct FromMat3x4fRaysNode : RaysNode
+{
+	const char* name() const override { return "FromMat3x4fRaysNode"; }
+	void setParameters(const rgl_mat3x4f* rays, size_t count);
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t) override {}
+	size_t rayCount() const override { return count; }
+	const rgl::Mat34* raysDev() const override { return rays.as<rgl::Mat34>(); }
+
+private:
+	rgl::DeviceBuffer rays;
+	size_t count = 0;
+};
+
+struct TransformRaysNode : RaysNodeSingleInput
+{
+	const char* name() const override { return "TransformRaysNode"; }
+	void setParameters(const rgl::Mat34& tf) { transform = tf; }
+	void enqueueImpl(cudaStream_t s) override;
+	const rgl::Mat34* raysDev() const override { return out.as<rgl::Mat34>(); }
+	rgl::Mat34 cumulativeRayTransform() const override { return rgl::mul(transform, input->cumulativeRayTransform()); }
+
+private:
+	rgl::Mat34 transform = rgl::Mat34::identity();
+	rgl::DeviceBuffer out;
+};
+
+struct SetRangeRaysNode : RaysNodeSingleInput
+{
+	const char* name() const override { return "SetRangeRaysNode"; }
+	void setParameters(const rgl_vec2f* ranges, size_t count);
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t) override {}
+	const float* rangesDev() const override { return ranges.as<float>(); }
+	size_t rangesCount() const override { return count; }
+
+private:
+	rgl::DeviceBuffer ranges;
+	size_t count = 0;
+};
+
+struct GaussianNoiseAngularRaysNode : RaysNodeSingleInput
+{
+	const char* name() const override { return "GaussianNoiseAngularRaysNode"; }
+	void setParameters(float mean, float stDev, rgl_axis_t axis);
+	void setSeed(uint64_t s, uint64_t f)
+	{
+		seed = s;
+		frame = f;
+	}
+	void enqueueImpl(cudaStream_t s) override;
+	const rgl::Mat34* raysDev() const override { return out.as<rgl::Mat34>(); }
+
+private:
+	float mean = 0, stDev = 0;
+	rgl_axis_t axis = RGL_AXIS_X;
+	uint64_t seed = 0, frame = 0;
+	rgl::DeviceBuffer out;
+};
+
+// ---------------------------------------------------------------- points
+
+struct PointsNode : virtual Node
+{
+	virtual std::vector<rgl_field_t> requiredFields() const { return {}; }
+	virtual bool isDense() const = 0;
+	virtual bool hasField(rgl_field_t f) const = 0;
+	// Upper bound of the point count, exact unless deviceCount() is set.
+	virtual size_t capacity() const = 0;
+	// Device int32 holding the exact count when it is only known on the device (after compaction).
+	virtual const int32_t* deviceCount() const { return nullptr; }
+	virtual int32_t returnMode() const { return RGL_RETURN_UNKNOWN; }
+	virtual rgl::Mat34 lookAtOriginTransform() const { return rgl::Mat34::identity(); }
+	// Device pointer with capacity() elements of `field`; valid after this node's enqueue.
+	virtual const void* fieldDev(rgl_field_t field) = 0;
+	virtual size_t fieldPointSize(rgl_field_t field) const { return rgl::fieldSize(field); }
+	// Exact point count; reads the device count (graph must be synchronised).
+	size_t pointCountHost();
+};
+
+struct PointsNodeSingleInput : PointsNode
+{
+	void validateImpl() override;
+	bool isDense() const override { return input->isDense(); }
+	bool hasField(rgl_field_t f) const override { return input->hasField(f); }
+	size_t capacity() const override { return input->capacity(); }
+	const int32_t* deviceCount() const override { return input->deviceCount(); }
+	int32_t returnMode() const override { return input->returnMode(); }
+	rgl::Mat34 lookAtOriginTransform() const override { return input->lookAtOriginTransform(); }
+	const void* fieldDev(rgl_field_t f) override { return input->fieldDev(f); }
+
+protected:
+	std::shared_ptr<PointsNode> input;
+};
+
+struct RaytraceNode : PointsNode
+{
+	const char* name() const override { return "RaytraceNode"; }
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t s) override;
+	bool isDense() const override { return false; }
+	bool hasField(rgl_field_t f) const override { return fields.count(f) != 0; }
+	size_t capacity() const override { return rays ? (size_t) returnCount() * rays->rayCount() : 0; }
+	int32_t returnMode() const override { return mode; }
+	rgl::Mat34 lookAtOriginTransform() const override { return rgl::inverse(rays->cumulativeRayTransform()); }
+	const void* fieldDev(rgl_field_t f) override;
+
+	int returnCount() const { return (int) (((uint32_t) mode) >> 24); }
+	void setReturnMode(int32_t m) { mode = m; }
+	void setBeamDivergence(float h, float v)
+	{
+		hDivergence = h;
+		vDivergence = v;
+	}
+	void setBeamSamples(int layers, int vertices)
+	{
+		sampleLayers = layers;
+		sampleVertices = vertices;
+	}
+	void setNonHits(float nearD, float farD)
+	{
+		nearDistance = nearD;
+		farDistance = farD;
+	}
+	void setDefaultIntensity(float i) { defaultIntensity = i; }
+	int sampleCount() const;
+	void checkErrors() override;
+	Scene* scene = nullptr;
+
+	// Timing (extension): device time of the traversal kernel of the last run.
+	cudaEvent_t evStart = nullptr, evStop = nullptr;
+
+private:
+	std::set<rgl_field_t> findFieldsToCompute();
+	std::shared_ptr<RaysNode> rays;
+	std::set<rgl_field_t> fields;
+	std::map<rgl_field_t, rgl::DeviceBuffer> outputs;
+	rgl::DeviceBuffer defaultRange;
+	rgl::DeviceBuffer sampleTable;
+	int uploadedSamples = -1;
+	float uploadedH = -1, uploadedV = -1;
+	int32_t mode = RGL_RETURN_FIRST;
+	float hDivergence = 0, vDivergence = 0;
+	int sampleLayers = 3, sampleVertices = 19; // reference pattern: 1 + 3 * 19 = 58 samples
+	float nearDistance = INFINITY, farDistance = INFINITY;
+	float defaultIntensity = 0.0f;
+	rgl::DeviceBuffer errorFlag;
+};
+
+struct YieldPointsNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "YieldPointsNode"; }
+	void setParameters(const std::vector<rgl_field_t>& f);
+	std::vector<rgl_field_t> requiredFields() const override { return fields; }
+	bool hasField(rgl_field_t f) const override;
+	void enqueueImpl(cudaStream_t) override {}
+
+private:
+	std::vector<rgl_field_t> fields;
+};
+
+struct FormatPointsNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "FormatPointsNode"; }
+	void setParameters(const std::vector<rgl_field_t>& f);
+	std::vector<rgl_field_t> requiredFields() const override { return fields; }
+	bool hasField(rgl_field_t f) const override;
+	void enqueueImpl(cudaStream_t s) override;
+	const void* fieldDev(rgl_field_t f) override;
+	size_t fieldPointSize(rgl_field_t f) const override;
+
+private:
+	std::vector<rgl_field_t> fields;
+	rgl::DeviceBuffer out;
+};
+
+struct CompactByFieldPointsNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "CompactByFieldPointsNode"; }
+	void setParameters(rgl_field_t f) { field = f; }
+	std::vector<rgl_field_t> requiredFields() const override { return {field}; }
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t s) override;
+	bool isDense() const override { return true; }
+	const int32_t* deviceCount() const override { return count.as<int32_t>(); }
+	const void* fieldDev(rgl_field_t f) override;
+	void checkErrors() override;
+
+private:
+	rgl_field_t field = RGL_FIELD_IS_HIT_I32;
+	std::set<rgl_field_t> eager;               // fields compacted during the run
+	std::map<rgl_field_t, rgl::DeviceBuffer> outputs;
+	std::set<rgl_field_t> lazyDone;            // fields compacted on demand after the run
+	rgl::DeviceBuffer count;
+	rgl::DeviceBuffer scratch;
+	rgl::DeviceBuffer errorFlag;
+	cudaStream_t lastStream = nullptr;
+	void compact(const std::vector<rgl_field_t>& which, cudaStream_t s);
+};
+
+struct TransformPointsNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "TransformPointsNode"; }
+	void setParameters(const rgl::Mat34& tf) { transform = tf; }
+	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32}; }
+	void enqueueImpl(cudaStream_t s) override;
+	rgl::Mat34 lookAtOriginTransform() const override
+	{
+		return rgl::mul(rgl::inverse(transform), input->lookAtOriginTransform());
+	}
+	const void* fieldDev(rgl_field_t f) override;
+
+private:
+	rgl::Mat34 transform = rgl::Mat34::identity();
+	rgl::DeviceBuffer out;
+};
+
+struct GaussianNoiseAngularHitpointNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "GaussianNoiseAngularHitpointNode"; }
+	void setParameters(float mean, float stDev, rgl_axis_t axis);
+	void setSeed(uint64_t s, uint64_t f)
+	{
+		seed = s;
+		frame = f;
+	}
+	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32}; }
+	void enqueueImpl(cudaStream_t s) override;
+	const void* fieldDev(rgl_field_t f) override;
+
+private:
+	float mean = 0, stDev = 0;
+	rgl_axis_t axis = RGL_AXIS_X;
+	uint64_t seed = 0, frame = 0;
+	bool withDistance = false;
+	rgl::DeviceBuffer outXyz, outDist;
+};
+
+struct GaussianNoiseDistanceNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "GaussianNoiseDistanceNode"; }
+	void setParameters(float mean, float base, float rise);
+	void setSeed(uint64_t s, uint64_t f)
+	{
+		seed = s;
+		frame = f;
+	}
+	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32, RGL_FIELD_DISTANCE_F32}; }
+	void enqueueImpl(cudaStream_t s) override;
+	const void* fieldDev(rgl_field_t f) override;
+
+private:
+	float mean = 0, base = 0, rise = 0;
+	uint64_t seed = 0, frame = 0;
+	rgl::DeviceBuffer outXyz, outDist;
+};
+
+struct FromArrayPointsNode : PointsNode
+{
+	const char* name() const override { return "FromArrayPointsNode"; }
+	void setParameters(const void* points, size_t count, const std::vector<rgl_field_t>& fields);
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t) override {}
+	bool isDense() const override { return true; }
+	bool hasField(rgl_field_t f) const override { return data.count(f) != 0; }
+	size_t capacity() const override { return count; }
+	const void* fieldDev(rgl_field_t f) override;
+
+private:
+	size_t count = 0;
+	std::map<rgl_field_t, rgl::DeviceBuffer> data;
+};
+
+// ---------------------------------------------------------------- run context
+
+struct GraphRunCtx : std::enable_shared_from_this<GraphRunCtx>
+{
+	static std::shared_ptr<GraphRunCtx> createAndAttach(const Node::Ptr& node);
+	static void synchronizeAll();
+	static std::vector<std::shared_ptr<GraphRunCtx>>& instances();
+
+	~GraphRunCtx();
+	void run();
+	void synchronize();
+	void detachAndDestroy();
+	cudaStream_t stream() const { return stream_; }
+	void invalidateOrder() { order.clear(); }
+
+	std::set<Node::Ptr> nodes;
+	float lastRunMs = 0.0f, lastTraceMs = 0.0f;
+
+private:
+	GraphRunCtx();
+	static std::vector<Node::Ptr> findExecutionOrder(std::set<Node::Ptr> nodes);
+	std::vector<Node::Ptr> order;
+	cudaStream_t stream_ = nullptr;
+	cudaEvent_t done = nullptr, runStart = nullptr, runStop = nullptr;
+	bool running = false;
+};
+
+bool timingEnabled();
+void setTimingEnabled(bool on);

@@ -1,0 +1,97 @@
+// Host-side launchers of the CUDA kernels (defined in the .cu files of this directory).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "device_types.hpp"
+
+namespace rgl {
+
+// Counts kernel launches issued by this library (reported by rgl_gb300_get_kernel_launch_count).
+void countLaunch(uint64_t n = 1);
+uint64_t launchCount();
+
+// ---- sort.cu
+size_t sortPairsScratchBytes(int n, int keyBits);
+void sortPairs(uint32_t* keys, uint32_t* values, int n, int keyBits, void* scratch, int32_t* errorFlag, cudaStream_t stream);
+
+// ---- bvh.cu
+struct BlasBuild
+{
+	WideNode* nodes = nullptr; // device
+	TriRecord* tris = nullptr; // device
+	uint32_t nodeCapacity = 0;
+	int32_t triCount = 0;
+	float bounds[6] = {0, 0, 0, 0, 0, 0}; // object-space box lo.xyz, hi.xyz (host copy)
+};
+// Builds the BLAS of a mesh (device vertices/indices); synchronises `stream` at the end (one-off).
+void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, int nTris, BlasBuild& out, cudaStream_t stream);
+void freeBlas(BlasBuild& b);
+
+struct TlasBuild
+{
+	BinNode* nodes = nullptr;        // nInstances - 1
+	int32_t* parents = nullptr;      // parent of internal node
+	int32_t* leafParents = nullptr;  // parent of instance (by instance index)
+	uint32_t* visits = nullptr;      // bottom-up counters
+	int32_t capacity = 0;
+	int32_t nInstances = 0;
+	void* scratch = nullptr;
+	size_t scratchBytes = 0;
+};
+// (Re)builds the TLAS topology and bounds over `nInstances` device instance records.
+void buildTlas(const InstanceRec* dInstances, int nInstances, TlasBuild& t, int32_t* dError, cudaStream_t stream);
+// Refits TLAS bounds after instance boxes changed (same instance set and order).
+void refitTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);
+void freeTlas(TlasBuild& t);
+
+// ---- trace.cu
+void launchTrace(const TraceParams& p, const Mat34* dSampleTable, cudaStream_t stream);
+
+// ---- points.cu
+void launchTransformRays(const Mat34* in, Mat34* out, int n, Mat34 tf, cudaStream_t s);
+void launchTransformPoints(const float* inXyz, float* outXyz, int cap, const int32_t* dCount, Mat34 tf, cudaStream_t s);
+
+struct NoiseParams
+{
+	uint32_t seedLo, seedHi;
+	uint32_t frameLo, frameHi;
+	uint32_t kind;
+	float mean, stDev, stDevRise;
+	int32_t axis;
+	Mat34 lookAt, lookAtInv;
+};
+void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams& np, cudaStream_t s);
+void launchNoiseAngularHitpoint(const float* inXyz, float* outXyz, float* outDist, int cap, const int32_t* dCount,
+                                const NoiseParams& np, cudaStream_t s);
+void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz, float* outDist, int cap, const int32_t* dCount,
+                         const NoiseParams& np, cudaStream_t s);
+
+// One field of a compaction or format: device source/destination and element size in bytes.
+struct FieldCopy
+{
+	const void* src;
+	void* dst;
+	int32_t size;   // bytes per element
+	int32_t offset; // byte offset inside a formatted point (format only)
+};
+constexpr int kMaxFieldCopies = 32;
+struct FieldCopies
+{
+	FieldCopy f[kMaxFieldCopies];
+	int32_t count;
+};
+
+size_t compactScratchBytes(int cap);
+// Stable compaction of `cap` points (first *dInCount valid when dInCount != null) by int32 flags.
+// Writes the kept count to *dOutCount.
+void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, int32_t* dOutCount,
+                   void* scratch, int32_t* dError, cudaStream_t s);
+// AoS packing: point i, field k -> out + i*pointSize + offset_k; padding fields (src == null) are zeroed.
+void launchFormat(const FieldCopies& fields, int pointSize, int cap, const int32_t* dCount, uint8_t* out, cudaStream_t s);
+// AoS -> SoA split for points given as an array (rgl_node_points_from_array).
+void launchAosToSoa(const uint8_t* in, int pointSize, int n, const FieldCopies& fields, cudaStream_t s);
+
+} // namespace rgl

@@ -1,0 +1,398 @@
+// Point-pipeline kernels: ray/point transforms, Gaussian noise, compaction and formatting.
+//
+// Reference counterparts: kTransformRays / kTransformPoints (src/gpu/nodeKernels.cu:45-56),
+// kAddGaussianNoise* (src/gpu/gaussianNoiseKernels.cu:20-66), gpuFindCompaction + kApplyCompaction
+// (nodeKernels.cu:58-68,424-436: a Thrust scan, a blocking count read-back and one scatter launch per
+// field), kFormatSoaToAos / kFormatAosToSoa (nodeKernels.cu:25-43: byte-wise memcpy per field).
+// Here compaction is one decoupled-look-back pass over all fields with the count left on the device,
+// and formatting writes the packed output word by word (coalesced 4-byte stores).
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+#include "philox.hpp"
+
+namespace rgl {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline int blocks(long n, int b) { return (int) ((n + b - 1) / b); }
+
+__device__ __forceinline__ int countOf(int cap, const int32_t* dCount) { return dCount ? *dCount : cap; }
+
+__device__ __forceinline__ Vec3 loadXyz(const float* p, int i) { return v3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+__device__ __forceinline__ void storeXyz(float* p, int i, Vec3 v)
+{
+	p[3 * i] = v.x;
+	p[3 * i + 1] = v.y;
+	p[3 * i + 2] = v.z;
+}
+
+__device__ __forceinline__ Mat34 loadMat(const Mat34* p)
+{
+	const float4* q = reinterpret_cast<const float4*>(p);
+	float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+	return Mat34{{{a.x, a.y, a.z, a.w}, {b.x, b.y, b.z, b.w}, {c.x, c.y, c.z, c.w}}};
+}
+__device__ __forceinline__ void storeMat(Mat34* p, const Mat34& m)
+{
+	float4* q = reinterpret_cast<float4*>(p);
+	q[0] = make_float4(m.m[0][0], m.m[0][1], m.m[0][2], m.m[0][3]);
+	q[1] = make_float4(m.m[1][0], m.m[1][1], m.m[1][2], m.m[1][3]);
+	q[2] = make_float4(m.m[2][0], m.m[2][1], m.m[2][2], m.m[2][3]);
+}
+
+__global__ void kTransformRays(const Mat34* __restrict__ in, Mat34* __restrict__ out, int n, Mat34 tf)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		storeMat(out + i, mul(tf, loadMat(in + i)));
+	}
+}
+
+__global__ void kTransformPoints(const float* __restrict__ in, float* __restrict__ out, int cap, const int32_t* dCount, Mat34 tf)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < countOf(cap, dCount)) {
+		storeXyz(out, i, tf.point(loadXyz(in, i)));
+	}
+}
+
+__device__ __forceinline__ float noiseNormal(const NoiseParams& np, int i)
+{
+	return standardNormal(np.seedLo, np.seedHi, np.kind, (uint32_t) i, np.frameLo, np.frameHi);
+}
+
+__device__ __forceinline__ Mat34 axisRotation(int axis, float angle)
+{
+	float s, c;
+	sincosf(angle, &s, &c);
+	return rotationAxis(axis, c, s);
+}
+
+__global__ void kNoiseAngularRay(const Mat34* __restrict__ in, Mat34* __restrict__ out, int n, NoiseParams np)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		float angle = np.mean + noiseNormal(np, i) * np.stDev;
+		Mat34 r = mul(np.lookAtInv, mul(axisRotation(np.axis, angle), mul(np.lookAt, loadMat(in + i))));
+		storeMat(out + i, r);
+	}
+}
+
+__global__ void kNoiseAngularHitpoint(const float* __restrict__ inXyz, float* __restrict__ outXyz, float* __restrict__ outDist,
+                                      int cap, const int32_t* dCount, NoiseParams np)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < countOf(cap, dCount)) {
+		float angle = np.mean + noiseNormal(np, i) * np.stDev;
+		Vec3 q = axisRotation(np.axis, angle).point(np.lookAt.point(loadXyz(inXyz, i)));
+		if (outDist) {
+			outDist[i] = length(q);
+		}
+		storeXyz(outXyz, i, np.lookAtInv.point(q));
+	}
+}
+
+__global__ void kNoiseDistance(const float* __restrict__ inXyz, const float* __restrict__ inDist, float* __restrict__ outXyz,
+                               float* __restrict__ outDist, int cap, const int32_t* dCount, NoiseParams np)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < countOf(cap, dCount)) {
+		float d = inDist[i];
+		float sigma = d * np.stDevRise + np.stDev; // stDev holds the base deviation for distance noise
+		float e = np.mean + noiseNormal(np, i) * sigma;
+		Vec3 pl = np.lookAt.point(loadXyz(inXyz, i));
+		Vec3 moved = pl + normalized(pl) * e;
+		storeXyz(outXyz, i, np.lookAtInv.point(moved));
+		outDist[i] = d + e;
+	}
+}
+
+// ---------------------------------------------------------------- compaction
+
+constexpr int kCompactItems = 4;
+constexpr int kCompactTile = kBlock * kCompactItems;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr int kSpinLimit = 1 << 24;
+
+__device__ __forceinline__ void copyElem(const uint8_t* src, uint8_t* dst, int size)
+{
+	switch (size) {
+		case 4: *reinterpret_cast<uint32_t*>(dst) = *reinterpret_cast<const uint32_t*>(src); break;
+		case 12: {
+			const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+			uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+			d[0] = s[0];
+			d[1] = s[1];
+			d[2] = s[2];
+			break;
+		}
+		case 1: *dst = *src; break;
+		case 2: *reinterpret_cast<uint16_t*>(dst) = *reinterpret_cast<const uint16_t*>(src); break;
+		case 8: *reinterpret_cast<uint2*>(dst) = *reinterpret_cast<const uint2*>(src); break;
+		default:
+			for (int b = 0; b < size; ++b) {
+				dst[b] = src[b];
+			}
+	}
+}
+
+// One pass: per-tile flag counts, decoupled look-back for the tile offset, scatter of every field.
+// scratch: [0] tile ticket, [1..tiles] tile status words (zeroed before the launch).
+__global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ flags, int cap, const int32_t* dInCount,
+                                                   FieldCopies fc, int32_t* dOutCount, uint32_t* scratch, int32_t* errorFlag)
+{
+	__shared__ uint32_t warpSums[kBlock / 32];
+	__shared__ uint32_t tileBase;
+	__shared__ int tileShared;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	if (tid == 0) {
+		tileShared = (int) atomicAdd(scratch, 1u);
+	}
+	__syncthreads();
+	const int tile = tileShared;
+	const int n = dInCount ? *dInCount : cap;
+	const int first = tile * kCompactTile + tid * kCompactItems;
+	int keep[kCompactItems];
+	int cnt = 0;
+#pragma unroll
+	for (int k = 0; k < kCompactItems; ++k) {
+		int i = first + k;
+		keep[k] = (i < n) && flags[i] != 0;
+		cnt += keep[k];
+	}
+	// block exclusive scan of cnt
+	int incl = cnt;
+#pragma unroll
+	for (int off = 1; off < 32; off <<= 1) {
+		int v = __shfl_up_sync(0xffffffffu, incl, off);
+		if (lane >= off) {
+			incl += v;
+		}
+	}
+	if (lane == 31) {
+		warpSums[warp] = (uint32_t) incl;
+	}
+	__syncthreads();
+	if (tid == 0) {
+		uint32_t run = 0;
+		for (int w = 0; w < kBlock / 32; ++w) {
+			uint32_t v = warpSums[w];
+			warpSums[w] = run;
+			run += v;
+		}
+		uint32_t* status = scratch + 1;
+		uint32_t prefix = 0;
+		if (tile == 0) {
+			atomicExch(&status[0], kFlagInc | run);
+		} else {
+			atomicExch(&status[tile], kFlagAgg | run);
+			int k = tile - 1, spins = 0;
+			while (k >= 0) {
+				uint32_t s = *((volatile uint32_t*) &status[k]);
+				uint32_t fl = s & ~kValueMask;
+				if (fl == 0u) {
+					if (++spins > kSpinLimit) {
+						atomicExch(errorFlag, 1);
+						break;
+					}
+					continue;
+				}
+				prefix += s & kValueMask;
+				if (fl == kFlagInc) {
+					break;
+				}
+				--k;
+			}
+			atomicExch(&status[tile], kFlagInc | (prefix + run));
+		}
+		tileBase = prefix;
+		const int tiles = (cap + kCompactTile - 1) / kCompactTile;
+		if (tile == tiles - 1) {
+			*dOutCount = (int32_t) (prefix + run);
+		}
+	}
+	__syncthreads();
+	uint32_t pos = tileBase + warpSums[warp] + (uint32_t) (incl - cnt);
+#pragma unroll
+	for (int k = 0; k < kCompactItems; ++k) {
+		if (keep[k]) {
+			const int i = first + k;
+			for (int f = 0; f < fc.count; ++f) {
+				const int sz = fc.f[f].size;
+				copyElem(static_cast<const uint8_t*>(fc.f[f].src) + (size_t) i * sz, static_cast<uint8_t*>(fc.f[f].dst) + (size_t) pos * sz,
+				         sz);
+			}
+			++pos;
+		}
+	}
+}
+
+// ---------------------------------------------------------------- format
+
+struct WordMap
+{
+	int8_t field[64];  // field index of output word k, -1 = padding
+	int8_t word[64];   // word index inside that field
+};
+
+// Word-aligned layouts: one thread per output 32-bit word, coalesced stores.
+__global__ void kFormatWords(FieldCopies fc, WordMap wm, int pointWords, int cap, const int32_t* dCount, uint32_t* __restrict__ out)
+{
+	long w = (long) blockIdx.x * blockDim.x + threadIdx.x;
+	long n = countOf(cap, dCount);
+	if (w >= n * pointWords) {
+		return;
+	}
+	int i = (int) (w / pointWords);
+	int k = (int) (w - (long) i * pointWords);
+	int f = wm.field[k];
+	uint32_t v = 0;
+	if (f >= 0) {
+		const int fw = fc.f[f].size >> 2;
+		v = static_cast<const uint32_t*>(fc.f[f].src)[(size_t) i * fw + wm.word[k]];
+	}
+	out[w] = v;
+}
+
+// Any layout: one thread per point, byte copies (padding bytes zeroed).
+__global__ void kFormatBytes(FieldCopies fc, int pointSize, int cap, const int32_t* dCount, uint8_t* __restrict__ out)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= countOf(cap, dCount)) {
+		return;
+	}
+	for (int f = 0; f < fc.count; ++f) {
+		const int sz = fc.f[f].size;
+		uint8_t* d = out + (size_t) i * pointSize + fc.f[f].offset;
+		const uint8_t* s = static_cast<const uint8_t*>(fc.f[f].src);
+		for (int b = 0; b < sz; ++b) {
+			d[b] = s ? s[(size_t) i * sz + b] : 0;
+		}
+	}
+}
+
+__global__ void kAosToSoa(const uint8_t* __restrict__ in, int pointSize, int n, FieldCopies fc)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) {
+		return;
+	}
+	for (int f = 0; f < fc.count; ++f) {
+		if (fc.f[f].dst == nullptr) {
+			continue;
+		}
+		const int sz = fc.f[f].size;
+		const uint8_t* s = in + (size_t) i * pointSize + fc.f[f].offset;
+		uint8_t* d = static_cast<uint8_t*>(fc.f[f].dst) + (size_t) i * sz;
+		for (int b = 0; b < sz; ++b) {
+			d[b] = s[b];
+		}
+	}
+}
+
+} // namespace
+
+void launchTransformRays(const Mat34* in, Mat34* out, int n, Mat34 tf, cudaStream_t s)
+{
+	if (n > 0) {
+		kTransformRays<<<blocks(n, kBlock), kBlock, 0, s>>>(in, out, n, tf);
+		countLaunch();
+	}
+}
+
+void launchTransformPoints(const float* in, float* out, int cap, const int32_t* dCount, Mat34 tf, cudaStream_t s)
+{
+	if (cap > 0) {
+		kTransformPoints<<<blocks(cap, kBlock), kBlock, 0, s>>>(in, out, cap, dCount, tf);
+		countLaunch();
+	}
+}
+
+void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams& np, cudaStream_t s)
+{
+	if (n > 0) {
+		kNoiseAngularRay<<<blocks(n, kBlock), kBlock, 0, s>>>(in, out, n, np);
+		countLaunch();
+	}
+}
+
+void launchNoiseAngularHitpoint(const float* inXyz, float* outXyz, float* outDist, int cap, const int32_t* dCount,
+                                const NoiseParams& np, cudaStream_t s)
+{
+	if (cap > 0) {
+		kNoiseAngularHitpoint<<<blocks(cap, kBlock), kBlock, 0, s>>>(inXyz, outXyz, outDist, cap, dCount, np);
+		countLaunch();
+	}
+}
+
+void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz, float* outDist, int cap, const int32_t* dCount,
+                         const NoiseParams& np, cudaStream_t s)
+{
+	if (cap > 0) {
+		kNoiseDistance<<<blocks(cap, kBlock), kBlock, 0, s>>>(inXyz, inDist, outXyz, outDist, cap, dCount, np);
+		countLaunch();
+	}
+}
+
+size_t compactScratchBytes(int cap) { return sizeof(uint32_t) * (size_t) (1 + (cap + kCompactTile - 1) / kCompactTile); }
+
+void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, int32_t* dOutCount,
+                   void* scratch, int32_t* dError, cudaStream_t s)
+{
+	if (cap <= 0) {
+		cudaMemsetAsync(dOutCount, 0, sizeof(int32_t), s);
+		return;
+	}
+	cudaMemsetAsync(scratch, 0, compactScratchBytes(cap), s);
+	int tiles = (cap + kCompactTile - 1) / kCompactTile;
+	kCompact<<<tiles, kBlock, 0, s>>>(flags, cap, dInCount, fields, dOutCount, static_cast<uint32_t*>(scratch), dError);
+	countLaunch();
+}
+
+void launchFormat(const FieldCopies& fields, int pointSize, int cap, const int32_t* dCount, uint8_t* out, cudaStream_t s)
+{
+	if (cap <= 0 || pointSize <= 0) {
+		return;
+	}
+	bool words = (pointSize % 4 == 0) && pointSize / 4 <= 64;
+	for (int f = 0; f < fields.count && words; ++f) {
+		words = (fields.f[f].size % 4 == 0) && (fields.f[f].offset % 4 == 0);
+	}
+	if (words) {
+		WordMap wm;
+		for (int k = 0; k < 64; ++k) {
+			wm.field[k] = -1;
+			wm.word[k] = 0;
+		}
+		for (int f = 0; f < fields.count; ++f) {
+			if (fields.f[f].src == nullptr) {
+				continue;
+			}
+			for (int k = 0; k < fields.f[f].size / 4; ++k) {
+				wm.field[fields.f[f].offset / 4 + k] = (int8_t) f;
+				wm.word[fields.f[f].offset / 4 + k] = (int8_t) k;
+			}
+		}
+		int pw = pointSize / 4;
+		long total = (long) cap * pw;
+		kFormatWords<<<blocks(total, kBlock), kBlock, 0, s>>>(fields, wm, pw, cap, dCount, reinterpret_cast<uint32_t*>(out));
+	} else {
+		kFormatBytes<<<blocks(cap, kBlock), kBlock, 0, s>>>(fields, pointSize, cap, dCount, out);
+	}
+	countLaunch();
+}
+
+void launchAosToSoa(const uint8_t* in, int pointSize, int n, const FieldCopies& fields, cudaStream_t s)
+{
+	if (n > 0) {
+		kAosToSoa<<<blocks(n, kBlock), kBlock, 0, s>>>(in, pointSize, n, fields);
+		countLaunch();
+	}
+}
+
+} // namespace rgl

@@ -1,0 +1,84 @@
+// Scene objects behind rgl_mesh_t / rgl_entity_t (reference src/scene/Mesh.cpp, Entity.cpp, Scene.cpp).
+//
+// A Mesh owns its device vertices/indices and, once a raytrace needs it, its BLAS (shared by every
+// entity of the mesh). A Scene owns the per-entity instance records and the TLAS. Pose and id changes
+// only mark the scene; the next raytrace refits the TLAS (same entity set) or rebuilds it (entities
+// added or removed) on its own stream, without blocking the host.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "common.hpp"
+#include "kernels.hpp"
+
+struct Scene;
+
+struct Mesh
+{
+	Mesh(const rgl_vec3f* vertices, int32_t vertexCount, const rgl_vec3i* indices, int32_t indexCount);
+	~Mesh();
+	void ensureBlas(cudaStream_t s);
+
+	int32_t vertexCount = 0;
+	int32_t triangleCount = 0;
+	rgl::DeviceBuffer dVertices;
+	rgl::DeviceBuffer dIndices;
+	rgl::BlasBuild blas;
+	bool blasBuilt = false;
+};
+
+struct Entity
+{
+	Entity(std::shared_ptr<Mesh> m, Scene* s);
+	void setTransform(const rgl::Mat34& tf);
+	void setId(int32_t id);
+
+	std::shared_ptr<Mesh> mesh;
+	Scene* scene;
+	rgl::Mat34 transform = rgl::Mat34::identity();
+	int32_t id = RGL_DEFAULT_ENTITY_ID;
+	float laserRetro = 0.0f;
+};
+
+struct Texture
+{
+};
+
+struct Scene
+{
+	static Scene& defaultScene();
+	Scene();
+	~Scene();
+
+	void addEntity(const std::shared_ptr<Entity>& e);
+	void removeEntity(Entity* e);
+	void clear();
+	void markPosesDirty() { posesDirty = true; }
+
+	// Builds/refits what changed on stream `s`; afterwards `s` may read view().
+	void prepare(cudaStream_t s);
+	const rgl::SceneView* view() const { return dView.as<rgl::SceneView>(); }
+	size_t entityCount() const { return entities.size(); }
+	int32_t* errorFlag() const { return dError.as<int32_t>(); }
+	void checkDeviceErrors();
+
+	uint64_t timeNs = 0;
+	bool timeSet = false;
+
+	// Statistics for the extension API.
+	uint64_t tlasBuilds = 0, tlasRefits = 0;
+
+private:
+	std::vector<std::shared_ptr<Entity>> entities;
+	bool topologyDirty = true;
+	bool posesDirty = true;
+	rgl::DeviceBuffer dInstances;
+	rgl::PinnedBuffer hInstances;
+	rgl::DeviceBuffer dView;
+	rgl::PinnedBuffer hView;
+	rgl::DeviceBuffer dError;
+	rgl::TlasBuild tlas;
+	cudaEvent_t ready = nullptr;
+	bool readyRecorded = false;
+};

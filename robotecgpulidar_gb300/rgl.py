@@ -1,0 +1,383 @@
+"""Python mirror of the RGL C API exported by libRobotecGPULidar.so (this project's build).
+
+Function names, argument meaning, enum values and status codes are those of RobotecGPULidar's
+include/rgl/api/core.h; every call goes through the C ABI with ctypes, so tests written with this
+module exercise exactly what an engine plugin links against.  ``check()`` turns a non-success status
+into ``RGLError`` carrying the library's last error string.
+
+The library is loaded lazily from ``robotecgpulidar_gb300/_build`` (built by ``build.build()``); a
+missing library raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+# ---- status codes
+RGL_SUCCESS = 0
+RGL_INVALID_ARGUMENT = 1
+RGL_INVALID_STATE = 2
+RGL_LOGGING_ERROR = 3
+RGL_INVALID_API_OBJECT = 4
+RGL_INVALID_FILE_PATH = 5
+RGL_TAPE_ERROR = 6
+RGL_UDP_ERROR = 7
+RGL_ROS2_ERROR = 8
+RGL_INVALID_PIPELINE = 9
+RGL_INITIALIZATION_ERROR = 10
+RGL_NOT_IMPLEMENTED = 404
+RGL_INTERNAL_EXCEPTION = 500
+
+# ---- fields
+RGL_FIELD_XYZ_VEC3_F32 = 1
+RGL_FIELD_INTENSITY_F32 = 2
+RGL_FIELD_INTENSITY_U8 = 3
+RGL_FIELD_IS_HIT_I32 = 4
+RGL_FIELD_IS_GROUND_I32 = 5
+RGL_FIELD_RAY_IDX_U32 = 6
+RGL_FIELD_ENTITY_ID_I32 = 7
+RGL_FIELD_DISTANCE_F32 = 8
+RGL_FIELD_AZIMUTH_F32 = 9
+RGL_FIELD_ELEVATION_F32 = 10
+RGL_FIELD_RING_ID_U16 = 11
+RGL_FIELD_RETURN_TYPE_U8 = 12
+RGL_FIELD_TIME_STAMP_F64 = 13
+RGL_FIELD_TIME_STAMP_U32 = 14
+RGL_FIELD_ABSOLUTE_VELOCITY_VEC3_F32 = 15
+RGL_FIELD_RELATIVE_VELOCITY_VEC3_F32 = 16
+RGL_FIELD_RADIAL_SPEED_F32 = 17
+RGL_FIELD_POWER_F32 = 18
+RGL_FIELD_RCS_F32 = 19
+RGL_FIELD_NOISE_F32 = 20
+RGL_FIELD_SNR_F32 = 21
+RGL_FIELD_NORMAL_VEC3_F32 = 22
+RGL_FIELD_INCIDENT_ANGLE_F32 = 23
+RGL_FIELD_RAY_POSE_MAT3x4_F32 = 24
+RGL_FIELD_LASER_RETRO_F32 = 25
+RGL_FIELD_PADDING_8 = 1024
+RGL_FIELD_PADDING_16 = 1025
+RGL_FIELD_PADDING_32 = 1026
+RGL_FIELD_DYNAMIC_FORMAT = 13842
+
+FIELD_SIZE = {
+    RGL_FIELD_XYZ_VEC3_F32: 12, RGL_FIELD_INTENSITY_F32: 4, RGL_FIELD_INTENSITY_U8: 1, RGL_FIELD_IS_HIT_I32: 4,
+    RGL_FIELD_IS_GROUND_I32: 4, RGL_FIELD_RAY_IDX_U32: 4, RGL_FIELD_ENTITY_ID_I32: 4, RGL_FIELD_DISTANCE_F32: 4,
+    RGL_FIELD_AZIMUTH_F32: 4, RGL_FIELD_ELEVATION_F32: 4, RGL_FIELD_RING_ID_U16: 2, RGL_FIELD_RETURN_TYPE_U8: 1,
+    RGL_FIELD_TIME_STAMP_F64: 8, RGL_FIELD_TIME_STAMP_U32: 4, RGL_FIELD_ABSOLUTE_VELOCITY_VEC3_F32: 12,
+    RGL_FIELD_RELATIVE_VELOCITY_VEC3_F32: 12, RGL_FIELD_RADIAL_SPEED_F32: 4, RGL_FIELD_POWER_F32: 4,
+    RGL_FIELD_RCS_F32: 4, RGL_FIELD_NOISE_F32: 4, RGL_FIELD_SNR_F32: 4, RGL_FIELD_NORMAL_VEC3_F32: 12,
+    RGL_FIELD_INCIDENT_ANGLE_F32: 4, RGL_FIELD_RAY_POSE_MAT3x4_F32: 48, RGL_FIELD_LASER_RETRO_F32: 4,
+    RGL_FIELD_PADDING_8: 1, RGL_FIELD_PADDING_16: 2, RGL_FIELD_PADDING_32: 4,
+}
+
+FIELD_DTYPE = {
+    RGL_FIELD_XYZ_VEC3_F32: (np.float32, 3), RGL_FIELD_INTENSITY_F32: (np.float32, 1),
+    RGL_FIELD_INTENSITY_U8: (np.uint8, 1), RGL_FIELD_IS_HIT_I32: (np.int32, 1), RGL_FIELD_IS_GROUND_I32: (np.int32, 1),
+    RGL_FIELD_RAY_IDX_U32: (np.uint32, 1), RGL_FIELD_ENTITY_ID_I32: (np.int32, 1),
+    RGL_FIELD_DISTANCE_F32: (np.float32, 1), RGL_FIELD_RETURN_TYPE_U8: (np.uint8, 1),
+    RGL_FIELD_NORMAL_VEC3_F32: (np.float32, 3), RGL_FIELD_INCIDENT_ANGLE_F32: (np.float32, 1),
+    RGL_FIELD_LASER_RETRO_F32: (np.float32, 1), RGL_FIELD_RING_ID_U16: (np.uint16, 1),
+    RGL_FIELD_TIME_STAMP_F64: (np.float64, 1), RGL_FIELD_TIME_STAMP_U32: (np.uint32, 1),
+    RGL_FIELD_AZIMUTH_F32: (np.float32, 1), RGL_FIELD_ELEVATION_F32: (np.float32, 1),
+    RGL_FIELD_RAY_POSE_MAT3x4_F32: (np.float32, 12),
+}
+
+# ---- return modes
+RGL_RETURN_TYPE_UNKNOWN = 0
+RGL_RETURN_TYPE_STRONGEST = 1
+RGL_RETURN_TYPE_LAST = 2
+RGL_RETURN_TYPE_SECOND = 3
+RGL_RETURN_TYPE_FIRST = 4
+RGL_RETURN_TYPE_SECOND_STRONGEST = 5
+_S = 1 << 24
+_D = 2 << 24
+RGL_RETURN_UNKNOWN = 0
+RGL_RETURN_FIRST = _S | RGL_RETURN_TYPE_FIRST
+RGL_RETURN_SECOND = _S | RGL_RETURN_TYPE_SECOND
+RGL_RETURN_LAST = _S | RGL_RETURN_TYPE_LAST
+RGL_RETURN_STRONGEST = _S | RGL_RETURN_TYPE_STRONGEST
+RGL_RETURN_LAST_STRONGEST = _D | RGL_RETURN_TYPE_LAST | (RGL_RETURN_TYPE_STRONGEST << 8)
+RGL_RETURN_FIRST_LAST = _D | RGL_RETURN_TYPE_FIRST | (RGL_RETURN_TYPE_LAST << 8)
+RGL_RETURN_FIRST_STRONGEST = _D | RGL_RETURN_TYPE_FIRST | (RGL_RETURN_TYPE_STRONGEST << 8)
+RGL_RETURN_STRONGEST_SECOND_STRONGEST = _D | RGL_RETURN_TYPE_STRONGEST | (RGL_RETURN_TYPE_SECOND_STRONGEST << 8)
+RGL_RETURN_FIRST_SECOND = _D | RGL_RETURN_TYPE_FIRST | (RGL_RETURN_TYPE_SECOND << 8)
+
+RGL_AXIS_X, RGL_AXIS_Y, RGL_AXIS_Z = 1, 2, 3
+RGL_ENTITY_INVALID_ID = 0
+RGL_DEFAULT_ENTITY_ID = 268435455
+RGL_LOG_LEVEL_OFF = 6
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build")
+LIB_PATH = os.path.join(LIB_DIR, "libRobotecGPULidar.so")
+
+_lib = None
+
+
+class RGLError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"RGL status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+def _proto(l):
+    vp, i32, f, u64 = C.c_void_p, C.c_int32, C.c_float, C.c_uint64
+    P = C.POINTER
+    sigs = {
+        "rgl_get_version_info": [P(i32), P(i32), P(i32)],
+        "rgl_get_extension_info": [i32, P(i32)],
+        "rgl_configure_logging": [i32, C.c_char_p, C.c_bool],
+        "rgl_cleanup": [],
+        "rgl_mesh_create": [P(vp), vp, i32, vp, i32],
+        "rgl_mesh_destroy": [vp],
+        "rgl_mesh_is_alive": [vp, P(C.c_bool)],
+        "rgl_mesh_set_texture_coords": [vp, vp, i32],
+        "rgl_entity_create": [P(vp), vp, vp],
+        "rgl_entity_destroy": [vp],
+        "rgl_entity_set_transform": [vp, vp],
+        "rgl_entity_set_id": [vp, i32],
+        "rgl_entity_set_laser_retro": [vp, f],
+        "rgl_entity_is_alive": [vp, P(C.c_bool)],
+        "rgl_scene_set_time": [vp, u64],
+        "rgl_node_rays_from_mat3x4f": [P(vp), vp, i32],
+        "rgl_node_rays_set_range": [P(vp), vp, i32],
+        "rgl_node_rays_set_ring_ids": [P(vp), vp, i32],
+        "rgl_node_rays_set_time_offsets": [P(vp), vp, i32],
+        "rgl_node_rays_transform": [P(vp), vp],
+        "rgl_node_points_transform": [P(vp), vp],
+        "rgl_node_raytrace": [P(vp), vp],
+        "rgl_node_raytrace_configure_velocity": [vp, vp, vp],
+        "rgl_node_raytrace_configure_distortion": [vp, C.c_bool],
+        "rgl_node_raytrace_configure_non_hits": [vp, f, f],
+        "rgl_node_raytrace_configure_mask": [vp, vp, i32],
+        "rgl_node_raytrace_configure_beam_divergence": [vp, f, f],
+        "rgl_node_raytrace_configure_default_intensity": [vp, f],
+        "rgl_node_raytrace_configure_return_mode": [vp, i32],
+        "rgl_node_points_format": [P(vp), vp, i32],
+        "rgl_node_points_yield": [P(vp), vp, i32],
+        "rgl_node_points_compact_by_field": [P(vp), i32],
+        "rgl_node_points_spatial_merge": [P(vp), vp, i32],
+        "rgl_node_points_temporal_merge": [P(vp), vp, i32],
+        "rgl_node_points_from_array": [P(vp), vp, i32, vp, i32],
+        "rgl_node_points_filter_ground": [P(vp), vp, f],
+        "rgl_node_gaussian_noise_angular_ray": [P(vp), f, f, i32],
+        "rgl_node_gaussian_noise_angular_hitpoint": [P(vp), f, f, i32],
+        "rgl_node_gaussian_noise_distance": [P(vp), f, f, f],
+        "rgl_node_is_alive": [vp, P(C.c_bool)],
+        "rgl_graph_run": [vp],
+        "rgl_graph_destroy": [vp],
+        "rgl_graph_get_result_size": [vp, i32, P(i32), P(i32)],
+        "rgl_graph_get_result_data": [vp, i32, vp],
+        "rgl_graph_node_add_child": [vp, vp],
+        "rgl_graph_node_remove_child": [vp, vp],
+        "rgl_graph_node_set_priority": [vp, i32],
+        "rgl_graph_node_get_priority": [vp, P(i32)],
+        # GB300 extensions (include/rgl/api/extensions/gb300.h)
+        "rgl_gb300_node_gaussian_noise_set_seed": [vp, u64, u64],
+        "rgl_gb300_node_raytrace_configure_beam_samples": [vp, i32, i32],
+        "rgl_gb300_configure_timing": [C.c_bool],
+        "rgl_gb300_graph_get_timing": [vp, P(f), P(f)],
+        "rgl_gb300_get_kernel_launch_count": [P(u64)],
+        "rgl_gb300_graph_sync": [vp],
+        "rgl_gb300_device_info": [P(i32), P(i32)],
+    }
+    for name, args in sigs.items():
+        fn = getattr(l, name)
+        fn.argtypes = args
+        fn.restype = C.c_int32
+    l.rgl_get_last_error_string.argtypes = [C.POINTER(C.c_char_p)]
+    l.rgl_get_last_error_string.restype = None
+
+
+def lib():
+    """Load libRobotecGPULidar.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libRobotecGPULidar.so not built ({LIB_PATH}); run __graft_entry__.build()")
+        l = C.CDLL(LIB_PATH)
+        _proto(l)
+        _lib = l
+    return _lib
+
+
+def last_error() -> str:
+    s = C.c_char_p()
+    lib().rgl_get_last_error_string(C.byref(s))
+    return (s.value or b"").decode()
+
+
+def check(status: int):
+    if status != RGL_SUCCESS:
+        raise RGLError(status, last_error())
+    return status
+
+
+def call(name: str, *args) -> int:
+    """Call an API function by name; returns the raw status (no check)."""
+    return getattr(lib(), name)(*args)
+
+
+def node() -> C.c_void_p:
+    return C.c_void_p(None)
+
+
+def ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def mat(m) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(m, dtype=np.float32).reshape(3, 4))
+
+
+# ---------------------------------------------------------------- convenience wrappers
+
+def mesh_create(vertices, indices) -> C.c_void_p:
+    v = np.ascontiguousarray(vertices, dtype=np.float32)
+    i = np.ascontiguousarray(indices, dtype=np.int32)
+    h = C.c_void_p()
+    check(lib().rgl_mesh_create(C.byref(h), ptr(v), v.shape[0], ptr(i), i.shape[0]))
+    return h
+
+
+def entity_create(mesh) -> C.c_void_p:
+    h = C.c_void_p()
+    check(lib().rgl_entity_create(C.byref(h), None, mesh))
+    return h
+
+
+def entity_set_transform(entity, tf):
+    m = mat(tf)
+    check(lib().rgl_entity_set_transform(entity, ptr(m)))
+
+
+def entity_set_id(entity, eid: int):
+    check(lib().rgl_entity_set_id(entity, int(eid)))
+
+
+def spawn_scene(scene):
+    """Creates meshes and entities of a scenes.Scene; returns (meshes, entities)."""
+    meshes = [mesh_create(m.vertices, m.indices) for m in scene.meshes]
+    ents = []
+    for e in scene.entities:
+        h = entity_create(meshes[e.mesh])
+        entity_set_transform(h, e.transform)
+        entity_set_id(h, e.entity_id)
+        ents.append(h)
+    return meshes, ents
+
+
+def rays_from_mat3x4f(node_ref, rays):
+    r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 12)
+    check(lib().rgl_node_rays_from_mat3x4f(C.byref(node_ref), ptr(r), r.shape[0]))
+    return node_ref
+
+
+def rays_set_range(node_ref, ranges):
+    r = np.ascontiguousarray(ranges, dtype=np.float32).reshape(-1, 2)
+    check(lib().rgl_node_rays_set_range(C.byref(node_ref), ptr(r), r.shape[0]))
+    return node_ref
+
+
+def rays_transform(node_ref, tf):
+    m = mat(tf)
+    check(lib().rgl_node_rays_transform(C.byref(node_ref), ptr(m)))
+    return node_ref
+
+
+def points_transform(node_ref, tf):
+    m = mat(tf)
+    check(lib().rgl_node_points_transform(C.byref(node_ref), ptr(m)))
+    return node_ref
+
+
+def raytrace(node_ref):
+    check(lib().rgl_node_raytrace(C.byref(node_ref), None))
+    return node_ref
+
+
+def _fields(fields):
+    return np.ascontiguousarray(np.asarray(fields, dtype=np.int32))
+
+
+def points_yield(node_ref, fields):
+    f = _fields(fields)
+    check(lib().rgl_node_points_yield(C.byref(node_ref), ptr(f), f.shape[0]))
+    return node_ref
+
+
+def points_format(node_ref, fields):
+    f = _fields(fields)
+    check(lib().rgl_node_points_format(C.byref(node_ref), ptr(f), f.shape[0]))
+    return node_ref
+
+
+def points_compact_by_field(node_ref, field=RGL_FIELD_IS_HIT_I32):
+    check(lib().rgl_node_points_compact_by_field(C.byref(node_ref), field))
+    return node_ref
+
+
+def points_from_array(node_ref, data: np.ndarray, count: int, fields):
+    f = _fields(fields)
+    d = np.ascontiguousarray(data)
+    check(lib().rgl_node_points_from_array(C.byref(node_ref), ptr(d), count, ptr(f), f.shape[0]))
+    return node_ref
+
+
+def add_child(parent, child):
+    check(lib().rgl_graph_node_add_child(parent, child))
+
+
+def chain(*nodes):
+    for a, b in zip(nodes[:-1], nodes[1:]):
+        add_child(a, b)
+
+
+def graph_run(n):
+    check(lib().rgl_graph_run(n))
+
+
+def result_size(n, field):
+    cnt, sz = C.c_int32(), C.c_int32()
+    check(lib().rgl_graph_get_result_size(n, field, C.byref(cnt), C.byref(sz)))
+    return cnt.value, sz.value
+
+
+def result(n, field) -> np.ndarray:
+    cnt, sz = result_size(n, field)
+    if field in FIELD_DTYPE:
+        dt, k = FIELD_DTYPE[field]
+        out = np.zeros((cnt, k) if k > 1 else cnt, dtype=dt)
+    else:
+        out = np.zeros(cnt * sz, dtype=np.uint8)
+    if cnt > 0:
+        check(lib().rgl_graph_get_result_data(n, field, ptr(out)))
+    return out
+
+
+def result_bytes(n, field) -> np.ndarray:
+    cnt, sz = result_size(n, field)
+    out = np.zeros(cnt * sz, dtype=np.uint8)
+    if cnt > 0:
+        check(lib().rgl_graph_get_result_data(n, field, ptr(out)))
+    return out
+
+
+def cleanup():
+    check(lib().rgl_cleanup())
+
+
+def set_noise_seed(n, seed: int, frame: int = 0):
+    check(lib().rgl_gb300_node_gaussian_noise_set_seed(n, seed, frame))
+
+
+def configure_beam_samples(n, layers: int, vertices: int):
+    check(lib().rgl_gb300_node_raytrace_configure_beam_samples(n, layers, vertices))
+
+
+def kernel_launch_count() -> int:
+    v = C.c_uint64()
+    check(lib().rgl_gb300_get_kernel_launch_count(C.byref(v)))
+    return v.value

@@ -1,0 +1,249 @@
+// CPU harness of the test-suite: runs the library's BVH build steps (bvh_core.hpp) and closest-hit
+// traversal (trace_core.hpp) serially on the host, so their logic can be checked against the oracle
+// without a GPU. The CUDA kernels wrap exactly these functions.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "bvh_core.hpp"
+#include "trace_core.hpp"
+
+using namespace rgl;
+
+namespace {
+
+struct Blas
+{
+	std::vector<WideNode> wide;
+	std::vector<TriRecord> tris;
+	Box bounds;
+};
+
+void buildLbvh(const std::vector<uint32_t>& codes, std::vector<BinNode>& bin, std::vector<int32_t>& rf, std::vector<int32_t>& rl,
+               std::vector<int32_t>& parentInt, std::vector<int32_t>& parentLeaf)
+{
+	int n = (int) codes.size();
+	bin.assign(std::max(0, n - 1), BinNode{});
+	rf.assign(std::max(0, n - 1), 0);
+	rl.assign(std::max(0, n - 1), 0);
+	parentInt.assign(std::max(0, n - 1), -1);
+	parentLeaf.assign(n, -1);
+	for (int i = 0; i < n - 1; ++i) {
+		int32_t l, r, f, la;
+		lbvhInternal(i, codes.data(), n, l, r, f, la);
+		bin[i].left = l;
+		bin[i].right = r;
+		rf[i] = f;
+		rl[i] = la;
+		if (l >= 0)
+			parentInt[l] = i;
+		else
+			parentLeaf[~l] = i;
+		if (r >= 0)
+			parentInt[r] = i;
+		else
+			parentLeaf[~r] = i;
+	}
+}
+
+void bottomUp(std::vector<BinNode>& bin, const std::vector<int32_t>& parentInt, const std::vector<int32_t>& parentLeaf,
+              const std::vector<Box>& leafBox)
+{
+	int n = (int) leafBox.size();
+	std::vector<int> visits(bin.size(), 0);
+	for (int k = 0; k < n; ++k) {
+		int node = parentLeaf[k];
+		while (node >= 0) {
+			if (visits[node]++ == 0)
+				break;
+			Box a = bin[node].left >= 0 ? binBox(bin[bin[node].left]) : leafBox[~bin[node].left];
+			Box b = bin[node].right >= 0 ? binBox(bin[bin[node].right]) : leafBox[~bin[node].right];
+			Box u = unite(a, b);
+			bin[node].lox = u.lox;
+			bin[node].loy = u.loy;
+			bin[node].loz = u.loz;
+			bin[node].hix = u.hix;
+			bin[node].hiy = u.hiy;
+			bin[node].hiz = u.hiz;
+			node = parentInt[node];
+		}
+	}
+}
+
+Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
+{
+	(void) nv;
+	std::vector<float4> lo(nt), hi(nt);
+	Box cb = emptyBox();
+	std::vector<float> cx(nt), cy(nt), cz(nt);
+	for (int t = 0; t < nt; ++t) {
+		const float* a = v + 3 * idx[3 * t];
+		const float* b = v + 3 * idx[3 * t + 1];
+		const float* c = v + 3 * idx[3 * t + 2];
+		lo[t] = make_float4(std::min({a[0], b[0], c[0]}), std::min({a[1], b[1], c[1]}), std::min({a[2], b[2], c[2]}), 0);
+		hi[t] = make_float4(std::max({a[0], b[0], c[0]}), std::max({a[1], b[1], c[1]}), std::max({a[2], b[2], c[2]}), 0);
+		cx[t] = 0.5f * (lo[t].x + hi[t].x);
+		cy[t] = 0.5f * (lo[t].y + hi[t].y);
+		cz[t] = 0.5f * (lo[t].z + hi[t].z);
+		cb = unite(cb, Box{cx[t], cy[t], cz[t], cx[t], cy[t], cz[t]});
+	}
+	std::vector<uint32_t> code(nt);
+	std::vector<int32_t> ids(nt);
+	for (int t = 0; t < nt; ++t) {
+		code[t] = morton30(cx[t], cy[t], cz[t], cb);
+		ids[t] = t;
+	}
+	std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return code[a] < code[b]; });
+	std::vector<uint32_t> sortedCode(nt);
+	for (int k = 0; k < nt; ++k)
+		sortedCode[k] = code[ids[k]];
+	std::vector<BinNode> bin;
+	std::vector<int32_t> rf, rl, pi, pl;
+	buildLbvh(sortedCode, bin, rf, rl, pi, pl);
+	std::vector<Box> leafBox(nt);
+	for (int k = 0; k < nt; ++k) {
+		int t = ids[k];
+		leafBox[k] = Box{lo[t].x, lo[t].y, lo[t].z, hi[t].x, hi[t].y, hi[t].z};
+	}
+	bottomUp(bin, pi, pl, leafBox);
+
+	Blas out;
+	out.wide.resize(std::max(1, nt));
+	out.tris.resize(nt);
+	uint32_t wideCounter = 1, triCounter = 0;
+	std::vector<int2> qa(std::max(1, nt)), qb(std::max(1, nt));
+	uint32_t qaCount = 1, qbCount = 0;
+	qa[0] = make_int2(nt == 1 ? ~0 : 0, 0);
+	CollapseInputs in{bin.data(), rf.data(), rl.data(), ids.data(), lo.data(), hi.data(), v, idx};
+	while (qaCount > 0) {
+		qbCount = 0;
+		CollapseOutputs o{out.wide.data(), out.tris.data(), &wideCounter, &triCounter, qb.data(), &qbCount};
+		for (uint32_t i = 0; i < qaCount; ++i)
+			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
+		std::swap(qa, qb);
+		qaCount = qbCount;
+	}
+	out.wide.resize(wideCounter);
+	out.bounds = nt == 1 ? leafBox[0] : binBox(bin[0]);
+	return out;
+}
+
+struct HostStack
+{
+	int32_t idx[512];
+	float tn[512];
+	int sp = 0;
+	bool overflow = false;
+	void push(int32_t i, float t)
+	{
+		if (sp >= 512) {
+			overflow = true;
+			return;
+		}
+		idx[sp] = i;
+		tn[sp] = t;
+		++sp;
+	}
+	void pop(int32_t& i, float& t)
+	{
+		--sp;
+		i = idx[sp];
+		t = tn[sp];
+	}
+	int size() const { return sp; }
+};
+
+struct HostLoader
+{
+	WideNode node(const WideNode* base, int32_t i) const { return base[i]; }
+	TriRecord tri(const TriRecord* base, int32_t i) const { return base[i]; }
+	const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
+	BinNode bin(const BinNode* base, int32_t i) const { return base[i]; }
+};
+
+} // namespace
+
+extern "C" {
+
+// Builds BLASes for `nMeshes` meshes and a TLAS over `nInst` instances, then casts `nRays` world
+// rays (origin, direction, tmax: 7 floats each). Outputs per ray: t, instance, original triangle id.
+// Returns the number of wide nodes of mesh 0 (for diagnostics), or -1 on stack overflow.
+int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, const int32_t* const* idx, const int* nTris,
+                 int nInst, const int* instMesh, const float* instTf, const int* instId, int nRays, const float* rays,
+                 float* outT, int32_t* outInst, int32_t* outPrim)
+{
+	std::vector<Blas> blas;
+	for (int m = 0; m < nMeshes; ++m)
+		blas.push_back(buildBlas(verts[m], nVerts[m], idx[m], nTris[m]));
+	std::vector<InstanceRec> inst(nInst);
+	std::vector<Box> ib(nInst);
+	Box cb = emptyBox();
+	for (int i = 0; i < nInst; ++i) {
+		Mat34 tf;
+		std::memcpy(tf.m, instTf + 12 * i, 48);
+		inst[i].objectToWorld = tf;
+		inst[i].worldToObject = inverse(tf);
+		inst[i].nodes = blas[instMesh[i]].wide.data();
+		inst[i].tris = blas[instMesh[i]].tris.data();
+		inst[i].entityId = instId[i];
+		Box b = blas[instMesh[i]].bounds;
+		Box w = emptyBox();
+		for (int c = 0; c < 8; ++c) {
+			Vec3 p = tf.point(v3((c & 1) ? b.hix : b.lox, (c & 2) ? b.hiy : b.loy, (c & 4) ? b.hiz : b.loz));
+			w = unite(w, Box{p.x, p.y, p.z, p.x, p.y, p.z});
+		}
+		float pad = 1e-6f * (std::max({std::fabs(w.lox), std::fabs(w.hix), std::fabs(w.loy), std::fabs(w.hiy),
+		                               std::fabs(w.loz), std::fabs(w.hiz)}) + 1.0f);
+		w = Box{w.lox - pad, w.loy - pad, w.loz - pad, w.hix + pad, w.hiy + pad, w.hiz + pad};
+		inst[i].lox = w.lox;
+		inst[i].loy = w.loy;
+		inst[i].loz = w.loz;
+		inst[i].hix = w.hix;
+		inst[i].hiy = w.hiy;
+		inst[i].hiz = w.hiz;
+		ib[i] = w;
+		float c3[3] = {0.5f * (w.lox + w.hix), 0.5f * (w.loy + w.hiy), 0.5f * (w.loz + w.hiz)};
+		cb = unite(cb, Box{c3[0], c3[1], c3[2], c3[0], c3[1], c3[2]});
+	}
+	std::vector<uint32_t> code(nInst);
+	std::vector<int32_t> ids(nInst);
+	for (int i = 0; i < nInst; ++i) {
+		code[i] = morton30(0.5f * (ib[i].lox + ib[i].hix), 0.5f * (ib[i].loy + ib[i].hiy), 0.5f * (ib[i].loz + ib[i].hiz), cb);
+		ids[i] = i;
+	}
+	std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return code[a] < code[b]; });
+	std::vector<uint32_t> sc(nInst);
+	for (int k = 0; k < nInst; ++k)
+		sc[k] = code[ids[k]];
+	std::vector<BinNode> tlas;
+	std::vector<int32_t> rf, rl, pi, pl;
+	buildLbvh(sc, tlas, rf, rl, pi, pl);
+	std::vector<Box> leafBox(nInst);
+	for (int k = 0; k < nInst; ++k)
+		leafBox[k] = ib[ids[k]];
+	bottomUp(tlas, pi, pl, leafBox);
+	for (auto& n : tlas) { // leaves reference original instance indices
+		if (n.left < 0)
+			n.left = ~ids[~n.left];
+		if (n.right < 0)
+			n.right = ~ids[~n.right];
+	}
+	SceneView sv{tlas.data(), inst.data(), nInst, 0};
+	HostLoader ld;
+	bool overflow = false;
+	for (int r = 0; r < nRays; ++r) {
+		const float* p = rays + 7 * r;
+		HostStack st;
+		HitRec h = traceClosest(sv, v3(p[0], p[1], p[2]), v3(p[3], p[4], p[5]), p[6], st, ld);
+		overflow = overflow || st.overflow;
+		outT[r] = h.t;
+		outInst[r] = h.inst;
+		outPrim[r] = h.inst >= 0 ? inst[h.inst].tris[h.tri].primId : -1;
+	}
+	if (overflow)
+		return -1;
+	return nMeshes > 0 ? (int) blas[0].wide.size() : 0;
+}
+
+} // extern "C"

@@ -1,0 +1,244 @@
+"""Raytrace node through the C API on the GPU, against the reference's known answers and the oracle.
+
+Known-answer cases restate reference test/src/graph/DistanceFieldTest.cpp:86-276,
+test/src/graph/nodes/RaytraceNodeTest.cpp:109-273, test/src/apiReadmeExample.cpp:19-55 and
+test/src/scene/entityIdTest.cpp:28-95 (golden values in tests/golden/reference_values.json).
+Tolerances: hit/miss and entity id exact except on rays the oracle flags as ambiguous (within 1e-6
+relative of an edge or range bound), distance within 1e-5 relative, XYZ within 1e-5 of the
+coordinate magnitude.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from robotecgpulidar_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_values.json")))
+F = None  # filled lazily with the rgl module
+
+
+def cube_scene(rgl, transforms, ids=None):
+    cube = scenes.cube_mesh(1.0)
+    ents = []
+    for k, tf in enumerate(transforms):
+        m = rgl.mesh_create(cube.vertices, cube.indices)
+        e = rgl.entity_create(m)
+        rgl.entity_set_transform(e, tf)
+        if ids is not None and ids[k] is not None:
+            rgl.entity_set_id(e, ids[k])
+        ents.append(e)
+    return ents
+
+
+def run_yield(rgl, rays, ranges=None, fields=None, configure=None):
+    fields = fields or [rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_XYZ_VEC3_F32]
+    n_rays, n_rng, n_rt, n_y = rgl.node(), rgl.node(), rgl.node(), rgl.node()
+    rgl.rays_from_mat3x4f(n_rays, rays)
+    chain = [n_rays]
+    if ranges is not None:
+        rgl.rays_set_range(n_rng, ranges)
+        chain.append(n_rng)
+    rgl.raytrace(n_rt)
+    if configure:
+        configure(n_rt)
+    rgl.points_yield(n_y, fields)
+    chain += [n_rt, n_y]
+    rgl.chain(*chain)
+    rgl.graph_run(n_rays)
+    return {f: rgl.result(n_y, f) for f in fields}
+
+
+@pytest.mark.parametrize("z", GOLD["distance_field_cube_z"])
+def test_distance_single_object_exact(rgl, z):
+    cube_scene(rgl, [scenes.translation(0, 0, np.float32(z))])
+    out = run_yield(rgl, [scenes.translation(0, 0, 0)], [[0.0, np.float32(z) + 10.0]])
+    d = out[rgl.RGL_FIELD_DISTANCE_F32][0]
+    xyz = out[rgl.RGL_FIELD_XYZ_VEC3_F32][0]
+    assert d == np.float32(np.float32(z) - np.float32(1.0))
+    assert d == np.float32(np.sqrt(np.float32(xyz @ xyz)))
+
+
+def test_distance_origin_on_cube_face(rgl):
+    cube_scene(rgl, [scenes.translation(0, 0, 1.0)])
+    out = run_yield(rgl, [scenes.translation(0, 0, 0)], [[0.0, 11.0]])
+    assert out[rgl.RGL_FIELD_DISTANCE_F32][0] == np.float32(2.0)
+
+
+def test_distance_origin_inside_cube(rgl):
+    z = np.float32(-0.001)
+    cube_scene(rgl, [scenes.translation(0, 0, z)])
+    out = run_yield(rgl, [scenes.translation(0, 0, 0)], [[0.0, z + 10.0]])
+    assert out[rgl.RGL_FIELD_DISTANCE_F32][0] == np.float32(np.float32(1.0) + z)
+
+
+def test_nonhit_off_path_is_infinite(rgl):
+    cube_scene(rgl, [scenes.translation(0, 55.5, 0)])
+    rays = [scenes.translation(0, 0, 0), scenes.rotation_xyz(math.pi, 0, 0)]
+    out = run_yield(rgl, rays, [[0.0, 10000.0]])
+    assert np.all(np.isinf(out[rgl.RGL_FIELD_DISTANCE_F32]))
+    assert np.all(out[rgl.RGL_FIELD_DISTANCE_F32] > 0)
+
+
+@pytest.mark.parametrize("z", GOLD["distance_field_cube_z"])
+def test_out_of_max_range(rgl, z):
+    z = np.float32(z)
+    cube_scene(rgl, [scenes.translation(0, 0, z)])
+    out = run_yield(rgl, [scenes.translation(0, 0, 0)], [[0.0, z - 1.0 - 1.0]])
+    assert np.isinf(out[rgl.RGL_FIELD_DISTANCE_F32][0])
+
+
+@pytest.mark.parametrize("z", GOLD["distance_field_cube_z"])
+def test_out_of_min_range(rgl, z):
+    z = np.float32(z)
+    cube_scene(rgl, [scenes.translation(0, 0, z)])
+    out = run_yield(rgl, [scenes.translation(0, 0, 0)], [[z + 1.0 + 1.0, z + 1.0 + 2.0]])
+    assert np.isinf(out[rgl.RGL_FIELD_DISTANCE_F32][0])
+
+
+@pytest.mark.parametrize("z", GOLD["distance_field_cube_z"])
+def test_object_in_range_behind_object_below_min_range(rgl, z):
+    z = np.float32(z)
+    cube_scene(rgl, [scenes.translation(0, 0, z), scenes.translation(0, 0, z + 10.0)])
+    out = run_yield(rgl, [scenes.translation(0, 0, 0)], [[z + 1.0 + 1.0, z + 10.0 + 1.0 + 1.0]])
+    assert np.isinf(out[rgl.RGL_FIELD_DISTANCE_F32][0])
+
+
+def test_distance_from_ray_beginning(rgl):
+    cube_scene(rgl, [scenes.translation(0, 0, 10.0)])
+    a = run_yield(rgl, [scenes.translation(0, 0, 0)], [[0.0, 20.0]])[rgl.RGL_FIELD_DISTANCE_F32][0]
+    b = run_yield(rgl, [scenes.translation(0, 0, 5.0)], [[0.0, 20.0]])
+    assert a == np.float32(9.0)
+    assert b[rgl.RGL_FIELD_DISTANCE_F32][0] == np.float32(4.0)
+    assert a - b[rgl.RGL_FIELD_DISTANCE_F32][0] == np.float32(5.0)
+
+
+@pytest.mark.parametrize("z", GOLD["distance_field_cube_z"])
+def test_various_angles(rgl, z):
+    z = np.float32(z)
+    cube_scene(rgl, [scenes.translation(0, 0, z)])
+    max_angle = math.atan(1.0 / (float(z) - 1.0))
+    angles = np.random.default_rng(7).uniform(-max_angle, max_angle, 100)
+    rays = np.stack([scenes.rotation_xyz(a, 0, 0) for a in angles])
+    out = run_yield(rgl, rays, [[0.0, z + 10.0]])
+    d = out[rgl.RGL_FIELD_DISTANCE_F32]
+    expected = (float(z) - 1.0) / np.cos(angles)
+    assert np.allclose(np.linalg.norm(out[rgl.RGL_FIELD_XYZ_VEC3_F32], axis=1), d, atol=GOLD["distance_field_epsilon"])
+    assert np.allclose(expected, d, atol=GOLD["distance_field_epsilon"])
+
+
+def test_readme_example(rgl):
+    cube_scene(rgl, [scenes.translation(0, 0, 5.0)])
+    n_rays, n_rt = rgl.node(), rgl.node()
+    rgl.rays_from_mat3x4f(n_rays, [scenes.translation(0, 0, 0)])
+    rgl.raytrace(n_rt)
+    rgl.chain(n_rays, n_rt)
+    rgl.graph_run(n_rt)
+    xyz = rgl.result(n_rt, rgl.RGL_FIELD_XYZ_VEC3_F32)
+    assert xyz.shape == (1, 3)
+    assert xyz[0, 2] == pytest.approx(GOLD["readme_hit_z"], rel=1e-6)
+
+
+def test_entity_ids(rgl, oracle):
+    tfs = [scenes.translation(6, -5, 0), scenes.translation(6, 0, 0), scenes.translation(6, 5, 0)]
+    cube_scene(rgl, tfs, ids=[1, 2, None])
+    rays = scenes.lidar_rays(50, 500, -90.0, 90.0)
+    out = run_yield(rgl, rays, None, [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32])
+    hit = out[rgl.RGL_FIELD_IS_HIT_I32] == 1
+    ids = out[rgl.RGL_FIELD_ENTITY_ID_I32]
+    y = out[rgl.RGL_FIELD_XYZ_VEC3_F32][:, 1]
+    assert hit.sum() > 100
+    assert np.all(ids[~hit] == rgl.RGL_ENTITY_INVALID_ID)
+    assert np.all(ids[hit & (y < -2.5)] == 1)
+    assert np.all(ids[hit & (y > -2.5) & (y < 2.5)] == 2)
+    assert np.all(ids[hit & (y > 2.5)] == rgl.RGL_DEFAULT_ENTITY_ID)
+
+
+def test_non_hits_configuration(rgl):
+    cube_scene(rgl, [scenes.translation(0, 0, 0)])
+    rays = scenes.lidar_rays(7, 12, -90.0, 90.0)
+    fields = [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_IS_HIT_I32, rgl.RGL_FIELD_DISTANCE_F32]
+    # Near non-hit: every ray hits the cube below min range.
+    out = run_yield(rgl, rays, [[2.0, 3.0]], fields,
+                    configure=lambda n: rgl.check(rgl.lib().rgl_node_raytrace_configure_non_hits(n, 12.34, 0.0)))
+    assert np.all(out[rgl.RGL_FIELD_IS_HIT_I32] == 0)
+    assert np.all(out[rgl.RGL_FIELD_DISTANCE_F32] == np.float32(12.34))
+    dirs = rays[:, :, 2].astype(np.float64)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    assert np.allclose(out[rgl.RGL_FIELD_XYZ_VEC3_F32], dirs * 12.34, atol=1e-5)
+
+
+def _parity(rgl, oracle, scene, rays, pose, ranges, mode, h_div=0.0, v_div=0.0, layers=3, vertices=19,
+            default_intensity=0.0, extra_fields=()):
+    rgl.spawn_scene(scene)
+    fields = [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_ENTITY_ID_I32,
+              rgl.RGL_FIELD_IS_HIT_I32, rgl.RGL_FIELD_RETURN_TYPE_U8, *extra_fields]
+    n_rays, n_tf, n_rng, n_rt, n_y = (rgl.node() for _ in range(5))
+    rgl.rays_from_mat3x4f(n_rays, rays)
+    rgl.rays_transform(n_tf, pose)
+    rgl.rays_set_range(n_rng, ranges)
+    rgl.raytrace(n_rt)
+    lib = rgl.lib()
+    rgl.check(lib.rgl_node_raytrace_configure_return_mode(n_rt, mode))
+    if h_div > 0:
+        rgl.check(lib.rgl_node_raytrace_configure_beam_divergence(n_rt, h_div, v_div))
+        rgl.configure_beam_samples(n_rt, layers, vertices)
+    if default_intensity > 0:
+        rgl.check(lib.rgl_node_raytrace_configure_default_intensity(n_rt, default_intensity))
+    rgl.points_yield(n_y, fields)
+    rgl.chain(n_rays, n_tf, n_rng, n_rt, n_y)
+    rgl.graph_run(n_rays)
+    got = {f: rgl.result(n_y, f) for f in fields}
+    osc = oracle.OracleScene(scene)
+    exp = osc.raytrace(rays, ray_transform=pose, ranges=ranges, return_mode=mode, h_div=h_div, v_div=v_div,
+                       layers=layers, vertices=vertices, default_intensity=default_intensity)
+    return got, exp
+
+
+def _check(rgl, got, exp, min_agreement=0.99999):
+    amb = exp["ambiguous"] != 0
+    hit_g, hit_e = got[rgl.RGL_FIELD_IS_HIT_I32], exp["is_hit"]
+    ent_g, ent_e = got[rgl.RGL_FIELD_ENTITY_ID_I32], exp["entity_id"]
+    mism = (hit_g != hit_e) | (ent_g != ent_e)
+    assert not (mism & ~amb).any(), f"{int((mism & ~amb).sum())} non-ambiguous mismatches"
+    assert 1.0 - mism.mean() >= min_agreement, f"agreement {1.0 - mism.mean()}"
+    assert np.all(got[rgl.RGL_FIELD_RETURN_TYPE_U8] == exp["return_type"])
+    both = (hit_g == 1) & (hit_e == 1) & ~amb
+    dg, de = got[rgl.RGL_FIELD_DISTANCE_F32][both], exp["distance"][both]
+    rel = np.abs(dg.astype(np.float64) - de) / np.maximum(np.abs(de), 1e-6)
+    assert rel.max(initial=0.0) <= 1e-5, f"max rel distance error {rel.max()}"
+    xg, xe = got[rgl.RGL_FIELD_XYZ_VEC3_F32][both], exp["xyz"][both]
+    scale = np.maximum(np.abs(xe).max(axis=1), 1.0)
+    assert (np.abs(xg - xe).max(axis=1, initial=0.0) <= 1e-5 * scale * 4).all()
+    # Non-hits: distances and XYZ follow the non-hit rule exactly.
+    nh = (hit_g == 0) & (hit_e == 0)
+    assert np.array_equal(got[rgl.RGL_FIELD_DISTANCE_F32][nh], exp["distance"][nh])
+    return rel
+
+
+def test_parity_plain_scene_first_return(rgl, oracle):
+    got, exp = _parity(rgl, oracle, scenes.plain_scene(), scenes.lidar_rays(32, 1024), scenes.translation(0, 0, 1.8),
+                       [[0.1, 100.0]], rgl.RGL_RETURN_FIRST)
+    _check(rgl, got, exp)
+
+
+@pytest.mark.parametrize("mode_name", ["RGL_RETURN_FIRST_LAST", "RGL_RETURN_LAST", "RGL_RETURN_STRONGEST",
+                                       "RGL_RETURN_FIRST_SECOND", "RGL_RETURN_LAST_STRONGEST",
+                                       "RGL_RETURN_STRONGEST_SECOND_STRONGEST", "RGL_RETURN_SECOND"])
+def test_parity_return_modes_reference_pattern(rgl, oracle, mode_name):
+    mode = getattr(rgl, mode_name)
+    got, exp = _parity(rgl, oracle, scenes.plain_scene(), scenes.lidar_rays(16, 256), scenes.translation(0, 0, 1.8),
+                       [[0.1, 100.0]], mode, h_div=math.radians(2.0), v_div=math.radians(1.0), default_intensity=100.0,
+                       extra_fields=[rgl.RGL_FIELD_INTENSITY_F32])
+    _check(rgl, got, exp)
+
+
+def test_parity_million_scene_dual_return_5_subrays(rgl, oracle):
+    got, exp = _parity(rgl, oracle, scenes.million_scene(), scenes.lidar_rays(32, 512), scenes.translation(0, 0, 8.0),
+                       [[0.1, 100.0]], rgl.RGL_RETURN_FIRST_LAST, h_div=math.radians(0.2), v_div=math.radians(0.2),
+                       layers=1, vertices=4)
+    _check(rgl, got, exp)
