@@ -36,5 +36,11 @@ RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node);
 /* Number of CUDA kernels this library launched since it was loaded. */
 RGL_API rgl_status_t rgl_gb300_get_kernel_launch_count(uint64_t* out_count);
 
+/*
+ * Size of the default scene's acceleration structure after the last raytrace: bytes of BLAS wide nodes
+ * and triangle records over all distinct meshes, and the number of entities (instances).
+ */
+RGL_API rgl_status_t rgl_gb300_scene_get_stats(int64_t* out_node_bytes, int64_t* out_triangle_bytes, int32_t* out_instances);
+
 /* SM count and compute capability (major * 10 + minor) of the device in use. */
 RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_compute_capability);

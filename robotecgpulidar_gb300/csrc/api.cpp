@@ -1028,3 +1028,21 @@ RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_c
 		}
 	});
 }
+
+RGL_API rgl_status_t rgl_gb300_scene_get_stats(int64_t* out_node_bytes, int64_t* out_triangle_bytes, int32_t* out_instances)
+{
+	return safeCall([&]() {
+		GraphRunCtx::synchronizeAll();
+		int64_t nb = 0, tb = 0;
+		Scene::defaultScene().stats(nb, tb);
+		if (out_node_bytes) {
+			*out_node_bytes = nb;
+		}
+		if (out_triangle_bytes) {
+			*out_triangle_bytes = tb;
+		}
+		if (out_instances) {
+			*out_instances = (int32_t) Scene::defaultScene().entityCount();
+		}
+	});
+}

@@ -306,6 +306,7 @@ void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, i
 		throw std::runtime_error("BVH build: collapse produced an inconsistent tree (tris " + std::to_string(hostCtr[1]) +
 		                         ", nodes " + std::to_string(hostCtr[0]) + ")");
 	}
+	out.nodeCount = hostCtr[0];
 	if (T > 1) {
 		out.bounds[0] = rootBox.lox;
 		out.bounds[1] = rootBox.loy;

@@ -23,6 +23,7 @@ struct BlasBuild
 	WideNode* nodes = nullptr; // device
 	TriRecord* tris = nullptr; // device
 	uint32_t nodeCapacity = 0;
+	uint32_t nodeCount = 0;      // wide nodes in use
 	int32_t triCount = 0;
 	float bounds[6] = {0, 0, 0, 0, 0, 0}; // object-space box lo.xyz, hi.xyz (host copy)
 };

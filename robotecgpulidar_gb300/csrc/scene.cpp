@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <set>
 
 using rgl::Mat34;
 
@@ -90,6 +91,21 @@ void Scene::clear()
 	posesDirty = true;
 	timeSet = false;
 	timeNs = 0;
+}
+
+void Scene::stats(int64_t& nodeBytes, int64_t& triangleBytes) const
+{
+	std::set<const Mesh*> seen;
+	nodeBytes = 0;
+	triangleBytes = 0;
+	for (auto& e : entities) {
+		const Mesh* m = e->mesh.get();
+		if (!m->blasBuilt || !seen.insert(m).second) {
+			continue;
+		}
+		nodeBytes += (int64_t) m->blas.nodeCount * (int64_t) sizeof(rgl::WideNode);
+		triangleBytes += (int64_t) m->blas.triCount * (int64_t) sizeof(rgl::TriRecord);
+	}
 }
 
 void Scene::checkDeviceErrors()

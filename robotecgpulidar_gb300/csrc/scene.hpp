@@ -60,6 +60,8 @@ struct Scene
 	void prepare(cudaStream_t s);
 	const rgl::SceneView* view() const { return dView.as<rgl::SceneView>(); }
 	size_t entityCount() const { return entities.size(); }
+	// Bytes of built BLAS wide nodes and triangle records over the distinct meshes in the scene.
+	void stats(int64_t& nodeBytes, int64_t& triangleBytes) const;
 	int32_t* errorFlag() const { return dError.as<int32_t>(); }
 	void checkDeviceErrors();
 
