@@ -116,10 +116,15 @@ RGL_HD void lbvhInternal(int i, const uint32_t* codes, int n, int32_t& left, int
 	last = hi;
 }
 
-// Smallest power of two 2^(e-127) with 255 * 2^(e-127) >= ext, as the biased exponent byte e.
+// Quantisation grid of a wide node: origin p = lo - 2^(e-127) and 2^(e-127) * kQuantSpan >= extent,
+// leaving one spare grid step below and above every child so each child box can be widened by one
+// step on each side (see quantizeAxis).
+constexpr double kQuantSpan = 252.0;
+
+// Smallest power of two 2^(e-127) with kQuantSpan * 2^(e-127) >= ext, as the biased exponent byte e.
 RGL_HD uint8_t quantExponent(float ext)
 {
-	double s = (double) ext / 255.0;
+	double s = (double) ext / kQuantSpan;
 	int e = 1; // 2^-126
 	double p = 1.1754943508222875e-38;
 	while (p < s && e < 254) {
@@ -143,13 +148,19 @@ RGL_HD void quantizeAxis(float p, float scale, float clo, float chi, uint8_t& ql
 	}
 	lo = lo < 0 ? 0 : (lo > 255 ? 255 : lo);
 	hi = hi < 0 ? 0 : (hi > 255 ? 255 : hi);
-	// Verify with the exact float expression the traversal evaluates.
+	// Verify the enclosure with the exact float sum p + q * scale.
 	while (lo > 0 && fadd(p, (float) lo * scale) > clo) {
 		--lo;
 	}
 	while (hi < 255 && fadd(p, (float) hi * scale) < chi) {
 		++hi;
 	}
+	// Widen by one grid step. The traversal evaluates planes as fma(q, scale * inv, (p - o) * inv),
+	// whose error is at most 4u|t| + 3u * 255 * scale * |inv| (u = 2^-24); the extra step moves every
+	// plane outward by scale, which exceeds the second term, and the traversal's relative slack on
+	// the exit distance covers the first. No hit inside the exact child box is lost.
+	lo = lo > 0 ? lo - 1 : 0;
+	hi = hi < 255 ? hi + 1 : 255;
 	qlo = (uint8_t) lo;
 	qhi = (uint8_t) hi;
 }
@@ -232,12 +243,12 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 		ch[n++] = in.bin[c].right;
 	}
 
-	Box cb[kWideArity];
+	Box cb0[kWideArity];
 	Box nb = emptyBox();
 	uint32_t nInternal = 0, nLeafTris = 0;
 	for (int k = 0; k < n; ++k) {
-		cb[k] = childBounds(in, ch[k]);
-		nb = unite(nb, cb[k]);
+		cb0[k] = childBounds(in, ch[k]);
+		nb = unite(nb, cb0[k]);
 		int cnt = binCount(in, ch[k]);
 		if (ch[k] >= 0 && cnt > kLeafMaxTris) {
 			++nInternal;
@@ -245,17 +256,70 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 			nLeafTris += (uint32_t) cnt;
 		}
 	}
+	// Slot assignment by octant: a child whose centre lies on the +x/+y/+z side of the node centre
+	// prefers slot bit 0/1/2 set, so a ray visiting slots in order j ^ (ray direction sign bits)
+	// meets children roughly front to back (the ordering idea of Ylitie et al., HPG 2017). Larger
+	// children choose first; a taken slot falls back to the free slot nearest in Hamming distance.
+	int32_t slotChild[kWideArity];
+	for (int s = 0; s < kWideArity; ++s) {
+		slotChild[s] = -1;
+	}
+	{
+		float ncx = 0.5f * (nb.lox + nb.hix), ncy = 0.5f * (nb.loy + nb.hiy), ncz = 0.5f * (nb.loz + nb.hiz);
+		bool placed[kWideArity] = {false, false, false, false, false, false, false, false};
+		for (int round = 0; round < n; ++round) {
+			int pick = -1;
+			float pickArea = -1.0f;
+			for (int k = 0; k < n; ++k) {
+				float a = halfArea(cb0[k]);
+				if (!placed[k] && a > pickArea) {
+					pickArea = a;
+					pick = k;
+				}
+			}
+			const Box& b = cb0[pick];
+			int oct = ((0.5f * (b.lox + b.hix) >= ncx) ? 1 : 0) | ((0.5f * (b.loy + b.hiy) >= ncy) ? 2 : 0) |
+			          ((0.5f * (b.loz + b.hiz) >= ncz) ? 4 : 0);
+			int best = -1, bestD = 99;
+			for (int s = 0; s < kWideArity; ++s) {
+				if (slotChild[s] < 0) {
+					int dd = popc8((uint32_t) (s ^ oct));
+					if (dd < bestD) {
+						bestD = dd;
+						best = s;
+					}
+				}
+			}
+			slotChild[best] = pick;
+			placed[pick] = true;
+		}
+	}
+	int32_t chs[kWideArity];
+	Box cb[kWideArity];
+	for (int s = 0; s < kWideArity; ++s) {
+		chs[s] = slotChild[s] >= 0 ? ch[slotChild[s]] : 0;
+		cb[s] = slotChild[s] >= 0 ? cb0[slotChild[s]] : emptyBox();
+	}
 	uint32_t childBase = nInternal ? atomicAddU32(out.wideCounter, nInternal) : 0;
 	uint32_t triBase = nLeafTris ? atomicAddU32(out.triCounter, nLeafTris) : 0;
 	uint32_t qBase = nInternal ? atomicAddU32(out.queueOutCount, nInternal) : 0;
 
 	WideNode w;
-	w.px = nb.lox;
-	w.py = nb.loy;
-	w.pz = nb.loz;
 	w.ex = quantExponent(nb.hix - nb.lox);
 	w.ey = quantExponent(nb.hiy - nb.loy);
 	w.ez = quantExponent(nb.hiz - nb.loz);
+	// Origin one grid step below the node box (rounded down), so children can be widened downward.
+	auto originBelow = [](float lo, uint8_t e) {
+		const double exact = (double) lo - (double) exp2Byte(e);
+		float p = (float) exact;
+		if ((double) p > exact) {
+			p = nextafterf(p, -FLT_MAX);
+		}
+		return p;
+	};
+	w.px = originBelow(nb.lox, w.ex);
+	w.py = originBelow(nb.loy, w.ey);
+	w.pz = originBelow(nb.loz, w.ez);
 	w.imask = 0;
 	w.childBase = childBase;
 	w.triBase = triBase;
@@ -266,11 +330,14 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 		w.qhix[k] = w.qhiy[k] = w.qhiz[k] = 0;
 	}
 	uint32_t rank = 0, triOff = 0;
-	for (int k = 0; k < n; ++k) {
+	for (int k = 0; k < kWideArity; ++k) {
+		if (slotChild[k] < 0) {
+			continue;
+		}
 		quantizeAxis(w.px, sx, cb[k].lox, cb[k].hix, w.qlox[k], w.qhix[k]);
 		quantizeAxis(w.py, sy, cb[k].loy, cb[k].hiy, w.qloy[k], w.qhiy[k]);
 		quantizeAxis(w.pz, sz, cb[k].loz, cb[k].hiz, w.qloz[k], w.qhiz[k]);
-		int32_t c = ch[k];
+		int32_t c = chs[k];
 		int cnt = binCount(in, c);
 		if (c >= 0 && cnt > kLeafMaxTris) {
 			w.imask |= (uint8_t) (1u << k);

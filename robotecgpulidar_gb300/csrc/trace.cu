@@ -1,15 +1,18 @@
-// Lidar traversal kernel: per beam, casts the primary ray and its beam-divergence sub-rays through the
-// two-level BVH, and reduces the samples to the requested returns in registers, writing RGL's
-// per-point fields directly.
+// Lidar traversal kernel: casts every beam's primary ray and beam-divergence sub-rays through the
+// two-level BVH and reduces the samples to the requested returns, writing RGL's per-point fields.
 //
 // Replaces reference src/gpu/optixPrograms.cu:46-216 (raygen + closest-hit + miss, which store 58
 // samples per beam in a scratch buffer) and src/gpu/nodeKernels.cu:334-422 (kReduceDivergentBeams,
-// which re-reads that buffer). The return-selection rules, including the reference's quirks, are kept:
+// which re-reads that buffer). Mapping: the S samples of a beam go to a group of G = min(S, 32)
+// neighbouring lanes (lane k of the group traces samples k, k + G); each warp holds 32 / G beams. The
+// group's first lane then reads the samples in sample order through warp shuffles and applies the
+// reference's selection rules, including its quirks:
 //  * the first hit sample (in sample order) seeds first/second/last/strongest/second-strongest;
 //  * a closer sample makes the old first the second; a sample strictly between first and second
-//    becomes second (which, with second seeded equal to first, never happens - kept as is);
+//    becomes second (with second seeded equal to first this never fires - kept as is);
 //  * last = strictly farther; strongest/second-strongest by strict intensity comparisons;
-//  * a beam without hits reports sample 0's non-hit distance for every return.
+//  * a beam without hits reports sample 0's non-hit distance (near below min range, far on a miss).
+// No per-sample scratch buffer exists: samples live in registers until the shuffle reduction.
 #include <cuda_runtime.h>
 
 #include "kernels.hpp"
@@ -20,19 +23,19 @@ namespace rgl {
 namespace {
 
 constexpr int kBlock = 128;
-constexpr int kSmemStack = 16;  // entries per thread in shared memory
-constexpr int kLocalStack = 48; // overflow entries per thread in local memory
+constexpr int kSmemStack = 24;  // entries per thread in shared memory
+constexpr int kLocalStack = 40; // overflow entries per thread in local memory
 
 struct DevStack
 {
-	uint2* sm; // column of this thread: sm[k * kBlock]
+	uint2* sm; // this thread's column: sm[k * kBlock]
 	int sp;
 	bool overflow;
 	uint2 local[kLocalStack];
 
-	__device__ void push(int32_t i, float t)
+	__device__ __forceinline__ void push(uint32_t a, uint32_t b)
 	{
-		uint2 e = make_uint2((uint32_t) i, __float_as_uint(t));
+		const uint2 e = make_uint2(a, b);
 		if (sp < kSmemStack) {
 			sm[sp * kBlock] = e;
 		} else if (sp < kSmemStack + kLocalStack) {
@@ -43,59 +46,81 @@ struct DevStack
 		}
 		++sp;
 	}
-	__device__ void pop(int32_t& i, float& t)
+	__device__ __forceinline__ void pop(uint32_t& a, uint32_t& b)
 	{
 		--sp;
-		uint2 e = sp < kSmemStack ? sm[sp * kBlock] : local[sp - kSmemStack];
-		i = (int32_t) e.x;
-		t = __uint_as_float(e.y);
+		const uint2 e = sp < kSmemStack ? sm[sp * kBlock] : local[sp - kSmemStack];
+		a = e.x;
+		b = e.y;
 	}
-	__device__ int size() const { return sp; }
+	__device__ __forceinline__ int size() const { return sp; }
 };
 
 struct DevLoader
 {
-	__device__ WideNode node(const WideNode* base, int32_t i) const
+	__device__ __forceinline__ void nodeWords(const WideNode* base, uint32_t i, uint4& w0, uint4& w1, uint4& w2, uint4& w3,
+	                                          uint4& w4) const
 	{
 		const uint4* p = reinterpret_cast<const uint4*>(base + i);
-		WideNode n;
-		uint4* q = reinterpret_cast<uint4*>(&n);
-		q[0] = __ldg(p);
-		q[1] = __ldg(p + 1);
-		q[2] = __ldg(p + 2);
-		q[3] = __ldg(p + 3);
-		q[4] = __ldg(p + 4);
-		return n;
+		w0 = __ldg(p);
+		w1 = __ldg(p + 1);
+		w2 = __ldg(p + 2);
+		w3 = __ldg(p + 3);
+		w4 = __ldg(p + 4);
 	}
-	__device__ TriRecord tri(const TriRecord* base, int32_t i) const
+	__device__ __forceinline__ TriRecord tri(const TriRecord* base, int32_t i) const
 	{
 		const float4* p = reinterpret_cast<const float4*>(base + i);
+		const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
 		TriRecord t;
-		float4* q = reinterpret_cast<float4*>(&t);
-		q[0] = __ldg(p);
-		q[1] = __ldg(p + 1);
-		q[2] = __ldg(p + 2);
+		t.v0x = a.x;
+		t.v0y = a.y;
+		t.v0z = a.z;
+		t.primId = __float_as_int(a.w);
+		t.v1x = b.x;
+		t.v1y = b.y;
+		t.v1z = b.z;
+		t.pad1 = 0;
+		t.v2x = c.x;
+		t.v2y = c.y;
+		t.v2z = c.z;
+		t.pad2 = 0;
 		return t;
 	}
-	__device__ const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
-	__device__ BinNode bin(const BinNode* base, int32_t i) const
+	__device__ __forceinline__ const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
+	__device__ __forceinline__ BinNode bin(const BinNode* base, int32_t i) const
 	{
 		const float4* p = reinterpret_cast<const float4*>(base + i);
+		const float4 a = __ldg(p), b = __ldg(p + 1);
 		BinNode n;
-		float4* q = reinterpret_cast<float4*>(&n);
-		q[0] = __ldg(p);
-		q[1] = __ldg(p + 1);
+		n.lox = a.x;
+		n.loy = a.y;
+		n.loz = a.z;
+		n.left = __float_as_int(a.w);
+		n.hix = b.x;
+		n.hiy = b.y;
+		n.hiz = b.z;
+		n.right = __float_as_int(b.w);
 		return n;
 	}
 };
 
-struct Sample
+// One traced sample. For non-hits `dist` holds the non-hit distance (near or far).
+struct SampleVal
+{
+	uint32_t hit;
+	float dist;
+	float intensity;
+	int32_t entity;
+	float nx, ny, nz, cosInc;
+};
+
+struct Selected
 {
 	float dist;
 	float intensity;
 	int32_t entity;
-	float nx, ny, nz;
-	float cosInc;
+	float nx, ny, nz, cosInc;
 };
 
 __device__ __forceinline__ Mat34 loadMat(const Mat34* p)
@@ -105,7 +130,52 @@ __device__ __forceinline__ Mat34 loadMat(const Mat34* p)
 	return Mat34{{{a.x, a.y, a.z, a.w}, {b.x, b.y, b.z, b.w}, {c.x, c.y, c.z, c.w}}};
 }
 
-__global__ void __launch_bounds__(kBlock) kTrace(TraceParams p, const Mat34* __restrict__ table)
+template<bool SHADING>
+__device__ __forceinline__ SampleVal traceSample(const TraceParams& p, const SceneView& sc, const Mat34& sr, float minRange,
+                                                 float maxRange, DevStack& st)
+{
+	DevLoader ld;
+	const Vec3 o = sr.rayOrigin();
+	const Vec3 d = sr.rayDir();
+	const HitRec h = traceClosest(sc, o, d, maxRange, st, ld);
+	SampleVal v;
+	v.hit = 0;
+	v.dist = p.farNonHitDistance;
+	v.intensity = 0.0f;
+	v.entity = 0;
+	v.nx = v.ny = v.nz = v.cosInc = 0.0f;
+	if (h.inst >= 0) {
+		const float dist = fmul(h.t, length(d));
+		if (dist < minRange) {
+			v.dist = p.nearNonHitDistance;
+		} else {
+			const InstanceRec& inst = sc.instances[h.inst];
+			v.hit = 1;
+			v.dist = dist;
+			v.entity = inst.entityId;
+			if (SHADING) {
+				const TriRecord tr = ld.tri(inst.tris, h.tri);
+				const Vec3 wa = inst.objectToWorld.point(v3(tr.v0x, tr.v0y, tr.v0z));
+				const Vec3 wb = inst.objectToWorld.point(v3(tr.v1x, tr.v1y, tr.v1z));
+				const Vec3 wc = inst.objectToWorld.point(v3(tr.v2x, tr.v2y, tr.v2z));
+				const Vec3 n = normalized(cross(wb - wa, wc - wa));
+				const float c = fabsf(dot(n, d));
+				v.nx = n.x;
+				v.ny = n.y;
+				v.nz = n.z;
+				v.cosInc = c;
+				v.intensity = fmul(p.defaultIntensity, c);
+			}
+		}
+	}
+	return v;
+}
+
+__device__ __forceinline__ float pick(int r, float a, float b) { return r == 0 ? a : b; }
+__device__ __forceinline__ uint32_t pickU(int r, uint32_t a, uint32_t b) { return r == 0 ? a : b; }
+
+template<int ROUNDS, bool SHADING>
+__global__ void __launch_bounds__(kBlock) kTrace(TraceParams p, const Mat34* __restrict__ table, int groupSize)
 {
 	extern __shared__ uint2 stackMem[];
 	__shared__ Mat34 sTable[kMaxBeamSamples];
@@ -113,63 +183,75 @@ __global__ void __launch_bounds__(kBlock) kTrace(TraceParams p, const Mat34* __r
 		reinterpret_cast<float*>(sTable)[i] = reinterpret_cast<const float*>(table)[i];
 	}
 	__syncthreads();
-	const int beam = blockIdx.x * kBlock + threadIdx.x;
-	if (beam >= p.nRays) {
-		return;
-	}
+
+	const int lane = threadIdx.x & 31;
+	const int warpId = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+	const int G = groupSize;
+	const int beamsPerWarp = 32 / G;
+	const int g = lane / G;
+	const int sub = lane - g * G;
+	const int beam = warpId * beamsPerWarp + g;
+	const bool valid = g < beamsPerWarp && beam < p.nRays;
 	const SceneView sc = *p.scene;
-	const Mat34 ray = (p.rays != nullptr) ? loadMat(p.rays + beam) : Mat34::identity();
-	const float* rg = p.ranges + 2 * (p.nRanges == 1 ? 0 : beam);
-	const float minRange = rg[0], maxRange = rg[1];
-	const bool wantShading = p.needIntensity != 0 || (p.out.normal != nullptr) || (p.out.incidentAngle != nullptr);
 
 	DevStack st;
 	st.sm = stackMem + threadIdx.x;
 	st.sp = 0;
 	st.overflow = false;
-	DevLoader ld;
 
+	Mat34 ray = Mat34::identity();
+	float minRange = 0.0f, maxRange = 0.0f;
+	if (valid) {
+		ray = loadMat(p.rays + beam);
+		const float* rg = p.ranges + 2 * (p.nRanges == 1 ? 0 : beam);
+		minRange = rg[0];
+		maxRange = rg[1];
+	}
+	SampleVal sv[ROUNDS];
+#pragma unroll
+	for (int r = 0; r < ROUNDS; ++r) {
+		const int s = sub + r * G;
+		if (valid && s < p.nSamples) {
+			const Mat34 sr = (s == 0) ? ray : mul(ray, sTable[s]);
+			sv[r] = traceSample<SHADING>(p, sc, sr, minRange, maxRange, st);
+		} else {
+			sv[r] = SampleVal{0u, 0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+		}
+	}
+	if (st.overflow && p.errorFlag) {
+		atomicExch(p.errorFlag, 1);
+	}
+
+	// In-order reduction by the group's first lane (all lanes take part in the shuffles).
+	const bool leader = valid && sub == 0;
+	const int groupLane0 = (g < beamsPerWarp) ? g * G : lane;
 	bool haveFirst = false;
 	float nonHitDist = p.farNonHitDistance;
-	Sample first{}, second{}, last{}, strongest{}, secondStrongest{};
-
+	Selected first{}, second{}, last{}, strongest{}, secondStrongest{};
 	for (int s = 0; s < p.nSamples; ++s) {
-		const Mat34 sr = (s == 0) ? ray : mul(ray, sTable[s]);
-		const Vec3 o = sr.rayOrigin();
-		const Vec3 d = sr.rayDir();
-		HitRec h = traceClosest(sc, o, d, maxRange, st, ld);
-		Sample cur;
-		bool hit = false;
-		if (h.inst >= 0) {
-			float dist = fmul(h.t, length(d));
-			if (dist < minRange) {
-				if (s == 0) {
-					nonHitDist = p.nearNonHitDistance;
-				}
-			} else {
-				hit = true;
-				const InstanceRec& inst = sc.instances[h.inst];
-				cur.dist = dist;
-				cur.entity = inst.entityId;
-				cur.intensity = 0.0f;
-				cur.nx = cur.ny = cur.nz = 0.0f;
-				cur.cosInc = 0.0f;
-				if (wantShading) {
-					TriRecord tr = ld.tri(inst.tris, h.tri);
-					Vec3 wa = inst.objectToWorld.point(v3(tr.v0x, tr.v0y, tr.v0z));
-					Vec3 wb = inst.objectToWorld.point(v3(tr.v1x, tr.v1y, tr.v1z));
-					Vec3 wc = inst.objectToWorld.point(v3(tr.v2x, tr.v2y, tr.v2z));
-					Vec3 n = normalized(cross(wb - wa, wc - wa));
-					float c = fabsf(dot(n, d));
-					cur.nx = n.x;
-					cur.ny = n.y;
-					cur.nz = n.z;
-					cur.cosInc = c;
-					cur.intensity = fmul(p.defaultIntensity, c);
-				}
-			}
-		} else if (s == 0) {
-			nonHitDist = p.farNonHitDistance;
+		const int r = (ROUNDS == 1) ? 0 : s / G;
+		const int src = groupLane0 + (s - r * G);
+		const uint32_t hit = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].hit : pickU(r, sv[0].hit, sv[ROUNDS - 1].hit), src);
+		const float dist = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].dist : pick(r, sv[0].dist, sv[ROUNDS - 1].dist), src);
+		const int32_t ent =
+		    __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].entity : (int32_t) pickU(r, (uint32_t) sv[0].entity, (uint32_t) sv[ROUNDS - 1].entity), src);
+		Selected cur;
+		cur.dist = dist;
+		cur.entity = ent;
+		cur.intensity = 0.0f;
+		cur.nx = cur.ny = cur.nz = cur.cosInc = 0.0f;
+		if (SHADING) {
+			cur.intensity = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].intensity : pick(r, sv[0].intensity, sv[ROUNDS - 1].intensity), src);
+			cur.nx = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].nx : pick(r, sv[0].nx, sv[ROUNDS - 1].nx), src);
+			cur.ny = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].ny : pick(r, sv[0].ny, sv[ROUNDS - 1].ny), src);
+			cur.nz = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].nz : pick(r, sv[0].nz, sv[ROUNDS - 1].nz), src);
+			cur.cosInc = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].cosInc : pick(r, sv[0].cosInc, sv[ROUNDS - 1].cosInc), src);
+		}
+		if (!leader) {
+			continue;
+		}
+		if (s == 0 && !hit) {
+			nonHitDist = dist;
 		}
 		if (!hit) {
 			continue;
@@ -195,8 +277,8 @@ __global__ void __launch_bounds__(kBlock) kTrace(TraceParams p, const Mat34* __r
 			secondStrongest = cur;
 		}
 	}
-	if (st.overflow && p.errorFlag) {
-		atomicExch(p.errorFlag, 1);
+	if (!leader) {
+		return;
 	}
 
 	const Vec3 org = ray.rayOrigin();
@@ -214,7 +296,7 @@ __global__ void __launch_bounds__(kBlock) kTrace(TraceParams p, const Mat34* __r
 			disp.y = isnan(disp.y) ? 0.0f : disp.y;
 			disp.z = isnan(disp.z) ? 0.0f : disp.z;
 			if (out.xyz) {
-				Vec3 q = org + disp;
+				const Vec3 q = org + disp;
 				out.xyz[3 * pi] = q.x;
 				out.xyz[3 * pi + 1] = q.y;
 				out.xyz[3 * pi + 2] = q.z;
@@ -234,17 +316,16 @@ __global__ void __launch_bounds__(kBlock) kTrace(TraceParams p, const Mat34* __r
 			if (out.laserRetro) out.laserRetro[pi] = 0.0f;
 			continue;
 		}
-		const Sample* sel = nullptr;
-		if (type == 4u) sel = &first;
-		else if (type == 3u) sel = &second;
-		else if (type == 2u) sel = &last;
-		else if (type == 1u) sel = &strongest;
-		else if (type == 5u) sel = &secondStrongest;
-		if (sel == nullptr) {
-			continue;
-		}
+		Selected chosen;
+		if (type == 4u) chosen = first;
+		else if (type == 3u) chosen = second;
+		else if (type == 2u) chosen = last;
+		else if (type == 1u) chosen = strongest;
+		else if (type == 5u) chosen = secondStrongest;
+		else continue;
+		const Selected* sel = &chosen;
 		if (out.xyz) {
-			Vec3 q = org + dn * sel->dist;
+			const Vec3 q = org + dn * sel->dist;
 			out.xyz[3 * pi] = q.x;
 			out.xyz[3 * pi + 1] = q.y;
 			out.xyz[3 * pi + 2] = q.z;
@@ -272,9 +353,26 @@ void launchTrace(const TraceParams& p, const Mat34* dSampleTable, cudaStream_t s
 	if (p.nRays <= 0) {
 		return;
 	}
-	int grid = (p.nRays + kBlock - 1) / kBlock;
-	size_t smem = sizeof(uint2) * kSmemStack * kBlock;
-	kTrace<<<grid, kBlock, smem, stream>>>(p, dSampleTable);
+	const int G = p.nSamples < 32 ? p.nSamples : 32;
+	const int rounds = (p.nSamples + G - 1) / G;
+	const int beamsPerWarp = 32 / G;
+	const long warps = ((long) p.nRays + beamsPerWarp - 1) / beamsPerWarp;
+	const int grid = (int) ((warps * 32 + kBlock - 1) / kBlock);
+	const size_t smem = sizeof(uint2) * kSmemStack * kBlock;
+	const bool shading = p.needIntensity != 0 || p.out.normal != nullptr || p.out.incidentAngle != nullptr;
+	if (rounds == 1) {
+		if (shading) {
+			kTrace<1, true><<<grid, kBlock, smem, stream>>>(p, dSampleTable, G);
+		} else {
+			kTrace<1, false><<<grid, kBlock, smem, stream>>>(p, dSampleTable, G);
+		}
+	} else {
+		if (shading) {
+			kTrace<2, true><<<grid, kBlock, smem, stream>>>(p, dSampleTable, G);
+		} else {
+			kTrace<2, false><<<grid, kBlock, smem, stream>>>(p, dSampleTable, G);
+		}
+	}
 	countLaunch();
 }
 

@@ -171,71 +171,131 @@ RGL_HD int popc8(uint32_t x)
 #endif
 }
 
-// Generic traversal stack interface: `Stack` provides push(idx, tnear), pop(idx&, tnear&), size(),
-// and an `overflow` flag.
+// ---------------------------------------------------------------- wide-node traversal
+//
+// Stack entries are two 32-bit words. BLAS entries are node groups (after Ylitie et al., HPG 2017):
+// (childBase, imask | remaining-hits << 8), where bit j of the hits selects slot j ^ octant. TLAS
+// entries are (node or ~instance, entry distance bits). `Stack` provides push(a, b), pop(a&, b&),
+// size().
+
+// Slab test of a dequantised child box in the FMA form t = q * (s * inv) + (p - o) * inv. The computed
+// t differs from the exact plane distance by at most 4u|t| + 3u * 255 * s * |inv| (u = 2^-24). The
+// builder widens every child box by one grid step s (bvh_core.hpp quantizeAxis), which moves each plane
+// outward by s * |inv| in t and covers the second term; entry <= exit * (1 + 5e-7) covers the first.
+// Axis-parallel rays (inv = +-1e30 after safeInv) stay exact: their slab only yields +-huge values.
+constexpr float kSlabRelSlack = 1.0000005f;
+
+RGL_HD uint32_t lowestBit(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+	return (uint32_t) (__ffs((int) x) - 1);
+#else
+	return (uint32_t) __builtin_ctz(x);
+#endif
+}
+
+RGL_HD float asFloat(uint32_t u)
+{
+#if defined(__CUDA_ARCH__)
+	return __uint_as_float(u);
+#else
+	float f;
+	__builtin_memcpy(&f, &u, 4);
+	return f;
+#endif
+}
+
+RGL_HD uint32_t asUint(float f)
+{
+#if defined(__CUDA_ARCH__)
+	return __float_as_uint(f);
+#else
+	uint32_t u;
+	__builtin_memcpy(&u, &f, 4);
+	return u;
+#endif
+}
+
+RGL_HD float byteF(uint32_t w, int sh) { return (float) ((w >> sh) & 0xffu); }
+
 template<class Stack, class NodeLoader>
 RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 d, Stack& st, HitRec& best,
                          const NodeLoader& load)
 {
-	Watertight wt = setupWatertight(d);
-	BoxRay br = makeBoxRay(o, d);
-	int base = st.size();
-	st.push(0, 0.0f);
-	while (st.size() > base) {
-		int32_t ni;
-		float tn;
-		st.pop(ni, tn);
-		if (tn > best.t) {
-			continue;
-		}
-		WideNode n = load.node(inst.nodes, ni);
-		int32_t cidx[kWideArity];
-		float ctn[kWideArity];
-		int nc = 0;
-		int internalRank = 0;
-		for (int i = 0; i < kWideArity; ++i) {
-			bool isInternal = (n.imask >> i) & 1u;
-			uint8_t meta = n.meta[i];
-			if (!isInternal && meta == 0) {
-				continue;
-			}
-			float lx, ly, lz, hx, hy, hz;
-			childBox(n, i, lx, ly, lz, hx, hy, hz);
-			float te = slabEnter(br, lx, ly, lz, hx, hy, hz, best.t);
-			if (isInternal) {
-				int32_t child = (int32_t) n.childBase + internalRank;
-				++internalRank;
-				if (te >= 0.0f) {
-					// insertion by ascending entry distance
-					int k = nc++;
-					while (k > 0 && ctn[k - 1] > te) {
-						ctn[k] = ctn[k - 1];
-						cidx[k] = cidx[k - 1];
-						--k;
-					}
-					ctn[k] = te;
-					cidx[k] = child;
-				}
-			} else if (te >= 0.0f) {
-				int first = (int) n.triBase + (meta & 31);
-				int cnt = meta >> 5;
-				for (int k = 0; k < cnt; ++k) {
-					TriRecord tr = load.tri(inst.tris, first + k);
-					float t;
-					if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), o, wt,
-					                      best.t, t)) {
-						best.t = t;
-						best.inst = instIdx;
-						best.tri = first + k;
-					}
+	const Watertight wt = setupWatertight(d);
+	const Vec3 inv = {safeInv(d.x), safeInv(d.y), safeInv(d.z)};
+	const bool negx = inv.x < 0.0f, negy = inv.y < 0.0f, negz = inv.z < 0.0f;
+	const uint32_t oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);
+	const int base = st.size();
+	uint32_t node = 0;
+	for (;;) {
+		uint4 w0, w1, w2, w3, w4;
+		load.nodeWords(inst.nodes, node, w0, w1, w2, w3, w4);
+		const float sx = exp2Byte((uint8_t) (w0.w & 0xffu)), sy = exp2Byte((uint8_t) ((w0.w >> 8) & 0xffu)),
+		            sz = exp2Byte((uint8_t) ((w0.w >> 16) & 0xffu));
+		const uint32_t imask = w0.w >> 24;
+		const uint32_t childBase = w1.x, triBase = w1.y;
+		const float Ax = sx * inv.x, Ay = sy * inv.y, Az = sz * inv.z;
+		const float Cx = (asFloat(w0.x) - o.x) * inv.x, Cy = (asFloat(w0.y) - o.y) * inv.y, Cz = (asFloat(w0.z) - o.z) * inv.z;
+		// near/far quantised planes per axis (packed bytes), swapped for negative directions
+		const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y, fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
+		const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w, fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
+		const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y, fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
+		uint32_t internalHits = 0, leafHits = 0; // both indexed by traversal order j (slot = j ^ oct)
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+		for (int s = 0; s < kWideArity; ++s) {
+			const int sh = (s & 3) * 8;
+			const bool hiw = s >= 4;
+			const float tnx = fmaf(byteF(hiw ? nx1 : nx0, sh), Ax, Cx), tfx = fmaf(byteF(hiw ? fx1 : fx0, sh), Ax, Cx);
+			const float tny = fmaf(byteF(hiw ? ny1 : ny0, sh), Ay, Cy), tfy = fmaf(byteF(hiw ? fy1 : fy0, sh), Ay, Cy);
+			const float tnz = fmaf(byteF(hiw ? nz1 : nz0, sh), Az, Cz), tfz = fmaf(byteF(hiw ? fz1 : fz0, sh), Az, Cz);
+			const float tEntry = maxf_(maxf_(tnx, tny), maxf_(tnz, 0.0f));
+			const float tExit = minf_(minf_(tfx, tfy), minf_(tfz, best.t));
+			if (tEntry <= tExit * kSlabRelSlack) {
+				if ((imask >> s) & 1u) {
+					internalHits |= 1u << (s ^ oct);
+				} else {
+					leafHits |= 1u << (s ^ oct);
 				}
 			}
 		}
-		for (int k = nc - 1; k >= 0; --k) {
-			if (ctn[k] <= best.t) {
-				st.push(cidx[k], ctn[k]);
+		// Triangles of hit leaf children, in ray order.
+		const uint32_t metaLo = w1.z, metaHi = w1.w;
+		while (leafHits) {
+			const uint32_t s = lowestBit(leafHits) ^ oct;
+			leafHits &= leafHits - 1u;
+			const uint32_t meta = ((s < 4 ? metaLo : metaHi) >> ((s & 3) * 8)) & 0xffu;
+			const int first = (int) triBase + (int) (meta & 31u);
+			const int cnt = (int) (meta >> 5);
+			for (int k = 0; k < cnt; ++k) {
+				TriRecord tr = load.tri(inst.tris, first + k);
+				float t;
+				if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), o, wt,
+				                      best.t, t)) {
+					best.t = t;
+					best.inst = instIdx;
+					best.tri = first + k;
+				}
 			}
 		}
+		uint32_t groupBase = childBase, groupMask = imask, hits = internalHits;
+		if (hits == 0) {
+			if (st.size() == base) {
+				break;
+			}
+			uint32_t b;
+			st.pop(groupBase, b);
+			groupMask = b & 0xffu;
+			hits = b >> 8;
+		}
+		const uint32_t s = lowestBit(hits) ^ oct;
+		hits &= hits - 1u;
+		if (hits) {
+			st.push(groupBase, groupMask | (hits << 8));
+		}
+		node = groupBase + (uint32_t) popc8(groupMask & ((1u << s) - 1u));
 	}
 }
 
@@ -250,33 +310,31 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 o, Vec3 d, float tmax, Stac
 	if (sc.nInstances <= 0) {
 		return best;
 	}
-	BoxRay br = makeBoxRay(o, d);
-	int base = st.size();
-	// TLAS entries: value >= 0 internal node, value < 0 instance ~value.
-	st.push(sc.nInstances == 1 ? ~0 : 0, 0.0f);
+	const BoxRay br = makeBoxRay(o, d);
+	const int base = st.size();
+	// TLAS entries: (value >= 0 internal node | value < 0 instance ~value, entry distance bits).
+	st.push((uint32_t) (sc.nInstances == 1 ? ~0 : 0), 0u);
 	while (st.size() > base) {
-		int32_t e;
-		float tn;
-		st.pop(e, tn);
-		if (tn > best.t) {
+		uint32_t ev, tb;
+		st.pop(ev, tb);
+		const int32_t e = (int32_t) ev;
+		if (asFloat(tb) > best.t) {
 			continue;
 		}
 		if (e < 0) {
-			int32_t ii = ~e;
+			const int32_t ii = ~e;
 			const InstanceRec& inst = load.instance(sc.instances, ii);
-			Vec3 oo = inst.worldToObject.point(o);
-			Vec3 dd = inst.worldToObject.vector(d);
-			traverseBlas(inst, ii, oo, dd, st, best, load);
+			traverseBlas(inst, ii, inst.worldToObject.point(o), inst.worldToObject.vector(d), st, best, load);
 			continue;
 		}
-		BinNode bn = load.bin(sc.tlas, e);
-		int32_t ch[2] = {bn.left, bn.right};
+		const BinNode bn = load.bin(sc.tlas, e);
+		const int32_t ch[2] = {bn.left, bn.right};
 		float te[2];
 		for (int k = 0; k < 2; ++k) {
-			int32_t c = ch[k];
+			const int32_t c = ch[k];
 			float lx, ly, lz, hx, hy, hz;
 			if (c >= 0) {
-				BinNode cn = load.bin(sc.tlas, c);
+				const BinNode cn = load.bin(sc.tlas, c);
 				lx = cn.lox;
 				ly = cn.loy;
 				lz = cn.loz;
@@ -294,13 +352,11 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 o, Vec3 d, float tmax, Stac
 			}
 			te[k] = slabEnter(br, lx, ly, lz, hx, hy, hz, best.t);
 		}
-		// push far child first
-		bool swap = te[1] >= 0.0f && te[0] >= 0.0f && te[1] < te[0];
-		int firstK = swap ? 0 : 1;
+		const int farK = (te[0] >= 0.0f && te[1] >= 0.0f && te[1] < te[0]) ? 0 : 1;
 		for (int q = 0; q < 2; ++q) {
-			int k = (q == 0) ? firstK : 1 - firstK;
+			const int k = (q == 0) ? farK : 1 - farK;
 			if (te[k] >= 0.0f) {
-				st.push(ch[k], te[k]);
+				st.push((uint32_t) ch[k], asUint(te[k]));
 			}
 		}
 	}

@@ -131,32 +131,44 @@ Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
 
 struct HostStack
 {
-	int32_t idx[512];
-	float tn[512];
+	uint32_t a[512], b[512];
 	int sp = 0;
+	int maxDepth = 0;
 	bool overflow = false;
-	void push(int32_t i, float t)
+	void push(uint32_t x, uint32_t y)
 	{
 		if (sp >= 512) {
 			overflow = true;
 			return;
 		}
-		idx[sp] = i;
-		tn[sp] = t;
+		a[sp] = x;
+		b[sp] = y;
 		++sp;
+		maxDepth = std::max(maxDepth, sp);
 	}
-	void pop(int32_t& i, float& t)
+	void pop(uint32_t& x, uint32_t& y)
 	{
 		--sp;
-		i = idx[sp];
-		t = tn[sp];
+		x = a[sp];
+		y = b[sp];
 	}
 	int size() const { return sp; }
 };
 
+int gNodeVisits = 0;
+
 struct HostLoader
 {
-	WideNode node(const WideNode* base, int32_t i) const { return base[i]; }
+	void nodeWords(const WideNode* base, uint32_t i, uint4& w0, uint4& w1, uint4& w2, uint4& w3, uint4& w4) const
+	{
+		++gNodeVisits;
+		const uint4* p = reinterpret_cast<const uint4*>(base + i);
+		w0 = p[0];
+		w1 = p[1];
+		w2 = p[2];
+		w3 = p[3];
+		w4 = p[4];
+	}
 	TriRecord tri(const TriRecord* base, int32_t i) const { return base[i]; }
 	const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
 	BinNode bin(const BinNode* base, int32_t i) const { return base[i]; }
@@ -165,6 +177,12 @@ struct HostLoader
 } // namespace
 
 extern "C" {
+
+// Largest number of wide-node visits of a single ray in the last harness_cast call.
+int gMaxNodeVisits = 0;
+long gTotalNodeVisits = 0;
+int harness_max_node_visits() { return gMaxNodeVisits; }
+long harness_total_node_visits() { return gTotalNodeVisits; }
 
 // Builds BLASes for `nMeshes` meshes and a TLAS over `nInst` instances, then casts `nRays` world
 // rays (origin, direction, tmax: 7 floats each). Outputs per ray: t, instance, original triangle id.
@@ -232,11 +250,16 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	SceneView sv{tlas.data(), inst.data(), nInst, 0};
 	HostLoader ld;
 	bool overflow = false;
+	gMaxNodeVisits = 0;
+	gTotalNodeVisits = 0;
 	for (int r = 0; r < nRays; ++r) {
 		const float* p = rays + 7 * r;
 		HostStack st;
+		gNodeVisits = 0;
 		HitRec h = traceClosest(sv, v3(p[0], p[1], p[2]), v3(p[3], p[4], p[5]), p[6], st, ld);
 		overflow = overflow || st.overflow;
+		gMaxNodeVisits = std::max(gMaxNodeVisits, gNodeVisits);
+		gTotalNodeVisits += gNodeVisits;
 		outT[r] = h.t;
 		outInst[r] = h.inst;
 		outPrim[r] = h.inst >= 0 ? inst[h.inst].tris[h.tri].primId : -1;

@@ -78,3 +78,15 @@ def test_harness_single_triangle_and_degenerate(harness):
     t, inst, dlen, _ = cast(harness, sc, rays, 100.0)
     assert inst[0] == 0 and t[0] == np.float32(5.0)
     assert inst[1] == -1
+
+
+def test_axis_parallel_rays_stay_cheap(harness):
+    """Rays with exact-zero direction components (azimuth 0/90/180/270 deg, vertical rays) must not
+    degrade into visiting the whole BVH: the slab test keeps such axes exact."""
+    scene = scenes.million_scene()
+    rays = scenes.lidar_rays(16, 4)  # azimuths 0, 90, 180, 270 deg
+    straight_down = scenes.rotation_xyz(np.pi, 0, 0)  # local +Z -> world -Z
+    rays = np.concatenate([rays, straight_down[None]])
+    rays[:, :, 3] = (0.0, 0.0, 6.0)
+    cast(harness, scene, rays, 100.0)
+    assert harness.harness_max_node_visits() < 3000
