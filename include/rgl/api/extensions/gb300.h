@@ -44,3 +44,23 @@ RGL_API rgl_status_t rgl_gb300_scene_get_stats(int64_t* out_node_bytes, int64_t*
 
 /* SM count and compute capability (major * 10 + minor) of the device in use. */
 RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_compute_capability);
+
+/*
+ * Compaction for callers that cannot allocate device memory. No counterpart in the reference API.
+ *
+ * Engines that give the library only buffers they pre-allocated from their own pool, and real-time
+ * loops that must never enter the CUDA allocator (cudaMalloc/cudaFree may synchronise the device),
+ * cannot use the graph API's compaction: it allocates its look-back scratch on first use. This call
+ * keeps that scratch in a fixed array inside the library and calls no cudaMalloc, cudaFree or
+ * allocating routine. It copies the elements of `src` whose int32 flag is non-zero, in order, to `dst`:
+ *   flags, src, dst   device pointers: `count` flags, `count * element_size` bytes in, room for as many out
+ *   out_count         host pointer, receives the number of elements kept
+ *   stream            a cudaStream_t, or NULL for the default stream; the call waits for its work on it
+ * Limits: count <= 16,777,216 (larger counts return RGL_INVALID_ARGUMENT), element_size 1..256 bytes.
+ * The fixed array (65,548 bytes) stays resident on every device that loads the library until exit.
+ * The first call on a device looks up the array's device address, so make it before any stream capture.
+ * All calls share the array and clear what they use when they start; calls whose GPU work overlaps
+ * (other streams or host threads) race on it and must be serialised by the caller.
+ */
+RGL_API rgl_status_t rgl_gb300_compact_by_flags_noalloc(const int32_t* flags, const void* src, int32_t count,
+                                                        int32_t element_size, void* dst, int32_t* out_count, void* stream);

@@ -1046,3 +1046,31 @@ RGL_API rgl_status_t rgl_gb300_scene_get_stats(int64_t* out_node_bytes, int64_t*
 		}
 	});
 }
+
+// Allocation-free compaction (include/rgl/api/extensions/gb300.h). Status handling as safeCall() but
+// without its first-call CUDA initialisation, which calls cudaFree(nullptr): this entry point uses the
+// caller's current device and context as they are.
+RGL_API rgl_status_t rgl_gb300_compact_by_flags_noalloc(const int32_t* flags, const void* src, int32_t count,
+                                                        int32_t element_size, void* dst, int32_t* out_count, void* stream)
+{
+	if (!recoverable(lastStatus)) {
+		return updateState(RGL_INVALID_STATE);
+	}
+	try {
+		CHECK_ARG(out_count != nullptr);
+		*out_count = compactNoAlloc(flags, src, count, element_size, dst, static_cast<cudaStream_t>(stream));
+	}
+	catch (InvalidAPIObject& e) {
+		return updateState(RGL_INVALID_API_OBJECT, std::string(e.what()));
+	}
+	catch (std::invalid_argument& e) {
+		return updateState(RGL_INVALID_ARGUMENT, std::string(e.what()));
+	}
+	catch (std::exception& e) {
+		return updateState(RGL_INTERNAL_EXCEPTION, std::string(e.what()));
+	}
+	catch (...) {
+		return updateState(RGL_INTERNAL_EXCEPTION, std::string("exceptional exception"));
+	}
+	return updateState(RGL_SUCCESS);
+}

@@ -96,3 +96,11 @@ void launchFormat(const FieldCopies& fields, int pointSize, int cap, const int32
 void launchAosToSoa(const uint8_t* in, int pointSize, int n, const FieldCopies& fields, cudaStream_t s);
 
 } // namespace rgl
+
+// ---- noalloc.cu: compaction whose scratch is a fixed device array (no allocation by the call)
+namespace rgl {
+constexpr int kNoAllocMaxPoints = 1 << 24;
+// Stable compaction of `count` elements of `elementSize` bytes from src to dst (device pointers) by
+// int32 flags; waits for completion on `stream` and returns the kept count.
+int32_t compactNoAlloc(const int32_t* flags, const void* src, int32_t count, int32_t elementSize, void* dst, cudaStream_t stream);
+} // namespace rgl

@@ -183,6 +183,7 @@ def _proto(l):
         "rgl_gb300_graph_sync": [vp],
         "rgl_gb300_device_info": [P(i32), P(i32)],
         "rgl_gb300_scene_get_stats": [P(C.c_int64), P(C.c_int64), P(i32)],
+        "rgl_gb300_compact_by_flags_noalloc": [vp, vp, i32, i32, vp, P(i32), vp],
     }
     for name, args in sigs.items():
         fn = getattr(l, name)
