@@ -30,6 +30,16 @@ RGL_API rgl_status_t rgl_gb300_configure_timing(bool enable);
 /* Device time of the last completed run of the node's graph, in milliseconds (timing enabled). */
 RGL_API rgl_status_t rgl_gb300_graph_get_timing(rgl_node_t node, float* out_run_ms, float* out_trace_ms);
 
+/*
+ * Enables or disables CUDA-graph execution of graph runs (default: enabled, or disabled by the
+ * environment variable RGL_GB300_CUDA_GRAPH=0). When enabled, a run's device work is captured into a
+ * CUDA graph once and replayed by later runs until a node's parameters, links or buffers change.
+ */
+RGL_API rgl_status_t rgl_gb300_configure_cuda_graphs(bool enable);
+
+/* Number of captures and replays performed for the node's graph so far. */
+RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t* out_captures, int64_t* out_replays);
+
 /* Waits until the last run of the node's graph completed (rgl_graph_get_result_* also wait). */
 RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node);
 

@@ -179,6 +179,9 @@ void createOrUpdateNode(rgl_node_t* handle, const char* typeName, Setter&& set)
 	}
 	set(*node);
 	node->dirty = true;
+	if (!node->lastUpdateContentOnly()) {
+		node->captureStale = true;
+	}
 	if (*handle == nullptr) {
 		*handle = Nodes::add(node);
 	}
@@ -681,6 +684,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_non_hits(rgl_node_t node, float
 			n->ctx->synchronize();
 		}
 		n->setNonHits(nearDistance, farDistance);
+		n->captureStale = true;
 	});
 }
 
@@ -706,6 +710,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_beam_divergence(rgl_node_t node
 			n->ctx->synchronize();
 		}
 		n->setBeamDivergence(horizontal_beam_divergence, vertical_beam_divergence);
+		n->captureStale = true;
 	});
 }
 
@@ -719,6 +724,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_default_intensity(rgl_node_t no
 			n->ctx->synchronize();
 		}
 		n->setDefaultIntensity(default_intensity);
+		n->captureStale = true;
 	});
 }
 
@@ -733,6 +739,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_return_mode(rgl_node_t node, rg
 		}
 		n->setReturnMode((int32_t) return_mode);
 		n->dirty = true;
+		n->captureStale = true;
 	});
 }
 
@@ -941,6 +948,7 @@ RGL_API rgl_status_t rgl_gb300_node_gaussian_noise_set_seed(rgl_node_t node, uin
 		if (n->ctx) {
 			n->ctx->synchronize();
 		}
+		n->captureStale = true;
 		if (auto a = std::dynamic_pointer_cast<GaussianNoiseAngularRaysNode>(n)) {
 			a->setSeed(seed, frame);
 		} else if (auto b = std::dynamic_pointer_cast<GaussianNoiseAngularHitpointNode>(n)) {
@@ -965,6 +973,7 @@ RGL_API rgl_status_t rgl_gb300_node_raytrace_configure_beam_samples(rgl_node_t n
 			n->ctx->synchronize();
 		}
 		n->setBeamSamples(layers, vertices);
+		n->captureStale = true;
 	});
 }
 
@@ -1073,4 +1082,26 @@ RGL_API rgl_status_t rgl_gb300_compact_by_flags_noalloc(const int32_t* flags, co
 		return updateState(RGL_INTERNAL_EXCEPTION, std::string("exceptional exception"));
 	}
 	return updateState(RGL_SUCCESS);
+}
+
+RGL_API rgl_status_t rgl_gb300_configure_cuda_graphs(bool enable)
+{
+	return safeCall([&]() {
+		GraphRunCtx::synchronizeAll();
+		setCudaGraphsEnabled(enable);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t* out_captures, int64_t* out_replays)
+{
+	return safeCall([&]() {
+		CHECK_ARG(node != nullptr);
+		auto n = getNode(node);
+		if (out_captures) {
+			*out_captures = n->ctx ? (int64_t) n->ctx->captures : 0;
+		}
+		if (out_replays) {
+			*out_replays = n->ctx ? (int64_t) n->ctx->replays : 0;
+		}
+	});
 }

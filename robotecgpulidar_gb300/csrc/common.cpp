@@ -161,12 +161,20 @@ void logMessage(LogLevel level, const std::string& msg)
 
 // ---------------------------------------------------------------- buffers
 
+namespace {
+std::atomic<uint64_t> allocEpoch{0};
+}
+uint64_t allocationEpoch() { return allocEpoch.load(std::memory_order_relaxed); }
+
 DeviceBuffer::~DeviceBuffer() { release(); }
 
 void DeviceBuffer::release()
 {
 	if (ptr_) {
 		cudaFree(ptr_);
+		if (tracked_) {
+			allocEpoch.fetch_add(1, std::memory_order_relaxed);
+		}
 	}
 	ptr_ = nullptr;
 	cap_ = 0;
@@ -185,6 +193,9 @@ void* DeviceBuffer::ensure(size_t bytes)
 	}
 	ptr_ = p;
 	cap_ = want;
+	if (tracked_) {
+		allocEpoch.fetch_add(1, std::memory_order_relaxed);
+	}
 	return ptr_;
 }
 

@@ -68,11 +68,18 @@ void logMessage(LogLevel level, const std::string& msg);
 
 // ---- device memory
 
+// Incremented whenever any DeviceBuffer changes its device address; a captured CUDA graph of a run is
+// replayed only while this value is unchanged.
+uint64_t allocationEpoch();
+
 // Grow-only device allocation owned by a node or scene.
 class DeviceBuffer
 {
 public:
 	DeviceBuffer() = default;
+	// A buffer that kernels reach only through another device-resident pointer (scene data behind the
+	// SceneView) does not invalidate captured runs when it moves.
+	explicit DeviceBuffer(bool affectsCapturedRuns) : tracked_(affectsCapturedRuns) {}
 	DeviceBuffer(const DeviceBuffer&) = delete;
 	DeviceBuffer& operator=(const DeviceBuffer&) = delete;
 	~DeviceBuffer();
@@ -90,6 +97,7 @@ public:
 private:
 	void* ptr_ = nullptr;
 	size_t cap_ = 0;
+	bool tracked_ = true;
 };
 
 // Grow-only pinned host allocation.

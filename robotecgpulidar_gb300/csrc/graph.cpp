@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 
@@ -14,9 +15,26 @@ using rgl::Mat34;
 
 namespace {
 bool gTiming = false;
-}
+bool gCudaGraphs = [] {
+	const char* v = std::getenv("RGL_GB300_CUDA_GRAPH");
+	return v == nullptr || std::string(v) != "0";
+}();
+} // namespace
 bool timingEnabled() { return gTiming; }
 void setTimingEnabled(bool on) { gTiming = on; }
+bool cudaGraphsEnabled() { return gCudaGraphs; }
+void setCudaGraphsEnabled(bool on) { gCudaGraphs = on; }
+
+void recordEvent(cudaEvent_t ev, cudaStream_t s)
+{
+	cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+	RGL_CHECK_CUDA(cudaStreamIsCapturing(s, &st));
+	if (st == cudaStreamCaptureStatusActive) {
+		RGL_CHECK_CUDA(cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal));
+	} else {
+		RGL_CHECK_CUDA(cudaEventRecord(ev, s));
+	}
+}
 
 // ================================================================ Node links
 // (reference src/graph/Node.cpp:23-215)
@@ -150,7 +168,9 @@ void RaysNodeSingleInput::validateImpl() { input = exactlyOneInput<RaysNode>("IR
 
 void FromMat3x4fRaysNode::setParameters(const rgl_mat3x4f* r, size_t n)
 {
+	const void* before = rays.get();
 	RGL_CHECK_CUDA(cudaMemcpy(rays.ensure(sizeof(rgl_mat3x4f) * n), r, sizeof(rgl_mat3x4f) * n, cudaMemcpyHostToDevice));
+	sameCount = (n == count) && (rays.get() == before);
 	count = n;
 }
 
@@ -161,11 +181,11 @@ void FromMat3x4fRaysNode::validateImpl()
 	}
 }
 
+void TransformRaysNode::prepareImpl(cudaStream_t) { out.ensure(sizeof(Mat34) * std::max<size_t>(1, rayCount())); }
+
 void TransformRaysNode::enqueueImpl(cudaStream_t s)
 {
-	size_t n = rayCount();
-	auto* o = static_cast<Mat34*>(out.ensure(sizeof(Mat34) * std::max<size_t>(1, n)));
-	rgl::launchTransformRays(input->raysDev(), o, (int) n, transform, s);
+	rgl::launchTransformRays(input->raysDev(), out.as<Mat34>(), (int) rayCount(), transform, s);
 }
 
 void SetRangeRaysNode::setParameters(const rgl_vec2f* r, size_t n)
@@ -202,10 +222,22 @@ void GaussianNoiseAngularRaysNode::setParameters(float m, float sd, rgl_axis_t a
 	axis = a;
 }
 
-static rgl::NoiseParams makeNoise(uint64_t seed, uint64_t frame, uint32_t kind, float mean, float sd, float rise, int axis,
-                                  const Mat34& lookAt)
+// Per-run noise frame: written to pinned host memory before the run and copied to the device by the
+// (possibly captured) enqueue, so replays of a captured run keep advancing it.
+static void stageFrame(rgl::PinnedBuffer& h, rgl::DeviceBuffer& d, uint64_t& frame)
 {
+	d.ensure(sizeof(uint64_t));
+	*static_cast<uint64_t*>(h.ensure(sizeof(uint64_t))) = frame;
+	++frame;
+}
+
+static rgl::NoiseParams makeNoise(uint64_t seed, uint64_t frame, uint32_t kind, float mean, float sd, float rise, int axis,
+                                  const Mat34& lookAt, const rgl::DeviceBuffer& dFrame, const rgl::PinnedBuffer& hFrame,
+                                  cudaStream_t s)
+{
+	RGL_CHECK_CUDA(cudaMemcpyAsync(dFrame.get(), hFrame.get(), sizeof(uint64_t), cudaMemcpyHostToDevice, s));
 	rgl::NoiseParams np{};
+	np.dFrame = dFrame.as<uint32_t>();
 	np.seedLo = (uint32_t) seed;
 	np.seedHi = (uint32_t) (seed >> 32);
 	np.frameLo = (uint32_t) frame;
@@ -220,13 +252,17 @@ static rgl::NoiseParams makeNoise(uint64_t seed, uint64_t frame, uint32_t kind, 
 	return np;
 }
 
+void GaussianNoiseAngularRaysNode::prepareImpl(cudaStream_t)
+{
+	out.ensure(sizeof(Mat34) * std::max<size_t>(1, rayCount()));
+	stageFrame(hFrame, dFrame, frame);
+}
+
 void GaussianNoiseAngularRaysNode::enqueueImpl(cudaStream_t s)
 {
-	size_t n = rayCount();
-	auto* o = static_cast<Mat34*>(out.ensure(sizeof(Mat34) * std::max<size_t>(1, n)));
 	Mat34 lookAt = rgl::inverse(input->cumulativeRayTransform());
-	rgl::launchNoiseAngularRay(input->raysDev(), o, (int) n, makeNoise(seed, frame, 1, mean, stDev, 0.0f, axis, lookAt), s);
-	++frame;
+	rgl::launchNoiseAngularRay(input->raysDev(), out.as<Mat34>(), (int) rayCount(),
+	                           makeNoise(seed, frame, 1, mean, stDev, 0.0f, axis, lookAt, dFrame, hFrame, s), s);
 }
 
 // ================================================================ points nodes
@@ -358,18 +394,25 @@ const void* RaytraceNode::fieldDev(rgl_field_t f)
 	return it->second.get();
 }
 
-void RaytraceNode::enqueueImpl(cudaStream_t s)
+void RaytraceNode::prepareImpl(cudaStream_t s)
 {
-	const size_t n = rays->rayCount();
-	const size_t cap = std::max<size_t>(1, (size_t) returnCount() * n);
+	const size_t cap = std::max<size_t>(1, (size_t) returnCount() * rays->rayCount());
 	for (auto f : fields) {
 		outputs[f].ensure(rgl::fieldSize(f) * cap);
 	}
 	for (auto it = outputs.begin(); it != outputs.end();) {
 		it = fields.count(it->first) ? std::next(it) : outputs.erase(it);
 	}
+	if (timingEnabled() && !evStart) {
+		RGL_CHECK_CUDA(cudaEventCreate(&evStart));
+		RGL_CHECK_CUDA(cudaEventCreate(&evStop));
+	}
 	scene->prepare(s);
+}
 
+void RaytraceNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t n = rays->rayCount();
 	rgl::TraceParams p{};
 	p.rays = rays->raysDev();
 	p.ranges = rays->rangesDev() ? rays->rangesDev() : defaultRange.as<float>();
@@ -401,17 +444,13 @@ void RaytraceNode::enqueueImpl(cudaStream_t s)
 	p.out.normal = static_cast<float*>(ptr(RGL_FIELD_NORMAL_VEC3_F32));
 	p.out.incidentAngle = static_cast<float*>(ptr(RGL_FIELD_INCIDENT_ANGLE_F32));
 	p.out.laserRetro = nullptr;
-	if (timingEnabled()) {
-		if (!evStart) {
-			RGL_CHECK_CUDA(cudaEventCreate(&evStart));
-			RGL_CHECK_CUDA(cudaEventCreate(&evStop));
-		}
-		RGL_CHECK_CUDA(cudaEventRecord(evStart, s));
+	if (timingEnabled() && evStart) {
+		recordEvent(evStart, s);
 	}
 	rgl::launchTrace(p, sampleTable.as<Mat34>(), s);
 	RGL_CHECK_CUDA(cudaGetLastError());
-	if (timingEnabled()) {
-		RGL_CHECK_CUDA(cudaEventRecord(evStop, s));
+	if (timingEnabled() && evStart) {
+		recordEvent(evStop, s);
 	}
 }
 
@@ -477,11 +516,12 @@ const void* FormatPointsNode::fieldDev(rgl_field_t f)
 	return input->fieldDev(f);
 }
 
+void FormatPointsNode::prepareImpl(cudaStream_t) { out.ensure(std::max<size_t>(1, rgl::pointSize(fields) * input->capacity())); }
+
 void FormatPointsNode::enqueueImpl(cudaStream_t s)
 {
 	const size_t ps = rgl::pointSize(fields);
 	const size_t cap = input->capacity();
-	out.ensure(std::max<size_t>(1, ps * cap));
 	if (fields.size() > (size_t) rgl::kMaxFieldCopies) {
 		throw rgl::InvalidAPIArgument(format("format of %zu fields exceeds %d", fields.size(), rgl::kMaxFieldCopies));
 	}
@@ -531,6 +571,17 @@ void CompactByFieldPointsNode::validateImpl()
 	}
 }
 
+void CompactByFieldPointsNode::sizeBuffers(const std::vector<rgl_field_t>& which)
+{
+	const size_t cap = input->capacity();
+	for (auto f : which) {
+		outputs[f].ensure(std::max<size_t>(1, rgl::fieldSize(f) * cap));
+	}
+	scratch.ensure(rgl::compactScratchBytes((int) cap));
+}
+
+void CompactByFieldPointsNode::prepareImpl(cudaStream_t) { sizeBuffers(std::vector<rgl_field_t>(eager.begin(), eager.end())); }
+
 void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cudaStream_t s)
 {
 	const size_t cap = input->capacity();
@@ -542,10 +593,9 @@ void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cu
 		rgl::FieldCopy c{};
 		c.size = (int32_t) rgl::fieldSize(f);
 		c.src = input->fieldDev(f);
-		c.dst = outputs[f].ensure(std::max<size_t>(1, c.size * cap));
+		c.dst = outputs[f].get();
 		fc.f[fc.count++] = c;
 	}
-	scratch.ensure(rgl::compactScratchBytes((int) cap));
 	rgl::launchCompact(static_cast<const int32_t*>(input->fieldDev(field)), (int) cap, input->deviceCount(), fc, count.as<int32_t>(),
 	                   scratch.get(), errorFlag.as<int32_t>(), s);
 }
@@ -566,6 +616,7 @@ const void* CompactByFieldPointsNode::fieldDev(rgl_field_t f)
 		throw InvalidPipeline(format("CompactByFieldPointsNode: input does not provide field %s", rgl::fieldName(f)));
 	}
 	// A field nobody downstream declared: compact it now on the graph's stream and wait for it.
+	sizeBuffers({f});
 	compact({f}, lastStream);
 	RGL_CHECK_CUDA(cudaStreamSynchronize(lastStream));
 	lazyDone.insert(f);
@@ -587,10 +638,11 @@ void CompactByFieldPointsNode::checkErrors()
 
 // ---- TransformPointsNode
 
+void TransformPointsNode::prepareImpl(cudaStream_t) { out.ensure(std::max<size_t>(1, 12 * input->capacity())); }
+
 void TransformPointsNode::enqueueImpl(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
-	out.ensure(std::max<size_t>(1, 12 * cap));
 	rgl::launchTransformPoints(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), out.as<float>(), (int) cap,
 	                           input->deviceCount(), transform, s);
 }
@@ -609,7 +661,7 @@ void GaussianNoiseAngularHitpointNode::setParameters(float m, float sd, rgl_axis
 	axis = a;
 }
 
-void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
+void GaussianNoiseAngularHitpointNode::prepareImpl(cudaStream_t)
 {
 	const size_t cap = input->capacity();
 	withDistance = input->hasField(RGL_FIELD_DISTANCE_F32);
@@ -617,10 +669,15 @@ void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
 	if (withDistance) {
 		outDist.ensure(std::max<size_t>(1, 4 * cap));
 	}
-	rgl::NoiseParams np = makeNoise(seed, frame, 2, mean, stDev, 0.0f, axis, input->lookAtOriginTransform());
+	stageFrame(hFrame, dFrame, frame);
+}
+
+void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t cap = input->capacity();
+	rgl::NoiseParams np = makeNoise(seed, frame, 2, mean, stDev, 0.0f, axis, input->lookAtOriginTransform(), dFrame, hFrame, s);
 	rgl::launchNoiseAngularHitpoint(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), outXyz.as<float>(),
 	                                withDistance ? outDist.as<float>() : nullptr, (int) cap, input->deviceCount(), np, s);
-	++frame;
 }
 
 const void* GaussianNoiseAngularHitpointNode::fieldDev(rgl_field_t f)
@@ -641,16 +698,21 @@ void GaussianNoiseDistanceNode::setParameters(float m, float b, float r)
 	rise = r;
 }
 
-void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
+void GaussianNoiseDistanceNode::prepareImpl(cudaStream_t)
 {
 	const size_t cap = input->capacity();
 	outXyz.ensure(std::max<size_t>(1, 12 * cap));
 	outDist.ensure(std::max<size_t>(1, 4 * cap));
-	rgl::NoiseParams np = makeNoise(seed, frame, 3, mean, base, rise, 0, input->lookAtOriginTransform());
+	stageFrame(hFrame, dFrame, frame);
+}
+
+void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
+{
+	const size_t cap = input->capacity();
+	rgl::NoiseParams np = makeNoise(seed, frame, 3, mean, base, rise, 0, input->lookAtOriginTransform(), dFrame, hFrame, s);
 	rgl::launchNoiseDistance(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)),
 	                         static_cast<const float*>(input->fieldDev(RGL_FIELD_DISTANCE_F32)), outXyz.as<float>(),
 	                         outDist.as<float>(), (int) cap, input->deviceCount(), np, s);
-	++frame;
 }
 
 const void* GaussianNoiseDistanceNode::fieldDev(rgl_field_t f)
@@ -730,6 +792,7 @@ GraphRunCtx::GraphRunCtx()
 
 GraphRunCtx::~GraphRunCtx()
 {
+	releaseGraph();
 	cudaEventDestroy(done);
 	cudaEventDestroy(runStart);
 	cudaEventDestroy(runStop);
@@ -782,22 +845,77 @@ std::vector<Node::Ptr> GraphRunCtx::findExecutionOrder(std::set<Node::Ptr> nodes
 	return {reverseOrder.rbegin(), reverseOrder.rend()};
 }
 
+void GraphRunCtx::releaseGraph()
+{
+	if (exec) {
+		cudaGraphExecDestroy(exec);
+		exec = nullptr;
+	}
+}
+
+// One run: validation and the prepare phase on the host, then the nodes' device work. The device
+// work is captured into a CUDA graph once and replayed by later runs while no node's kernel
+// parameters changed (captureStale) and no device buffer moved (allocation epoch); otherwise it is
+// captured again. With CUDA graphs disabled (RGL_GB300_CUDA_GRAPH=0) the work is enqueued directly.
 void GraphRunCtx::run()
 {
 	synchronize();
 	if (order.empty()) {
 		order = findExecutionOrder(nodes);
+		releaseGraph();
 	}
+	bool stale = false;
 	for (auto& n : order) {
 		n->validateImpl();
 		n->dirty = false;
+		stale = stale || n->captureStale;
 	}
 	running = true;
+	for (auto& n : order) {
+		n->prepareImpl(stream_);
+	}
 	if (timingEnabled()) {
 		RGL_CHECK_CUDA(cudaEventRecord(runStart, stream_));
 	}
-	for (auto& n : order) {
-		n->enqueueImpl(stream_);
+	if (!cudaGraphsEnabled()) {
+		releaseGraph();
+		for (auto& n : order) {
+			n->enqueueImpl(stream_);
+		}
+	} else {
+		if (stale || exec == nullptr || execEpoch != rgl::allocationEpoch()) {
+			releaseGraph();
+			const uint64_t launches0 = rgl::launchCount();
+			RGL_CHECK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+			try {
+				for (auto& n : order) {
+					n->enqueueImpl(stream_);
+				}
+			}
+			catch (...) {
+				cudaGraph_t partial = nullptr;
+				cudaStreamEndCapture(stream_, &partial);
+				if (partial) {
+					cudaGraphDestroy(partial);
+				}
+				throw;
+			}
+			cudaGraph_t graph = nullptr;
+			RGL_CHECK_CUDA(cudaStreamEndCapture(stream_, &graph));
+			const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+			cudaGraphDestroy(graph);
+			RGL_CHECK_CUDA(inst);
+			execKernels = rgl::launchCount() - launches0;
+			execEpoch = rgl::allocationEpoch();
+			++captures;
+			for (auto& n : order) {
+				n->captureStale = false;
+			}
+		} else {
+			++replays;
+			rgl::countLaunch(execKernels);
+		}
+		RGL_CHECK_CUDA(cudaGraphLaunch(exec, stream_));
 	}
 	if (timingEnabled()) {
 		RGL_CHECK_CUDA(cudaEventRecord(runStop, stream_));

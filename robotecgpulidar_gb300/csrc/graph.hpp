@@ -36,6 +36,10 @@ struct Node : std::enable_shared_from_this<Node>
 	std::set<Ptr> disconnectConnectedNodes();
 
 	virtual void validateImpl() = 0;
+	// Host-side work of a run that must not be captured into a CUDA graph: sizing buffers, scene
+	// builds and refits, per-run parameters. Runs before every run, in execution order.
+	virtual void prepareImpl(cudaStream_t) {}
+	// Enqueues the node's device work; must not allocate (it may be captured into a CUDA graph).
 	virtual void enqueueImpl(cudaStream_t s) = 0;
 	// Called after the graph's stream completed; throws if a kernel of this node raised its error flag.
 	virtual void checkErrors() {}
@@ -45,9 +49,14 @@ struct Node : std::enable_shared_from_this<Node>
 	template<class T>
 	std::shared_ptr<T> exactlyOneInput(const char* ifaceName);
 
+	// True when the last parameter update changed only device-buffer contents (same sizes), so a
+	// captured run stays valid.
+	virtual bool lastUpdateContentOnly() const { return false; }
+
 	std::vector<Ptr> inputs, outputs;
 	int32_t priority = 0;
 	bool dirty = true;
+	bool captureStale = true; // kernel parameters changed since the run was captured
 	std::shared_ptr<GraphRunCtx> ctx;
 };
 
@@ -83,16 +92,19 @@ struct FromMat3x4fRaysNode : RaysNode
 	void enqueueImpl(cudaStream_t) override {}
 	size_t rayCount() const override { return count; }
 	const rgl::Mat34* raysDev() const override { return rays.as<rgl::Mat34>(); }
+	bool lastUpdateContentOnly() const override { return sameCount; }
 
 private:
 	rgl::DeviceBuffer rays;
 	size_t count = 0;
+	bool sameCount = false;
 };
 
 struct TransformRaysNode : RaysNodeSingleInput
 {
 	const char* name() const override { return "TransformRaysNode"; }
 	void setParameters(const rgl::Mat34& tf) { transform = tf; }
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const rgl::Mat34* raysDev() const override { return out.as<rgl::Mat34>(); }
 	rgl::Mat34 cumulativeRayTransform() const override { return rgl::mul(transform, input->cumulativeRayTransform()); }
@@ -125,6 +137,7 @@ struct GaussianNoiseAngularRaysNode : RaysNodeSingleInput
 		seed = s;
 		frame = f;
 	}
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const rgl::Mat34* raysDev() const override { return out.as<rgl::Mat34>(); }
 
@@ -133,6 +146,8 @@ private:
 	rgl_axis_t axis = RGL_AXIS_X;
 	uint64_t seed = 0, frame = 0;
 	rgl::DeviceBuffer out;
+	rgl::PinnedBuffer hFrame;
+	rgl::DeviceBuffer dFrame;
 };
 
 // ---------------------------------------------------------------- points
@@ -174,6 +189,7 @@ struct RaytraceNode : PointsNode
 {
 	const char* name() const override { return "RaytraceNode"; }
 	void validateImpl() override;
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	bool isDense() const override { return false; }
 	bool hasField(rgl_field_t f) const override { return fields.count(f) != 0; }
@@ -242,6 +258,7 @@ struct FormatPointsNode : PointsNodeSingleInput
 	void setParameters(const std::vector<rgl_field_t>& f);
 	std::vector<rgl_field_t> requiredFields() const override { return fields; }
 	bool hasField(rgl_field_t f) const override;
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
 	size_t fieldPointSize(rgl_field_t f) const override;
@@ -257,6 +274,7 @@ struct CompactByFieldPointsNode : PointsNodeSingleInput
 	void setParameters(rgl_field_t f) { field = f; }
 	std::vector<rgl_field_t> requiredFields() const override { return {field}; }
 	void validateImpl() override;
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	bool isDense() const override { return true; }
 	const int32_t* deviceCount() const override { return count.as<int32_t>(); }
@@ -272,6 +290,7 @@ private:
 	rgl::DeviceBuffer scratch;
 	rgl::DeviceBuffer errorFlag;
 	cudaStream_t lastStream = nullptr;
+	void sizeBuffers(const std::vector<rgl_field_t>& which);
 	void compact(const std::vector<rgl_field_t>& which, cudaStream_t s);
 };
 
@@ -280,6 +299,7 @@ struct TransformPointsNode : PointsNodeSingleInput
 	const char* name() const override { return "TransformPointsNode"; }
 	void setParameters(const rgl::Mat34& tf) { transform = tf; }
 	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32}; }
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	rgl::Mat34 lookAtOriginTransform() const override
 	{
@@ -302,6 +322,7 @@ struct GaussianNoiseAngularHitpointNode : PointsNodeSingleInput
 		frame = f;
 	}
 	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32}; }
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
 
@@ -311,6 +332,8 @@ private:
 	uint64_t seed = 0, frame = 0;
 	bool withDistance = false;
 	rgl::DeviceBuffer outXyz, outDist;
+	rgl::PinnedBuffer hFrame;
+	rgl::DeviceBuffer dFrame;
 };
 
 struct GaussianNoiseDistanceNode : PointsNodeSingleInput
@@ -323,6 +346,7 @@ struct GaussianNoiseDistanceNode : PointsNodeSingleInput
 		frame = f;
 	}
 	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32, RGL_FIELD_DISTANCE_F32}; }
+	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
 
@@ -330,6 +354,8 @@ private:
 	float mean = 0, base = 0, rise = 0;
 	uint64_t seed = 0, frame = 0;
 	rgl::DeviceBuffer outXyz, outDist;
+	rgl::PinnedBuffer hFrame;
+	rgl::DeviceBuffer dFrame;
 };
 
 struct FromArrayPointsNode : PointsNode
@@ -365,15 +391,25 @@ struct GraphRunCtx : std::enable_shared_from_this<GraphRunCtx>
 
 	std::set<Node::Ptr> nodes;
 	float lastRunMs = 0.0f, lastTraceMs = 0.0f;
+	uint64_t captures = 0, replays = 0;
 
 private:
 	GraphRunCtx();
 	static std::vector<Node::Ptr> findExecutionOrder(std::set<Node::Ptr> nodes);
+	void releaseGraph();
 	std::vector<Node::Ptr> order;
 	cudaStream_t stream_ = nullptr;
 	cudaEvent_t done = nullptr, runStart = nullptr, runStop = nullptr;
 	bool running = false;
+	// Captured run: replayed while no node changed and no buffer moved.
+	cudaGraphExec_t exec = nullptr;
+	uint64_t execEpoch = 0;
+	uint64_t execKernels = 0;
 };
 
 bool timingEnabled();
 void setTimingEnabled(bool on);
+bool cudaGraphsEnabled();
+void setCudaGraphsEnabled(bool on);
+// Records `ev` on `s`; inside a stream capture the record becomes a node of the captured graph.
+void recordEvent(cudaEvent_t ev, cudaStream_t s);

@@ -59,6 +59,7 @@ struct NoiseParams
 {
 	uint32_t seedLo, seedHi;
 	uint32_t frameLo, frameHi;
+	const uint32_t* dFrame; // when set, frame lo/hi are read from device memory (changes between graph replays)
 	uint32_t kind;
 	float mean, stDev, stDevRise;
 	int32_t axis;

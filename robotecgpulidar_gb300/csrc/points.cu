@@ -61,7 +61,9 @@ __global__ void kTransformPoints(const float* __restrict__ in, float* __restrict
 
 __device__ __forceinline__ float noiseNormal(const NoiseParams& np, int i)
 {
-	return standardNormal(np.seedLo, np.seedHi, np.kind, (uint32_t) i, np.frameLo, np.frameHi);
+	const uint32_t lo = np.dFrame ? __ldg(np.dFrame) : np.frameLo;
+	const uint32_t hi = np.dFrame ? __ldg(np.dFrame + 1) : np.frameHi;
+	return standardNormal(np.seedLo, np.seedHi, np.kind, (uint32_t) i, lo, hi);
 }
 
 __device__ __forceinline__ Mat34 axisRotation(int axis, float angle)

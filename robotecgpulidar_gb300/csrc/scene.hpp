@@ -22,8 +22,8 @@ struct Mesh
 
 	int32_t vertexCount = 0;
 	int32_t triangleCount = 0;
-	rgl::DeviceBuffer dVertices;
-	rgl::DeviceBuffer dIndices;
+	rgl::DeviceBuffer dVertices{false};
+	rgl::DeviceBuffer dIndices{false};
 	rgl::BlasBuild blas;
 	bool blasBuilt = false;
 };
@@ -75,11 +75,11 @@ private:
 	std::vector<std::shared_ptr<Entity>> entities;
 	bool topologyDirty = true;
 	bool posesDirty = true;
-	rgl::DeviceBuffer dInstances;
+	rgl::DeviceBuffer dInstances{false};
 	rgl::PinnedBuffer hInstances;
-	rgl::DeviceBuffer dView;
+	rgl::DeviceBuffer dView; // fixed size: its address never changes once allocated
 	rgl::PinnedBuffer hView;
-	rgl::DeviceBuffer dError;
+	rgl::DeviceBuffer dError{false};
 	rgl::TlasBuild tlas;
 	cudaEvent_t ready = nullptr;
 	bool readyRecorded = false;
