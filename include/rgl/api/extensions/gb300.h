@@ -40,6 +40,14 @@ RGL_API rgl_status_t rgl_gb300_configure_cuda_graphs(bool enable);
 /* Number of captures and replays performed for the node's graph so far. */
 RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t* out_captures, int64_t* out_replays);
 
+/*
+ * Traversal schedule of graph runs (rgl_graph_run). Every raytrace runs on the persistent traversal
+ * kernel of batched frames as a one-job launch; this sets its block size (64, 128, 256), packing
+ * (0: a beam's sub-rays on adjacent lanes, 1: one lane per beam), tasks per fetch (1..64) and
+ * register budget (64, 80, 96, 128). The default is 256, 0, 1, 80. Changes speed only, never results.
+ */
+RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs);
+
 /* Waits until the last run of the node's graph completed (rgl_graph_get_result_* also wait). */
 RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node);
 
@@ -74,3 +82,108 @@ RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_c
  */
 RGL_API rgl_status_t rgl_gb300_compact_by_flags_noalloc(const int32_t* flags, const void* src, int32_t count,
                                                         int32_t element_size, void* dst, int32_t* out_count, void* stream);
+
+/*
+ * Batched multi-sensor frames. The reference has no batched form: every sensor's graph runs on its
+ * own with rgl_graph_run (src/api/apiCore.cpp:530-544).
+ *
+ * A batch is a list of ordinary graphs, given by any one node of each; each graph must hold exactly
+ * one raytrace node (the graphs may trace different scenes). rgl_gb300_batch_run runs one frame:
+ * every graph is validated and prepared as by rgl_graph_run, then one CUDA graph holds the frame's
+ * device work (instance upload and TLAS refit after rgl_entity_set_transform, every graph's nodes,
+ * and ONE persistent traversal launch over all sensors). It is captured on the first frame and
+ * replayed while nothing structural changes. Results are read per graph with
+ * rgl_graph_get_result_size/_data and equal what rgl_graph_run of that graph alone writes.
+ * At most 1024 graphs per batch. Destroy a batch before destroying its graphs.
+ */
+typedef struct BatchRun* rgl_gb300_batch_t;
+
+RGL_API rgl_status_t rgl_gb300_batch_create(rgl_gb300_batch_t* out_batch, const rgl_node_t* nodes, int32_t node_count);
+RGL_API rgl_status_t rgl_gb300_batch_run(rgl_gb300_batch_t batch);
+RGL_API rgl_status_t rgl_gb300_batch_destroy(rgl_gb300_batch_t batch);
+
+/*
+ * Traversal schedule of a batch. With `autotune` (the default) the library times a staged set of
+ * candidates on the first frame of every new batch shape (per-graph ray and sample counts) and keeps
+ * the fastest; otherwise the given schedule is used:
+ *   block    threads per block: 64, 128 or 256
+ *   packing  0: a beam's sub-rays on adjacent lanes; 1: one lane per beam, sub-rays in turn
+ *   order    beam visiting order. 0: as given; 1: sorted by octahedral direction; 2: by Morton code
+ *   chunk    tasks (one warp's beams each) taken per fetch from the shared work counter, 1..64
+ *   regs     registers per thread: 64, 80, 96 or 128 (fewer registers, more resident warps)
+ * The schedule changes speed only, never results.
+ */
+RGL_API rgl_status_t rgl_gb300_batch_configure_schedule(rgl_gb300_batch_t batch, bool autotune, int32_t block, int32_t packing,
+                                                        int32_t order, int32_t chunk, int32_t regs);
+RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32_t* out_block, int32_t* out_packing,
+                                                  int32_t* out_order, int32_t* out_chunk, int32_t* out_regs);
+
+/*
+ * Statistics of a batch: device time of the last completed frame and of its traversal launch (ms),
+ * beams and traced rays (beams x sub-rays) of the last frame, and the number of captures, replays and
+ * tunings so far. Waits for the last frame.
+ */
+RGL_API rgl_status_t rgl_gb300_batch_get_stats(rgl_gb300_batch_t batch, float* out_frame_ms, float* out_trace_ms, int64_t* out_beams,
+                                               int64_t* out_rays, int64_t* out_captures, int64_t* out_replays, int64_t* out_tunings);
+
+/*
+ * Resident scenes. The reference accepts only NULL (its one default scene) wherever an rgl_scene_t is
+ * passed (src/api/apiCore.cpp:297,516,922). This build also accepts scenes made here: rgl_entity_create,
+ * rgl_scene_set_time and rgl_node_raytrace take them, and NULL keeps meaning the default scene. Meshes
+ * (and their acceleration structures) are shared by all scenes. Destroying a scene destroys its
+ * entities; raytrace nodes that trace it keep an empty scene.
+ */
+RGL_API rgl_status_t rgl_gb300_scene_create(rgl_scene_t* out_scene);
+RGL_API rgl_status_t rgl_gb300_scene_destroy(rgl_scene_t scene);
+/* As rgl_gb300_scene_get_stats, for any scene (NULL: the default scene). */
+RGL_API rgl_status_t rgl_gb300_scene_get_stats_of(rgl_scene_t scene, int64_t* out_node_bytes, int64_t* out_triangle_bytes,
+                                                 int32_t* out_instances);
+
+/*
+ * Serving loop. No counterpart in the reference, whose clients run one rgl_graph_run per scan.
+ *
+ * Robots register their ray patterns (sensor-local rgl_mat3x4f rays, as for rgl_node_rays_from_mat3x4f)
+ * once; the patterns stay on the device. A scan request names a scene, a pattern, the sensor pose,
+ * a return mode and a range. A scheduler thread admits requests first come first served while the
+ * bytes of admitted requests (24 B per point while on the GPU, 20 B per point until released, points =
+ * rays x returns) stay within `hbm_budget_bytes` and fewer than `max_in_flight_batches` batches run,
+ * and launches all admitted requests as one batch (one persistent traversal launch plus one segmented
+ * compaction). Requests arriving meanwhile go into the next batch (continuous batching).
+ *
+ * A request's result is XYZ_VEC3_F32, DISTANCE_F32 and ENTITY_ID_I32 of its hit points, in point order:
+ * the same bytes as the graph rays_from_mat3x4f(pattern) -> rays_transform(pose) ->
+ * rays_set_range({min, max}) -> raytrace(scene, mode) -> points_compact_by_field(IS_HIT) -> yield.
+ * Scenes used by a server must not be modified while it has requests (rgl_gb300_server_drain first).
+ */
+typedef struct Server* rgl_gb300_server_t;
+
+RGL_API rgl_status_t rgl_gb300_server_create(rgl_gb300_server_t* out_server, int64_t hbm_budget_bytes, int32_t max_in_flight_batches);
+RGL_API rgl_status_t rgl_gb300_server_destroy(rgl_gb300_server_t server);
+RGL_API rgl_status_t rgl_gb300_server_add_pattern(rgl_gb300_server_t server, const rgl_mat3x4f* rays, int32_t ray_count,
+                                                  int32_t* out_pattern);
+RGL_API rgl_status_t rgl_gb300_server_submit(rgl_gb300_server_t server, rgl_scene_t scene, int32_t pattern,
+                                             const rgl_mat3x4f* sensor_pose, rgl_return_mode_t return_mode, float min_range,
+                                             float max_range, int64_t* out_request);
+/* Waits up to timeout_ms (negative: without limit) for a request; *out_done tells whether it completed. */
+RGL_API rgl_status_t rgl_gb300_server_wait(rgl_gb300_server_t server, int64_t request, float timeout_ms, bool* out_done);
+/* Moves up to `capacity` ids of requests completed since the last call into out_requests. */
+RGL_API rgl_status_t rgl_gb300_server_take_completed(rgl_gb300_server_t server, int64_t* out_requests, int32_t capacity,
+                                                     int32_t* out_count);
+/* As rgl_gb300_server_take_completed, but first waits up to timeout_ms for a completed request. */
+RGL_API rgl_status_t rgl_gb300_server_wait_completed(rgl_gb300_server_t server, float timeout_ms, int64_t* out_requests, int32_t capacity,
+                                                     int32_t* out_count);
+RGL_API rgl_status_t rgl_gb300_server_get_result_size(rgl_gb300_server_t server, int64_t request, rgl_field_t field,
+                                                      int32_t* out_count, int32_t* out_size_of);
+RGL_API rgl_status_t rgl_gb300_server_get_result_data(rgl_gb300_server_t server, int64_t request, rgl_field_t field, void* out_data);
+/* Seconds from submission to admission into a batch, and from submission to completion. */
+RGL_API rgl_status_t rgl_gb300_server_get_request_timing(rgl_gb300_server_t server, int64_t request, double* out_queued_s,
+                                                         double* out_total_s);
+/* Frees a completed request's result (waits for it first if it is still running). */
+RGL_API rgl_status_t rgl_gb300_server_release(rgl_gb300_server_t server, int64_t request);
+/* Waits until no request is pending or running. */
+RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server);
+/* Counters: requests submitted, completed (including failed), failed; batches launched and the requests
+ * they held; the largest admitted byte total. */
+RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64_t* out_submitted, int64_t* out_completed,
+                                                int64_t* out_failed, int64_t* out_batches, int64_t* out_requests_in_batches,
+                                                int64_t* out_peak_reserved_bytes);

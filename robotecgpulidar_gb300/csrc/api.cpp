@@ -6,6 +6,7 @@
 // latches RGL_INVALID_STATE after an unrecoverable error. Argument checks produce the reference's
 // message "RGL API Error: Invalid argument, condition unsatisfied: <expression>"; unknown handles
 // produce "RGL API Error: Object does not exist: <Type> <pointer>".
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <optional>
@@ -17,6 +18,8 @@
 #include <rgl/api/extensions/gb300.h>
 #include <rgl/api/extensions/tape.h>
 
+#include "batch.hpp"
+#include "serve.hpp"
 #include "graph.hpp"
 #include "scene.hpp"
 
@@ -150,6 +153,19 @@ using Nodes = Registry<Node>;
 using Meshes = Registry<Mesh>;
 using Entities = Registry<Entity>;
 using Textures = Registry<Texture>;
+using Batches = Registry<BatchRun>;
+using Servers = Registry<Server>;
+using Scenes = Registry<Scene>; // scenes made by rgl_gb300_scene_create (NULL is the default scene)
+
+// The scene behind a handle: NULL is the default scene, as in the reference; other handles come from
+// rgl_gb300_scene_create. The returned pointer keeps a created scene alive for nodes that trace it.
+std::shared_ptr<Scene> sceneOf(rgl_scene_t scene)
+{
+	if (scene == nullptr) {
+		return std::shared_ptr<Scene>(&Scene::defaultScene(), [](Scene*) {});
+	}
+	return Scenes::get(scene, "Scene");
+}
 
 std::shared_ptr<Node> getNode(rgl_node_t n) { return Nodes::get(n, "Node"); }
 
@@ -180,7 +196,7 @@ void createOrUpdateNode(rgl_node_t* handle, const char* typeName, Setter&& set)
 	set(*node);
 	node->dirty = true;
 	if (!node->lastUpdateContentOnly()) {
-		node->captureStale = true;
+		node->markParamsChanged();
 	}
 	if (*handle == nullptr) {
 		*handle = Nodes::add(node);
@@ -260,6 +276,8 @@ RGL_API void rgl_get_last_error_string(const char** out_error_string)
 RGL_API rgl_status_t rgl_cleanup(void)
 {
 	return safeCall([&]() {
+		Batches::map().clear();
+		Servers::map().clear();
 		while (!Nodes::map().empty()) {
 			auto node = Nodes::map().begin()->second;
 			releaseGraph(node);
@@ -268,6 +286,11 @@ RGL_API rgl_status_t rgl_cleanup(void)
 			c->detachAndDestroy();
 		}
 		Scene::defaultScene().clear();
+		for (auto& kv : Scenes::map()) {
+			kv.second->clear();
+			kv.second->releaseDevice();
+		}
+		Scenes::map().clear();
 		Entities::map().clear();
 		Meshes::map().clear();
 		Textures::map().clear();
@@ -344,12 +367,11 @@ RGL_API rgl_status_t rgl_entity_create(rgl_entity_t* out_entity, rgl_scene_t sce
 	return safeCall([&]() {
 		CHECK_ARG(out_entity != nullptr);
 		CHECK_ARG(mesh != nullptr);
-		CHECK_ARG(scene == nullptr);
 		GraphRunCtx::synchronizeAll();
 		auto m = Meshes::get(mesh, "Mesh");
-		Scene& sc = Scene::defaultScene();
-		auto e = std::make_shared<Entity>(m, &sc);
-		sc.addEntity(e);
+		auto sc = sceneOf(scene);
+		auto e = std::make_shared<Entity>(m, sc.get());
+		sc->addEntity(e);
 		*out_entity = Entities::add(e);
 	});
 }
@@ -464,10 +486,10 @@ RGL_API rgl_status_t rgl_texture_is_alive(rgl_texture_t texture, bool* out_alive
 RGL_API rgl_status_t rgl_scene_set_time(rgl_scene_t scene, uint64_t nanoseconds)
 {
 	return safeCall([&]() {
-		CHECK_ARG(scene == nullptr);
 		GraphRunCtx::synchronizeAll();
-		Scene::defaultScene().timeNs = nanoseconds;
-		Scene::defaultScene().timeSet = true;
+		auto sc = sceneOf(scene);
+		sc->timeNs = nanoseconds;
+		sc->timeSet = true;
 	});
 }
 
@@ -646,8 +668,11 @@ RGL_API rgl_status_t rgl_node_raytrace(rgl_node_t* node, rgl_scene_t scene)
 {
 	return safeCall([&]() {
 		CHECK_ARG(node != nullptr);
-		CHECK_ARG(scene == nullptr);
-		createOrUpdateNode<RaytraceNode>(node, "RaytraceNode", [&](RaytraceNode& n) { n.scene = &Scene::defaultScene(); });
+		auto sc = sceneOf(scene);
+		createOrUpdateNode<RaytraceNode>(node, "RaytraceNode", [&](RaytraceNode& n) {
+			n.sceneRef = sc;
+			n.scene = sc.get();
+		});
 	});
 }
 
@@ -684,7 +709,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_non_hits(rgl_node_t node, float
 			n->ctx->synchronize();
 		}
 		n->setNonHits(nearDistance, farDistance);
-		n->captureStale = true;
+		n->markParamsChanged();
 	});
 }
 
@@ -710,7 +735,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_beam_divergence(rgl_node_t node
 			n->ctx->synchronize();
 		}
 		n->setBeamDivergence(horizontal_beam_divergence, vertical_beam_divergence);
-		n->captureStale = true;
+		n->markParamsChanged();
 	});
 }
 
@@ -724,7 +749,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_default_intensity(rgl_node_t no
 			n->ctx->synchronize();
 		}
 		n->setDefaultIntensity(default_intensity);
-		n->captureStale = true;
+		n->markParamsChanged();
 	});
 }
 
@@ -739,7 +764,7 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_return_mode(rgl_node_t node, rg
 		}
 		n->setReturnMode((int32_t) return_mode);
 		n->dirty = true;
-		n->captureStale = true;
+		n->markParamsChanged();
 	});
 }
 
@@ -948,7 +973,7 @@ RGL_API rgl_status_t rgl_gb300_node_gaussian_noise_set_seed(rgl_node_t node, uin
 		if (n->ctx) {
 			n->ctx->synchronize();
 		}
-		n->captureStale = true;
+		// Seed and frame are staged before every run: no recapture needed.
 		if (auto a = std::dynamic_pointer_cast<GaussianNoiseAngularRaysNode>(n)) {
 			a->setSeed(seed, frame);
 		} else if (auto b = std::dynamic_pointer_cast<GaussianNoiseAngularHitpointNode>(n)) {
@@ -973,7 +998,7 @@ RGL_API rgl_status_t rgl_gb300_node_raytrace_configure_beam_samples(rgl_node_t n
 			n->ctx->synchronize();
 		}
 		n->setBeamSamples(layers, vertices);
-		n->captureStale = true;
+		n->markParamsChanged();
 	});
 }
 
@@ -1102,6 +1127,295 @@ RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t*
 		}
 		if (out_replays) {
 			*out_replays = n->ctx ? (int64_t) n->ctx->replays : 0;
+		}
+	});
+}
+
+// ---------------------------------------------------------------- batched multi-sensor frames
+
+RGL_API rgl_status_t rgl_gb300_batch_create(rgl_gb300_batch_t* out_batch, const rgl_node_t* nodes, int32_t node_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_batch != nullptr);
+		CHECK_ARG(nodes != nullptr);
+		CHECK_ARG(node_count > 0);
+		CHECK_ARG(node_count <= rgl::kMaxBatchJobs);
+		std::vector<Node::Ptr> anchors;
+		for (int32_t i = 0; i < node_count; ++i) {
+			CHECK_ARG(nodes[i] != nullptr);
+			anchors.push_back(getNode(nodes[i]));
+		}
+		*out_batch = Batches::add(std::make_shared<BatchRun>(std::move(anchors)));
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_batch_run(rgl_gb300_batch_t batch)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		Batches::get(batch, "Batch")->run();
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_batch_destroy(rgl_gb300_batch_t batch)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		Batches::get(batch, "Batch")->synchronize();
+		Batches::release(batch, "Batch");
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_batch_configure_schedule(rgl_gb300_batch_t batch, bool autotune, int32_t block, int32_t packing,
+                                                        int32_t order, int32_t chunk, int32_t regs)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		CHECK_ARG(block == 64 || block == 128 || block == 256);
+		CHECK_ARG(packing == rgl::kPackLaneGroup || packing == rgl::kPackSerial);
+		CHECK_ARG(order == rgl::kOrderNatural || order == rgl::kOrderOctahedral || order == rgl::kOrderMorton);
+		CHECK_ARG(chunk >= 1 && chunk <= 64);
+		CHECK_ARG(regs == 64 || regs == 80 || regs == 96 || regs == 128);
+		auto b = Batches::get(batch, "Batch");
+		b->synchronize();
+		b->autotune = autotune;
+		if (!autotune) {
+			b->schedule = rgl::BatchSchedule{block, packing, order, chunk, regs};
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32_t* out_block, int32_t* out_packing, int32_t* out_order,
+                                                  int32_t* out_chunk, int32_t* out_regs)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		auto b = Batches::get(batch, "Batch");
+		const rgl::BatchSchedule s = b->schedule;
+		if (out_block) *out_block = s.block;
+		if (out_packing) *out_packing = s.packing;
+		if (out_order) *out_order = s.order;
+		if (out_chunk) *out_chunk = s.chunk;
+		if (out_regs) *out_regs = s.regs;
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_batch_get_stats(rgl_gb300_batch_t batch, float* out_frame_ms, float* out_trace_ms, int64_t* out_beams,
+                                               int64_t* out_rays, int64_t* out_captures, int64_t* out_replays, int64_t* out_tunings)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		auto b = Batches::get(batch, "Batch");
+		b->synchronize();
+		if (out_frame_ms) *out_frame_ms = b->lastFrameMs;
+		if (out_trace_ms) *out_trace_ms = b->lastTraceMs;
+		if (out_beams) *out_beams = b->beams;
+		if (out_rays) *out_rays = b->rays;
+		if (out_captures) *out_captures = (int64_t) b->captures;
+		if (out_replays) *out_replays = (int64_t) b->replays;
+		if (out_tunings) *out_tunings = (int64_t) b->tunings;
+	});
+}
+
+// ---------------------------------------------------------------- resident scenes
+
+RGL_API rgl_status_t rgl_gb300_scene_create(rgl_scene_t* out_scene)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_scene != nullptr);
+		*out_scene = Scenes::add(std::make_shared<Scene>());
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_scene_destroy(rgl_scene_t scene)
+{
+	return safeCall([&]() {
+		CHECK_ARG(scene != nullptr);
+		auto sc = Scenes::get(scene, "Scene");
+		GraphRunCtx::synchronizeAll();
+		for (auto it = Entities::map().begin(); it != Entities::map().end();) {
+			it = (it->second->scene == sc.get()) ? Entities::map().erase(it) : std::next(it);
+		}
+		sc->clear();
+		sc->releaseDevice();
+		Scenes::release(scene, "Scene");
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_scene_get_stats_of(rgl_scene_t scene, int64_t* out_node_bytes, int64_t* out_triangle_bytes,
+                                                 int32_t* out_instances)
+{
+	return safeCall([&]() {
+		auto sc = sceneOf(scene);
+		int64_t nb = 0, tb = 0;
+		sc->stats(nb, tb);
+		if (out_node_bytes) *out_node_bytes = nb;
+		if (out_triangle_bytes) *out_triangle_bytes = tb;
+		if (out_instances) *out_instances = (int32_t) sc->entityCount();
+	});
+}
+
+// ---------------------------------------------------------------- serving loop
+
+RGL_API rgl_status_t rgl_gb300_server_create(rgl_gb300_server_t* out_server, int64_t hbm_budget_bytes, int32_t max_in_flight_batches)
+{
+	return safeCall([&]() {
+		CHECK_ARG(out_server != nullptr);
+		CHECK_ARG(hbm_budget_bytes > 0);
+		CHECK_ARG(max_in_flight_batches >= 1 && max_in_flight_batches <= 8);
+		*out_server = Servers::add(std::make_shared<Server>(hbm_budget_bytes, max_in_flight_batches));
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_destroy(rgl_gb300_server_t server)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		Servers::release(server, "Server");
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_add_pattern(rgl_gb300_server_t server, const rgl_mat3x4f* rays, int32_t ray_count,
+                                                  int32_t* out_pattern)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(rays != nullptr);
+		CHECK_ARG(ray_count > 0);
+		CHECK_ARG(out_pattern != nullptr);
+		*out_pattern = Servers::get(server, "Server")->addPattern(rays, ray_count);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_submit(rgl_gb300_server_t server, rgl_scene_t scene, int32_t pattern,
+                                             const rgl_mat3x4f* sensor_pose, rgl_return_mode_t return_mode, float min_range,
+                                             float max_range, int64_t* out_request)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(sensor_pose != nullptr);
+		CHECK_ARG(out_request != nullptr);
+		CHECK_ARG(return_mode != RGL_RETURN_UNKNOWN);
+		CHECK_ARG(!std::isnan(min_range) && !std::isnan(max_range) && min_range >= 0.0f && min_range <= max_range);
+		auto srv = Servers::get(server, "Server");
+		*out_request = srv->submit(sceneOf(scene), pattern, toMat(*sensor_pose), (int32_t) return_mode, min_range, max_range);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_wait(rgl_gb300_server_t server, int64_t request, float timeout_ms, bool* out_done)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		const bool done = Servers::get(server, "Server")->wait(request, timeout_ms);
+		if (out_done) {
+			*out_done = done;
+		}
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_take_completed(rgl_gb300_server_t server, int64_t* out_requests, int32_t capacity,
+                                                     int32_t* out_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(out_requests != nullptr);
+		CHECK_ARG(capacity > 0);
+		CHECK_ARG(out_count != nullptr);
+		*out_count = Servers::get(server, "Server")->takeCompleted(out_requests, capacity);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_wait_completed(rgl_gb300_server_t server, float timeout_ms, int64_t* out_requests, int32_t capacity,
+                                                     int32_t* out_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(out_requests != nullptr);
+		CHECK_ARG(capacity > 0);
+		CHECK_ARG(out_count != nullptr);
+		*out_count = Servers::get(server, "Server")->waitCompleted(out_requests, capacity, timeout_ms);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_get_result_size(rgl_gb300_server_t server, int64_t request, rgl_field_t field,
+                                                      int32_t* out_count, int32_t* out_size_of)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		int32_t c = 0, sz = 0;
+		Servers::get(server, "Server")->resultSize(request, field, c, sz);
+		if (out_count) *out_count = c;
+		if (out_size_of) *out_size_of = sz;
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_get_result_data(rgl_gb300_server_t server, int64_t request, rgl_field_t field, void* out_data)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(out_data != nullptr);
+		Servers::get(server, "Server")->resultData(request, field, out_data);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_get_request_timing(rgl_gb300_server_t server, int64_t request, double* out_queued_s,
+                                                         double* out_total_s)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		double q = 0, t = 0;
+		Servers::get(server, "Server")->timing(request, q, t);
+		if (out_queued_s) *out_queued_s = q;
+		if (out_total_s) *out_total_s = t;
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_release(rgl_gb300_server_t server, int64_t request)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		Servers::get(server, "Server")->release(request);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		Servers::get(server, "Server")->drain();
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64_t* out_submitted, int64_t* out_completed,
+                                                int64_t* out_failed, int64_t* out_batches, int64_t* out_requests_in_batches,
+                                                int64_t* out_peak_reserved_bytes)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		const Server::Stats s = Servers::get(server, "Server")->stats();
+		if (out_submitted) *out_submitted = s.submitted;
+		if (out_completed) *out_completed = s.completed;
+		if (out_failed) *out_failed = s.failed;
+		if (out_batches) *out_batches = s.batches;
+		if (out_requests_in_batches) *out_requests_in_batches = s.jobsInBatches;
+		if (out_peak_reserved_bytes) *out_peak_reserved_bytes = s.peakReserved;
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs)
+{
+	return safeCall([&]() {
+		CHECK_ARG(block == 64 || block == 128 || block == 256);
+		CHECK_ARG(packing == rgl::kPackLaneGroup || packing == rgl::kPackSerial);
+		CHECK_ARG(chunk >= 1 && chunk <= 64);
+		CHECK_ARG(regs == 64 || regs == 80 || regs == 96 || regs == 128);
+		GraphRunCtx::synchronizeAll();
+		setTraceSchedule(rgl::BatchSchedule{block, packing, rgl::kOrderNatural, chunk, regs});
+		// Captured runs baked the old schedule into their launches.
+		for (auto& kv : Nodes::map()) {
+			if (std::dynamic_pointer_cast<RaytraceNode>(kv.second)) {
+				kv.second->markParamsChanged();
+			}
 		}
 	});
 }

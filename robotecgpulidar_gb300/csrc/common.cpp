@@ -222,6 +222,101 @@ void* PinnedBuffer::ensure(size_t bytes)
 	return ptr_;
 }
 
+// ---------------------------------------------------------------- error slots
+
+namespace {
+constexpr int kSlotsPerChunk = 4096;
+struct SlotChunk
+{
+	int32_t* dev = nullptr;
+	int32_t* host = nullptr;
+	int highWater = 0; // slots ever handed out; the refresh copies this many
+	std::vector<int> freeList;
+};
+std::mutex slotMutex;
+// Never destroyed: slots owned by static objects (the default scene) are released during exit,
+// possibly after function-local statics constructed later than them are gone.
+std::vector<SlotChunk>& slotChunks()
+{
+	static auto* chunks = new std::vector<SlotChunk>();
+	return *chunks;
+}
+} // namespace
+
+ErrorSlot::~ErrorSlot()
+{
+	if (chunk_ < 0) {
+		return;
+	}
+	std::lock_guard<std::mutex> g(slotMutex);
+	slotChunks()[chunk_].freeList.push_back(index_); // zeroed again when handed out
+}
+
+int32_t* ErrorSlot::device()
+{
+	std::lock_guard<std::mutex> g(slotMutex);
+	auto& chunks = slotChunks();
+	if (chunk_ < 0) {
+		int c = -1, i = -1;
+		for (size_t k = 0; k < chunks.size() && c < 0; ++k) {
+			if (!chunks[k].freeList.empty()) {
+				c = (int) k;
+				i = chunks[k].freeList.back();
+				chunks[k].freeList.pop_back();
+			} else if (chunks[k].highWater < kSlotsPerChunk) {
+				c = (int) k;
+				i = chunks[k].highWater++;
+			}
+		}
+		if (c < 0) {
+			SlotChunk n;
+			RGL_CHECK_CUDA(cudaMalloc(&n.dev, sizeof(int32_t) * kSlotsPerChunk));
+			RGL_CHECK_CUDA(cudaMemset(n.dev, 0, sizeof(int32_t) * kSlotsPerChunk));
+			RGL_CHECK_CUDA(cudaMallocHost(&n.host, sizeof(int32_t) * kSlotsPerChunk));
+			std::memset(n.host, 0, sizeof(int32_t) * kSlotsPerChunk);
+			n.highWater = 1;
+			chunks.push_back(std::move(n));
+			c = (int) chunks.size() - 1;
+			i = 0;
+		}
+		RGL_CHECK_CUDA(cudaMemset(chunks[c].dev + i, 0, sizeof(int32_t)));
+		chunks[c].host[i] = 0;
+		chunk_ = c;
+		index_ = i;
+	}
+	return chunks[chunk_].dev + index_;
+}
+
+bool ErrorSlot::raised() const
+{
+	if (chunk_ < 0) {
+		return false;
+	}
+	std::lock_guard<std::mutex> g(slotMutex);
+	return slotChunks()[chunk_].host[index_] != 0;
+}
+
+void ErrorSlot::clear()
+{
+	if (chunk_ < 0) {
+		return;
+	}
+	std::lock_guard<std::mutex> g(slotMutex);
+	auto& c = slotChunks()[chunk_];
+	RGL_CHECK_CUDA(cudaMemset(c.dev + index_, 0, sizeof(int32_t)));
+	c.host[index_] = 0;
+}
+
+void refreshErrorSlots()
+{
+	std::lock_guard<std::mutex> g(slotMutex);
+	for (auto& c : slotChunks()) {
+		if (c.highWater > 0) {
+			RGL_CHECK_CUDA(cudaMemcpy(c.host, c.dev, sizeof(int32_t) * c.highWater, cudaMemcpyDeviceToHost));
+		}
+	}
+}
+
 void ensureCudaInitialized()
 {
 	static bool done = false;

@@ -100,6 +100,30 @@ private:
 	bool tracked_ = true;
 };
 
+// Device-side error flag of a kernel (stack overflow, look-back timeout, ...). The flags of all
+// nodes live in shared chunks of int32 slots, so a completed run checks every flag with one
+// device-to-host copy per chunk (refreshErrorSlots) instead of one blocking copy per node.
+class ErrorSlot
+{
+public:
+	ErrorSlot() = default;
+	ErrorSlot(const ErrorSlot&) = delete;
+	ErrorSlot& operator=(const ErrorSlot&) = delete;
+	~ErrorSlot();
+	// Device address of the flag (zero when first handed out). Allocates: call outside stream capture.
+	int32_t* device();
+	// Value of the flag at the last refreshErrorSlots().
+	bool raised() const;
+	// Resets the flag on the device and in the host copy.
+	void clear();
+
+private:
+	int chunk_ = -1;
+	int index_ = -1;
+};
+// Copies every flag to the host. Call after the work that may raise them has completed.
+void refreshErrorSlots();
+
 // Grow-only pinned host allocation.
 class PinnedBuffer
 {
@@ -118,5 +142,25 @@ private:
 
 // Library-wide CUDA state: device selected lazily on the first API call.
 void ensureCudaInitialized();
+
+// A small parameter block (a transform, noise parameters) staged in pinned host memory before every
+// run and copied to device memory by the run itself, so a captured run replayed later reads the
+// current values. Call host() and device() in the prepare phase, enqueue() in the enqueue phase.
+template<class T>
+class StagedParam
+{
+public:
+	T& host() { return *static_cast<T*>(h_.ensure(sizeof(T))); }
+	const T* device() { return static_cast<const T*>(d_.ensure(sizeof(T))); }
+	const T* enqueue(cudaStream_t s)
+	{
+		RGL_CHECK_CUDA(cudaMemcpyAsync(d_.get(), h_.get(), sizeof(T), cudaMemcpyHostToDevice, s));
+		return d_.as<T>();
+	}
+
+private:
+	PinnedBuffer h_;
+	DeviceBuffer d_;
+};
 
 } // namespace rgl

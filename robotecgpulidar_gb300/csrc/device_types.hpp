@@ -143,4 +143,19 @@ struct TraceParams
 	TraceOutputs out;
 };
 
+// One sensor (or served request) of a batched traversal launch (trace_batch.cu): its raytrace
+// parameters including its scene, its sub-ray rotations, an optional beam visiting order, the
+// lane-group width of lane-group packing, and optionally a sensor pose applied to sensor-local rays
+// and an inline range.
+struct BatchJob
+{
+	TraceParams p;         // p.ranges == null: inlineRange applies to every ray
+	const Mat34* samples;  // p.nSamples rotations (entry 0 is the primary ray and is not read)
+	const uint32_t* order; // permutation of [0, p.nRays), or null for the natural order
+	int32_t groupSize;     // min(p.nSamples, 32)
+	int32_t hasRayTransform; // world ray = mul(rayTransform, ray), as a rays-transform node computes it
+	Mat34 rayTransform;
+	float inlineRange[2];
+};
+
 } // namespace rgl

@@ -1,6 +1,7 @@
 #include "graph.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
@@ -14,12 +15,22 @@ using rgl::InvalidPipeline;
 using rgl::Mat34;
 
 namespace {
+std::atomic<uint64_t> gParamVersion{0};
 bool gTiming = false;
 bool gCudaGraphs = [] {
 	const char* v = std::getenv("RGL_GB300_CUDA_GRAPH");
 	return v == nullptr || std::string(v) != "0";
 }();
 } // namespace
+uint64_t Node::nextParamVersion() { return gParamVersion.fetch_add(1, std::memory_order_relaxed) + 1; }
+
+namespace {
+// Schedule of single-graph traversals (a batch of one job). The default is the fastest measured on
+// the 1M-triangle single-sensor scan: lane-group packing, one task per fetch, 80 registers.
+rgl::BatchSchedule gTraceSchedule{256, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 80};
+} // namespace
+rgl::BatchSchedule traceSchedule() { return gTraceSchedule; }
+void setTraceSchedule(const rgl::BatchSchedule& s) { gTraceSchedule = s; }
 bool timingEnabled() { return gTiming; }
 void setTimingEnabled(bool on) { gTiming = on; }
 bool cudaGraphsEnabled() { return gCudaGraphs; }
@@ -181,11 +192,16 @@ void FromMat3x4fRaysNode::validateImpl()
 	}
 }
 
-void TransformRaysNode::prepareImpl(cudaStream_t) { out.ensure(sizeof(Mat34) * std::max<size_t>(1, rayCount())); }
+void TransformRaysNode::prepareImpl(cudaStream_t)
+{
+	out.ensure(sizeof(Mat34) * std::max<size_t>(1, rayCount()));
+	staged.host() = transform;
+	(void) staged.device();
+}
 
 void TransformRaysNode::enqueueImpl(cudaStream_t s)
 {
-	rgl::launchTransformRays(input->raysDev(), out.as<Mat34>(), (int) rayCount(), transform, s);
+	rgl::launchTransformRays(input->raysDev(), out.as<Mat34>(), (int) rayCount(), staged.enqueue(s), s);
 }
 
 void SetRangeRaysNode::setParameters(const rgl_vec2f* r, size_t n)
@@ -222,22 +238,13 @@ void GaussianNoiseAngularRaysNode::setParameters(float m, float sd, rgl_axis_t a
 	axis = a;
 }
 
-// Per-run noise frame: written to pinned host memory before the run and copied to the device by the
-// (possibly captured) enqueue, so replays of a captured run keep advancing it.
-static void stageFrame(rgl::PinnedBuffer& h, rgl::DeviceBuffer& d, uint64_t& frame)
+// Noise parameters of one run, staged before the run (the frame advances by one per run, also across
+// replays of a captured run). Reference frame algebra: src/gpu/gaussianNoiseKernels.cu:20-66.
+static void stageNoise(rgl::StagedParam<rgl::NoiseParams>& staged, uint64_t seed, uint64_t& frame, uint32_t kind, float mean, float sd,
+                       float rise, int axis, const Mat34& lookAt)
 {
-	d.ensure(sizeof(uint64_t));
-	*static_cast<uint64_t*>(h.ensure(sizeof(uint64_t))) = frame;
-	++frame;
-}
-
-static rgl::NoiseParams makeNoise(uint64_t seed, uint64_t frame, uint32_t kind, float mean, float sd, float rise, int axis,
-                                  const Mat34& lookAt, const rgl::DeviceBuffer& dFrame, const rgl::PinnedBuffer& hFrame,
-                                  cudaStream_t s)
-{
-	RGL_CHECK_CUDA(cudaMemcpyAsync(dFrame.get(), hFrame.get(), sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-	rgl::NoiseParams np{};
-	np.dFrame = dFrame.as<uint32_t>();
+	rgl::NoiseParams& np = staged.host();
+	np = rgl::NoiseParams{};
 	np.seedLo = (uint32_t) seed;
 	np.seedHi = (uint32_t) (seed >> 32);
 	np.frameLo = (uint32_t) frame;
@@ -249,26 +256,28 @@ static rgl::NoiseParams makeNoise(uint64_t seed, uint64_t frame, uint32_t kind, 
 	np.axis = axis;
 	np.lookAt = lookAt;
 	np.lookAtInv = rgl::inverse(lookAt);
-	return np;
+	(void) staged.device();
+	++frame;
 }
 
 void GaussianNoiseAngularRaysNode::prepareImpl(cudaStream_t)
 {
 	out.ensure(sizeof(Mat34) * std::max<size_t>(1, rayCount()));
-	stageFrame(hFrame, dFrame, frame);
+	stageNoise(staged, seed, frame, 1, mean, stDev, 0.0f, axis, rgl::inverse(input->cumulativeRayTransform()));
 }
 
 void GaussianNoiseAngularRaysNode::enqueueImpl(cudaStream_t s)
 {
-	Mat34 lookAt = rgl::inverse(input->cumulativeRayTransform());
-	rgl::launchNoiseAngularRay(input->raysDev(), out.as<Mat34>(), (int) rayCount(),
-	                           makeNoise(seed, frame, 1, mean, stDev, 0.0f, axis, lookAt, dFrame, hFrame, s), s);
+	rgl::launchNoiseAngularRay(input->raysDev(), out.as<Mat34>(), (int) rayCount(), staged.enqueue(s), s);
 }
 
 // ================================================================ points nodes
 
 size_t PointsNode::pointCountHost()
 {
+	if (const int32_t* hc = hostCount()) {
+		return (size_t) *hc;
+	}
 	const int32_t* dc = deviceCount();
 	if (dc == nullptr) {
 		return capacity();
@@ -377,9 +386,7 @@ void RaytraceNode::validateImpl()
 		const float r[2] = {0.0f, FLT_MAX};
 		RGL_CHECK_CUDA(cudaMemcpy(defaultRange.ensure(sizeof(r)), r, sizeof(r), cudaMemcpyHostToDevice));
 	}
-	if (errorFlag.get() == nullptr) {
-		RGL_CHECK_CUDA(cudaMemset(errorFlag.ensure(sizeof(int32_t)), 0, sizeof(int32_t)));
-	}
+	(void) errorFlag.device();
 	if (scene == nullptr) {
 		scene = &Scene::defaultScene();
 	}
@@ -408,9 +415,10 @@ void RaytraceNode::prepareImpl(cudaStream_t s)
 		RGL_CHECK_CUDA(cudaEventCreate(&evStop));
 	}
 	scene->prepare(s);
+	stageJob();
 }
 
-void RaytraceNode::enqueueImpl(cudaStream_t s)
+rgl::TraceParams RaytraceNode::traceParams()
 {
 	const size_t n = rays->rayCount();
 	rgl::TraceParams p{};
@@ -430,7 +438,7 @@ void RaytraceNode::enqueueImpl(cudaStream_t s)
 		strongestSelected = strongestSelected || t == RGL_RETURN_TYPE_STRONGEST || t == RGL_RETURN_TYPE_SECOND_STRONGEST;
 	}
 	p.needIntensity = (fields.count(RGL_FIELD_INTENSITY_F32) || fields.count(RGL_FIELD_INTENSITY_U8) || strongestSelected) ? 1 : 0;
-	p.errorFlag = errorFlag.as<int32_t>();
+	p.errorFlag = errorFlag.device();
 	p.scene = scene->view();
 	auto ptr = [&](rgl_field_t f) -> void* { return fields.count(f) ? outputs[f].get() : nullptr; };
 	p.out.xyz = static_cast<float*>(ptr(RGL_FIELD_XYZ_VEC3_F32));
@@ -444,10 +452,42 @@ void RaytraceNode::enqueueImpl(cudaStream_t s)
 	p.out.normal = static_cast<float*>(ptr(RGL_FIELD_NORMAL_VEC3_F32));
 	p.out.incidentAngle = static_cast<float*>(ptr(RGL_FIELD_INCIDENT_ANGLE_F32));
 	p.out.laserRetro = nullptr;
+	return p;
+}
+
+// The traversal is the persistent kernel of batched frames with this node as its only job: the job
+// record and the task count are staged every run (new ray contents need no re-capture).
+void RaytraceNode::stageJob()
+{
+	const rgl::TraceParams p = traceParams();
+	rgl::BatchJob& b = job.host();
+	b = rgl::BatchJob{};
+	b.p = p;
+	b.samples = sampleTable.as<Mat34>();
+	b.order = nullptr;
+	b.groupSize = std::min(p.nSamples, 32);
+	(void) job.device();
+	schedule = traceSchedule();
+	const int per = rgl::batchBeamsPerTask(schedule.packing, p.nSamples);
+	rgl::TaskRange& tr = tasks.host();
+	tr.base[0] = 0;
+	tr.base[1] = (p.nRays + per - 1) / per;
+	(void) tasks.device();
+	shading = p.needIntensity != 0 || p.out.normal != nullptr || p.out.incidentAngle != nullptr;
+	if (counter.get() == nullptr) {
+		RGL_CHECK_CUDA(cudaMemset(counter.ensure(sizeof(uint32_t)), 0, sizeof(uint32_t)));
+	}
+	rgl::prepareTraceBatch(1, p.nSamples, shading, schedule);
+}
+
+void RaytraceNode::enqueueImpl(cudaStream_t s)
+{
+	const rgl::BatchJob* dJob = job.enqueue(s);
+	const rgl::TaskRange* dTasks = tasks.enqueue(s);
 	if (timingEnabled() && evStart) {
 		recordEvent(evStart, s);
 	}
-	rgl::launchTrace(p, sampleTable.as<Mat34>(), s);
+	rgl::launchTraceBatch(dJob, dTasks->base, 1, job.host().p.nSamples, shading, schedule, counter.as<uint32_t>(), s);
 	RGL_CHECK_CUDA(cudaGetLastError());
 	if (timingEnabled() && evStart) {
 		recordEvent(evStop, s);
@@ -456,13 +496,8 @@ void RaytraceNode::enqueueImpl(cudaStream_t s)
 
 void RaytraceNode::checkErrors()
 {
-	if (errorFlag.get() == nullptr) {
-		return;
-	}
-	int32_t e = 0;
-	RGL_CHECK_CUDA(cudaMemcpy(&e, errorFlag.get(), sizeof(e), cudaMemcpyDeviceToHost));
-	if (e != 0) {
-		RGL_CHECK_CUDA(cudaMemset(errorFlag.get(), 0, sizeof(int32_t)));
+	if (errorFlag.raised()) {
+		errorFlag.clear();
 		throw std::runtime_error("RaytraceNode: traversal stack overflow on the device (scene BVH too deep)");
 	}
 	if (scene) {
@@ -566,9 +601,7 @@ void CompactByFieldPointsNode::validateImpl()
 		count.ensure(sizeof(int32_t));
 		RGL_CHECK_CUDA(cudaMemset(count.get(), 0, sizeof(int32_t)));
 	}
-	if (errorFlag.get() == nullptr) {
-		RGL_CHECK_CUDA(cudaMemset(errorFlag.ensure(sizeof(int32_t)), 0, sizeof(int32_t)));
-	}
+	(void) errorFlag.device();
 }
 
 void CompactByFieldPointsNode::sizeBuffers(const std::vector<rgl_field_t>& which)
@@ -580,7 +613,14 @@ void CompactByFieldPointsNode::sizeBuffers(const std::vector<rgl_field_t>& which
 	scratch.ensure(rgl::compactScratchBytes((int) cap));
 }
 
-void CompactByFieldPointsNode::prepareImpl(cudaStream_t) { sizeBuffers(std::vector<rgl_field_t>(eager.begin(), eager.end())); }
+// Per-run host state lives here, not in enqueueImpl: a replayed capture does not call enqueueImpl.
+void CompactByFieldPointsNode::prepareImpl(cudaStream_t s)
+{
+	sizeBuffers(std::vector<rgl_field_t>(eager.begin(), eager.end()));
+	hCount.ensure(sizeof(int32_t));
+	lastStream = s;
+	lazyDone.clear();
+}
 
 void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cudaStream_t s)
 {
@@ -597,14 +637,14 @@ void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cu
 		fc.f[fc.count++] = c;
 	}
 	rgl::launchCompact(static_cast<const int32_t*>(input->fieldDev(field)), (int) cap, input->deviceCount(), fc, count.as<int32_t>(),
-	                   scratch.get(), errorFlag.as<int32_t>(), s);
+	                   scratch.get(), errorFlag.device(), s);
 }
 
 void CompactByFieldPointsNode::enqueueImpl(cudaStream_t s)
 {
-	lastStream = s;
-	lazyDone.clear();
 	compact(std::vector<rgl_field_t>(eager.begin(), eager.end()), s);
+	// The count reaches the host with the run: reading results needs no extra blocking copy.
+	RGL_CHECK_CUDA(cudaMemcpyAsync(hCount.get(), count.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
 }
 
 const void* CompactByFieldPointsNode::fieldDev(rgl_field_t f)
@@ -625,26 +665,26 @@ const void* CompactByFieldPointsNode::fieldDev(rgl_field_t f)
 
 void CompactByFieldPointsNode::checkErrors()
 {
-	if (errorFlag.get() == nullptr) {
-		return;
-	}
-	int32_t e = 0;
-	RGL_CHECK_CUDA(cudaMemcpy(&e, errorFlag.get(), sizeof(e), cudaMemcpyDeviceToHost));
-	if (e != 0) {
-		RGL_CHECK_CUDA(cudaMemset(errorFlag.get(), 0, sizeof(int32_t)));
+	if (errorFlag.raised()) {
+		errorFlag.clear();
 		throw std::runtime_error("CompactByFieldPointsNode: decoupled look-back did not complete on the device");
 	}
 }
 
 // ---- TransformPointsNode
 
-void TransformPointsNode::prepareImpl(cudaStream_t) { out.ensure(std::max<size_t>(1, 12 * input->capacity())); }
+void TransformPointsNode::prepareImpl(cudaStream_t)
+{
+	out.ensure(std::max<size_t>(1, 12 * input->capacity()));
+	staged.host() = transform;
+	(void) staged.device();
+}
 
 void TransformPointsNode::enqueueImpl(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
 	rgl::launchTransformPoints(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), out.as<float>(), (int) cap,
-	                           input->deviceCount(), transform, s);
+	                           input->deviceCount(), staged.enqueue(s), s);
 }
 
 const void* TransformPointsNode::fieldDev(rgl_field_t f)
@@ -669,15 +709,14 @@ void GaussianNoiseAngularHitpointNode::prepareImpl(cudaStream_t)
 	if (withDistance) {
 		outDist.ensure(std::max<size_t>(1, 4 * cap));
 	}
-	stageFrame(hFrame, dFrame, frame);
+	stageNoise(staged, seed, frame, 2, mean, stDev, 0.0f, axis, input->lookAtOriginTransform());
 }
 
 void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
-	rgl::NoiseParams np = makeNoise(seed, frame, 2, mean, stDev, 0.0f, axis, input->lookAtOriginTransform(), dFrame, hFrame, s);
 	rgl::launchNoiseAngularHitpoint(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), outXyz.as<float>(),
-	                                withDistance ? outDist.as<float>() : nullptr, (int) cap, input->deviceCount(), np, s);
+	                                withDistance ? outDist.as<float>() : nullptr, (int) cap, input->deviceCount(), staged.enqueue(s), s);
 }
 
 const void* GaussianNoiseAngularHitpointNode::fieldDev(rgl_field_t f)
@@ -703,16 +742,15 @@ void GaussianNoiseDistanceNode::prepareImpl(cudaStream_t)
 	const size_t cap = input->capacity();
 	outXyz.ensure(std::max<size_t>(1, 12 * cap));
 	outDist.ensure(std::max<size_t>(1, 4 * cap));
-	stageFrame(hFrame, dFrame, frame);
+	stageNoise(staged, seed, frame, 3, mean, base, rise, 0, input->lookAtOriginTransform());
 }
 
 void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
-	rgl::NoiseParams np = makeNoise(seed, frame, 3, mean, base, rise, 0, input->lookAtOriginTransform(), dFrame, hFrame, s);
 	rgl::launchNoiseDistance(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)),
 	                         static_cast<const float*>(input->fieldDev(RGL_FIELD_DISTANCE_F32)), outXyz.as<float>(),
-	                         outDist.as<float>(), (int) cap, input->deviceCount(), np, s);
+	                         outDist.as<float>(), (int) cap, input->deviceCount(), staged.enqueue(s), s);
 }
 
 const void* GaussianNoiseDistanceNode::fieldDev(rgl_field_t f)
@@ -855,7 +893,7 @@ void GraphRunCtx::releaseGraph()
 
 // One run: validation and the prepare phase on the host, then the nodes' device work. The device
 // work is captured into a CUDA graph once and replayed by later runs while no node's kernel
-// parameters changed (captureStale) and no device buffer moved (allocation epoch); otherwise it is
+// parameters changed (parameter versions) and no device buffer moved (allocation epoch); otherwise it is
 // captured again. With CUDA graphs disabled (RGL_GB300_CUDA_GRAPH=0) the work is enqueued directly.
 void GraphRunCtx::run()
 {
@@ -864,13 +902,14 @@ void GraphRunCtx::run()
 		order = findExecutionOrder(nodes);
 		releaseGraph();
 	}
-	bool stale = false;
+	uint64_t version = 0;
 	for (auto& n : order) {
 		n->validateImpl();
 		n->dirty = false;
-		stale = stale || n->captureStale;
+		version = std::max(version, n->paramVersion);
 	}
 	running = true;
+	batchedLast = false;
 	for (auto& n : order) {
 		n->prepareImpl(stream_);
 	}
@@ -883,7 +922,7 @@ void GraphRunCtx::run()
 			n->enqueueImpl(stream_);
 		}
 	} else {
-		if (stale || exec == nullptr || execEpoch != rgl::allocationEpoch()) {
+		if (version > execVersion || exec == nullptr || execEpoch != rgl::allocationEpoch()) {
 			releaseGraph();
 			const uint64_t launches0 = rgl::launchCount();
 			RGL_CHECK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
@@ -907,10 +946,8 @@ void GraphRunCtx::run()
 			RGL_CHECK_CUDA(inst);
 			execKernels = rgl::launchCount() - launches0;
 			execEpoch = rgl::allocationEpoch();
+			execVersion = version;
 			++captures;
-			for (auto& n : order) {
-				n->captureStale = false;
-			}
 		} else {
 			++replays;
 			rgl::countLaunch(execKernels);
@@ -923,7 +960,38 @@ void GraphRunCtx::run()
 	RGL_CHECK_CUDA(cudaEventRecord(done, stream_));
 }
 
-void GraphRunCtx::synchronize()
+uint64_t GraphRunCtx::validateForBatch()
+{
+	synchronize();
+	if (order.empty()) {
+		order = findExecutionOrder(nodes);
+		releaseGraph();
+	}
+	uint64_t version = 0;
+	for (auto& n : order) {
+		n->validateImpl();
+		n->dirty = false;
+		version = std::max(version, n->paramVersion);
+	}
+	return version;
+}
+
+void GraphRunCtx::prepareForBatch(cudaStream_t s)
+{
+	running = true; // a failure from here on leaves the graph to be synchronised like a run
+	for (auto& n : order) {
+		n->prepareImpl(s);
+	}
+}
+
+void GraphRunCtx::markBatchedRun(cudaStream_t s)
+{
+	RGL_CHECK_CUDA(cudaEventRecord(done, s));
+	running = true;
+	batchedLast = true;
+}
+
+void GraphRunCtx::synchronize(bool refreshErrors)
 {
 	if (!running) {
 		return;
@@ -931,7 +999,10 @@ void GraphRunCtx::synchronize()
 	running = false;
 	RGL_CHECK_CUDA(cudaEventSynchronize(done));
 	RGL_CHECK_CUDA(cudaGetLastError());
-	if (timingEnabled()) {
+	if (refreshErrors) {
+		rgl::refreshErrorSlots();
+	}
+	if (timingEnabled() && !batchedLast) {
 		cudaEventElapsedTime(&lastRunMs, runStart, runStop);
 		for (auto& n : order) {
 			if (auto rt = std::dynamic_pointer_cast<RaytraceNode>(n); rt && rt->evStart) {

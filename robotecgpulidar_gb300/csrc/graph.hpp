@@ -53,10 +53,16 @@ struct Node : std::enable_shared_from_this<Node>
 	// captured run stays valid.
 	virtual bool lastUpdateContentOnly() const { return false; }
 
+	// A parameter baked into this node's launches changed: captured runs that contain the node are
+	// stale. Versions come from one process-wide counter, so a capture that remembers the largest
+	// version of its nodes detects every later change, whoever else captured the node meanwhile.
+	void markParamsChanged() { paramVersion = nextParamVersion(); }
+	static uint64_t nextParamVersion();
+
 	std::vector<Ptr> inputs, outputs;
 	int32_t priority = 0;
 	bool dirty = true;
-	bool captureStale = true; // kernel parameters changed since the run was captured
+	uint64_t paramVersion = nextParamVersion();
 	std::shared_ptr<GraphRunCtx> ctx;
 };
 
@@ -108,9 +114,11 @@ struct TransformRaysNode : RaysNodeSingleInput
 	void enqueueImpl(cudaStream_t s) override;
 	const rgl::Mat34* raysDev() const override { return out.as<rgl::Mat34>(); }
 	rgl::Mat34 cumulativeRayTransform() const override { return rgl::mul(transform, input->cumulativeRayTransform()); }
+	bool lastUpdateContentOnly() const override { return true; } // the transform is staged every run
 
 private:
 	rgl::Mat34 transform = rgl::Mat34::identity();
+	rgl::StagedParam<rgl::Mat34> staged;
 	rgl::DeviceBuffer out;
 };
 
@@ -140,14 +148,14 @@ struct GaussianNoiseAngularRaysNode : RaysNodeSingleInput
 	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const rgl::Mat34* raysDev() const override { return out.as<rgl::Mat34>(); }
+	bool lastUpdateContentOnly() const override { return true; } // parameters are staged every run
 
 private:
 	float mean = 0, stDev = 0;
 	rgl_axis_t axis = RGL_AXIS_X;
 	uint64_t seed = 0, frame = 0;
 	rgl::DeviceBuffer out;
-	rgl::PinnedBuffer hFrame;
-	rgl::DeviceBuffer dFrame;
+	rgl::StagedParam<rgl::NoiseParams> staged;
 };
 
 // ---------------------------------------------------------------- points
@@ -161,6 +169,8 @@ struct PointsNode : virtual Node
 	virtual size_t capacity() const = 0;
 	// Device int32 holding the exact count when it is only known on the device (after compaction).
 	virtual const int32_t* deviceCount() const { return nullptr; }
+	// Pinned host copy of deviceCount(), written by the run itself; valid once the run completed.
+	virtual const int32_t* hostCount() const { return nullptr; }
 	virtual int32_t returnMode() const { return RGL_RETURN_UNKNOWN; }
 	virtual rgl::Mat34 lookAtOriginTransform() const { return rgl::Mat34::identity(); }
 	// Device pointer with capacity() elements of `field`; valid after this node's enqueue.
@@ -177,6 +187,7 @@ struct PointsNodeSingleInput : PointsNode
 	bool hasField(rgl_field_t f) const override { return input->hasField(f); }
 	size_t capacity() const override { return input->capacity(); }
 	const int32_t* deviceCount() const override { return input->deviceCount(); }
+	const int32_t* hostCount() const override { return input->hostCount(); }
 	int32_t returnMode() const override { return input->returnMode(); }
 	rgl::Mat34 lookAtOriginTransform() const override { return input->lookAtOriginTransform(); }
 	const void* fieldDev(rgl_field_t f) override { return input->fieldDev(f); }
@@ -218,6 +229,11 @@ struct RaytraceNode : PointsNode
 	void setDefaultIntensity(float i) { defaultIntensity = i; }
 	int sampleCount() const;
 	void checkErrors() override;
+	std::shared_ptr<Scene> sceneRef; // keeps a scene made by rgl_gb300_scene_create alive
+	// Launch parameters of the traversal for the current buffers (valid after prepareImpl).
+	rgl::TraceParams traceParams();
+	void stageJob();
+	const rgl::Mat34* sampleTableDev() const { return sampleTable.as<rgl::Mat34>(); }
 	Scene* scene = nullptr;
 
 	// Timing (extension): device time of the traversal kernel of the last run.
@@ -237,7 +253,13 @@ private:
 	int sampleLayers = 3, sampleVertices = 19; // reference pattern: 1 + 3 * 19 = 58 samples
 	float nearDistance = INFINITY, farDistance = INFINITY;
 	float defaultIntensity = 0.0f;
-	rgl::DeviceBuffer errorFlag;
+	rgl::ErrorSlot errorFlag;
+	// The node's traversal as a one-job persistent launch.
+	rgl::StagedParam<rgl::BatchJob> job;
+	rgl::StagedParam<rgl::TaskRange> tasks;
+	rgl::DeviceBuffer counter;
+	rgl::BatchSchedule schedule{};
+	bool shading = false;
 };
 
 struct YieldPointsNode : PointsNodeSingleInput
@@ -278,6 +300,7 @@ struct CompactByFieldPointsNode : PointsNodeSingleInput
 	void enqueueImpl(cudaStream_t s) override;
 	bool isDense() const override { return true; }
 	const int32_t* deviceCount() const override { return count.as<int32_t>(); }
+	const int32_t* hostCount() const override { return static_cast<const int32_t*>(hCount.get()); }
 	const void* fieldDev(rgl_field_t f) override;
 	void checkErrors() override;
 
@@ -287,8 +310,9 @@ private:
 	std::map<rgl_field_t, rgl::DeviceBuffer> outputs;
 	std::set<rgl_field_t> lazyDone;            // fields compacted on demand after the run
 	rgl::DeviceBuffer count;
+	rgl::PinnedBuffer hCount;
 	rgl::DeviceBuffer scratch;
-	rgl::DeviceBuffer errorFlag;
+	rgl::ErrorSlot errorFlag;
 	cudaStream_t lastStream = nullptr;
 	void sizeBuffers(const std::vector<rgl_field_t>& which);
 	void compact(const std::vector<rgl_field_t>& which, cudaStream_t s);
@@ -306,9 +330,11 @@ struct TransformPointsNode : PointsNodeSingleInput
 		return rgl::mul(rgl::inverse(transform), input->lookAtOriginTransform());
 	}
 	const void* fieldDev(rgl_field_t f) override;
+	bool lastUpdateContentOnly() const override { return true; } // the transform is staged every run
 
 private:
 	rgl::Mat34 transform = rgl::Mat34::identity();
+	rgl::StagedParam<rgl::Mat34> staged;
 	rgl::DeviceBuffer out;
 };
 
@@ -325,6 +351,7 @@ struct GaussianNoiseAngularHitpointNode : PointsNodeSingleInput
 	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
+	bool lastUpdateContentOnly() const override { return true; } // parameters are staged every run
 
 private:
 	float mean = 0, stDev = 0;
@@ -332,8 +359,7 @@ private:
 	uint64_t seed = 0, frame = 0;
 	bool withDistance = false;
 	rgl::DeviceBuffer outXyz, outDist;
-	rgl::PinnedBuffer hFrame;
-	rgl::DeviceBuffer dFrame;
+	rgl::StagedParam<rgl::NoiseParams> staged;
 };
 
 struct GaussianNoiseDistanceNode : PointsNodeSingleInput
@@ -349,13 +375,13 @@ struct GaussianNoiseDistanceNode : PointsNodeSingleInput
 	void prepareImpl(cudaStream_t s) override;
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
+	bool lastUpdateContentOnly() const override { return true; } // parameters are staged every run
 
 private:
 	float mean = 0, base = 0, rise = 0;
 	uint64_t seed = 0, frame = 0;
 	rgl::DeviceBuffer outXyz, outDist;
-	rgl::PinnedBuffer hFrame;
-	rgl::DeviceBuffer dFrame;
+	rgl::StagedParam<rgl::NoiseParams> staged;
 };
 
 struct FromArrayPointsNode : PointsNode
@@ -384,10 +410,20 @@ struct GraphRunCtx : std::enable_shared_from_this<GraphRunCtx>
 
 	~GraphRunCtx();
 	void run();
-	void synchronize();
+	// Waits for the last run and checks the nodes' device error flags (re-reading them from the
+	// device unless the caller has just done so for this run).
+	void synchronize(bool refreshErrors = true);
 	void detachAndDestroy();
 	cudaStream_t stream() const { return stream_; }
 	void invalidateOrder() { order.clear(); }
+
+	// Batched frames (batch.cpp) drive the graph themselves: they validate and prepare it, enqueue
+	// its nodes inside the frame's capture and then mark the graph as running on the frame's stream,
+	// so results are read through the usual calls.
+	uint64_t validateForBatch(); // waits for the previous run; returns the largest parameter version
+	void prepareForBatch(cudaStream_t s);
+	void markBatchedRun(cudaStream_t s);
+	const std::vector<Node::Ptr>& executionOrder() const { return order; }
 
 	std::set<Node::Ptr> nodes;
 	float lastRunMs = 0.0f, lastTraceMs = 0.0f;
@@ -401,14 +437,19 @@ private:
 	cudaStream_t stream_ = nullptr;
 	cudaEvent_t done = nullptr, runStart = nullptr, runStop = nullptr;
 	bool running = false;
+	bool batchedLast = false; // the last run was part of a batched frame (no per-graph timing)
 	// Captured run: replayed while no node changed and no buffer moved.
 	cudaGraphExec_t exec = nullptr;
 	uint64_t execEpoch = 0;
+	uint64_t execVersion = 0;
 	uint64_t execKernels = 0;
 };
 
 bool timingEnabled();
 void setTimingEnabled(bool on);
+// Traversal schedule of single-graph runs (rgl_gb300_configure_trace_schedule).
+rgl::BatchSchedule traceSchedule();
+void setTraceSchedule(const rgl::BatchSchedule& s);
 bool cudaGraphsEnabled();
 void setCudaGraphsEnabled(bool on);
 // Records `ev` on `s`; inside a stream capture the record becomes a node of the captured graph.

@@ -48,28 +48,84 @@ void buildTlas(const InstanceRec* dInstances, int nInstances, TlasBuild& t, int3
 void refitTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);
 void freeTlas(TlasBuild& t);
 
-// ---- trace.cu
-void launchTrace(const TraceParams& p, const Mat34* dSampleTable, cudaStream_t stream);
+// ---- trace_batch.cu: the traversal, one persistent launch over one or many sensors
+constexpr int kMaxBatchJobs = 1024;
+enum BatchPacking : int32_t
+{
+	kPackLaneGroup = 0, // a beam's samples on adjacent lanes, in-order shuffle reduction
+	kPackSerial = 1,    // one lane per beam, samples traced one after another
+};
+enum BeamOrder : int32_t
+{
+	kOrderNatural = 0,    // beams in the order the client gave them
+	kOrderOctahedral = 1, // sorted by an octahedral encoding of the world direction
+	kOrderMorton = 2,     // sorted by the Morton code of a point a fixed distance along the ray
+};
+struct BatchSchedule
+{
+	int32_t block;   // threads per block: 64, 128 or 256
+	int32_t packing; // BatchPacking
+	int32_t order;   // BeamOrder
+	int32_t chunk;   // tasks taken per atomic fetch
+	int32_t regs;    // register budget per thread: 64, 80, 96 or 128
+};
+// Task prefix sums of a one-job launch.
+struct TaskRange
+{
+	int32_t base[2];
+};
+// Beams covered by one task (one warp's worth of work) of a sensor with `nSamples` samples.
+int batchBeamsPerTask(int packing, int nSamples);
+// Resolves and caches the launch configuration (occupancy, shared-memory opt-in) of a schedule;
+// call it outside stream capture before the first captured launch of that schedule.
+void prepareTraceBatch(int nJobs, int maxSamples, bool shading, const BatchSchedule& s);
+// Persistent launch over `nJobs` sensors; dTaskBase holds nJobs + 1 prefix sums of tasks per sensor.
+// Resets *dCounter on the stream first.
+void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs, int maxSamples, bool shading,
+                      const BatchSchedule& s, uint32_t* dCounter, cudaStream_t stream);
+// ---- segcompact.cu: compaction of many requests' points in three launches
+constexpr int kSegTile = 1024; // points per tile
+struct SegCompactJob
+{
+	const int32_t* flags; // nPoints is-hit flags
+	const float* xyz;     // nPoints x 3
+	const float* dist;
+	const int32_t* ent;
+	float* outXyz; // kept points, in order
+	float* outDist;
+	int32_t* outEnt;
+	int32_t nPoints;
+	int32_t pad;
+};
+// dTileBase: nSeg + 1 prefix sums of ceil(nPoints / kSegTile) per segment; dCounts receives the
+// kept count of every segment.
+void launchSegCompact(const SegCompactJob* dSegs, const int32_t* dTileBase, int nSeg, int totalTiles, uint32_t* dTileCounts,
+                      uint32_t* dTileOffsets, int32_t* dCounts, cudaStream_t s);
+
+// Sort keys of one sensor's beams (job index in the top bits) and their local indices.
+void launchBeamKeys(const Mat34* rays, int n, uint32_t jobIndex, int order, const float* worldLo, const float* worldHi,
+                    uint32_t* keys, uint32_t* values, cudaStream_t stream);
 
 // ---- points.cu
-void launchTransformRays(const Mat34* in, Mat34* out, int n, Mat34 tf, cudaStream_t s);
-void launchTransformPoints(const float* inXyz, float* outXyz, int cap, const int32_t* dCount, Mat34 tf, cudaStream_t s);
+// Transforms and noise parameters are device pointers to values the host stages before each run.
+void launchTransformRays(const Mat34* in, Mat34* out, int n, const Mat34* dTf, cudaStream_t s);
+void launchTransformPoints(const float* inXyz, float* outXyz, int cap, const int32_t* dCount, const Mat34* dTf, cudaStream_t s);
 
 struct NoiseParams
 {
 	uint32_t seedLo, seedHi;
 	uint32_t frameLo, frameHi;
-	const uint32_t* dFrame; // when set, frame lo/hi are read from device memory (changes between graph replays)
 	uint32_t kind;
 	float mean, stDev, stDevRise;
 	int32_t axis;
+	int32_t pad[3];
 	Mat34 lookAt, lookAtInv;
 };
-void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams& np, cudaStream_t s);
+void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams* dNp, cudaStream_t s);
 void launchNoiseAngularHitpoint(const float* inXyz, float* outXyz, float* outDist, int cap, const int32_t* dCount,
-                                const NoiseParams& np, cudaStream_t s);
+                                const NoiseParams* dNp, cudaStream_t s);
 void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz, float* outDist, int cap, const int32_t* dCount,
-                         const NoiseParams& np, cudaStream_t s);
+                         const NoiseParams* dNp, cudaStream_t s);
 
 // One field of a compaction or format: device source/destination and element size in bytes.
 struct FieldCopy

@@ -43,27 +43,40 @@ __device__ __forceinline__ void storeMat(Mat34* p, const Mat34& m)
 	q[2] = make_float4(m.m[2][0], m.m[2][1], m.m[2][2], m.m[2][3]);
 }
 
-__global__ void kTransformRays(const Mat34* __restrict__ in, Mat34* __restrict__ out, int n, Mat34 tf)
+// Transforms and noise parameters are read from device memory: the host stages them before every
+// run and the (possibly captured and replayed) run copies them in, so new poses, seeds and frames
+// need no new launch.
+__global__ void kTransformRays(const Mat34* __restrict__ in, Mat34* __restrict__ out, int n, const Mat34* __restrict__ dTf)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < n) {
-		storeMat(out + i, mul(tf, loadMat(in + i)));
+		storeMat(out + i, mul(loadMat(dTf), loadMat(in + i)));
 	}
 }
 
-__global__ void kTransformPoints(const float* __restrict__ in, float* __restrict__ out, int cap, const int32_t* dCount, Mat34 tf)
+__global__ void kTransformPoints(const float* __restrict__ in, float* __restrict__ out, int cap, const int32_t* dCount,
+                                 const Mat34* __restrict__ dTf)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < countOf(cap, dCount)) {
-		storeXyz(out, i, tf.point(loadXyz(in, i)));
+		storeXyz(out, i, loadMat(dTf).point(loadXyz(in, i)));
 	}
+}
+
+// Block-wide copy of the staged noise parameters.
+__device__ __forceinline__ void loadNoise(NoiseParams& sp, const NoiseParams* __restrict__ dNp)
+{
+	constexpr int words = sizeof(NoiseParams) / 4;
+	static_assert(sizeof(NoiseParams) % 4 == 0, "NoiseParams must be a whole number of words");
+	for (int w = threadIdx.x; w < words; w += blockDim.x) {
+		reinterpret_cast<uint32_t*>(&sp)[w] = __ldg(reinterpret_cast<const uint32_t*>(dNp) + w);
+	}
+	__syncthreads();
 }
 
 __device__ __forceinline__ float noiseNormal(const NoiseParams& np, int i)
 {
-	const uint32_t lo = np.dFrame ? __ldg(np.dFrame) : np.frameLo;
-	const uint32_t hi = np.dFrame ? __ldg(np.dFrame + 1) : np.frameHi;
-	return standardNormal(np.seedLo, np.seedHi, np.kind, (uint32_t) i, lo, hi);
+	return standardNormal(np.seedLo, np.seedHi, np.kind, (uint32_t) i, np.frameLo, np.frameHi);
 }
 
 __device__ __forceinline__ Mat34 axisRotation(int axis, float angle)
@@ -73,8 +86,10 @@ __device__ __forceinline__ Mat34 axisRotation(int axis, float angle)
 	return rotationAxis(axis, c, s);
 }
 
-__global__ void kNoiseAngularRay(const Mat34* __restrict__ in, Mat34* __restrict__ out, int n, NoiseParams np)
+__global__ void kNoiseAngularRay(const Mat34* __restrict__ in, Mat34* __restrict__ out, int n, const NoiseParams* __restrict__ dNp)
 {
+	__shared__ NoiseParams np;
+	loadNoise(np, dNp);
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < n) {
 		float angle = np.mean + noiseNormal(np, i) * np.stDev;
@@ -84,8 +99,10 @@ __global__ void kNoiseAngularRay(const Mat34* __restrict__ in, Mat34* __restrict
 }
 
 __global__ void kNoiseAngularHitpoint(const float* __restrict__ inXyz, float* __restrict__ outXyz, float* __restrict__ outDist,
-                                      int cap, const int32_t* dCount, NoiseParams np)
+                                      int cap, const int32_t* dCount, const NoiseParams* __restrict__ dNp)
 {
+	__shared__ NoiseParams np;
+	loadNoise(np, dNp);
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < countOf(cap, dCount)) {
 		float angle = np.mean + noiseNormal(np, i) * np.stDev;
@@ -98,8 +115,10 @@ __global__ void kNoiseAngularHitpoint(const float* __restrict__ inXyz, float* __
 }
 
 __global__ void kNoiseDistance(const float* __restrict__ inXyz, const float* __restrict__ inDist, float* __restrict__ outXyz,
-                               float* __restrict__ outDist, int cap, const int32_t* dCount, NoiseParams np)
+                               float* __restrict__ outDist, int cap, const int32_t* dCount, const NoiseParams* __restrict__ dNp)
 {
+	__shared__ NoiseParams np;
+	loadNoise(np, dNp);
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < countOf(cap, dCount)) {
 		float d = inDist[i];
@@ -299,23 +318,23 @@ __global__ void kAosToSoa(const uint8_t* __restrict__ in, int pointSize, int n, 
 
 } // namespace
 
-void launchTransformRays(const Mat34* in, Mat34* out, int n, Mat34 tf, cudaStream_t s)
+void launchTransformRays(const Mat34* in, Mat34* out, int n, const Mat34* dTf, cudaStream_t s)
 {
 	if (n > 0) {
-		kTransformRays<<<blocks(n, kBlock), kBlock, 0, s>>>(in, out, n, tf);
+		kTransformRays<<<blocks(n, kBlock), kBlock, 0, s>>>(in, out, n, dTf);
 		countLaunch();
 	}
 }
 
-void launchTransformPoints(const float* in, float* out, int cap, const int32_t* dCount, Mat34 tf, cudaStream_t s)
+void launchTransformPoints(const float* in, float* out, int cap, const int32_t* dCount, const Mat34* dTf, cudaStream_t s)
 {
 	if (cap > 0) {
-		kTransformPoints<<<blocks(cap, kBlock), kBlock, 0, s>>>(in, out, cap, dCount, tf);
+		kTransformPoints<<<blocks(cap, kBlock), kBlock, 0, s>>>(in, out, cap, dCount, dTf);
 		countLaunch();
 	}
 }
 
-void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams& np, cudaStream_t s)
+void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams* np, cudaStream_t s)
 {
 	if (n > 0) {
 		kNoiseAngularRay<<<blocks(n, kBlock), kBlock, 0, s>>>(in, out, n, np);
@@ -324,7 +343,7 @@ void launchNoiseAngularRay(const Mat34* in, Mat34* out, int n, const NoiseParams
 }
 
 void launchNoiseAngularHitpoint(const float* inXyz, float* outXyz, float* outDist, int cap, const int32_t* dCount,
-                                const NoiseParams& np, cudaStream_t s)
+                                const NoiseParams* np, cudaStream_t s)
 {
 	if (cap > 0) {
 		kNoiseAngularHitpoint<<<blocks(cap, kBlock), kBlock, 0, s>>>(inXyz, outXyz, outDist, cap, dCount, np);
@@ -333,7 +352,7 @@ void launchNoiseAngularHitpoint(const float* inXyz, float* outXyz, float* outDis
 }
 
 void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz, float* outDist, int cap, const int32_t* dCount,
-                         const NoiseParams& np, cudaStream_t s)
+                         const NoiseParams* np, cudaStream_t s)
 {
 	if (cap > 0) {
 		kNoiseDistance<<<blocks(cap, kBlock), kBlock, 0, s>>>(inXyz, inDist, outXyz, outDist, cap, dCount, np);

@@ -93,6 +93,20 @@ void Scene::clear()
 	timeNs = 0;
 }
 
+void Scene::releaseDevice()
+{
+	rgl::freeTlas(tlas);
+	dInstances.release();
+	dView.release();
+	if (ready) {
+		cudaEventDestroy(ready);
+		ready = nullptr;
+	}
+	readyRecorded = false;
+	topologyDirty = true;
+	posesDirty = true;
+}
+
 void Scene::stats(int64_t& nodeBytes, int64_t& triangleBytes) const
 {
 	std::set<const Mesh*> seen;
@@ -110,34 +124,18 @@ void Scene::stats(int64_t& nodeBytes, int64_t& triangleBytes) const
 
 void Scene::checkDeviceErrors()
 {
-	if (dError.get() == nullptr) {
-		return;
-	}
-	int32_t e = 0;
-	RGL_CHECK_CUDA(cudaMemcpy(&e, dError.get(), sizeof(e), cudaMemcpyDeviceToHost));
-	if (e != 0) {
-		RGL_CHECK_CUDA(cudaMemset(dError.get(), 0, sizeof(int32_t)));
+	if (dError.raised()) {
+		dError.clear();
 		throw std::runtime_error("acceleration structure build failed on the device (radix sort look-back timed out)");
 	}
 }
 
-void Scene::prepare(cudaStream_t s)
+// Instance records (world boxes padded outward) in pinned host memory, and the world bounds.
+rgl::InstanceRec* Scene::fillInstanceRecords()
 {
-	if (ready == nullptr) {
-		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-	}
-	if (dError.get() == nullptr) {
-		dError.ensure(sizeof(int32_t));
-		RGL_CHECK_CUDA(cudaMemset(dError.get(), 0, sizeof(int32_t)));
-	}
-	if (!topologyDirty && !posesDirty && readyRecorded) {
-		RGL_CHECK_CUDA(cudaStreamWaitEvent(s, ready, 0));
-		return;
-	}
 	const int n = (int) entities.size();
-	for (auto& e : entities) {
-		e->mesh->ensureBlas(s);
-	}
+	worldLo[0] = worldLo[1] = worldLo[2] = INFINITY;
+	worldHi[0] = worldHi[1] = worldHi[2] = -INFINITY;
 	auto* rec = static_cast<rgl::InstanceRec*>(hInstances.ensure(sizeof(rgl::InstanceRec) * std::max(1, n)));
 	for (int i = 0; i < n; ++i) {
 		const Entity& e = *entities[i];
@@ -170,13 +168,35 @@ void Scene::prepare(cudaStream_t s)
 		r.hiy = hi[1] + pad;
 		r.hiz = hi[2] + pad;
 		rec[i] = r;
+		for (int a = 0; a < 3; ++a) {
+			worldLo[a] = std::min(worldLo[a], (&r.lox)[a]);
+			worldHi[a] = std::max(worldHi[a], (&r.hix)[a]);
+		}
 	}
+	return rec;
+}
+
+void Scene::prepare(cudaStream_t s)
+{
+	if (ready == nullptr) {
+		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+	}
+	(void) dError.device();
+	if (!topologyDirty && !posesDirty && readyRecorded) {
+		RGL_CHECK_CUDA(cudaStreamWaitEvent(s, ready, 0));
+		return;
+	}
+	const int n = (int) entities.size();
+	for (auto& e : entities) {
+		e->mesh->ensureBlas(s);
+	}
+	auto* rec = fillInstanceRecords();
 	auto* dInst = static_cast<rgl::InstanceRec*>(dInstances.ensure(sizeof(rgl::InstanceRec) * std::max(1, n)));
 	if (n > 0) {
 		RGL_CHECK_CUDA(cudaMemcpyAsync(dInst, rec, sizeof(rgl::InstanceRec) * n, cudaMemcpyHostToDevice, s));
 	}
 	if (topologyDirty || tlas.nInstances != n) {
-		rgl::buildTlas(dInst, n, tlas, dError.as<int32_t>(), s);
+		rgl::buildTlas(dInst, n, tlas, dError.device(), s);
 		++tlasBuilds;
 	} else {
 		rgl::refitTlas(dInst, tlas, s);
@@ -192,4 +212,32 @@ void Scene::prepare(cudaStream_t s)
 	readyRecorded = true;
 	topologyDirty = false;
 	posesDirty = false;
+}
+
+void Scene::prepareBatched(cudaStream_t s)
+{
+	if (topologyDirty || !readyRecorded || tlas.nInstances != (int) entities.size()) {
+		prepare(s);
+		return;
+	}
+	if (posesDirty) {
+		fillInstanceRecords();
+		posesDirty = false;
+	}
+}
+
+void Scene::enqueueRefit(cudaStream_t s)
+{
+	const int n = (int) entities.size();
+	if (n == 0) {
+		return;
+	}
+	RGL_CHECK_CUDA(cudaMemcpyAsync(dInstances.get(), hInstances.get(), sizeof(rgl::InstanceRec) * n, cudaMemcpyHostToDevice, s));
+	rgl::refitTlas(dInstances.as<rgl::InstanceRec>(), tlas, s);
+}
+
+void Scene::recordReady(cudaStream_t s)
+{
+	RGL_CHECK_CUDA(cudaEventRecord(ready, s));
+	readyRecorded = true;
 }

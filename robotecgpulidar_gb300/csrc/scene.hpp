@@ -54,15 +54,29 @@ struct Scene
 	void addEntity(const std::shared_ptr<Entity>& e);
 	void removeEntity(Entity* e);
 	void clear();
+	// Frees the TLAS and instance buffers (a scene made by rgl_gb300_scene_create being destroyed).
+	void releaseDevice();
 	void markPosesDirty() { posesDirty = true; }
 
 	// Builds/refits what changed on stream `s`; afterwards `s` may read view().
 	void prepare(cudaStream_t s);
+	// Batched frames refit inside their captured graph: prepareBatched() does what cannot be
+	// captured (new BLAS, TLAS topology: through prepare()) and otherwise only refreshes the pinned
+	// instance records after pose changes; enqueueRefit() uploads the records and refits the TLAS on
+	// `s` and may be captured. structureVersion() changes whenever the buffers enqueueRefit() uses
+	// may have moved.
+	void prepareBatched(cudaStream_t s);
+	void enqueueRefit(cudaStream_t s);
+	void recordReady(cudaStream_t s);
+	uint64_t structureVersion() const { return tlasBuilds; }
+	// World bounds of the instance boxes at the last prepare.
+	const float* worldLower() const { return worldLo; }
+	const float* worldUpper() const { return worldHi; }
 	const rgl::SceneView* view() const { return dView.as<rgl::SceneView>(); }
 	size_t entityCount() const { return entities.size(); }
 	// Bytes of built BLAS wide nodes and triangle records over the distinct meshes in the scene.
 	void stats(int64_t& nodeBytes, int64_t& triangleBytes) const;
-	int32_t* errorFlag() const { return dError.as<int32_t>(); }
+	int32_t* errorFlag() { return dError.device(); }
 	void checkDeviceErrors();
 
 	uint64_t timeNs = 0;
@@ -72,14 +86,16 @@ struct Scene
 	uint64_t tlasBuilds = 0, tlasRefits = 0;
 
 private:
+	rgl::InstanceRec* fillInstanceRecords();
 	std::vector<std::shared_ptr<Entity>> entities;
+	float worldLo[3] = {0, 0, 0}, worldHi[3] = {0, 0, 0};
 	bool topologyDirty = true;
 	bool posesDirty = true;
 	rgl::DeviceBuffer dInstances{false};
 	rgl::PinnedBuffer hInstances;
 	rgl::DeviceBuffer dView; // fixed size: its address never changes once allocated
 	rgl::PinnedBuffer hView;
-	rgl::DeviceBuffer dError{false};
+	rgl::ErrorSlot dError;
 	rgl::TlasBuild tlas;
 	cudaEvent_t ready = nullptr;
 	bool readyRecorded = false;

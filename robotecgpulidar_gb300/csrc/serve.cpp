@@ -1,0 +1,473 @@
+#include "serve.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "scene.hpp"
+
+using rgl::format;
+
+Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmBudgetBytes), maxInFlight(std::max(1, maxInFlightBatches))
+{
+	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+	int dev = 0;
+	RGL_CHECK_CUDA(cudaGetDevice(&dev));
+	cudaMemPoolProps props{};
+	props.allocType = cudaMemAllocationTypePinned;
+	props.location.type = cudaMemLocationTypeDevice;
+	props.location.id = dev;
+	RGL_CHECK_CUDA(cudaMemPoolCreate(&pool, &props));
+	uint64_t keep = UINT64_MAX; // freed blocks stay reserved for the next requests
+	RGL_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+	for (int i = 0; i < maxInFlight; ++i) {
+		auto s = std::make_unique<Slot>();
+		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+		s->counter.ensure(sizeof(uint32_t));
+		slots.push_back(std::move(s));
+	}
+	worker = std::thread([this] { loop(); });
+}
+
+Server::~Server()
+{
+	{
+		std::lock_guard<std::mutex> g(m);
+		stop = true;
+	}
+	cvWork.notify_all();
+	if (worker.joinable()) {
+		worker.join();
+	}
+	cudaStreamSynchronize(stream);
+	for (auto& kv : requests) {
+		if (kv.second->outXyz) {
+			cudaFreeAsync(kv.second->outXyz, stream);
+		}
+	}
+	for (float* p : toFree) {
+		cudaFreeAsync(p, stream);
+	}
+	cudaStreamSynchronize(stream);
+	for (auto& s : slots) {
+		cudaEventDestroy(s->done);
+	}
+	cudaMemPoolDestroy(pool);
+	cudaStreamDestroy(stream);
+}
+
+int32_t Server::addPattern(const void* rays, int32_t count)
+{
+	auto p = std::make_unique<Pattern>();
+	RGL_CHECK_CUDA(cudaMemcpy(p->rays.ensure(sizeof(rgl::Mat34) * (size_t) count), rays, sizeof(rgl::Mat34) * (size_t) count,
+	                          cudaMemcpyHostToDevice));
+	p->count = count;
+	std::lock_guard<std::mutex> g(m);
+	patterns.push_back(std::move(p));
+	return (int32_t) patterns.size() - 1;
+}
+
+int64_t Server::submit(std::shared_ptr<Scene> scene, int32_t pattern, const rgl::Mat34& pose, int32_t returnMode, float minRange,
+                       float maxRange)
+{
+	std::unique_lock<std::mutex> lk(m);
+	if (pattern < 0 || pattern >= (int32_t) patterns.size()) {
+		throw rgl::InvalidAPIArgument(format("pattern %d was not added to this server", (int) pattern));
+	}
+	auto r = std::make_unique<Request>();
+	r->id = nextId++;
+	r->scene = std::move(scene);
+	r->pattern = pattern;
+	r->pose = pose;
+	r->returnMode = returnMode;
+	r->returnCount = (int32_t) (((uint32_t) returnMode) >> 24);
+	r->minRange = minRange;
+	r->maxRange = maxRange;
+	r->beams = patterns[pattern]->count;
+	r->points = r->beams * r->returnCount;
+	r->reservedBytes = r->points * (kRawBytesPerPoint + kOutBytesPerPoint);
+	if (r->reservedBytes > budget) {
+		throw rgl::InvalidAPIArgument(
+		    format("request needs %lld bytes, more than the server's HBM budget of %lld", (long long) r->reservedBytes, (long long) budget));
+	}
+	r->submitted = Clock::now();
+	const int64_t id = r->id;
+	pending.push_back(r.get());
+	requests.emplace(id, std::move(r));
+	++st.submitted;
+	++wakeups;
+	lk.unlock();
+	cvWork.notify_one();
+	return id;
+}
+
+Server::Request& Server::get(int64_t id)
+{
+	auto it = requests.find(id);
+	if (it == requests.end()) {
+		throw rgl::InvalidAPIObject(format("RGL API Error: Object does not exist: Request %lld", (long long) id));
+	}
+	return *it->second;
+}
+
+bool Server::wait(int64_t id, double timeoutMs)
+{
+	std::unique_lock<std::mutex> lk(m);
+	Request& r = get(id);
+	auto ready = [&] { return r.state == State::Done || r.state == State::Failed; };
+	if (timeoutMs < 0) {
+		cvDone.wait(lk, ready);
+		return true;
+	}
+	return cvDone.wait_for(lk, std::chrono::duration<double, std::milli>(timeoutMs), ready);
+}
+
+int32_t Server::waitCompleted(int64_t* ids, int32_t capacity, double timeoutMs)
+{
+	{
+		std::unique_lock<std::mutex> lk(m);
+		cvDone.wait_for(lk, std::chrono::duration<double, std::milli>(std::max(0.0, timeoutMs)), [&] { return !completedIds.empty(); });
+	}
+	return takeCompleted(ids, capacity);
+}
+
+int32_t Server::takeCompleted(int64_t* ids, int32_t capacity)
+{
+	std::lock_guard<std::mutex> g(m);
+	int32_t n = 0;
+	while (n < capacity && !completedIds.empty()) {
+		const int64_t id = completedIds.front();
+		completedIds.pop_front();
+		if (requests.count(id)) { // released requests are not reported
+			ids[n++] = id;
+		}
+	}
+	return n;
+}
+
+void Server::resultSize(int64_t id, rgl_field_t field, int32_t& count, int32_t& size)
+{
+	std::lock_guard<std::mutex> g(m);
+	Request& r = get(id);
+	if (r.state == State::Failed) {
+		// Recoverable: one failed request leaves the server and the library usable.
+		throw rgl::InvalidPipeline(format("served request %lld failed: %s", (long long) id, r.error.c_str()));
+	}
+	if (r.state != State::Done) {
+		throw rgl::InvalidPipeline(format("request %lld has not completed", (long long) id));
+	}
+	if (field != RGL_FIELD_XYZ_VEC3_F32 && field != RGL_FIELD_DISTANCE_F32 && field != RGL_FIELD_ENTITY_ID_I32) {
+		throw rgl::InvalidAPIArgument(format("served requests provide XYZ_VEC3_F32, DISTANCE_F32 and ENTITY_ID_I32, not %s",
+		                                     rgl::fieldName(field)));
+	}
+	count = r.count;
+	size = (int32_t) rgl::fieldSize(field);
+}
+
+void Server::resultData(int64_t id, rgl_field_t field, void* dst)
+{
+	int32_t count = 0, size = 0;
+	resultSize(id, field, count, size);
+	const void* src = nullptr;
+	{
+		std::lock_guard<std::mutex> g(m);
+		Request& r = get(id);
+		float* base = r.outXyz;
+		if (field == RGL_FIELD_XYZ_VEC3_F32) {
+			src = base;
+		} else if (field == RGL_FIELD_DISTANCE_F32) {
+			src = base + 3 * r.points;
+		} else {
+			src = base + 4 * r.points;
+		}
+	}
+	if (count > 0) {
+		RGL_CHECK_CUDA(cudaMemcpy(dst, src, (size_t) count * size, cudaMemcpyDeviceToHost));
+	}
+}
+
+void Server::timing(int64_t id, double& queuedS, double& totalS)
+{
+	std::lock_guard<std::mutex> g(m);
+	Request& r = get(id);
+	if (r.state != State::Done && r.state != State::Failed) {
+		throw rgl::InvalidPipeline(format("request %lld has not completed", (long long) id));
+	}
+	queuedS = std::chrono::duration<double>(r.admitted - r.submitted).count();
+	totalS = std::chrono::duration<double>(r.completed - r.submitted).count();
+}
+
+void Server::release(int64_t id)
+{
+	std::unique_lock<std::mutex> lk(m);
+	Request& r = get(id);
+	if (r.state == State::Pending || r.state == State::InFlight) {
+		lk.unlock();
+		wait(id, -1.0);
+		lk.lock();
+	}
+	Request& q = get(id);
+	if (q.outXyz) {
+		toFree.push_back(q.outXyz); // freed on the server's stream by its thread
+	}
+	reserved -= q.points * kOutBytesPerPoint;
+	requests.erase(id);
+	++wakeups;
+	lk.unlock();
+	cvWork.notify_one();
+}
+
+void Server::drain()
+{
+	std::unique_lock<std::mutex> lk(m);
+	cvDone.wait(lk, [&] { return pending.empty() && inFlight.empty(); });
+}
+
+Server::Stats Server::stats()
+{
+	std::lock_guard<std::mutex> g(m);
+	Stats s = st;
+	s.reserved = reserved;
+	s.inFlight = (int64_t) inFlight.size();
+	s.pending = (int64_t) pending.size();
+	return s;
+}
+
+// Builds and enqueues one batch from slot.reqs (already admitted, outputs allocated).
+void Server::launch(Slot& slot)
+{
+	const int n = (int) slot.reqs.size();
+	int64_t points = 0;
+	for (auto* r : slot.reqs) {
+		points += r->points;
+	}
+	auto* flags = static_cast<int32_t*>(slot.rawFlags.ensure(sizeof(int32_t) * std::max<int64_t>(points, 1)));
+	auto* xyz = static_cast<float*>(slot.rawXyz.ensure(sizeof(float) * 3 * std::max<int64_t>(points, 1)));
+	auto* dist = static_cast<float*>(slot.rawDist.ensure(sizeof(float) * std::max<int64_t>(points, 1)));
+	auto* ent = static_cast<int32_t*>(slot.rawEnt.ensure(sizeof(int32_t) * std::max<int64_t>(points, 1)));
+
+	// Table layout (16-byte aligned parts): jobs[n] | task bases[n+1] | segments[n] | tile bases[n+1].
+	auto align = [](size_t x) { return (x + 15) & ~size_t{15}; };
+	const size_t offTask = align(sizeof(rgl::BatchJob) * n);
+	const size_t offSeg = offTask + align(sizeof(int32_t) * (n + 1));
+	const size_t offTile = offSeg + align(sizeof(rgl::SegCompactJob) * n);
+	const size_t tableBytes = offTile + align(sizeof(int32_t) * (n + 1));
+	auto* hBase = static_cast<uint8_t*>(slot.hTables.ensure(tableBytes));
+	auto* dBase = static_cast<uint8_t*>(slot.tables.ensure(tableBytes));
+	auto* jobs = reinterpret_cast<rgl::BatchJob*>(hBase);
+	auto* taskBase = reinterpret_cast<int32_t*>(hBase + offTask);
+	auto* segs = reinterpret_cast<rgl::SegCompactJob*>(hBase + offSeg);
+	auto* tileBase = reinterpret_cast<int32_t*>(hBase + offTile);
+	// Results: counts[n], then one traversal error flag per request.
+	auto* dResults = static_cast<int32_t*>(slot.results.ensure(sizeof(int32_t) * 2 * n));
+	int64_t pointBase = 0, tasks = 0, tiles = 0;
+	for (int j = 0; j < n; ++j) {
+		Request& r = *slot.reqs[j];
+		rgl::BatchJob b{};
+		b.p.rays = patterns[r.pattern]->rays.as<rgl::Mat34>();
+		b.p.ranges = nullptr;
+		b.p.nRanges = 1;
+		b.p.nRays = (int32_t) r.beams;
+		b.p.nSamples = 1;
+		b.p.returnMode = r.returnMode;
+		b.p.returnCount = r.returnCount;
+		b.p.nearNonHitDistance = INFINITY;
+		b.p.farNonHitDistance = INFINITY;
+		b.p.defaultIntensity = 0.0f;
+		b.p.needIntensity = 0;
+		b.p.errorFlag = dResults + n + j;
+		b.p.scene = r.scene->view();
+		b.p.out.xyz = xyz + 3 * pointBase;
+		b.p.out.distance = dist + pointBase;
+		b.p.out.isHit = flags + pointBase;
+		b.p.out.entityId = ent + pointBase;
+		b.samples = nullptr; // one sample per beam: never read
+		b.order = nullptr;
+		b.groupSize = 1;
+		b.hasRayTransform = 1;
+		b.rayTransform = r.pose;
+		b.inlineRange[0] = r.minRange;
+		b.inlineRange[1] = r.maxRange;
+		jobs[j] = b;
+		taskBase[j] = (int32_t) tasks;
+		tasks += (r.beams + 31) / 32;
+
+		rgl::SegCompactJob sg{};
+		sg.flags = flags + pointBase;
+		sg.xyz = xyz + 3 * pointBase;
+		sg.dist = dist + pointBase;
+		sg.ent = ent + pointBase;
+		sg.outXyz = r.outXyz;
+		sg.outDist = r.outXyz + 3 * r.points;
+		sg.outEnt = reinterpret_cast<int32_t*>(r.outXyz + 4 * r.points);
+		sg.nPoints = (int32_t) r.points;
+		segs[j] = sg;
+		tileBase[j] = (int32_t) tiles;
+		tiles += (r.points + rgl::kSegTile - 1) / rgl::kSegTile;
+		pointBase += r.points;
+	}
+	taskBase[n] = (int32_t) tasks;
+	tileBase[n] = (int32_t) tiles;
+
+	auto* dTileCounts = slot.tileCounts.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
+	auto* dTileOffsets = slot.tileOffsets.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
+	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, stream));
+	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, stream));
+	rgl::launchTraceBatch(reinterpret_cast<const rgl::BatchJob*>(dBase), reinterpret_cast<const int32_t*>(dBase + offTask), n, 1, false,
+	                      schedule, slot.counter.as<uint32_t>(), stream);
+	rgl::launchSegCompact(reinterpret_cast<const rgl::SegCompactJob*>(dBase + offSeg), reinterpret_cast<const int32_t*>(dBase + offTile), n,
+	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, stream);
+	auto* hResults = static_cast<int32_t*>(slot.hResults.ensure(sizeof(int32_t) * 2 * n));
+	RGL_CHECK_CUDA(cudaMemcpyAsync(hResults, dResults, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.done, stream));
+	RGL_CHECK_CUDA(cudaLaunchHostFunc(stream, &Server::batchDone, this));
+}
+
+// Runs on a CUDA host thread once a batch's stream work is done: wakes the scheduler, which then
+// finds the batch's event complete. Makes no CUDA call.
+void CUDART_CB Server::batchDone(void* self)
+{
+	auto* s = static_cast<Server*>(self);
+	{
+		// The scheduler never makes a CUDA call that waits for this stream while holding m.
+		std::lock_guard<std::mutex> g(s->m);
+		++s->wakeups;
+	}
+	s->cvWork.notify_all();
+}
+
+void Server::retire(Slot& slot)
+{
+	const auto* hCounts = static_cast<const int32_t*>(slot.hResults.get());
+	const size_t n = slot.reqs.size();
+	const auto now = Clock::now();
+	std::lock_guard<std::mutex> g(m);
+	for (size_t j = 0; j < n; ++j) {
+		Request& r = *slot.reqs[j];
+		const bool failed = hCounts[n + j] != 0;
+		r.count = hCounts[j];
+		r.state = failed ? State::Failed : State::Done;
+		if (failed) {
+			r.error = "traversal stack overflow on the device";
+			++st.failed;
+		}
+		r.completed = now;
+		reserved -= r.points * kRawBytesPerPoint;
+		completedIds.push_back(r.id);
+		++st.completed;
+	}
+	slot.reqs.clear();
+	slot.busy = false;
+	inFlight.pop_front();
+	cvDone.notify_all();
+}
+
+// Scheduler thread: retire finished batches, admit and launch the next batch whenever a slot is free,
+// otherwise wait for work or for the oldest batch.
+void Server::loop()
+{
+	const int dev = [] {
+		int d = 0;
+		cudaGetDevice(&d);
+		return d;
+	}();
+	cudaSetDevice(dev);
+	std::unique_lock<std::mutex> lk(m);
+	for (;;) {
+		const uint64_t seen = wakeups;
+		while (!inFlight.empty() && cudaEventQuery(inFlight.front()->done) == cudaSuccess) {
+			Slot* s = inFlight.front();
+			lk.unlock();
+			retire(*s);
+			lk.lock();
+		}
+		for (float* p : toFree) {
+			cudaFreeAsync(p, stream);
+		}
+		toFree.clear();
+		if (stop && pending.empty() && inFlight.empty()) {
+			break;
+		}
+		Slot* freeSlot = nullptr;
+		for (auto& s : slots) {
+			if (!s->busy) {
+				freeSlot = s.get();
+				break;
+			}
+		}
+		if (freeSlot != nullptr && !pending.empty()) {
+			// Admission: first come first served, within the HBM budget and the batch limits.
+			std::vector<Request*> batch;
+			int64_t beams = 0;
+			while (!pending.empty() && (int) batch.size() < rgl::kMaxBatchJobs) {
+				Request* r = pending.front();
+				if (reserved + r->reservedBytes > budget || (!batch.empty() && beams + r->beams > maxBatchBeams)) {
+					break;
+				}
+				pending.pop_front();
+				reserved += r->reservedBytes;
+				st.peakReserved = std::max(st.peakReserved, reserved);
+				beams += r->beams;
+				r->state = State::InFlight;
+				r->admitted = Clock::now();
+				batch.push_back(r);
+			}
+			if (!batch.empty()) {
+				freeSlot->busy = true;
+				freeSlot->reqs = batch;
+				inFlight.push_back(freeSlot);
+				++st.batches;
+				st.jobsInBatches += (int64_t) batch.size();
+				lk.unlock();
+				bool ok = true;
+				std::string why;
+				try {
+					std::vector<Scene*> prepared;
+					for (auto* r : batch) {
+						if (std::find(prepared.begin(), prepared.end(), r->scene.get()) == prepared.end()) {
+							r->scene->prepare(stream);
+							prepared.push_back(r->scene.get());
+						}
+						const size_t bytes = (size_t) r->points * kOutBytesPerPoint;
+						void* p = nullptr;
+						RGL_CHECK_CUDA(cudaMallocFromPoolAsync(&p, std::max<size_t>(bytes, 256), pool, stream));
+						r->outXyz = static_cast<float*>(p);
+					}
+					launch(*freeSlot);
+				}
+				catch (std::exception& e) {
+					ok = false;
+					why = e.what();
+				}
+				catch (...) {
+					ok = false;
+					why = "unknown exception";
+				}
+				lk.lock();
+				if (!ok) {
+					// The batch never reached the device: fail its requests.
+					const auto now = Clock::now();
+					for (auto* r : batch) {
+						r->state = State::Failed;
+						r->error = "batch launch failed: " + why;
+						++st.failed;
+						r->completed = now;
+						reserved -= r->points * kRawBytesPerPoint;
+						completedIds.push_back(r->id);
+					}
+					freeSlot->reqs.clear();
+					freeSlot->busy = false;
+					inFlight.erase(std::find(inFlight.begin(), inFlight.end(), freeSlot));
+					cvDone.notify_all();
+				}
+				continue;
+			}
+		}
+		if (inFlight.empty()) {
+			cvDone.notify_all(); // drain() waiters
+		}
+		// Sleep until a submission, a release or a finished batch (its host function) changes the
+		// picture; the timeout is only a safety net.
+		cvWork.wait_for(lk, std::chrono::milliseconds(5), [&] { return wakeups != seen || stop; });
+	}
+}

@@ -1,0 +1,140 @@
+// Serving loop behind rgl_gb300_server_t (extension; the reference has no serving layer: a client
+// runs one rgl_graph_run per scan, src/api/apiCore.cpp:530-544).
+//
+// Virtual robots register their lidar ray patterns once (resident on the device) and then submit
+// scan requests: (scene, pattern, sensor pose, return mode, range). A scheduler thread admits
+// requests first-come-first-served while the bytes of admitted requests stay under an HBM budget
+// and fewer than `maxInFlight` batches are on the GPU, coalesces every admitted request into one
+// batch, and launches it: one persistent traversal over all requests (trace_batch.cu; each job
+// names its scene and applies its pose in-kernel with the arithmetic of a rays-transform node) and
+// one segmented compaction by is-hit (segcompact.cu). Requests that arrive while batches run are
+// admitted as slots and memory free up and go into the next batch, so the device always has the
+// next batch queued behind the running one (continuous batching).
+//
+// Each request's result is XYZ, distance and entity id of its hit points, in point order, equal to
+// what the graph rays_from_mat3x4f(pattern) -> rays_transform(pose) -> rays_set_range ->
+// raytrace(scene, mode) -> compact_by_field(IS_HIT) -> yield writes. Results stay on the device until
+// the client copies them; release() frees them.
+//
+// While a server runs, the scenes it traces must not be modified (drain() first).
+#pragma once
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "common.hpp"
+#include "kernels.hpp"
+
+struct Scene;
+
+struct Server
+{
+	using Clock = std::chrono::steady_clock;
+
+	Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches);
+	~Server();
+
+	int32_t addPattern(const void* rays, int32_t count);
+	int64_t submit(std::shared_ptr<Scene> scene, int32_t pattern, const rgl::Mat34& pose, int32_t returnMode, float minRange,
+	               float maxRange);
+	// True when the request completed (or failed) within timeoutMs; timeoutMs < 0 waits forever.
+	bool wait(int64_t id, double timeoutMs);
+	int32_t takeCompleted(int64_t* ids, int32_t capacity);
+	// As takeCompleted, but waits up to timeoutMs for at least one completed request.
+	int32_t waitCompleted(int64_t* ids, int32_t capacity, double timeoutMs);
+	void resultSize(int64_t id, rgl_field_t field, int32_t& count, int32_t& size);
+	void resultData(int64_t id, rgl_field_t field, void* dst);
+	// Seconds from submission to admission into a batch, and to completion.
+	void timing(int64_t id, double& queuedS, double& totalS);
+	void release(int64_t id);
+	void drain();
+
+	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 80};
+	int64_t maxBatchBeams = 32 << 20;
+
+	struct Stats
+	{
+		int64_t submitted = 0, completed = 0, failed = 0, batches = 0, jobsInBatches = 0, peakReserved = 0, reserved = 0, inFlight = 0,
+		        pending = 0;
+	};
+	Stats stats();
+
+private:
+	enum class State
+	{
+		Pending,
+		InFlight,
+		Done,
+		Failed
+	};
+	struct Request
+	{
+		int64_t id;
+		std::shared_ptr<Scene> scene;
+		int32_t pattern;
+		rgl::Mat34 pose;
+		int32_t returnMode, returnCount;
+		float minRange, maxRange;
+		int64_t beams, points;
+		int64_t reservedBytes;
+		float* outXyz = nullptr; // one allocation: xyz | distance | entity id, `points` capacity each
+		int32_t count = 0;
+		State state = State::Pending;
+		std::string error; // why a failed request failed
+		Clock::time_point submitted, admitted, completed;
+	};
+	struct Pattern
+	{
+		rgl::DeviceBuffer rays{false};
+		int32_t count = 0;
+	};
+	// One in-flight batch slot: device and pinned buffers reused by every batch launched from it.
+	// The job table, task bases, compaction segments and tile bases travel in one upload; the
+	// per-request counts and the traversal's error flag come back in one download.
+	struct Slot
+	{
+		std::vector<Request*> reqs;
+		cudaEvent_t done = nullptr;
+		rgl::DeviceBuffer tables{false}, tileCounts{false}, tileOffsets{false}, results{false}, counter{false};
+		rgl::DeviceBuffer rawFlags{false}, rawXyz{false}, rawDist{false}, rawEnt{false};
+		rgl::PinnedBuffer hTables, hResults;
+		bool busy = false;
+	};
+
+	static constexpr int64_t kRawBytesPerPoint = 4 + 12 + 4 + 4; // flags, xyz, distance, entity id
+	static constexpr int64_t kOutBytesPerPoint = 12 + 4 + 4;
+
+	void loop();
+	void launch(Slot& slot);
+	void retire(Slot& slot);
+	Request& get(int64_t id);
+	static void CUDART_CB batchDone(void* self);
+
+	int64_t budget;
+	int maxInFlight;
+	cudaStream_t stream = nullptr;
+	cudaMemPool_t pool = nullptr;
+	std::vector<std::unique_ptr<Pattern>> patterns;
+	std::vector<std::unique_ptr<Slot>> slots;
+	std::deque<Slot*> inFlight;
+
+	std::mutex m;
+	std::condition_variable cvWork, cvDone;
+	std::deque<Request*> pending;
+	std::unordered_map<int64_t, std::unique_ptr<Request>> requests;
+	std::deque<int64_t> completedIds;
+	std::vector<float*> toFree;
+	int64_t nextId = 1;
+	int64_t reserved = 0;
+	Stats st;
+	bool stop = false;
+	uint64_t wakeups = 0; // bumped (under m) by submissions, releases and finished batches
+	std::thread worker;
+};

@@ -216,7 +216,38 @@ RGL_HD uint32_t asUint(float f)
 #endif
 }
 
-RGL_HD float byteF(uint32_t w, int sh) { return (float) ((w >> sh) & 0xffu); }
+// Byte k of w as a float. On the device: the byte placed under the exponent of 2^23 (PRMT) minus
+// 2^23, which is exact for 0..255 and keeps the conversion off the integer pipe.
+RGL_HD float byteF(uint32_t w, int k)
+{
+#if defined(__CUDA_ARCH__)
+	return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t) k)) - 8388608.0f;
+#else
+	return (float) ((w >> (8 * k)) & 0xffu);
+#endif
+}
+
+// max(a, b, c, d) and min(a, b, c, d) of the slab test; three-input min/max on the device.
+RGL_HD float max4(float a, float b, float c, float d)
+{
+#if defined(__CUDA_ARCH__)
+	float m;
+	asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+	return fmaxf(m, d);
+#else
+	return maxf_(maxf_(a, b), maxf_(c, d));
+#endif
+}
+RGL_HD float min4(float a, float b, float c, float d)
+{
+#if defined(__CUDA_ARCH__)
+	float m;
+	asm("min.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+	return fminf(m, d);
+#else
+	return minf_(minf_(a, b), minf_(c, d));
+#endif
+}
 
 template<class Stack, class NodeLoader>
 RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 d, Stack& st, HitRec& best,
@@ -246,13 +277,13 @@ RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 
 #pragma unroll
 #endif
 		for (int s = 0; s < kWideArity; ++s) {
-			const int sh = (s & 3) * 8;
+			const int k = s & 3;
 			const bool hiw = s >= 4;
-			const float tnx = fmaf(byteF(hiw ? nx1 : nx0, sh), Ax, Cx), tfx = fmaf(byteF(hiw ? fx1 : fx0, sh), Ax, Cx);
-			const float tny = fmaf(byteF(hiw ? ny1 : ny0, sh), Ay, Cy), tfy = fmaf(byteF(hiw ? fy1 : fy0, sh), Ay, Cy);
-			const float tnz = fmaf(byteF(hiw ? nz1 : nz0, sh), Az, Cz), tfz = fmaf(byteF(hiw ? fz1 : fz0, sh), Az, Cz);
-			const float tEntry = maxf_(maxf_(tnx, tny), maxf_(tnz, 0.0f));
-			const float tExit = minf_(minf_(tfx, tfy), minf_(tfz, best.t));
+			const float tnx = fmaf(byteF(hiw ? nx1 : nx0, k), Ax, Cx), tfx = fmaf(byteF(hiw ? fx1 : fx0, k), Ax, Cx);
+			const float tny = fmaf(byteF(hiw ? ny1 : ny0, k), Ay, Cy), tfy = fmaf(byteF(hiw ? fy1 : fy0, k), Ay, Cy);
+			const float tnz = fmaf(byteF(hiw ? nz1 : nz0, k), Az, Cz), tfz = fmaf(byteF(hiw ? fz1 : fz0, k), Az, Cz);
+			const float tEntry = max4(tnx, tny, tnz, 0.0f);
+			const float tExit = min4(tfx, tfy, tfz, best.t);
 			if (tEntry <= tExit * kSlabRelSlack) {
 				if ((imask >> s) & 1u) {
 					internalHits |= 1u << (s ^ oct);

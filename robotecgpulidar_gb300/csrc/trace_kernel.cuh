@@ -1,0 +1,325 @@
+// Device pieces shared by the single-sensor traversal kernel (trace.cu) and the batched
+// multi-sensor kernel (trace_batch.cu): the traversal stack, the loaders, one traced sample, the
+// in-order return selection and the per-point field writes.
+//
+// Return selection restates reference src/gpu/nodeKernels.cu:334-422 (kReduceDivergentBeams) with
+// its quirks:
+//  * the first hit sample (in sample order) seeds first/second/last/strongest/second-strongest;
+//  * a closer sample makes the old first the second; a sample strictly between first and second
+//    becomes second (with second seeded equal to first this never fires - kept as is);
+//  * last = strictly farther; strongest/second-strongest by strict intensity comparisons;
+//  * a beam without hits reports sample 0's non-hit distance (near below min range, far on a miss).
+// Field writes restate nodeKernels.cu:103-207 (saveReturnAsHit / saveReturnAsNonHit).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+#include "trace_core.hpp"
+
+namespace rgl {
+namespace tracedev {
+
+constexpr int kSmemStack = 24;  // entries per thread in shared memory
+constexpr int kLocalStack = 40; // overflow entries per thread in local memory
+
+// Traversal stack: the first kSmemStack entries in this thread's shared-memory column (stride =
+// threads per block), the rest in local memory. Overflow past both is flagged, never written.
+struct DevStack
+{
+	uint2* sm;
+	int stride;
+	int sp;
+	bool overflow;
+	uint2 local[kLocalStack];
+
+	__device__ __forceinline__ void push(uint32_t a, uint32_t b)
+	{
+		const uint2 e = make_uint2(a, b);
+		if (sp < kSmemStack) {
+			sm[sp * stride] = e;
+		} else if (sp < kSmemStack + kLocalStack) {
+			local[sp - kSmemStack] = e;
+		} else {
+			overflow = true;
+			return;
+		}
+		++sp;
+	}
+	__device__ __forceinline__ void pop(uint32_t& a, uint32_t& b)
+	{
+		--sp;
+		const uint2 e = sp < kSmemStack ? sm[sp * stride] : local[sp - kSmemStack];
+		a = e.x;
+		b = e.y;
+	}
+	__device__ __forceinline__ int size() const { return sp; }
+};
+
+struct DevLoader
+{
+	__device__ __forceinline__ void nodeWords(const WideNode* base, uint32_t i, uint4& w0, uint4& w1, uint4& w2, uint4& w3,
+	                                          uint4& w4) const
+	{
+		const uint4* p = reinterpret_cast<const uint4*>(base + i);
+		w0 = __ldg(p);
+		w1 = __ldg(p + 1);
+		w2 = __ldg(p + 2);
+		w3 = __ldg(p + 3);
+		w4 = __ldg(p + 4);
+	}
+	__device__ __forceinline__ TriRecord tri(const TriRecord* base, int32_t i) const
+	{
+		const float4* p = reinterpret_cast<const float4*>(base + i);
+		const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+		TriRecord t;
+		t.v0x = a.x;
+		t.v0y = a.y;
+		t.v0z = a.z;
+		t.primId = __float_as_int(a.w);
+		t.v1x = b.x;
+		t.v1y = b.y;
+		t.v1z = b.z;
+		t.pad1 = 0;
+		t.v2x = c.x;
+		t.v2y = c.y;
+		t.v2z = c.z;
+		t.pad2 = 0;
+		return t;
+	}
+	__device__ __forceinline__ const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
+	__device__ __forceinline__ BinNode bin(const BinNode* base, int32_t i) const
+	{
+		const float4* p = reinterpret_cast<const float4*>(base + i);
+		const float4 a = __ldg(p), b = __ldg(p + 1);
+		BinNode n;
+		n.lox = a.x;
+		n.loy = a.y;
+		n.loz = a.z;
+		n.left = __float_as_int(a.w);
+		n.hix = b.x;
+		n.hiy = b.y;
+		n.hiz = b.z;
+		n.right = __float_as_int(b.w);
+		return n;
+	}
+};
+
+// One traced sample. For non-hits `dist` holds the non-hit distance (near or far).
+struct SampleVal
+{
+	uint32_t hit;
+	float dist;
+	float intensity;
+	int32_t entity;
+	float nx, ny, nz, cosInc;
+};
+
+struct Selected
+{
+	float dist;
+	float intensity;
+	int32_t entity;
+	float nx, ny, nz, cosInc;
+};
+
+__device__ __forceinline__ SampleVal emptySample() { return SampleVal{0u, 0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f}; }
+
+__device__ __forceinline__ Mat34 loadMat(const Mat34* p)
+{
+	const float4* q = reinterpret_cast<const float4*>(p);
+	float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+	return Mat34{{{a.x, a.y, a.z, a.w}, {b.x, b.y, b.z, b.w}, {c.x, c.y, c.z, c.w}}};
+}
+
+// Closest hit of sample ray `sr` (reference optixPrograms.cu:89-136): distance = t * |dir| (the
+// reference's FP64 norm of the object-space offset equals this within the stated tolerance), the
+// min-range rule turns a closer hit into the near non-hit without continuing, a miss gives the far
+// non-hit distance. With SHADING the world normal, |cos| of the incidence and intensity are added.
+template<bool SHADING>
+__device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
+                                                 const Mat34& sr, float minRange, float maxRange, DevStack& st)
+{
+	DevLoader ld;
+	const Vec3 o = sr.rayOrigin();
+	const Vec3 d = sr.rayDir();
+	const HitRec h = traceClosest(sc, o, d, maxRange, st, ld);
+	SampleVal v = emptySample();
+	v.dist = farNonHit;
+	if (h.inst >= 0) {
+		const float dist = fmul(h.t, length(d));
+		if (dist < minRange) {
+			v.dist = nearNonHit;
+		} else {
+			const InstanceRec& inst = sc.instances[h.inst];
+			v.hit = 1;
+			v.dist = dist;
+			v.entity = inst.entityId;
+			if (SHADING) {
+				const TriRecord tr = ld.tri(inst.tris, h.tri);
+				const Vec3 wa = inst.objectToWorld.point(v3(tr.v0x, tr.v0y, tr.v0z));
+				const Vec3 wb = inst.objectToWorld.point(v3(tr.v1x, tr.v1y, tr.v1z));
+				const Vec3 wc = inst.objectToWorld.point(v3(tr.v2x, tr.v2y, tr.v2z));
+				const Vec3 n = normalized(cross(wb - wa, wc - wa));
+				const float c = fabsf(dot(n, d));
+				v.nx = n.x;
+				v.ny = n.y;
+				v.nz = n.z;
+				v.cosInc = c;
+				v.intensity = fmul(defaultIntensity, c);
+			}
+		}
+	}
+	return v;
+}
+
+__device__ __forceinline__ Selected toSelected(const SampleVal& v)
+{
+	return Selected{v.dist, v.intensity, v.entity, v.nx, v.ny, v.nz, v.cosInc};
+}
+
+// In-order selection over a beam's samples; add() must see samples 0, 1, 2, ... in order.
+struct ReturnReducer
+{
+	bool haveFirst;
+	float nonHitDist;
+	Selected first, second, last, strongest, secondStrongest;
+
+	__device__ __forceinline__ void init(float farNonHit)
+	{
+		haveFirst = false;
+		nonHitDist = farNonHit;
+		first = second = last = strongest = secondStrongest = Selected{0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+	}
+	__device__ __forceinline__ void add(int s, uint32_t hit, const Selected& cur)
+	{
+		if (s == 0 && !hit) {
+			nonHitDist = cur.dist;
+		}
+		if (!hit) {
+			return;
+		}
+		if (!haveFirst) {
+			first = second = last = strongest = secondStrongest = cur;
+			haveFirst = true;
+			return;
+		}
+		if (cur.dist < first.dist) {
+			second = first;
+			first = cur;
+		} else if (first.dist < cur.dist && cur.dist < second.dist) {
+			second = cur;
+		}
+		if (cur.dist > last.dist) {
+			last = cur;
+		}
+		if (cur.intensity > strongest.intensity) {
+			secondStrongest = strongest;
+			strongest = cur;
+		} else if (strongest.intensity > cur.intensity && cur.intensity > secondStrongest.intensity) {
+			secondStrongest = cur;
+		}
+	}
+};
+
+// Writes beam `beam`'s returns at points beam * returnCount + r. `ray` is the primary ray pose.
+__device__ __forceinline__ void writeReturns(const TraceOutputs& out, uint32_t beam, int32_t returnMode, int returnCount,
+                                             const Mat34& ray, const ReturnReducer& red)
+{
+	const Vec3 org = ray.rayOrigin();
+	const Vec3 dn = normalized(ray.rayDir());
+	for (int r = 0; r < returnCount; ++r) {
+		const size_t pi = (size_t) beam * returnCount + r;
+		const uint32_t type = (((uint32_t) returnMode) >> (8 * r)) & 0xffu;
+		if (out.rayIdx) {
+			out.rayIdx[pi] = beam;
+		}
+		if (!red.haveFirst) {
+			const float nonHitDist = red.nonHitDist;
+			Vec3 disp = dn * nonHitDist;
+			disp.x = isnan(disp.x) ? 0.0f : disp.x;
+			disp.y = isnan(disp.y) ? 0.0f : disp.y;
+			disp.z = isnan(disp.z) ? 0.0f : disp.z;
+			if (out.xyz) {
+				const Vec3 q = org + disp;
+				out.xyz[3 * pi] = q.x;
+				out.xyz[3 * pi + 1] = q.y;
+				out.xyz[3 * pi + 2] = q.z;
+			}
+			if (out.distance) out.distance[pi] = nonHitDist;
+			if (out.isHit) out.isHit[pi] = 0;
+			if (out.entityId) out.entityId[pi] = 0;
+			if (out.returnType) out.returnType[pi] = (uint8_t) type;
+			if (out.intensityF32) out.intensityF32[pi] = 0.0f;
+			if (out.intensityU8) out.intensityU8[pi] = 0;
+			if (out.normal) {
+				out.normal[3 * pi] = __int_as_float(0x7fc00000);
+				out.normal[3 * pi + 1] = __int_as_float(0x7fc00000);
+				out.normal[3 * pi + 2] = __int_as_float(0x7fc00000);
+			}
+			if (out.incidentAngle) out.incidentAngle[pi] = __int_as_float(0x7fc00000);
+			if (out.laserRetro) out.laserRetro[pi] = 0.0f;
+			continue;
+		}
+		Selected sel;
+		if (type == 4u) sel = red.first;
+		else if (type == 3u) sel = red.second;
+		else if (type == 2u) sel = red.last;
+		else if (type == 1u) sel = red.strongest;
+		else if (type == 5u) sel = red.secondStrongest;
+		else continue;
+		if (out.xyz) {
+			const Vec3 q = org + dn * sel.dist;
+			out.xyz[3 * pi] = q.x;
+			out.xyz[3 * pi + 1] = q.y;
+			out.xyz[3 * pi + 2] = q.z;
+		}
+		if (out.distance) out.distance[pi] = sel.dist;
+		if (out.isHit) out.isHit[pi] = 1;
+		if (out.entityId) out.entityId[pi] = sel.entity;
+		if (out.returnType) out.returnType[pi] = (uint8_t) type;
+		if (out.intensityF32) out.intensityF32[pi] = sel.intensity;
+		if (out.intensityU8) out.intensityU8[pi] = sel.intensity < 255.0f ? (uint8_t) roundf(sel.intensity) : (uint8_t) 255;
+		if (out.normal) {
+			out.normal[3 * pi] = sel.nx;
+			out.normal[3 * pi + 1] = sel.ny;
+			out.normal[3 * pi + 2] = sel.nz;
+		}
+		if (out.incidentAngle) out.incidentAngle[pi] = acosf(sel.cosInc);
+		if (out.laserRetro) out.laserRetro[pi] = 0.0f;
+	}
+}
+
+__device__ __forceinline__ float pick(int r, float a, float b) { return r == 0 ? a : b; }
+__device__ __forceinline__ uint32_t pickU(int r, uint32_t a, uint32_t b) { return r == 0 ? a : b; }
+
+// Lane-group packing: the S samples of a beam sit on G = min(S, 32) adjacent lanes (lane k of the
+// group holds samples k and k + G in sv[0], sv[1]); every lane of the warp takes part in the
+// shuffles, and the group's first lane (`leader`) feeds the samples in order to `red`.
+template<int ROUNDS, bool SHADING>
+__device__ __forceinline__ void reduceGroup(const SampleVal (&sv)[ROUNDS], int nSamples, int G, int groupLane0, bool leader,
+                                            ReturnReducer& red)
+{
+	for (int s = 0; s < nSamples; ++s) {
+		const int r = (ROUNDS == 1) ? 0 : s / G;
+		const int src = groupLane0 + (s - r * G);
+		const uint32_t hit = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].hit : pickU(r, sv[0].hit, sv[ROUNDS - 1].hit), src);
+		const float dist = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].dist : pick(r, sv[0].dist, sv[ROUNDS - 1].dist), src);
+		const int32_t ent = __shfl_sync(
+		    0xffffffffu, ROUNDS == 1 ? sv[0].entity : (int32_t) pickU(r, (uint32_t) sv[0].entity, (uint32_t) sv[ROUNDS - 1].entity), src);
+		Selected cur{dist, 0.0f, ent, 0.0f, 0.0f, 0.0f, 0.0f};
+		if (SHADING) {
+			cur.intensity = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].intensity : pick(r, sv[0].intensity, sv[ROUNDS - 1].intensity), src);
+			cur.nx = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].nx : pick(r, sv[0].nx, sv[ROUNDS - 1].nx), src);
+			cur.ny = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].ny : pick(r, sv[0].ny, sv[ROUNDS - 1].ny), src);
+			cur.nz = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].nz : pick(r, sv[0].nz, sv[ROUNDS - 1].nz), src);
+			cur.cosInc = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].cosInc : pick(r, sv[0].cosInc, sv[ROUNDS - 1].cosInc), src);
+		}
+		if (leader) {
+			red.add(s, hit, cur);
+		}
+	}
+}
+
+} // namespace tracedev
+} // namespace rgl

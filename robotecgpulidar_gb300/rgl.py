@@ -186,6 +186,29 @@ def _proto(l):
         "rgl_gb300_compact_by_flags_noalloc": [vp, vp, i32, i32, vp, P(i32), vp],
         "rgl_gb300_configure_cuda_graphs": [C.c_bool],
         "rgl_gb300_graph_get_capture_stats": [vp, P(C.c_int64), P(C.c_int64)],
+        "rgl_gb300_batch_create": [P(vp), P(vp), i32],
+        "rgl_gb300_batch_run": [vp],
+        "rgl_gb300_batch_destroy": [vp],
+        "rgl_gb300_batch_configure_schedule": [vp, C.c_bool, i32, i32, i32, i32, i32],
+        "rgl_gb300_batch_get_schedule": [vp, P(i32), P(i32), P(i32), P(i32), P(i32)],
+        "rgl_gb300_batch_get_stats": [vp, P(f), P(f), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)],
+        "rgl_gb300_configure_trace_schedule": [i32, i32, i32, i32],
+        "rgl_gb300_scene_create": [P(vp)],
+        "rgl_gb300_scene_destroy": [vp],
+        "rgl_gb300_scene_get_stats_of": [vp, P(C.c_int64), P(C.c_int64), P(i32)],
+        "rgl_gb300_server_create": [P(vp), C.c_int64, i32],
+        "rgl_gb300_server_destroy": [vp],
+        "rgl_gb300_server_add_pattern": [vp, vp, i32, P(i32)],
+        "rgl_gb300_server_submit": [vp, vp, i32, vp, i32, f, f, P(C.c_int64)],
+        "rgl_gb300_server_wait": [vp, C.c_int64, f, P(C.c_bool)],
+        "rgl_gb300_server_take_completed": [vp, P(C.c_int64), i32, P(i32)],
+        "rgl_gb300_server_wait_completed": [vp, f, P(C.c_int64), i32, P(i32)],
+        "rgl_gb300_server_get_result_size": [vp, C.c_int64, i32, P(i32), P(i32)],
+        "rgl_gb300_server_get_result_data": [vp, C.c_int64, i32, vp],
+        "rgl_gb300_server_get_request_timing": [vp, C.c_int64, P(C.c_double), P(C.c_double)],
+        "rgl_gb300_server_release": [vp, C.c_int64],
+        "rgl_gb300_server_drain": [vp],
+        "rgl_gb300_server_get_stats": [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)],
     }
     for name, args in sigs.items():
         fn = getattr(l, name)
@@ -385,3 +408,149 @@ def kernel_launch_count() -> int:
     v = C.c_uint64()
     check(lib().rgl_gb300_get_kernel_launch_count(C.byref(v)))
     return v.value
+
+
+# ---------------------------------------------------------------- batched multi-sensor frames
+
+PACK_LANE_GROUP, PACK_SERIAL = 0, 1
+ORDER_NATURAL, ORDER_OCTAHEDRAL, ORDER_MORTON = 0, 1, 2
+
+
+def batch_create(nodes) -> C.c_void_p:
+    """One batch over the graphs of `nodes` (any node of each graph)."""
+    arr = (C.c_void_p * len(nodes))(*[n.value if isinstance(n, C.c_void_p) else n for n in nodes])
+    b = C.c_void_p()
+    check(lib().rgl_gb300_batch_create(C.byref(b), arr, len(nodes)))
+    return b
+
+
+def batch_run(b):
+    check(lib().rgl_gb300_batch_run(b))
+
+
+def batch_destroy(b):
+    check(lib().rgl_gb300_batch_destroy(b))
+
+
+def batch_configure_schedule(b, autotune=True, block=128, packing=PACK_LANE_GROUP, order=ORDER_NATURAL, chunk=2, regs=96):
+    check(lib().rgl_gb300_batch_configure_schedule(b, autotune, block, packing, order, chunk, regs))
+
+
+def batch_schedule(b) -> dict:
+    v = [C.c_int32() for _ in range(5)]
+    check(lib().rgl_gb300_batch_get_schedule(b, *[C.byref(x) for x in v]))
+    return dict(zip(["block", "packing", "order", "chunk", "regs"], [x.value for x in v]))
+
+
+def batch_stats(b) -> dict:
+    fm, tm = C.c_float(), C.c_float()
+    ints = [C.c_int64() for _ in range(5)]
+    check(lib().rgl_gb300_batch_get_stats(b, C.byref(fm), C.byref(tm), *[C.byref(x) for x in ints]))
+    out = {"frame_ms": fm.value, "trace_ms": tm.value}
+    out.update(zip(["beams", "rays", "captures", "replays", "tunings"], [x.value for x in ints]))
+    return out
+
+
+# ---------------------------------------------------------------- resident scenes and serving
+
+
+def scene_create() -> C.c_void_p:
+    sc = C.c_void_p()
+    check(lib().rgl_gb300_scene_create(C.byref(sc)))
+    return sc
+
+
+def scene_destroy(sc):
+    check(lib().rgl_gb300_scene_destroy(sc))
+
+
+def entity_create_in(scene, mesh) -> C.c_void_p:
+    e = C.c_void_p()
+    check(lib().rgl_entity_create(C.byref(e), scene, mesh))
+    return e
+
+
+def spawn_scene_in(scene_handle, scene, meshes=None):
+    """Creates a scenes.Scene's entities in a resident scene (meshes created unless given)."""
+    meshes = meshes or [mesh_create(m.vertices, m.indices) for m in scene.meshes]
+    ents = []
+    for e in scene.entities:
+        h = entity_create_in(scene_handle, meshes[e.mesh])
+        entity_set_transform(h, e.transform)
+        entity_set_id(h, e.entity_id)
+        ents.append(h)
+    return meshes, ents
+
+
+def raytrace_in(node_ref, scene):
+    check(lib().rgl_node_raytrace(C.byref(node_ref), scene))
+    return node_ref
+
+
+class Server:
+    """ctypes wrapper of rgl_gb300_server_*."""
+
+    def __init__(self, budget_bytes: int, max_in_flight: int = 2):
+        self.h = C.c_void_p()
+        check(lib().rgl_gb300_server_create(C.byref(self.h), int(budget_bytes), int(max_in_flight)))
+
+    def destroy(self):
+        if self.h:
+            check(lib().rgl_gb300_server_destroy(self.h))
+            self.h = C.c_void_p()
+
+    def add_pattern(self, rays) -> int:
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 12)
+        out = C.c_int32()
+        check(lib().rgl_gb300_server_add_pattern(self.h, ptr(r), r.shape[0], C.byref(out)))
+        return out.value
+
+    def submit(self, scene, pattern: int, pose, mode: int, min_range: float = 0.0, max_range: float = float("inf")) -> int:
+        m = mat(pose)
+        out = C.c_int64()
+        check(lib().rgl_gb300_server_submit(self.h, scene, int(pattern), ptr(m), int(np.int32(np.uint32(mode))), min_range, max_range,
+                                            C.byref(out)))
+        return out.value
+
+    def wait(self, req: int, timeout_ms: float = -1.0) -> bool:
+        done = C.c_bool()
+        check(lib().rgl_gb300_server_wait(self.h, req, timeout_ms, C.byref(done)))
+        return done.value
+
+    def take_completed(self, capacity: int = 4096) -> list:
+        buf = (C.c_int64 * capacity)()
+        n = C.c_int32()
+        check(lib().rgl_gb300_server_take_completed(self.h, buf, capacity, C.byref(n)))
+        return list(buf[: n.value])
+
+    def wait_completed(self, timeout_ms: float, capacity: int = 4096) -> list:
+        buf = (C.c_int64 * capacity)()
+        n = C.c_int32()
+        check(lib().rgl_gb300_server_wait_completed(self.h, timeout_ms, buf, capacity, C.byref(n)))
+        return list(buf[: n.value])
+
+    def result(self, req: int, field: int) -> np.ndarray:
+        cnt, sz = C.c_int32(), C.c_int32()
+        check(lib().rgl_gb300_server_get_result_size(self.h, req, field, C.byref(cnt), C.byref(sz)))
+        dt, k = FIELD_DTYPE[field]
+        out = np.zeros((cnt.value, k) if k > 1 else cnt.value, dtype=dt)
+        if cnt.value > 0:
+            check(lib().rgl_gb300_server_get_result_data(self.h, req, field, ptr(out)))
+        return out
+
+    def timing(self, req: int):
+        q, t = C.c_double(), C.c_double()
+        check(lib().rgl_gb300_server_get_request_timing(self.h, req, C.byref(q), C.byref(t)))
+        return q.value, t.value
+
+    def release(self, req: int):
+        check(lib().rgl_gb300_server_release(self.h, req))
+
+    def drain(self):
+        check(lib().rgl_gb300_server_drain(self.h))
+
+    def stats(self) -> dict:
+        v = [C.c_int64() for _ in range(6)]
+        check(lib().rgl_gb300_server_get_stats(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(["submitted", "completed", "failed", "batches", "requests_in_batches", "peak_reserved_bytes"],
+                        [x.value for x in v]))

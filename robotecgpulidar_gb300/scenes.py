@@ -12,6 +12,15 @@ The shapes follow the workloads this engine is measured on:
   U[0.5, 5] -> 1,000,448 triangles.
 * ``lidar_rays``: channels x azimuth steps ray poses; a ray pose maps local +Z to
   (cos e cos a, cos e sin a, sin e) in a Z-up world.
+* ``solid_state_rays``: a rows x columns grid of directions over +-60 deg azimuth x +-12.5 deg
+  elevation (a solid-state lidar).
+* ``sensor_rig``: sensors with patterns drawn uniformly from 16x1800, 32x1024, 64x2048, 128x2048
+  and the 120x640 solid-state grid, posed uniformly over the terrain at 1-3 m above the ground.
+* ``repose``: new random poses for a fraction of a scene's posed entities (one animation frame).
+* ``serving_scene``: a scene built like ``million_scene`` scaled to a triangle budget: half of it a
+  value-noise heightfield, half icosphere instances, extent growing with the square root of the size.
+* ``robot_fleet``: robots with a lidar pattern each (ray count log-uniform in [10k, 1M]), a home
+  scene and a home pose.
 
 Ray poses and transforms are fp32 3x4 row-major matrices (``rgl_mat3x4f``).
 """
@@ -34,7 +43,14 @@ __all__ = [
     "rotation_xyz",
     "trs",
     "lidar_rays",
+    "solid_state_rays",
     "grid_rays",
+    "SENSOR_PATTERNS",
+    "Sensor",
+    "sensor_rig",
+    "repose",
+    "serving_scene",
+    "robot_fleet",
     "plain_scene",
     "million_scene",
 ]
@@ -61,6 +77,20 @@ class Entity:
 class Scene:
     meshes: list = field(default_factory=list)
     entities: list = field(default_factory=list)
+    # Heightfield of the terrain, when the scene has one: (heights (n+1, n+1), extent in metres).
+    heightfield: tuple = None
+
+    def ground_height(self, x: float, y: float) -> float:
+        """Bilinear height of the terrain heightfield at (x, y) (0 without a heightfield)."""
+        if self.heightfield is None:
+            return 0.0
+        h, extent = self.heightfield
+        n = h.shape[0] - 1
+        u = min(max((x / extent + 0.5) * n, 0.0), n - 1e-6)
+        v = min(max((y / extent + 0.5) * n, 0.0), n - 1e-6)
+        i, j = int(u), int(v)
+        fu, fv = u - i, v - j
+        return float((h[j, i] * (1 - fu) + h[j, i + 1] * fu) * (1 - fv) + (h[j + 1, i] * (1 - fu) + h[j + 1, i + 1] * fu) * fv)
 
     @property
     def triangle_count(self) -> int:
@@ -218,6 +248,86 @@ def lidar_rays(channels: int, azimuths: int, elev_min_deg: float = -25.0, elev_m
     return m.astype(np.float32)
 
 
+def _direction_poses(A: np.ndarray, E: np.ndarray) -> np.ndarray:
+    """Ray poses R = Rz(a) @ Ry(pi/2 - e): local +Z -> (cos e cos a, cos e sin a, sin e)."""
+    th = np.pi / 2 - E
+    ct, st, ca, sa = np.cos(th), np.sin(th), np.cos(A), np.sin(A)
+    m = np.zeros((A.size, 3, 4))
+    m[:, 0, 0] = ca * ct
+    m[:, 0, 1] = -sa
+    m[:, 0, 2] = ca * st
+    m[:, 1, 0] = sa * ct
+    m[:, 1, 1] = ca
+    m[:, 1, 2] = sa * st
+    m[:, 2, 0] = -st
+    m[:, 2, 2] = ct
+    return m.astype(np.float32)
+
+
+def solid_state_rays(rows: int = 120, cols: int = 640, h_fov_deg: float = 120.0, v_fov_deg: float = 25.0) -> np.ndarray:
+    """(rows*cols, 3, 4) ray poses on a grid over +-h_fov/2 azimuth x +-v_fov/2 elevation, row-major
+    (all columns of one elevation row are consecutive)."""
+    e = np.deg2rad(np.linspace(-v_fov_deg / 2, v_fov_deg / 2, rows))
+    a = np.deg2rad(np.linspace(-h_fov_deg / 2, h_fov_deg / 2, cols))
+    E, A = np.meshgrid(e, a, indexing="ij")
+    return _direction_poses(A.ravel(), E.ravel())
+
+
+# Sensor patterns of the multi-sensor workload: (channels, azimuth steps) of a spinning lidar, or
+# ("grid", rows, columns) of a solid-state one.
+SENSOR_PATTERNS = [(16, 1800), (32, 1024), (64, 2048), (128, 2048), ("grid", 120, 640)]
+
+
+@dataclass
+class Sensor:
+    pattern: tuple
+    pose: np.ndarray  # (3, 4) float32 sensor-to-world
+
+    def rays(self) -> np.ndarray:
+        if self.pattern[0] == "grid":
+            return solid_state_rays(self.pattern[1], self.pattern[2])
+        return lidar_rays(self.pattern[0], self.pattern[1])
+
+    @property
+    def beam_count(self) -> int:
+        return self.pattern[1] * self.pattern[2] if self.pattern[0] == "grid" else self.pattern[0] * self.pattern[1]
+
+
+def sensor_rig(scene: Scene, count: int = 64, seed: int = 4, margin: float = 0.45) -> list:
+    """`count` sensors, pattern uniform over SENSOR_PATTERNS, position uniform over the middle
+    (2*margin)^2 of the terrain at 1-3 m above the ground, yaw uniform."""
+    rng = np.random.default_rng(seed)
+    extent = scene.heightfield[1] if scene.heightfield is not None else 200.0
+    out = []
+    for _ in range(count):
+        pattern = SENSOR_PATTERNS[int(rng.integers(0, len(SENSOR_PATTERNS)))]
+        x, y = rng.uniform(-margin * extent, margin * extent, size=2)
+        z = scene.ground_height(x, y) + rng.uniform(1.0, 3.0)
+        yaw = rng.uniform(-np.pi, np.pi)
+        out.append(Sensor(pattern, trs((x, y, z), (0.0, 0.0, yaw))))
+    return out
+
+
+def repose(scene: Scene, fraction: float, rng: np.random.Generator, extent: float = None) -> list:
+    """New random rigid poses (scale kept) for `fraction` of the scene's entities other than entity 0
+    (the terrain); returns [(entity index, new transform)] and updates scene.entities."""
+    if extent is None:
+        extent = scene.heightfield[1] if scene.heightfield is not None else 200.0
+    movable = list(range(1, len(scene.entities)))
+    k = int(round(fraction * len(movable)))
+    picked = rng.choice(movable, size=k, replace=False) if k > 0 else []
+    out = []
+    for i in picked:
+        e = scene.entities[int(i)]
+        scale = float(np.linalg.norm(e.transform[:, 0].astype(np.float64)))
+        x, y = rng.uniform(-0.4 * extent, 0.4 * extent, size=2)
+        rot = rng.uniform(-np.pi, np.pi, size=3)
+        tf = trs((x, y, scale + 1.0), rot, (scale, scale, scale))
+        scene.entities[int(i)] = Entity(e.mesh, tf, e.entity_id)
+        out.append((int(i), tf))
+    return out
+
+
 def grid_rays(min_xy, max_xy, count_xy) -> np.ndarray:
     """Grid of parallel rays along +Z (translations only)."""
     sx = (max_xy[0] - min_xy[0]) / (count_xy[0] + 1)
@@ -261,6 +371,7 @@ def million_scene(seed: int = 2, instances: int = 93, spheres: int = 8, cells: i
     rng = np.random.default_rng(seed)
     heights = _value_noise(cells, 4, 3.0, rng)
     s = Scene()
+    s.heightfield = (heights, extent)
     s.meshes.append(terrain_mesh(cells, cells, extent, extent, heights))
     srng = np.random.default_rng(seed + 1)
     for _ in range(spheres):
@@ -274,3 +385,42 @@ def million_scene(seed: int = 2, instances: int = 93, spheres: int = 8, cells: i
         rot = prng.uniform(-np.pi, np.pi, size=3)
         s.entities.append(Entity(mesh, trs((x, y, scale + 1.0), rot, (scale, scale, scale)), 2 + k))
     return s
+
+
+def serving_scene(triangles: int, seed: int) -> Scene:
+    """About `triangles` triangles: a square heightfield of triangles/2 and triangles/2 / 5,120
+    icosphere instances over 8 meshes; extent 512 m x sqrt(triangles / 1M)."""
+    cells = max(16, int(round(math.sqrt(triangles / 4.0))))
+    instances = max(1, int(round(triangles / 2.0 / 5120.0)))
+    extent = 512.0 * math.sqrt(triangles / 1.0e6)
+    return million_scene(seed=seed, instances=instances, spheres=8, cells=cells, extent=extent)
+
+
+@dataclass
+class Robot:
+    pattern: tuple  # (channels, azimuth steps)
+    scene: int
+    pose: np.ndarray
+
+    @property
+    def rays(self) -> int:
+        return self.pattern[0] * self.pattern[1]
+
+
+def robot_fleet(scene_list, count: int = 256, seed: int = 5, min_rays: int = 10_000, max_rays: int = 1_000_000) -> list:
+    """`count` robots: ray count log-uniform in [min_rays, max_rays] as channels x azimuth steps
+    (16, 32, 64 or 128 channels by size), a uniformly drawn home scene and a pose 1-3 m above its
+    ground."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = math.exp(rng.uniform(math.log(min_rays), math.log(max_rays)))
+        ch = 16 if n < 40_000 else 32 if n < 150_000 else 64 if n < 500_000 else 128
+        az = max(1, int(round(n / ch)))
+        k = int(rng.integers(0, len(scene_list)))
+        sc = scene_list[k]
+        extent = sc.heightfield[1]
+        x, y = rng.uniform(-0.4 * extent, 0.4 * extent, size=2)
+        z = sc.ground_height(x, y) + rng.uniform(1.0, 3.0)
+        out.append(Robot((ch, az), k, trs((x, y, z), (0.0, 0.0, rng.uniform(-np.pi, np.pi)))))
+    return out

@@ -156,6 +156,7 @@ struct HostStack
 };
 
 int gNodeVisits = 0;
+long gTriTests = 0, gBinLoads = 0, gInstLoads = 0;
 
 struct HostLoader
 {
@@ -169,9 +170,21 @@ struct HostLoader
 		w3 = p[3];
 		w4 = p[4];
 	}
-	TriRecord tri(const TriRecord* base, int32_t i) const { return base[i]; }
-	const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
-	BinNode bin(const BinNode* base, int32_t i) const { return base[i]; }
+	TriRecord tri(const TriRecord* base, int32_t i) const
+	{
+		++gTriTests;
+		return base[i];
+	}
+	const InstanceRec& instance(const InstanceRec* base, int32_t i) const
+	{
+		++gInstLoads;
+		return base[i];
+	}
+	BinNode bin(const BinNode* base, int32_t i) const
+	{
+		++gBinLoads;
+		return base[i];
+	}
 };
 
 } // namespace
@@ -181,8 +194,18 @@ extern "C" {
 // Largest number of wide-node visits of a single ray in the last harness_cast call.
 int gMaxNodeVisits = 0;
 long gTotalNodeVisits = 0;
+int gMaxStackDepth = 0;
 int harness_max_node_visits() { return gMaxNodeVisits; }
+// Deepest traversal stack of a single ray in the last harness_cast call.
+int harness_max_stack_depth() { return gMaxStackDepth; }
 long harness_total_node_visits() { return gTotalNodeVisits; }
+// Totals of the last harness_cast call: triangle tests, TLAS node loads, instance record loads.
+void harness_work_counters(long* out)
+{
+	out[0] = gTriTests;
+	out[1] = gBinLoads;
+	out[2] = gInstLoads;
+}
 
 // Builds BLASes for `nMeshes` meshes and a TLAS over `nInst` instances, then casts `nRays` world
 // rays (origin, direction, tmax: 7 floats each). Outputs per ray: t, instance, original triangle id.
@@ -252,12 +275,15 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	bool overflow = false;
 	gMaxNodeVisits = 0;
 	gTotalNodeVisits = 0;
+	gTriTests = gBinLoads = gInstLoads = 0;
+	gMaxStackDepth = 0;
 	for (int r = 0; r < nRays; ++r) {
 		const float* p = rays + 7 * r;
 		HostStack st;
 		gNodeVisits = 0;
 		HitRec h = traceClosest(sv, v3(p[0], p[1], p[2]), v3(p[3], p[4], p[5]), p[6], st, ld);
 		overflow = overflow || st.overflow;
+		gMaxStackDepth = std::max(gMaxStackDepth, st.maxDepth);
 		gMaxNodeVisits = std::max(gMaxNodeVisits, gNodeVisits);
 		gTotalNodeVisits += gNodeVisits;
 		outT[r] = h.t;

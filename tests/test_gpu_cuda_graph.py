@@ -83,3 +83,62 @@ def test_recapture_only_on_parameter_changes(rgl):
     rgl.rays_from_mat3x4f(n["rays"], scenes.lidar_rays(32, 1024))
     runs(rgl, n, 1)
     assert stats(rgl, n["rays"])[0] == 3
+
+
+def test_on_demand_compaction_after_replay_is_fresh(rgl):
+    """A field nobody downstream declared is compacted when it is first read after a run; a replayed
+    run must not serve the previous run's copy (the per-run state is reset outside the capture)."""
+    rgl.spawn_scene(scenes.plain_scene())
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "cmp", "y", "side")}
+    rgl.rays_from_mat3x4f(n["rays"], scenes.lidar_rays(16, 256))
+    rgl.rays_transform(n["pose"], scenes.translation(0, 0, 1.8))
+    rgl.raytrace(n["trace"])
+    rgl.points_compact_by_field(n["cmp"])
+    rgl.points_yield(n["y"], [rgl.RGL_FIELD_XYZ_VEC3_F32])
+    # DISTANCE is requested on a sibling branch, so the raytrace node computes it while nothing below
+    # the compaction declares it: reading it from the compaction node compacts it on demand.
+    rgl.points_yield(n["side"], [rgl.RGL_FIELD_DISTANCE_F32])
+    rgl.chain(n["rays"], n["pose"], n["trace"], n["cmp"], n["y"])
+    rgl.add_child(n["trace"], n["side"])
+    origin = np.array([0.0, 0.0, 1.8])
+    seen = []
+    # Same ray count, new directions: content-only updates. The first on-demand read allocates the
+    # field's buffer, which re-captures the next run once; the last two runs are replays.
+    for lo, hi in ((-25.0, 15.0), (-12.0, -2.0), (-25.0, 15.0), (-12.0, -2.0)):
+        rgl.rays_from_mat3x4f(n["rays"], scenes.lidar_rays(16, 256, lo, hi))
+        rgl.graph_run(n["rays"])
+        xyz = rgl.result(n["y"], rgl.RGL_FIELD_XYZ_VEC3_F32)
+        dist = rgl.result(n["cmp"], rgl.RGL_FIELD_DISTANCE_F32)  # compacted on demand
+        assert dist.shape[0] == xyz.shape[0]
+        assert np.allclose(np.linalg.norm(xyz - origin, axis=1), dist, rtol=1e-5, atol=1e-4)
+        seen.append(dist)
+    assert stats(rgl, n["rays"]) == (2, 2)
+    assert not np.array_equal(seen[2], seen[3]) and np.array_equal(seen[0], seen[2])
+
+
+def test_moving_sensor_replays_one_capture(rgl):
+    """A new sensor pose every run (rgl_node_rays_transform) and a reseeded noise node are staged
+    per run: the run is captured once and replayed, with results equal to direct enqueue."""
+    lib = rgl.lib()
+
+    def frames(n):
+        out = []
+        for k in range(4):
+            rgl.rays_transform(n["pose"], scenes.trs((k * 3.0, -k * 2.0, 1.8 + 0.2 * k), (0.0, 0.0, 0.3 * k)))
+            rgl.set_noise_seed(n["ang"], 40 + k, k)
+            rgl.graph_run(n["rays"])
+            out.append((rgl.result(n["y"], rgl.RGL_FIELD_XYZ_VEC3_F32), rgl.result(n["y"], rgl.RGL_FIELD_DISTANCE_F32)))
+        return out
+
+    rgl.check(lib.rgl_gb300_configure_cuda_graphs(False))
+    try:
+        direct = frames(build(rgl))
+    finally:
+        rgl.check(lib.rgl_gb300_configure_cuda_graphs(True))
+    rgl.cleanup()
+    n = build(rgl)
+    graphed = frames(n)
+    assert stats(rgl, n["rays"]) == (1, 3)
+    for (x0, d0), (x1, d1) in zip(direct, graphed):
+        assert np.array_equal(x0, x1) and np.array_equal(d0, d1)
+    assert not np.array_equal(graphed[0][0], graphed[1][0])
