@@ -530,9 +530,10 @@ def run_serving(args):
     """Scan requests from 256 virtual robots arriving by a Poisson process over 4 resident scenes
     (0.2M/1M/2M/4M triangles), ray count log-uniform in [10k, 1M], FIRST or FIRST_LAST 50/50, range
     [0.1, 100] m, compaction by is-hit; results (XYZ, distance, entity id) read back into pinned host
-    memory. Served: rgl_gb300_server_* (continuous batching under an 80 GB budget). Plain: one
-    rgl_graph_run per request on the robot's own graph, in arrival order. Latency = arrival to results
-    in host memory."""
+    memory. Served: rgl_gb300_server_* (continuous batching under an 80 GB budget; results land in the
+    server's pinned host memory). Plain: one rgl_graph_run per request on the robot's own graph, in
+    arrival order, results copied with rgl_graph_get_result_data into pinned host buffers. Latency =
+    arrival to results in host memory."""
     from robotecgpulidar_gb300 import build as b
 
     b.build()
@@ -586,15 +587,15 @@ def run_serving(args):
                 "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))] if lat_ms else None, "saturated": saturated}
 
     failures = []
+    host_ptr = C.c_void_p()
 
     def read_served(q):
-        """Reads a served request's three result fields; a failed request is recorded, not read."""
-        for f, buf in outs:
-            if lib.rgl_gb300_server_get_result_size(srv.h, q, f, C.byref(cnt), C.byref(sz)) != rgl.RGL_SUCCESS:
+        """Takes a served request's three result fields, already in the server's pinned host memory
+        (the address and count of each); a failed request is recorded."""
+        for f, _ in outs:
+            if lib.rgl_gb300_server_get_result_host(srv.h, q, f, C.byref(host_ptr), C.byref(cnt)) != rgl.RGL_SUCCESS:
                 failures.append(rgl.last_error())
                 return
-            if cnt.value:
-                rgl.check(lib.rgl_gb300_server_get_result_data(srv.h, q, f, rgl.ptr(buf)))
 
     # ---- served
     srv = rgl.Server(SERVE_BUDGET, 2)

@@ -145,8 +145,9 @@ RGL_API rgl_status_t rgl_gb300_scene_get_stats_of(rgl_scene_t scene, int64_t* ou
  * Robots register their ray patterns (sensor-local rgl_mat3x4f rays, as for rgl_node_rays_from_mat3x4f)
  * once; the patterns stay on the device. A scan request names a scene, a pattern, the sensor pose,
  * a return mode and a range. A scheduler thread admits requests first come first served while the
- * bytes of admitted requests (24 B per point while on the GPU, 20 B per point until released, points =
- * rays x returns) stay within `hbm_budget_bytes` and fewer than `max_in_flight_batches` batches run,
+ * bytes of admitted requests (24 B per point of device buffers while on the GPU and 20 B per point of
+ * pinned host results until released; points = rays x returns) stay within `hbm_budget_bytes` and
+ * fewer than `max_in_flight_batches` batches run,
  * and launches all admitted requests as one batch (one persistent traversal launch plus one segmented
  * compaction). Requests arriving meanwhile go into the next batch (continuous batching).
  *
@@ -175,6 +176,13 @@ RGL_API rgl_status_t rgl_gb300_server_wait_completed(rgl_gb300_server_t server, 
 RGL_API rgl_status_t rgl_gb300_server_get_result_size(rgl_gb300_server_t server, int64_t request, rgl_field_t field,
                                                       int32_t* out_count, int32_t* out_size_of);
 RGL_API rgl_status_t rgl_gb300_server_get_result_data(rgl_gb300_server_t server, int64_t request, rgl_field_t field, void* out_data);
+/*
+ * Host address of a completed request's field and its element count. Results are written by the GPU
+ * straight into the server's pinned host memory, so this needs no copy; the address stays valid
+ * until rgl_gb300_server_release.
+ */
+RGL_API rgl_status_t rgl_gb300_server_get_result_host(rgl_gb300_server_t server, int64_t request, rgl_field_t field,
+                                                      const void** out_data, int32_t* out_count);
 /* Seconds from submission to admission into a batch, and from submission to completion. */
 RGL_API rgl_status_t rgl_gb300_server_get_request_timing(rgl_gb300_server_t server, int64_t request, double* out_queued_s,
                                                          double* out_total_s);

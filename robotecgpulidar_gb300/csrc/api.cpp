@@ -1358,6 +1358,18 @@ RGL_API rgl_status_t rgl_gb300_server_get_result_data(rgl_gb300_server_t server,
 	});
 }
 
+RGL_API rgl_status_t rgl_gb300_server_get_result_host(rgl_gb300_server_t server, int64_t request, rgl_field_t field,
+                                                      const void** out_data, int32_t* out_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(out_data != nullptr);
+		int32_t c = 0;
+		*out_data = Servers::get(server, "Server")->resultHost(request, field, c);
+		if (out_count) *out_count = c;
+	});
+}
+
 RGL_API rgl_status_t rgl_gb300_server_get_request_timing(rgl_gb300_server_t server, int64_t request, double* out_queued_s,
                                                          double* out_total_s)
 {

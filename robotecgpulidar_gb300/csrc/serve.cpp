@@ -11,15 +11,6 @@ using rgl::format;
 Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmBudgetBytes), maxInFlight(std::max(1, maxInFlightBatches))
 {
 	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-	int dev = 0;
-	RGL_CHECK_CUDA(cudaGetDevice(&dev));
-	cudaMemPoolProps props{};
-	props.allocType = cudaMemAllocationTypePinned;
-	props.location.type = cudaMemLocationTypeDevice;
-	props.location.id = dev;
-	RGL_CHECK_CUDA(cudaMemPoolCreate(&pool, &props));
-	uint64_t keep = UINT64_MAX; // freed blocks stay reserved for the next requests
-	RGL_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
 	for (int i = 0; i < maxInFlight; ++i) {
 		auto s = std::make_unique<Slot>();
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
@@ -40,21 +31,39 @@ Server::~Server()
 		worker.join();
 	}
 	cudaStreamSynchronize(stream);
-	for (auto& kv : requests) {
-		if (kv.second->outXyz) {
-			cudaFreeAsync(kv.second->outXyz, stream);
-		}
+	for (void* p : allBlocks) {
+		cudaFreeHost(p);
 	}
-	for (float* p : toFree) {
-		cudaFreeAsync(p, stream);
-	}
-	cudaStreamSynchronize(stream);
 	for (auto& s : slots) {
 		cudaEventDestroy(s->done);
 	}
-	cudaMemPoolDestroy(pool);
 	cudaStreamDestroy(stream);
 }
+
+Server::HostBlock Server::takeHostBlock(size_t bytes, size_t& cls)
+{
+	cls = 65536;
+	while (cls < bytes) {
+		cls <<= 1;
+	}
+	{
+		std::lock_guard<std::mutex> g(m);
+		auto& fl = freeBlocks[cls];
+		if (!fl.empty()) {
+			HostBlock b = fl.back();
+			fl.pop_back();
+			return b;
+		}
+	}
+	HostBlock b{};
+	RGL_CHECK_CUDA(cudaHostAlloc(&b.host, cls, cudaHostAllocMapped | cudaHostAllocPortable));
+	RGL_CHECK_CUDA(cudaHostGetDevicePointer(&b.dev, b.host, 0));
+	std::lock_guard<std::mutex> g(m);
+	allBlocks.push_back(b.host);
+	return b;
+}
+
+void Server::giveHostBlock(const HostBlock& b, size_t cls) { freeBlocks[cls].push_back(b); }
 
 int32_t Server::addPattern(const void* rays, int32_t count)
 {
@@ -164,25 +173,25 @@ void Server::resultSize(int64_t id, rgl_field_t field, int32_t& count, int32_t& 
 	size = (int32_t) rgl::fieldSize(field);
 }
 
+const void* Server::resultHost(int64_t id, rgl_field_t field, int32_t& count)
+{
+	int32_t size = 0;
+	resultSize(id, field, count, size);
+	std::lock_guard<std::mutex> g(m);
+	Request& r = get(id);
+	const float* base = r.hostOut;
+	if (field == RGL_FIELD_XYZ_VEC3_F32) {
+		return base;
+	}
+	return field == RGL_FIELD_DISTANCE_F32 ? base + 3 * r.points : base + 4 * r.points;
+}
+
 void Server::resultData(int64_t id, rgl_field_t field, void* dst)
 {
-	int32_t count = 0, size = 0;
-	resultSize(id, field, count, size);
-	const void* src = nullptr;
-	{
-		std::lock_guard<std::mutex> g(m);
-		Request& r = get(id);
-		float* base = r.outXyz;
-		if (field == RGL_FIELD_XYZ_VEC3_F32) {
-			src = base;
-		} else if (field == RGL_FIELD_DISTANCE_F32) {
-			src = base + 3 * r.points;
-		} else {
-			src = base + 4 * r.points;
-		}
-	}
+	int32_t count = 0;
+	const void* src = resultHost(id, field, count);
 	if (count > 0) {
-		RGL_CHECK_CUDA(cudaMemcpy(dst, src, (size_t) count * size, cudaMemcpyDeviceToHost));
+		std::memcpy(dst, src, (size_t) count * rgl::fieldSize(field));
 	}
 }
 
@@ -207,8 +216,8 @@ void Server::release(int64_t id)
 		lk.lock();
 	}
 	Request& q = get(id);
-	if (q.outXyz) {
-		toFree.push_back(q.outXyz); // freed on the server's stream by its thread
+	if (q.hostOut) {
+		giveHostBlock(HostBlock{q.hostOut, q.devOut}, q.outClass); // the GPU finished writing it
 	}
 	reserved -= q.points * kOutBytesPerPoint;
 	requests.erase(id);
@@ -297,9 +306,9 @@ void Server::launch(Slot& slot)
 		sg.xyz = xyz + 3 * pointBase;
 		sg.dist = dist + pointBase;
 		sg.ent = ent + pointBase;
-		sg.outXyz = r.outXyz;
-		sg.outDist = r.outXyz + 3 * r.points;
-		sg.outEnt = reinterpret_cast<int32_t*>(r.outXyz + 4 * r.points);
+		sg.outXyz = r.devOut;
+		sg.outDist = r.devOut + 3 * r.points;
+		sg.outEnt = reinterpret_cast<int32_t*>(r.devOut + 4 * r.points);
 		sg.nPoints = (int32_t) r.points;
 		segs[j] = sg;
 		tileBase[j] = (int32_t) tiles;
@@ -381,10 +390,6 @@ void Server::loop()
 			retire(*s);
 			lk.lock();
 		}
-		for (float* p : toFree) {
-			cudaFreeAsync(p, stream);
-		}
-		toFree.clear();
 		if (stop && pending.empty() && inFlight.empty()) {
 			break;
 		}
@@ -428,10 +433,11 @@ void Server::loop()
 							r->scene->prepare(stream);
 							prepared.push_back(r->scene.get());
 						}
-						const size_t bytes = (size_t) r->points * kOutBytesPerPoint;
-						void* p = nullptr;
-						RGL_CHECK_CUDA(cudaMallocFromPoolAsync(&p, std::max<size_t>(bytes, 256), pool, stream));
-						r->outXyz = static_cast<float*>(p);
+						if (r->hostOut == nullptr) {
+							const HostBlock hb = takeHostBlock((size_t) r->points * kOutBytesPerPoint, r->outClass);
+							r->hostOut = static_cast<float*>(hb.host);
+							r->devOut = static_cast<float*>(hb.dev);
+						}
 					}
 					launch(*freeSlot);
 				}

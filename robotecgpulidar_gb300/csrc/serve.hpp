@@ -13,8 +13,9 @@
 //
 // Each request's result is XYZ, distance and entity id of its hit points, in point order, equal to
 // what the graph rays_from_mat3x4f(pattern) -> rays_transform(pose) -> rays_set_range ->
-// raytrace(scene, mode) -> compact_by_field(IS_HIT) -> yield writes. Results stay on the device until
-// the client copies them; release() frees them.
+// raytrace(scene, mode) -> compact_by_field(IS_HIT) -> yield writes. The compaction writes it straight
+// into pinned host memory (mapped for the device), so a completed request's result is already in
+// host memory; release() returns the block to the server's pool.
 //
 // While a server runs, the scenes it traces must not be modified (drain() first).
 #pragma once
@@ -51,6 +52,8 @@ struct Server
 	int32_t waitCompleted(int64_t* ids, int32_t capacity, double timeoutMs);
 	void resultSize(int64_t id, rgl_field_t field, int32_t& count, int32_t& size);
 	void resultData(int64_t id, rgl_field_t field, void* dst);
+	// Host address of a completed request's field (valid until release) and its element count.
+	const void* resultHost(int64_t id, rgl_field_t field, int32_t& count);
 	// Seconds from submission to admission into a batch, and to completion.
 	void timing(int64_t id, double& queuedS, double& totalS);
 	void release(int64_t id);
@@ -84,7 +87,11 @@ private:
 		float minRange, maxRange;
 		int64_t beams, points;
 		int64_t reservedBytes;
-		float* outXyz = nullptr; // one allocation: xyz | distance | entity id, `points` capacity each
+		// Result block in pinned host memory mapped for the device: xyz | distance | entity id, `points`
+		// capacity each. The compaction writes it directly; no copy follows.
+		float* hostOut = nullptr;
+		float* devOut = nullptr; // the device address of hostOut
+		size_t outClass = 0;
 		int32_t count = 0;
 		State state = State::Pending;
 		std::string error; // why a failed request failed
@@ -111,6 +118,17 @@ private:
 	static constexpr int64_t kRawBytesPerPoint = 4 + 12 + 4 + 4; // flags, xyz, distance, entity id
 	static constexpr int64_t kOutBytesPerPoint = 12 + 4 + 4;
 
+	// Pinned, device-mapped host blocks in power-of-two size classes, reused across requests.
+	struct HostBlock
+	{
+		void* host;
+		void* dev;
+	};
+	HostBlock takeHostBlock(size_t bytes, size_t& cls);
+	void giveHostBlock(const HostBlock& b, size_t cls);
+	std::unordered_map<size_t, std::vector<HostBlock>> freeBlocks; // guarded by m
+	std::vector<void*> allBlocks;
+
 	void loop();
 	void launch(Slot& slot);
 	void retire(Slot& slot);
@@ -120,7 +138,6 @@ private:
 	int64_t budget;
 	int maxInFlight;
 	cudaStream_t stream = nullptr;
-	cudaMemPool_t pool = nullptr;
 	std::vector<std::unique_ptr<Pattern>> patterns;
 	std::vector<std::unique_ptr<Slot>> slots;
 	std::deque<Slot*> inFlight;
@@ -130,7 +147,7 @@ private:
 	std::deque<Request*> pending;
 	std::unordered_map<int64_t, std::unique_ptr<Request>> requests;
 	std::deque<int64_t> completedIds;
-	std::vector<float*> toFree;
+
 	int64_t nextId = 1;
 	int64_t reserved = 0;
 	Stats st;

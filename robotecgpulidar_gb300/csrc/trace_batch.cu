@@ -261,14 +261,19 @@ int residentBlocks(const void* fn, int block, size_t smem)
 {
 	static std::mutex m;
 	static std::map<std::tuple<const void*, int, size_t>, int> cache;
+	static std::map<const void*, bool> optedIn;
 	std::lock_guard<std::mutex> g(m);
 	auto key = std::make_tuple(fn, block, smem);
 	auto it = cache.find(key);
 	if (it != cache.end()) {
 		return it->second;
 	}
-	if (smem > 48 * 1024) {
-		RGL_BATCH_CUDA_OK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+	if (!optedIn[fn]) {
+		// Opt in once to the largest launch of this kernel (256-thread stack + the largest job
+		// table), so no later launch, whatever its shape, exceeds the limit.
+		const int most = (int) (sizeof(uint2) * kSmemStack * 256 + sizeof(int32_t) * (kMaxBatchJobs + 2));
+		RGL_BATCH_CUDA_OK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+		optedIn[fn] = true;
 	}
 	int n = 0;
 	RGL_BATCH_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem));

@@ -179,9 +179,10 @@ RGL_HD int popc8(uint32_t x)
 // size().
 
 // Slab test of a dequantised child box in the FMA form t = q * (s * inv) + (p - o) * inv. The computed
-// t differs from the exact plane distance by at most 4u|t| + 3u * 255 * s * |inv| (u = 2^-24). The
-// builder widens every child box by one grid step s (bvh_core.hpp quantizeAxis), which moves each plane
-// outward by s * |inv| in t and covers the second term; entry <= exit * (1 + 5e-7) covers the first.
+// t differs from the exact plane distance by at most 4u|t| + 3u * 255 * s * |inv| (u = 2^-24), plus
+// the rounding of the folded offset described in traverseBlas. The builder widens every child box by
+// one grid step s (bvh_core.hpp quantizeAxis), which moves each plane outward by s * |inv| in t and
+// covers the absolute terms; entry <= exit * (1 + 5e-7) covers the relative ones.
 // Axis-parallel rays (inv = +-1e30 after safeInv) stay exact: their slab only yields +-huge values.
 constexpr float kSlabRelSlack = 1.0000005f;
 
@@ -216,15 +217,30 @@ RGL_HD uint32_t asUint(float f)
 #endif
 }
 
-// Byte k of w as a float. On the device: the byte placed under the exponent of 2^23 (PRMT) minus
-// 2^23, which is exact for 0..255 and keeps the conversion off the integer pipe.
-RGL_HD float byteF(uint32_t w, int k)
+// Byte k of w placed in bits 8..15 of the mantissa of 1.0: the float 1 + q * 2^-15, exact for every
+// byte q. One byte permute on the device.
+RGL_HD float byteMantissa(uint32_t w, int k)
 {
 #if defined(__CUDA_ARCH__)
-	return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t) k)) - 8388608.0f;
+	return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t) k << 4)));
 #else
-	return (float) ((w >> (8 * k)) & 0xffu);
+	return asFloat(0x3F800000u | (((w >> (8 * k)) & 0xffu) << 8));
 #endif
+}
+
+// Bit j of each byte of x moves to bit j ^ oct (x holds two 8-bit child masks).
+RGL_HD uint32_t octantPermute(uint32_t x, uint32_t oct)
+{
+	if (oct & 1u) {
+		x = ((x & 0x5555u) << 1) | ((x >> 1) & 0x5555u);
+	}
+	if (oct & 2u) {
+		x = ((x & 0x3333u) << 2) | ((x >> 2) & 0x3333u);
+	}
+	if (oct & 4u) {
+		x = ((x & 0x0F0Fu) << 4) | ((x >> 4) & 0x0F0Fu);
+	}
+	return x;
 }
 
 // max(a, b, c, d) and min(a, b, c, d) of the slab test; three-input min/max on the device.
@@ -268,30 +284,33 @@ RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 
 		const uint32_t childBase = w1.x, triBase = w1.y;
 		const float Ax = sx * inv.x, Ay = sy * inv.y, Az = sz * inv.z;
 		const float Cx = (asFloat(w0.x) - o.x) * inv.x, Cy = (asFloat(w0.y) - o.y) * inv.y, Cz = (asFloat(w0.z) - o.z) * inv.z;
+		// Plane distance q * A + C evaluated as fma(1 + q * 2^-15, 2^15 * A, C - 2^15 * A): 2^15 * A is
+		// exact and the product term is exact, so the only extra rounding is that of C - 2^15 * A,
+		// at most u|C| + 2^-9 |A|. With |C| <= |t| + 255 |A|, the relative slack (5u of 8.4u used) and
+		// the one-grid-step widening |A| (2^-9 + 1020u of 1 used) still cover every error.
+		const float Sx = 32768.0f * Ax, Sy = 32768.0f * Ay, Sz = 32768.0f * Az;
+		const float Dx = Cx - Sx, Dy = Cy - Sy, Dz = Cz - Sz;
 		// near/far quantised planes per axis (packed bytes), swapped for negative directions
 		const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y, fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
 		const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w, fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
 		const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y, fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
-		uint32_t internalHits = 0, leafHits = 0; // both indexed by traversal order j (slot = j ^ oct)
+		uint32_t hitSlots = 0; // bit s: child slot s is hit
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
 		for (int s = 0; s < kWideArity; ++s) {
 			const int k = s & 3;
 			const bool hiw = s >= 4;
-			const float tnx = fmaf(byteF(hiw ? nx1 : nx0, k), Ax, Cx), tfx = fmaf(byteF(hiw ? fx1 : fx0, k), Ax, Cx);
-			const float tny = fmaf(byteF(hiw ? ny1 : ny0, k), Ay, Cy), tfy = fmaf(byteF(hiw ? fy1 : fy0, k), Ay, Cy);
-			const float tnz = fmaf(byteF(hiw ? nz1 : nz0, k), Az, Cz), tfz = fmaf(byteF(hiw ? fz1 : fz0, k), Az, Cz);
+			const float tnx = fmaf(byteMantissa(hiw ? nx1 : nx0, k), Sx, Dx), tfx = fmaf(byteMantissa(hiw ? fx1 : fx0, k), Sx, Dx);
+			const float tny = fmaf(byteMantissa(hiw ? ny1 : ny0, k), Sy, Dy), tfy = fmaf(byteMantissa(hiw ? fy1 : fy0, k), Sy, Dy);
+			const float tnz = fmaf(byteMantissa(hiw ? nz1 : nz0, k), Sz, Dz), tfz = fmaf(byteMantissa(hiw ? fz1 : fz0, k), Sz, Dz);
 			const float tEntry = max4(tnx, tny, tnz, 0.0f);
 			const float tExit = min4(tfx, tfy, tfz, best.t);
-			if (tEntry <= tExit * kSlabRelSlack) {
-				if ((imask >> s) & 1u) {
-					internalHits |= 1u << (s ^ oct);
-				} else {
-					leafHits |= 1u << (s ^ oct);
-				}
-			}
+			hitSlots |= (tEntry <= tExit * kSlabRelSlack) ? (1u << s) : 0u;
 		}
+		// Internal and leaf hits in traversal order j (slot = j ^ oct): one permutation for both.
+		const uint32_t ordered = octantPermute((hitSlots & imask) | ((hitSlots & ~imask & 0xffu) << 8), oct);
+		uint32_t internalHits = ordered & 0xffu, leafHits = ordered >> 8;
 		// Triangles of hit leaf children, in ray order.
 		const uint32_t metaLo = w1.z, metaHi = w1.w;
 		while (leafHits) {

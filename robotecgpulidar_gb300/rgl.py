@@ -206,6 +206,7 @@ def _proto(l):
         "rgl_gb300_server_get_result_size": [vp, C.c_int64, i32, P(i32), P(i32)],
         "rgl_gb300_server_get_result_data": [vp, C.c_int64, i32, vp],
         "rgl_gb300_server_get_request_timing": [vp, C.c_int64, P(C.c_double), P(C.c_double)],
+        "rgl_gb300_server_get_result_host": [vp, C.c_int64, i32, P(vp), P(i32)],
         "rgl_gb300_server_release": [vp, C.c_int64],
         "rgl_gb300_server_drain": [vp],
         "rgl_gb300_server_get_stats": [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)],

@@ -208,3 +208,28 @@ def test_batch_over_two_scenes_equals_solo(rgl):
         solo.append(collect(rgl, g))
     assert_same(rgl, batched, solo)
     rgl.batch_destroy(batch)
+
+
+def test_batches_of_varying_size_complete_and_host_results_match(rgl):
+    """Batches of 1, 60, 3 and 200 requests in turn (launch shapes that grow and shrink) all complete;
+    the host-resident result equals the copied one."""
+    (sa, _), (sb, _) = two_scenes(rgl)
+    srv = rgl.Server(8 << 30, 2)
+    try:
+        pats = [srv.add_pattern(pattern_rays(p)) for p in PATTERNS]
+        rng = np.random.default_rng(21)
+        for wave in (1, 60, 3, 200):
+            reqs = [srv.submit(sa if k % 2 else sb, pats[int(rng.integers(0, len(pats)))], pose(k), rgl.RGL_RETURN_FIRST_LAST, 0.1, 90.0)
+                    for k in range(wave)]
+            for r in reqs:
+                assert srv.wait(r, 20000.0)
+            r0 = reqs[-1]
+            ptr, cnt = C.c_void_p(), C.c_int32()
+            rgl.check(rgl.lib().rgl_gb300_server_get_result_host(srv.h, r0, rgl.RGL_FIELD_DISTANCE_F32, C.byref(ptr), C.byref(cnt)))
+            host = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float)), shape=(cnt.value,)).copy() if cnt.value else np.zeros(0, np.float32)
+            assert np.array_equal(host, srv.result(r0, rgl.RGL_FIELD_DISTANCE_F32))
+            for r in reqs:
+                srv.release(r)
+        assert srv.stats()["failed"] == 0
+    finally:
+        srv.destroy()
