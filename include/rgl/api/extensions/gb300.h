@@ -191,7 +191,7 @@ RGL_API rgl_status_t rgl_gb300_server_release(rgl_gb300_server_t server, int64_t
 /* Waits until no request is pending or running. */
 RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server);
 /* Counters: requests submitted, completed (including failed), failed; batches launched and the requests
- * they held; the largest admitted byte total. */
+ * they held; the largest admitted byte total; the summed device time of the batches in microseconds. */
 RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64_t* out_submitted, int64_t* out_completed,
                                                 int64_t* out_failed, int64_t* out_batches, int64_t* out_requests_in_batches,
-                                                int64_t* out_peak_reserved_bytes);
+                                                int64_t* out_peak_reserved_bytes, int64_t* out_device_us);

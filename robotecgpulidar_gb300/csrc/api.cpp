@@ -1400,7 +1400,7 @@ RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server)
 
 RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64_t* out_submitted, int64_t* out_completed,
                                                 int64_t* out_failed, int64_t* out_batches, int64_t* out_requests_in_batches,
-                                                int64_t* out_peak_reserved_bytes)
+                                                int64_t* out_peak_reserved_bytes, int64_t* out_device_us)
 {
 	return safeCall([&]() {
 		CHECK_ARG(server != nullptr);
@@ -1411,6 +1411,7 @@ RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64
 		if (out_batches) *out_batches = s.batches;
 		if (out_requests_in_batches) *out_requests_in_batches = s.jobsInBatches;
 		if (out_peak_reserved_bytes) *out_peak_reserved_bytes = s.peakReserved;
+		if (out_device_us) *out_device_us = (int64_t) (s.deviceSeconds * 1e6);
 	});
 }
 

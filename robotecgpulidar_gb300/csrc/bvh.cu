@@ -6,9 +6,11 @@
 #include <cuda_runtime.h>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "bvh_core.hpp"
 #include "kernels.hpp"
+#include "tlas_sah.hpp"
 
 namespace rgl {
 
@@ -88,7 +90,7 @@ __global__ void kMorton(const float4* __restrict__ lo, const float4* __restrict_
 }
 
 __global__ void kLbvh(const uint32_t* __restrict__ codes, int n, BinNode* bin, int32_t* rangeFirst, int32_t* rangeLast,
-                      int32_t* parentInt, int32_t* parentLeaf, const uint32_t* __restrict__ remapIds)
+                      int32_t* parentInt, int32_t* parentLeaf)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n - 1) {
@@ -105,14 +107,6 @@ __global__ void kLbvh(const uint32_t* __restrict__ codes, int n, BinNode* bin, i
 		parentInt[r] = i;
 	} else {
 		parentLeaf[~r] = i;
-	}
-	if (remapIds) { // TLAS: leaves reference instance indices
-		if (l < 0) {
-			l = ~(int32_t) remapIds[~l];
-		}
-		if (r < 0) {
-			r = ~(int32_t) remapIds[~r];
-		}
 	}
 	bin[i].left = l;
 	bin[i].right = r;
@@ -133,11 +127,10 @@ __device__ __forceinline__ Box loadBoxCg(const BinNode* n)
 }
 
 // Bottom-up bounds: the second child to arrive at a node unites both children and moves up.
-// Leaf boxes: lo/hi[ids[k]] for sorted position k; a leaf child ~c indexes lo/hi directly when
-// `leafChildIsId` (TLAS, remapped) or through ids[] otherwise (BLAS).
+// Leaf boxes: lo/hi[ids[k]] for sorted position k.
 __global__ void kBottomUp(int n, const uint32_t* __restrict__ ids, const float4* __restrict__ lo, const float4* __restrict__ hi,
                           BinNode* bin, const int32_t* __restrict__ parentInt, const int32_t* __restrict__ parentLeaf,
-                          uint32_t* visits, int leafChildIsId)
+                          uint32_t* visits)
 {
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= n) {
@@ -155,7 +148,7 @@ __global__ void kBottomUp(int n, const uint32_t* __restrict__ ids, const float4*
 			if (c[q] >= 0) {
 				bx[q] = loadBoxCg(&bin[c[q]]);
 			} else {
-				int li = leafChildIsId ? ~c[q] : (int) ids[~c[q]];
+				int li = (int) ids[~c[q]];
 				float4 l = lo[li], h = hi[li];
 				bx[q] = Box{l.x, l.y, l.z, h.x, h.y, h.z};
 			}
@@ -178,29 +171,6 @@ __global__ void kCollapse(const int2* __restrict__ qIn, const uint32_t* __restri
 	}
 }
 
-__global__ void kInstBoxes(const InstanceRec* __restrict__ inst, int n, float4* lo, float4* hi)
-{
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) {
-		const InstanceRec& r = inst[i];
-		lo[i] = make_float4(r.lox, r.loy, r.loz, 0.f);
-		hi[i] = make_float4(r.hix, r.hiy, r.hiz, 0.f);
-	}
-}
-
-__global__ void kCentroidBounds(const float4* __restrict__ lo, const float4* __restrict__ hi, int n, uint32_t* cbounds)
-{
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t < n) {
-		float4 l = lo[t], h = hi[t];
-		float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
-		for (int a = 0; a < 3; ++a) {
-			atomicMin(&cbounds[a], orderedBits(c[a]));
-			atomicMax(&cbounds[3 + a], orderedBits(c[a]));
-		}
-	}
-}
-
 inline int blocks(int n, int b) { return (n + b - 1) / b; }
 
 template<class T>
@@ -209,6 +179,103 @@ T* mallocAsync(size_t count, cudaStream_t s)
 	void* p = nullptr;
 	RGL_CUDA_OK(cudaMallocAsync(&p, sizeof(T) * (count ? count : 1), s));
 	return static_cast<T*>(p);
+}
+
+} // namespace
+
+namespace {
+
+struct WideBuildResult
+{
+	uint32_t nodeCount;
+	Box bounds;
+};
+
+// Wide BVH over n primitive boxes lo/hi (device) whose centroid bounds are in cb (6 ordered uints),
+// all written on stream s: Morton codes, onesweep sort, LBVH, bottom-up bounds, collapse into 8-wide
+// nodes. Leaf records are triangles (dV/dI given) or primitive indices (dV null). Frees lo, hi, cb and
+// its temporaries and synchronises s (a one-off build).
+WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const float* dV, const int32_t* dI, int leafMax,
+                          WideNode* outNodes, TriRecord* outLeaves, Box* outBoxes, cudaStream_t s)
+{
+	uint32_t* codes = mallocAsync<uint32_t>(n, s);
+	uint32_t* ids = mallocAsync<uint32_t>(n, s);
+	void* sortScratch = mallocAsync<uint8_t>(sortPairsScratchBytes(n, 30), s);
+	BinNode* bin = mallocAsync<BinNode>(n, s);
+	int32_t* rf = mallocAsync<int32_t>(n, s);
+	int32_t* rl = mallocAsync<int32_t>(n, s);
+	int32_t* pi = mallocAsync<int32_t>(n, s);
+	int32_t* pl = mallocAsync<int32_t>(n, s);
+	uint32_t* visits = mallocAsync<uint32_t>(n, s);
+	int2* q0 = mallocAsync<int2>(n, s);
+	int2* q1 = mallocAsync<int2>(n, s);
+	// counters: [0] wide, [1] leaf records, [2] q0 count, [3] q1 count, [4] error
+	uint32_t* ctr = mallocAsync<uint32_t>(8, s);
+	RGL_CUDA_OK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * n, s));
+	RGL_CUDA_OK(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 8, s));
+	int32_t* err = reinterpret_cast<int32_t*>(ctr + 4);
+
+	kMorton<<<blocks(n, 256), 256, 0, s>>>(lo, hi, n, cb, codes, ids);
+	countLaunch();
+	sortPairs(codes, ids, n, 30, sortScratch, err, s);
+	if (n > 1) {
+		kLbvh<<<blocks(n - 1, 256), 256, 0, s>>>(codes, n, bin, rf, rl, pi, pl);
+		countLaunch();
+		kBottomUp<<<blocks(n, 256), 256, 0, s>>>(n, ids, lo, hi, bin, pi, pl, visits);
+		countLaunch();
+	}
+	int2 root = make_int2(n == 1 ? ~0 : 0, 0);
+	uint32_t one[2] = {1u, 0u};
+	RGL_CUDA_OK(cudaMemcpyAsync(q0, &root, sizeof(int2), cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(ctr, one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));     // wide counter = 1 (root)
+	RGL_CUDA_OK(cudaMemcpyAsync(ctr + 2, one, sizeof(uint32_t), cudaMemcpyHostToDevice, s)); // q0 count = 1
+	CollapseInputs ci{bin, rf, rl, reinterpret_cast<const int32_t*>(ids), lo, hi, dV, dI, leafMax};
+	int2* qa = q0;
+	int2* qb = q1;
+	uint32_t* ca = ctr + 2;
+	uint32_t* cbn = ctr + 3;
+	// A wide level descends at least one binary level; binary depth is below 64 for 30-bit keys with
+	// index tie-break, so 64 launches always drain the queue (empty launches exit immediately).
+	const int grid = 152 * 4;
+	for (int level = 0; level < 64; ++level) {
+		RGL_CUDA_OK(cudaMemsetAsync(cbn, 0, sizeof(uint32_t), s));
+		CollapseOutputs co{outNodes, outLeaves, ctr, ctr + 1, qb, cbn, outBoxes};
+		kCollapse<<<grid, 128, 0, s>>>(qa, ca, ci, co);
+		countLaunch();
+		int2* tq = qa;
+		qa = qb;
+		qb = tq;
+		uint32_t* tc = ca;
+		ca = cbn;
+		cbn = tc;
+	}
+	uint32_t hostCtr[8];
+	RGL_CUDA_OK(cudaMemcpyAsync(hostCtr, ctr, sizeof(hostCtr), cudaMemcpyDeviceToHost, s));
+	BinNode rootBox{};
+	float4 leafLo{}, leafHi{};
+	if (n > 1) {
+		RGL_CUDA_OK(cudaMemcpyAsync(&rootBox, bin, sizeof(BinNode), cudaMemcpyDeviceToHost, s));
+	} else {
+		RGL_CUDA_OK(cudaMemcpyAsync(&leafLo, lo, sizeof(float4), cudaMemcpyDeviceToHost, s));
+		RGL_CUDA_OK(cudaMemcpyAsync(&leafHi, hi, sizeof(float4), cudaMemcpyDeviceToHost, s));
+	}
+	void* temps[] = {lo, hi, cb, codes, ids, sortScratch, bin, rf, rl, pi, pl, visits, q0, q1, ctr};
+	for (void* p : temps) {
+		RGL_CUDA_OK(cudaFreeAsync(p, s));
+	}
+	RGL_CUDA_OK(cudaStreamSynchronize(s));
+	if (hostCtr[4] != 0) {
+		throw std::runtime_error("BVH build: radix sort look-back did not complete");
+	}
+	if (hostCtr[1] != (uint32_t) n || hostCtr[0] > (uint32_t) n || hostCtr[ca - ctr] != 0) {
+		throw std::runtime_error("BVH build: collapse produced an inconsistent tree (leaf records " + std::to_string(hostCtr[1]) +
+		                         ", nodes " + std::to_string(hostCtr[0]) + ")");
+	}
+	WideBuildResult r;
+	r.nodeCount = hostCtr[0];
+	r.bounds = n > 1 ? Box{rootBox.lox, rootBox.loy, rootBox.loz, rootBox.hix, rootBox.hiy, rootBox.hiz}
+	                 : Box{leafLo.x, leafLo.y, leafLo.z, leafHi.x, leafHi.y, leafHi.z};
+	return r;
 }
 
 } // namespace
@@ -223,105 +290,22 @@ void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, i
 	float4* lo = mallocAsync<float4>(T, s);
 	float4* hi = mallocAsync<float4>(T, s);
 	uint32_t* cb = mallocAsync<uint32_t>(8, s);
-	uint32_t* codes = mallocAsync<uint32_t>(T, s);
-	uint32_t* ids = mallocAsync<uint32_t>(T, s);
-	void* sortScratch = mallocAsync<uint8_t>(sortPairsScratchBytes(T, 30), s);
-	BinNode* bin = mallocAsync<BinNode>(T, s);
-	int32_t* rf = mallocAsync<int32_t>(T, s);
-	int32_t* rl = mallocAsync<int32_t>(T, s);
-	int32_t* pi = mallocAsync<int32_t>(T, s);
-	int32_t* pl = mallocAsync<int32_t>(T, s);
-	uint32_t* visits = mallocAsync<uint32_t>(T, s);
-	int2* q0 = mallocAsync<int2>(T, s);
-	int2* q1 = mallocAsync<int2>(T, s);
-	// counters: [0] wide, [1] tri, [2] q0 count, [3] q1 count, [4] error
-	uint32_t* ctr = mallocAsync<uint32_t>(8, s);
-
 	out.nodeCapacity = (uint32_t) T;
 	out.triCount = T;
 	RGL_CUDA_OK(cudaMalloc(&out.nodes, sizeof(WideNode) * (size_t) T));
 	RGL_CUDA_OK(cudaMalloc(&out.tris, sizeof(TriRecord) * (size_t) T));
-
 	uint32_t cbInit[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
 	RGL_CUDA_OK(cudaMemcpyAsync(cb, cbInit, sizeof(cbInit), cudaMemcpyHostToDevice, s));
-	RGL_CUDA_OK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * T, s));
-	RGL_CUDA_OK(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 8, s));
-	int32_t* err = reinterpret_cast<int32_t*>(ctr + 4);
-
 	kTriBounds<<<blocks(T, 256), 256, 0, s>>>(dVertices, dIndices, T, lo, hi, cb);
 	countLaunch();
-	kMorton<<<blocks(T, 256), 256, 0, s>>>(lo, hi, T, cb, codes, ids);
-	countLaunch();
-	sortPairs(codes, ids, T, 30, sortScratch, err, s);
-	if (T > 1) {
-		kLbvh<<<blocks(T - 1, 256), 256, 0, s>>>(codes, T, bin, rf, rl, pi, pl, nullptr);
-		countLaunch();
-		kBottomUp<<<blocks(T, 256), 256, 0, s>>>(T, ids, lo, hi, bin, pi, pl, visits, 0);
-		countLaunch();
-	}
-	int2 root = make_int2(T == 1 ? ~0 : 0, 0);
-	uint32_t one[2] = {1u, 0u};
-	RGL_CUDA_OK(cudaMemcpyAsync(q0, &root, sizeof(int2), cudaMemcpyHostToDevice, s));
-	RGL_CUDA_OK(cudaMemcpyAsync(ctr, one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));     // wide counter = 1 (root)
-	RGL_CUDA_OK(cudaMemcpyAsync(ctr + 2, one, sizeof(uint32_t), cudaMemcpyHostToDevice, s)); // q0 count = 1
-	CollapseInputs ci{bin, rf, rl, reinterpret_cast<const int32_t*>(ids), lo, hi, dVertices, dIndices};
-	int2* qa = q0;
-	int2* qb = q1;
-	uint32_t* ca = ctr + 2;
-	uint32_t* cbn = ctr + 3;
-	// A wide level descends at least one binary level; binary depth is below 64 for 30-bit keys with
-	// index tie-break, so 64 launches always drain the queue (empty launches exit immediately).
-	const int grid = 152 * 4;
-	for (int level = 0; level < 64; ++level) {
-		RGL_CUDA_OK(cudaMemsetAsync(cbn, 0, sizeof(uint32_t), s));
-		CollapseOutputs co{out.nodes, out.tris, ctr, ctr + 1, qb, cbn};
-		kCollapse<<<grid, 128, 0, s>>>(qa, ca, ci, co);
-		countLaunch();
-		int2* tq = qa;
-		qa = qb;
-		qb = tq;
-		uint32_t* tc = ca;
-		ca = cbn;
-		cbn = tc;
-	}
-	uint32_t hostCtr[8];
-	RGL_CUDA_OK(cudaMemcpyAsync(hostCtr, ctr, sizeof(hostCtr), cudaMemcpyDeviceToHost, s));
-	BinNode rootBox{};
-	float4 leafLo{}, leafHi{};
-	if (T > 1) {
-		RGL_CUDA_OK(cudaMemcpyAsync(&rootBox, bin, sizeof(BinNode), cudaMemcpyDeviceToHost, s));
-	} else {
-		RGL_CUDA_OK(cudaMemcpyAsync(&leafLo, lo, sizeof(float4), cudaMemcpyDeviceToHost, s));
-		RGL_CUDA_OK(cudaMemcpyAsync(&leafHi, hi, sizeof(float4), cudaMemcpyDeviceToHost, s));
-	}
-	void* temps[] = {lo, hi, cb, codes, ids, sortScratch, bin, rf, rl, pi, pl, visits, q0, q1, ctr};
-	for (void* p : temps) {
-		RGL_CUDA_OK(cudaFreeAsync(p, s));
-	}
-	RGL_CUDA_OK(cudaStreamSynchronize(s));
-	if (hostCtr[4] != 0) {
-		throw std::runtime_error("BVH build: radix sort look-back did not complete");
-	}
-	if (hostCtr[1] != (uint32_t) T || hostCtr[0] > (uint32_t) T || hostCtr[ca - ctr] != 0) {
-		throw std::runtime_error("BVH build: collapse produced an inconsistent tree (tris " + std::to_string(hostCtr[1]) +
-		                         ", nodes " + std::to_string(hostCtr[0]) + ")");
-	}
-	out.nodeCount = hostCtr[0];
-	if (T > 1) {
-		out.bounds[0] = rootBox.lox;
-		out.bounds[1] = rootBox.loy;
-		out.bounds[2] = rootBox.loz;
-		out.bounds[3] = rootBox.hix;
-		out.bounds[4] = rootBox.hiy;
-		out.bounds[5] = rootBox.hiz;
-	} else {
-		out.bounds[0] = leafLo.x;
-		out.bounds[1] = leafLo.y;
-		out.bounds[2] = leafLo.z;
-		out.bounds[3] = leafHi.x;
-		out.bounds[4] = leafHi.y;
-		out.bounds[5] = leafHi.z;
-	}
+	const WideBuildResult r = buildWide(lo, hi, cb, T, dVertices, dIndices, kLeafMaxTris, out.nodes, out.tris, nullptr, s);
+	out.nodeCount = r.nodeCount;
+	out.bounds[0] = r.bounds.lox;
+	out.bounds[1] = r.bounds.loy;
+	out.bounds[2] = r.bounds.loz;
+	out.bounds[3] = r.bounds.hix;
+	out.bounds[4] = r.bounds.hiy;
+	out.bounds[5] = r.bounds.hiz;
 }
 
 void freeBlas(BlasBuild& b)
@@ -333,83 +317,157 @@ void freeBlas(BlasBuild& b)
 }
 
 namespace {
-struct TlasTemps
+
+// TLAS refit after pose changes, one block: depth by depth from the leaves up, every wide node takes
+// the union of its children's boxes (child nodes' stored boxes, instances' world boxes) and
+// re-quantises its children in a new frame with the builder's arithmetic. Topology and slots stay.
+__global__ void __launch_bounds__(256) kRefitTlas(WideNode* nodes, const TriRecord* __restrict__ leaves, Box* boxes,
+                                                  const InstanceRec* __restrict__ inst, const int32_t* __restrict__ levelStarts,
+                                                  int nLevels)
 {
-	float4* lo;
-	float4* hi;
-	uint32_t* codes;
-	uint32_t* ids;
-	uint32_t* cbounds;
-};
-TlasTemps tlasTemps(TlasBuild& t)
-{
-	uint8_t* p = static_cast<uint8_t*>(t.scratch);
-	int n = t.capacity;
-	TlasTemps r;
-	r.lo = reinterpret_cast<float4*>(p);
-	r.hi = r.lo + n;
-	r.codes = reinterpret_cast<uint32_t*>(r.hi + n);
-	r.ids = r.codes + n;
-	r.cbounds = r.ids + n;
-	return r;
+	for (int L = nLevels - 1; L >= 0; --L) {
+		const int a = levelStarts[L], b = levelStarts[L + 1];
+		for (int i = a + (int) threadIdx.x; i < b; i += blockDim.x) {
+			WideNode w = nodes[i];
+			Box cbx[kWideArity];
+			uint32_t present = 0;
+			Box nb = emptyBox();
+			for (int k = 0; k < kWideArity; ++k) {
+				const bool internal = (w.imask >> k) & 1u;
+				if (!internal && w.meta[k] == 0) {
+					continue;
+				}
+				if (internal) {
+					cbx[k] = boxes[w.childBase + (uint32_t) __popc(w.imask & ((1u << k) - 1u))];
+				} else {
+					const InstanceRec& r = inst[leaves[w.triBase + (w.meta[k] & 31u)].primId];
+					cbx[k] = Box{r.lox, r.loy, r.loz, r.hix, r.hiy, r.hiz};
+				}
+				present |= 1u << k;
+				nb = unite(nb, cbx[k]);
+			}
+			setWideFrame(w, nb);
+			for (int k = 0; k < kWideArity; ++k) {
+				if ((present >> k) & 1u) {
+					quantizeChild(w, k, cbx[k]);
+				} else {
+					clearChild(w, k);
+				}
+			}
+			nodes[i] = w;
+			boxes[i] = nb;
+		}
+		__syncthreads();
+	}
 }
+
 } // namespace
 
-void buildTlas(const InstanceRec* dInst, int n, TlasBuild& t, int32_t* dError, cudaStream_t s)
+// The TLAS is a wide BVH over the instances' world boxes, one instance per leaf child. Its topology is
+// built on the host by a full sweep SAH over the (few) instance boxes and collapsed with the BLAS
+// collapse (tlas_sah.hpp); node depths (contiguous per depth: the collapse allocates nodes level by
+// level) drive the refit kernel, which keeps the topology on pose changes.
+void buildTlas(const InstanceRec* hInst, int n, TlasBuild& t, cudaStream_t s)
 {
 	t.nInstances = n;
-	if (n <= 1) {
+	t.nodeCount = 0;
+	t.nLevels = 0;
+	if (n <= 0) {
 		return;
 	}
 	if (n > t.capacity) {
 		freeTlas(t);
 		t.capacity = n;
-		size_t sortBytes = sortPairsScratchBytes(n, 30);
-		t.scratchBytes = sizeof(float4) * 2 * (size_t) n + sizeof(uint32_t) * (2 * (size_t) n + 8) + sortBytes;
-		RGL_CUDA_OK(cudaMalloc(&t.nodes, sizeof(BinNode) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.parents, sizeof(int32_t) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.leafParents, sizeof(int32_t) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.visits, sizeof(uint32_t) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.scratch, t.scratchBytes));
+		RGL_CUDA_OK(cudaMalloc(&t.nodes, sizeof(WideNode) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.leaves, sizeof(TriRecord) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.boxes, sizeof(Box) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.levelStarts, sizeof(int32_t) * 66));
 		t.nInstances = n;
 	}
-	TlasTemps tt = tlasTemps(t);
-	void* sortScratch = reinterpret_cast<uint8_t*>(tt.cbounds + 8);
-	kInstBoxes<<<blocks(n, 128), 128, 0, s>>>(dInst, n, tt.lo, tt.hi);
-	countLaunch();
-	uint32_t cbInit[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-	RGL_CUDA_OK(cudaMemcpyAsync(tt.cbounds, cbInit, sizeof(cbInit), cudaMemcpyHostToDevice, s));
-	kCentroidBounds<<<blocks(n, 128), 128, 0, s>>>(tt.lo, tt.hi, n, tt.cbounds);
-	countLaunch();
-	kMorton<<<blocks(n, 128), 128, 0, s>>>(tt.lo, tt.hi, n, tt.cbounds, tt.codes, tt.ids);
-	countLaunch();
-	sortPairs(tt.codes, tt.ids, n, 30, sortScratch, dError, s);
-	kLbvh<<<blocks(n - 1, 128), 128, 0, s>>>(tt.codes, n, t.nodes, nullptr, nullptr, t.parents, t.leafParents, tt.ids);
-	countLaunch();
-	refitTlas(dInst, t, s);
+	std::vector<Box> boxes(n);
+	std::vector<float4> lo(n), hi(n);
+	for (int i = 0; i < n; ++i) {
+		const InstanceRec& r = hInst[i];
+		boxes[i] = Box{r.lox, r.loy, r.loz, r.hix, r.hiy, r.hiz};
+		lo[i] = make_float4(r.lox, r.loy, r.loz, 0.0f);
+		hi[i] = make_float4(r.hix, r.hiy, r.hiz, 0.0f);
+	}
+	SahTree tree = buildSahTree(boxes);
+	std::vector<WideNode> wide(n);
+	std::vector<TriRecord> leaves(n);
+	std::vector<Box> wideBoxes(n);
+	uint32_t wideCounter = 1, leafCounter = 0;
+	std::vector<int2> qa(n), qb(n);
+	uint32_t qaCount = 1, qbCount = 0;
+	qa[0] = make_int2(n == 1 ? ~0 : 0, 0);
+	CollapseInputs in{tree.bin.data(), tree.rangeFirst.data(), tree.rangeLast.data(), tree.sortedIds.data(), lo.data(), hi.data(),
+	                  nullptr, nullptr, 1};
+	while (qaCount > 0) {
+		qbCount = 0;
+		CollapseOutputs o{wide.data(), leaves.data(), &wideCounter, &leafCounter, qb.data(), &qbCount, wideBoxes.data()};
+		for (uint32_t i = 0; i < qaCount; ++i) {
+			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
+		}
+		std::swap(qa, qb);
+		qaCount = qbCount;
+	}
+	if (leafCounter != (uint32_t) n || wideCounter > (uint32_t) n) {
+		throw std::runtime_error("TLAS build: collapse produced an inconsistent tree");
+	}
+	t.nodeCount = wideCounter;
+	// Depth of every node, then the first index per depth.
+	std::vector<int> depth(wideCounter, 0);
+	int maxDepth = 0;
+	for (uint32_t i = 0; i < wideCounter; ++i) {
+		uint32_t rank = 0;
+		for (int k = 0; k < kWideArity; ++k) {
+			if ((wide[i].imask >> k) & 1u) {
+				depth[wide[i].childBase + rank] = depth[i] + 1;
+				maxDepth = std::max(maxDepth, depth[i] + 1);
+				++rank;
+			}
+		}
+	}
+	for (uint32_t i = 1; i < wideCounter; ++i) {
+		if (depth[i] < depth[i - 1]) {
+			throw std::runtime_error("TLAS build: node depths are not contiguous");
+		}
+	}
+	if (maxDepth + 2 > 66) {
+		throw std::runtime_error("TLAS build: tree deeper than 64 levels");
+	}
+	std::vector<int32_t> starts(maxDepth + 2, (int32_t) wideCounter);
+	for (int L = maxDepth; L >= 0; --L) {
+		for (uint32_t i = 0; i < wideCounter; ++i) {
+			if (depth[i] == L) {
+				starts[L] = (int32_t) i;
+				break;
+			}
+		}
+	}
+	t.nLevels = maxDepth + 1;
+	// Pageable sources: each copy is staged before the call returns.
+	RGL_CUDA_OK(cudaMemcpyAsync(t.nodes, wide.data(), sizeof(WideNode) * wideCounter, cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(t.leaves, leaves.data(), sizeof(TriRecord) * (size_t) n, cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(t.boxes, wideBoxes.data(), sizeof(Box) * wideCounter, cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(t.levelStarts, starts.data(), sizeof(int32_t) * starts.size(), cudaMemcpyHostToDevice, s));
 }
 
 void refitTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
 {
-	int n = t.nInstances;
-	if (n <= 1) {
+	if (t.nInstances <= 0 || t.nLevels <= 0) {
 		return;
 	}
-	TlasTemps tt = tlasTemps(t);
-	kInstBoxes<<<blocks(n, 128), 128, 0, s>>>(dInst, n, tt.lo, tt.hi);
-	countLaunch();
-	RGL_CUDA_OK(cudaMemsetAsync(t.visits, 0, sizeof(uint32_t) * (size_t) (n - 1), s));
-	kBottomUp<<<blocks(n, 128), 128, 0, s>>>(n, tt.ids, tt.lo, tt.hi, t.nodes, t.parents, t.leafParents, t.visits, 1);
+	kRefitTlas<<<1, 256, 0, s>>>(t.nodes, t.leaves, reinterpret_cast<Box*>(t.boxes), dInst, t.levelStarts, t.nLevels);
 	countLaunch();
 }
 
 void freeTlas(TlasBuild& t)
 {
 	cudaFree(t.nodes);
-	cudaFree(t.parents);
-	cudaFree(t.leafParents);
-	cudaFree(t.visits);
-	cudaFree(t.scratch);
+	cudaFree(t.leaves);
+	cudaFree(t.boxes);
+	cudaFree(t.levelStarts);
 	t = TlasBuild{};
 }
 

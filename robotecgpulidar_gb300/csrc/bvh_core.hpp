@@ -177,6 +177,42 @@ RGL_HD uint32_t atomicAddU32(uint32_t* p, uint32_t v)
 #endif
 }
 
+// Quantisation frame of a wide node over its box nb: per-axis exponents and an origin one grid step
+// below the box (rounded down), so child boxes can be widened downward by a step.
+RGL_HD void setWideFrame(WideNode& w, const Box& nb)
+{
+	w.ex = quantExponent(nb.hix - nb.lox);
+	w.ey = quantExponent(nb.hiy - nb.loy);
+	w.ez = quantExponent(nb.hiz - nb.loz);
+	auto originBelow = [](float lo, uint8_t e) {
+		const double exact = (double) lo - (double) exp2Byte(e);
+		float p = (float) exact;
+		if ((double) p > exact) {
+			p = nextafterf(p, -FLT_MAX);
+		}
+		return p;
+	};
+	w.px = originBelow(nb.lox, w.ex);
+	w.py = originBelow(nb.loy, w.ey);
+	w.pz = originBelow(nb.loz, w.ez);
+}
+
+// An empty child slot: a box that no ray enters.
+RGL_HD void clearChild(WideNode& w, int k)
+{
+	w.qlox[k] = w.qloy[k] = w.qloz[k] = 255;
+	w.qhix[k] = w.qhiy[k] = w.qhiz[k] = 0;
+}
+
+// Conservative 8-bit box of child slot k in the node's frame (verified and widened, quantizeAxis).
+RGL_HD void quantizeChild(WideNode& w, int k, const Box& b)
+{
+	const float sx = exp2Byte(w.ex), sy = exp2Byte(w.ey), sz = exp2Byte(w.ez);
+	quantizeAxis(w.px, sx, b.lox, b.hix, w.qlox[k], w.qhix[k]);
+	quantizeAxis(w.py, sy, b.loy, b.hiy, w.qloy[k], w.qhiy[k]);
+	quantizeAxis(w.pz, sz, b.loz, b.hiz, w.qloz[k], w.qhiz[k]);
+}
+
 struct CollapseInputs
 {
 	const BinNode* bin;        // n-1 internal nodes with bounds (n >= 2)
@@ -185,8 +221,9 @@ struct CollapseInputs
 	const int32_t* sortedIds;  // sorted position -> original triangle
 	const float4* triLo;       // per original triangle
 	const float4* triHi;
-	const float* vertices;     // 3 floats per vertex
+	const float* vertices;     // 3 floats per vertex; null: leaf records carry only primId (TLAS)
 	const int32_t* indices;    // 3 ints per triangle
+	int32_t leafMax;           // primitives per leaf child: kLeafMaxTris (BLAS) or 1 (TLAS)
 };
 
 struct CollapseOutputs
@@ -197,6 +234,7 @@ struct CollapseOutputs
 	uint32_t* triCounter;
 	int2* queueOut;
 	uint32_t* queueOutCount;
+	Box* wideBoxes; // optional: float box of every wide node (TLAS refit)
 };
 
 RGL_HD int binCount(const CollapseInputs& in, int32_t c) { return c < 0 ? 1 : (in.rangeLast[c] - in.rangeFirst[c] + 1); }
@@ -227,7 +265,7 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 		float bestA = -1.0f;
 		for (int k = 0; k < n; ++k) {
 			int32_t c = ch[k];
-			if (c >= 0 && binCount(in, c) > kLeafMaxTris) {
+			if (c >= 0 && binCount(in, c) > in.leafMax) {
 				float a = halfArea(binBox(in.bin[c]));
 				if (a > bestA) {
 					bestA = a;
@@ -250,7 +288,7 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 		cb0[k] = childBounds(in, ch[k]);
 		nb = unite(nb, cb0[k]);
 		int cnt = binCount(in, ch[k]);
-		if (ch[k] >= 0 && cnt > kLeafMaxTris) {
+		if (ch[k] >= 0 && cnt > in.leafMax) {
 			++nInternal;
 		} else {
 			nLeafTris += (uint32_t) cnt;
@@ -305,41 +343,23 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 	uint32_t qBase = nInternal ? atomicAddU32(out.queueOutCount, nInternal) : 0;
 
 	WideNode w;
-	w.ex = quantExponent(nb.hix - nb.lox);
-	w.ey = quantExponent(nb.hiy - nb.loy);
-	w.ez = quantExponent(nb.hiz - nb.loz);
-	// Origin one grid step below the node box (rounded down), so children can be widened downward.
-	auto originBelow = [](float lo, uint8_t e) {
-		const double exact = (double) lo - (double) exp2Byte(e);
-		float p = (float) exact;
-		if ((double) p > exact) {
-			p = nextafterf(p, -FLT_MAX);
-		}
-		return p;
-	};
-	w.px = originBelow(nb.lox, w.ex);
-	w.py = originBelow(nb.loy, w.ey);
-	w.pz = originBelow(nb.loz, w.ez);
+	setWideFrame(w, nb);
 	w.imask = 0;
 	w.childBase = childBase;
 	w.triBase = triBase;
-	float sx = exp2Byte(w.ex), sy = exp2Byte(w.ey), sz = exp2Byte(w.ez);
 	for (int k = 0; k < kWideArity; ++k) {
 		w.meta[k] = 0;
-		w.qlox[k] = w.qloy[k] = w.qloz[k] = 255;
-		w.qhix[k] = w.qhiy[k] = w.qhiz[k] = 0;
+		clearChild(w, k);
 	}
 	uint32_t rank = 0, triOff = 0;
 	for (int k = 0; k < kWideArity; ++k) {
 		if (slotChild[k] < 0) {
 			continue;
 		}
-		quantizeAxis(w.px, sx, cb[k].lox, cb[k].hix, w.qlox[k], w.qhix[k]);
-		quantizeAxis(w.py, sy, cb[k].loy, cb[k].hiy, w.qloy[k], w.qhiy[k]);
-		quantizeAxis(w.pz, sz, cb[k].loz, cb[k].hiz, w.qloz[k], w.qhiz[k]);
+		quantizeChild(w, k, cb[k]);
 		int32_t c = chs[k];
 		int cnt = binCount(in, c);
-		if (c >= 0 && cnt > kLeafMaxTris) {
+		if (c >= 0 && cnt > in.leafMax) {
 			w.imask |= (uint8_t) (1u << k);
 			out.queueOut[qBase + rank] = make_int2(c, (int) (childBase + rank));
 			++rank;
@@ -348,6 +368,12 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 			w.meta[k] = (uint8_t) ((cnt << 5) | (int) triOff);
 			for (int m = 0; m < cnt; ++m) {
 				int tid = in.sortedIds[firstPos + m];
+				if (in.vertices == nullptr) { // TLAS leaf: the instance index only
+					TriRecord tr{};
+					tr.primId = tid;
+					out.tris[triBase + triOff + m] = tr;
+					continue;
+				}
 				const int32_t* ix = in.indices + 3 * (size_t) tid;
 				const float* a = in.vertices + 3 * (size_t) ix[0];
 				const float* b = in.vertices + 3 * (size_t) ix[1];
@@ -371,6 +397,9 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 		}
 	}
 	out.wide[wideIdx] = w;
+	if (out.wideBoxes) {
+		out.wideBoxes[wideIdx] = nb;
+	}
 }
 
 } // namespace rgl

@@ -84,7 +84,8 @@ struct alignas(16) InstanceRec
 // stays valid when the acceleration structure is rebuilt.
 struct SceneView
 {
-	const BinNode* tlas;       // nInstances - 1 internal nodes (root = 0); unused when nInstances == 1
+	const WideNode* tlas;         // wide nodes over the instances (root = 0), the BLAS node format
+	const TriRecord* tlasLeaves;  // leaf records of the TLAS: primId = instance index
 	const InstanceRec* instances;
 	int32_t nInstances;
 	int32_t pad;

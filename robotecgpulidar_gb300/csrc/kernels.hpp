@@ -33,18 +33,19 @@ void freeBlas(BlasBuild& b);
 
 struct TlasBuild
 {
-	BinNode* nodes = nullptr;        // nInstances - 1
-	int32_t* parents = nullptr;      // parent of internal node
-	int32_t* leafParents = nullptr;  // parent of instance (by instance index)
-	uint32_t* visits = nullptr;      // bottom-up counters
+	WideNode* nodes = nullptr;       // wide nodes over the instances (at most nInstances)
+	TriRecord* leaves = nullptr;     // one record per instance; primId = instance index
+	float* boxes = nullptr;          // float box (6 floats) of every wide node, kept for the refit
+	int32_t* levelStarts = nullptr;  // first node index of each depth, nLevels + 1 entries
+	int32_t nLevels = 0;
 	int32_t capacity = 0;
 	int32_t nInstances = 0;
-	void* scratch = nullptr;
-	size_t scratchBytes = 0;
+	uint32_t nodeCount = 0;
 };
-// (Re)builds the TLAS topology and bounds over `nInstances` device instance records.
-void buildTlas(const InstanceRec* dInstances, int nInstances, TlasBuild& t, int32_t* dError, cudaStream_t stream);
-// Refits TLAS bounds after instance boxes changed (same instance set and order).
+// (Re)builds the TLAS over `nInstances` instance records given in HOST memory: SAH topology on the host,
+// then the device copies of nodes, leaf records, node boxes and depth ranges on `stream`.
+void buildTlas(const InstanceRec* hInstances, int nInstances, TlasBuild& t, cudaStream_t stream);
+// Refits the TLAS after instance boxes changed (same instance set): one single-block launch.
 void refitTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);
 void freeTlas(TlasBuild& t);
 

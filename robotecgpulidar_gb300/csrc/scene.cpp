@@ -196,7 +196,7 @@ void Scene::prepare(cudaStream_t s)
 		RGL_CHECK_CUDA(cudaMemcpyAsync(dInst, rec, sizeof(rgl::InstanceRec) * n, cudaMemcpyHostToDevice, s));
 	}
 	if (topologyDirty || tlas.nInstances != n) {
-		rgl::buildTlas(dInst, n, tlas, dError.device(), s);
+		rgl::buildTlas(rec, n, tlas, s);
 		++tlasBuilds;
 	} else {
 		rgl::refitTlas(dInst, tlas, s);
@@ -204,6 +204,7 @@ void Scene::prepare(cudaStream_t s)
 	}
 	auto* v = static_cast<rgl::SceneView*>(hView.ensure(sizeof(rgl::SceneView)));
 	v->tlas = tlas.nodes;
+	v->tlasLeaves = tlas.leaves;
 	v->instances = dInst;
 	v->nInstances = n;
 	v->pad = 0;

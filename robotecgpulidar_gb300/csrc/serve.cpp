@@ -11,9 +11,27 @@ using rgl::format;
 Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmBudgetBytes), maxInFlight(std::max(1, maxInFlightBatches))
 {
 	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+	// Result arena: a quarter of the budget, between 64 MB and 8 GB, rounded down to a power of two
+	// of the minimum block.
+	const size_t want = (size_t) std::min<int64_t>(std::max<int64_t>(budget / 4, 64ll << 20), 8ll << 30);
+	int order = 0;
+	while ((Arena::kMinBlock << (order + 1)) <= want) {
+		++order;
+	}
+	arena.maxOrder = order;
+	arena.freeByOrder.assign(order + 1, {});
+	arena.freeByOrder[order].insert(0);
+	void* h = nullptr;
+	RGL_CHECK_CUDA(cudaHostAlloc(&h, Arena::kMinBlock << order, cudaHostAllocMapped | cudaHostAllocPortable));
+	void* d = nullptr;
+	RGL_CHECK_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+	arena.host = static_cast<uint8_t*>(h);
+	arena.dev = static_cast<uint8_t*>(d);
 	for (int i = 0; i < maxInFlight; ++i) {
 		auto s = std::make_unique<Slot>();
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+		RGL_CHECK_CUDA(cudaEventCreate(&s->t0));
+		RGL_CHECK_CUDA(cudaEventCreate(&s->t1));
 		s->counter.ensure(sizeof(uint32_t));
 		slots.push_back(std::move(s));
 	}
@@ -31,44 +49,102 @@ Server::~Server()
 		worker.join();
 	}
 	cudaStreamSynchronize(stream);
-	for (void* p : allBlocks) {
-		cudaFreeHost(p);
-	}
+	cudaFreeHost(arena.host);
 	for (auto& s : slots) {
 		cudaEventDestroy(s->done);
+		cudaEventDestroy(s->t0);
+		cudaEventDestroy(s->t1);
 	}
 	cudaStreamDestroy(stream);
 }
 
-Server::HostBlock Server::takeHostBlock(size_t bytes, size_t& cls)
+int Server::Arena::orderFor(size_t bytes)
 {
-	cls = 65536;
-	while (cls < bytes) {
-		cls <<= 1;
+	int o = 0;
+	while ((kMinBlock << o) < bytes) {
+		++o;
 	}
-	{
-		std::lock_guard<std::mutex> g(m);
-		auto& fl = freeBlocks[cls];
-		if (!fl.empty()) {
-			HostBlock b = fl.back();
-			fl.pop_back();
-			return b;
-		}
-	}
-	HostBlock b{};
-	RGL_CHECK_CUDA(cudaHostAlloc(&b.host, cls, cudaHostAllocMapped | cudaHostAllocPortable));
-	RGL_CHECK_CUDA(cudaHostGetDevicePointer(&b.dev, b.host, 0));
-	std::lock_guard<std::mutex> g(m);
-	allBlocks.push_back(b.host);
-	return b;
+	return o;
 }
 
-void Server::giveHostBlock(const HostBlock& b, size_t cls) { freeBlocks[cls].push_back(b); }
+bool Server::Arena::take(size_t bytes, size_t& offset, int& order)
+{
+	order = orderFor(bytes);
+	int o = order;
+	while (o <= maxOrder && freeByOrder[o].empty()) {
+		++o;
+	}
+	if (o > maxOrder) {
+		return false;
+	}
+	offset = *freeByOrder[o].begin();
+	freeByOrder[o].erase(freeByOrder[o].begin());
+	while (o > order) { // split, keeping the lower half
+		--o;
+		freeByOrder[o].insert(offset + (kMinBlock << o));
+	}
+	return true;
+}
+
+void Server::Arena::give(size_t offset, int order)
+{
+	while (order < maxOrder) {
+		const size_t buddy = offset ^ (kMinBlock << order);
+		auto it = freeByOrder[order].find(buddy);
+		if (it == freeByOrder[order].end()) {
+			break;
+		}
+		freeByOrder[order].erase(it);
+		offset = std::min(offset, buddy);
+		++order;
+	}
+	freeByOrder[order].insert(offset);
+}
+
+namespace {
+uint32_t spread2(uint32_t v)
+{
+	v &= 0xffffu;
+	v = (v | (v << 8)) & 0x00ff00ffu;
+	v = (v | (v << 4)) & 0x0f0f0f0fu;
+	v = (v | (v << 2)) & 0x33333333u;
+	v = (v | (v << 1)) & 0x55555555u;
+	return v;
+}
+
+// 22-bit key of a sensor-local ray direction: the direction folded onto the octahedron, 11 bits per
+// coordinate, interleaved. Neighbouring keys are neighbouring directions.
+uint32_t octahedralKey(const rgl::Mat34& m)
+{
+	float x = m.m[0][2], y = m.m[1][2], z = m.m[2][2];
+	const float l1 = std::fabs(x) + std::fabs(y) + std::fabs(z);
+	float u = l1 > 0.0f ? x / l1 : 0.0f, v = l1 > 0.0f ? y / l1 : 0.0f;
+	if (z < 0.0f) {
+		const float fu = (1.0f - std::fabs(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+		const float fv = (1.0f - std::fabs(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+		u = fu;
+		v = fv;
+	}
+	auto q = [](float c) { return (uint32_t) std::min(2047.0f, std::max(0.0f, (c * 0.5f + 0.5f) * 2048.0f)); };
+	return (spread2(q(u)) << 1) | spread2(q(v));
+}
+} // namespace
 
 int32_t Server::addPattern(const void* rays, int32_t count)
 {
 	auto p = std::make_unique<Pattern>();
 	RGL_CHECK_CUDA(cudaMemcpy(p->rays.ensure(sizeof(rgl::Mat34) * (size_t) count), rays, sizeof(rgl::Mat34) * (size_t) count,
+	                          cudaMemcpyHostToDevice));
+	// Visiting order: a warp casts 32 beams; sorted by direction, they form a compact patch of the
+	// pattern instead of, e.g., one column of channels. Results stay in beam order.
+	const auto* mats = static_cast<const rgl::Mat34*>(rays);
+	std::vector<uint32_t> key(count), order(count);
+	for (int32_t i = 0; i < count; ++i) {
+		key[i] = octahedralKey(mats[i]);
+		order[i] = (uint32_t) i;
+	}
+	std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+	RGL_CHECK_CUDA(cudaMemcpy(p->order.ensure(sizeof(uint32_t) * (size_t) count), order.data(), sizeof(uint32_t) * (size_t) count,
 	                          cudaMemcpyHostToDevice));
 	p->count = count;
 	std::lock_guard<std::mutex> g(m);
@@ -98,6 +174,10 @@ int64_t Server::submit(std::shared_ptr<Scene> scene, int32_t pattern, const rgl:
 	if (r->reservedBytes > budget) {
 		throw rgl::InvalidAPIArgument(
 		    format("request needs %lld bytes, more than the server's HBM budget of %lld", (long long) r->reservedBytes, (long long) budget));
+	}
+	if ((size_t) (r->points * kOutBytesPerPoint) > (Arena::kMinBlock << arena.maxOrder)) {
+		throw rgl::InvalidAPIArgument(format("request results need %lld bytes, more than the server's result arena of %lld",
+		                                     (long long) (r->points * kOutBytesPerPoint), (long long) (Arena::kMinBlock << arena.maxOrder)));
 	}
 	r->submitted = Clock::now();
 	const int64_t id = r->id;
@@ -216,8 +296,8 @@ void Server::release(int64_t id)
 		lk.lock();
 	}
 	Request& q = get(id);
-	if (q.hostOut) {
-		giveHostBlock(HostBlock{q.hostOut, q.devOut}, q.outClass); // the GPU finished writing it
+	if (q.outOrder >= 0) {
+		arena.give(q.outOffset, q.outOrder); // the GPU finished writing it
 	}
 	reserved -= q.points * kOutBytesPerPoint;
 	requests.erase(id);
@@ -291,7 +371,7 @@ void Server::launch(Slot& slot)
 		b.p.out.isHit = flags + pointBase;
 		b.p.out.entityId = ent + pointBase;
 		b.samples = nullptr; // one sample per beam: never read
-		b.order = nullptr;
+		b.order = patterns[r.pattern]->order.as<uint32_t>();
 		b.groupSize = 1;
 		b.hasRayTransform = 1;
 		b.rayTransform = r.pose;
@@ -320,6 +400,7 @@ void Server::launch(Slot& slot)
 
 	auto* dTileCounts = slot.tileCounts.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
 	auto* dTileOffsets = slot.tileOffsets.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.t0, stream));
 	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, stream));
 	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, stream));
 	rgl::launchTraceBatch(reinterpret_cast<const rgl::BatchJob*>(dBase), reinterpret_cast<const int32_t*>(dBase + offTask), n, 1, false,
@@ -328,6 +409,7 @@ void Server::launch(Slot& slot)
 	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, stream);
 	auto* hResults = static_cast<int32_t*>(slot.hResults.ensure(sizeof(int32_t) * 2 * n));
 	RGL_CHECK_CUDA(cudaMemcpyAsync(hResults, dResults, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.t1, stream));
 	RGL_CHECK_CUDA(cudaEventRecord(slot.done, stream));
 	RGL_CHECK_CUDA(cudaLaunchHostFunc(stream, &Server::batchDone, this));
 }
@@ -350,7 +432,10 @@ void Server::retire(Slot& slot)
 	const auto* hCounts = static_cast<const int32_t*>(slot.hResults.get());
 	const size_t n = slot.reqs.size();
 	const auto now = Clock::now();
+	float ms = 0.0f;
+	cudaEventElapsedTime(&ms, slot.t0, slot.t1);
 	std::lock_guard<std::mutex> g(m);
+	st.deviceSeconds += ms * 1e-3;
 	for (size_t j = 0; j < n; ++j) {
 		Request& r = *slot.reqs[j];
 		const bool failed = hCounts[n + j] != 0;
@@ -409,6 +494,11 @@ void Server::loop()
 				if (reserved + r->reservedBytes > budget || (!batch.empty() && beams + r->beams > maxBatchBeams)) {
 					break;
 				}
+				if (!arena.take((size_t) std::max<int64_t>(r->points * kOutBytesPerPoint, 1), r->outOffset, r->outOrder)) {
+					break; // the result arena is full until clients release results
+				}
+				r->hostOut = reinterpret_cast<float*>(arena.host + r->outOffset);
+				r->devOut = reinterpret_cast<float*>(arena.dev + r->outOffset);
 				pending.pop_front();
 				reserved += r->reservedBytes;
 				st.peakReserved = std::max(st.peakReserved, reserved);
@@ -418,6 +508,9 @@ void Server::loop()
 				batch.push_back(r);
 			}
 			if (!batch.empty()) {
+				// Jobs of one scene next to each other: warps take tasks in job order, so the device
+				// works on few scenes at a time (L2 locality). Results do not depend on the order.
+				std::stable_sort(batch.begin(), batch.end(), [](const Request* a, const Request* b) { return a->scene.get() < b->scene.get(); });
 				freeSlot->busy = true;
 				freeSlot->reqs = batch;
 				inFlight.push_back(freeSlot);
@@ -433,11 +526,7 @@ void Server::loop()
 							r->scene->prepare(stream);
 							prepared.push_back(r->scene.get());
 						}
-						if (r->hostOut == nullptr) {
-							const HostBlock hb = takeHostBlock((size_t) r->points * kOutBytesPerPoint, r->outClass);
-							r->hostOut = static_cast<float*>(hb.host);
-							r->devOut = static_cast<float*>(hb.dev);
-						}
+
 					}
 					launch(*freeSlot);
 				}

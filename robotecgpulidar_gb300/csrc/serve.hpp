@@ -25,6 +25,7 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -66,6 +67,7 @@ struct Server
 	{
 		int64_t submitted = 0, completed = 0, failed = 0, batches = 0, jobsInBatches = 0, peakReserved = 0, reserved = 0, inFlight = 0,
 		        pending = 0;
+		double deviceSeconds = 0.0; // summed device time of the batches (they may overlap)
 	};
 	Stats stats();
 
@@ -87,11 +89,12 @@ private:
 		float minRange, maxRange;
 		int64_t beams, points;
 		int64_t reservedBytes;
-		// Result block in pinned host memory mapped for the device: xyz | distance | entity id, `points`
+		// Result block in the pinned arena, mapped for the device: xyz | distance | entity id, `points`
 		// capacity each. The compaction writes it directly; no copy follows.
 		float* hostOut = nullptr;
 		float* devOut = nullptr; // the device address of hostOut
-		size_t outClass = 0;
+		size_t outOffset = 0;
+		int outOrder = -1;
 		int32_t count = 0;
 		State state = State::Pending;
 		std::string error; // why a failed request failed
@@ -100,6 +103,7 @@ private:
 	struct Pattern
 	{
 		rgl::DeviceBuffer rays{false};
+		rgl::DeviceBuffer order{false}; // beams sorted by octahedral direction: warps get compact patches
 		int32_t count = 0;
 	};
 	// One in-flight batch slot: device and pinned buffers reused by every batch launched from it.
@@ -109,6 +113,7 @@ private:
 	{
 		std::vector<Request*> reqs;
 		cudaEvent_t done = nullptr;
+		cudaEvent_t t0 = nullptr, t1 = nullptr; // device time of the batch
 		rgl::DeviceBuffer tables{false}, tileCounts{false}, tileOffsets{false}, results{false}, counter{false};
 		rgl::DeviceBuffer rawFlags{false}, rawXyz{false}, rawDist{false}, rawEnt{false};
 		rgl::PinnedBuffer hTables, hResults;
@@ -118,16 +123,20 @@ private:
 	static constexpr int64_t kRawBytesPerPoint = 4 + 12 + 4 + 4; // flags, xyz, distance, entity id
 	static constexpr int64_t kOutBytesPerPoint = 12 + 4 + 4;
 
-	// Pinned, device-mapped host blocks in power-of-two size classes, reused across requests.
-	struct HostBlock
+	// Result arena: one pinned, device-mapped host allocation made with the server, handed out by a
+	// buddy allocator (blocks of 64 KB << order, coalesced on release). Guarded by m.
+	struct Arena
 	{
-		void* host;
-		void* dev;
+		uint8_t* host = nullptr;
+		uint8_t* dev = nullptr;
+		int maxOrder = 0;
+		std::vector<std::set<size_t>> freeByOrder; // block offsets
+		static constexpr size_t kMinBlock = 64 << 10;
+		static int orderFor(size_t bytes);
+		bool take(size_t bytes, size_t& offset, int& order);
+		void give(size_t offset, int order);
 	};
-	HostBlock takeHostBlock(size_t bytes, size_t& cls);
-	void giveHostBlock(const HostBlock& b, size_t cls);
-	std::unordered_map<size_t, std::vector<HostBlock>> freeBlocks; // guarded by m
-	std::vector<void*> allBlocks;
+	Arena arena;
 
 	void loop();
 	void launch(Slot& slot);

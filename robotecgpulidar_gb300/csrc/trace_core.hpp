@@ -95,13 +95,6 @@ RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& 
 	return true;
 }
 
-struct BoxRay
-{
-	Vec3 o;
-	Vec3 inv;
-	bool negx, negy, negz;
-};
-
 RGL_HD float safeInv(float d)
 {
 	const float tiny = 1e-30f;
@@ -109,32 +102,6 @@ RGL_HD float safeInv(float d)
 		d = d < 0.0f ? -tiny : tiny;
 	}
 	return 1.0f / d;
-}
-
-RGL_HD BoxRay makeBoxRay(Vec3 o, Vec3 d)
-{
-	BoxRay r;
-	r.o = o;
-	r.inv = {safeInv(d.x), safeInv(d.y), safeInv(d.z)};
-	r.negx = r.inv.x < 0.0f;
-	r.negy = r.inv.y < 0.0f;
-	r.negz = r.inv.z < 0.0f;
-	return r;
-}
-
-// Conservative slack on the exit distance of a slab test: covers the three roundings of
-// (plane - o) * inv (Ize, "Robust BVH Ray Traversal", JCGT 2013).
-constexpr float kSlabSlack = 1.0000004f;
-
-// Slab test of a float box; returns entry distance or -1 when the box is missed within [0, tBest].
-RGL_HD float slabEnter(const BoxRay& r, float lox, float loy, float loz, float hix, float hiy, float hiz, float tBest)
-{
-	float nx = r.negx ? hix : lox, fx = r.negx ? lox : hix;
-	float ny = r.negy ? hiy : loy, fy = r.negy ? loy : hiy;
-	float nz = r.negz ? hiz : loz, fz = r.negz ? loz : hiz;
-	float t0 = maxf_(maxf_((nx - r.o.x) * r.inv.x, (ny - r.o.y) * r.inv.y), maxf_((nz - r.o.z) * r.inv.z, 0.0f));
-	float t1 = minf_(minf_((fx - r.o.x) * r.inv.x, (fy - r.o.y) * r.inv.y), minf_((fz - r.o.z) * r.inv.z, tBest));
-	return (t0 <= t1 * kSlabSlack) ? t0 : -1.0f;
 }
 
 RGL_HD float exp2Byte(uint8_t e)
@@ -150,18 +117,6 @@ RGL_HD float exp2Byte(uint8_t e)
 	return f;
 }
 
-// Dequantised box of child slot i of a wide node (same float expression the builder verified).
-RGL_HD void childBox(const WideNode& n, int i, float& lox, float& loy, float& loz, float& hix, float& hiy, float& hiz)
-{
-	float sx = exp2Byte(n.ex), sy = exp2Byte(n.ey), sz = exp2Byte(n.ez);
-	lox = fadd(n.px, (float) n.qlox[i] * sx);
-	loy = fadd(n.py, (float) n.qloy[i] * sy);
-	loz = fadd(n.pz, (float) n.qloz[i] * sz);
-	hix = fadd(n.px, (float) n.qhix[i] * sx);
-	hiy = fadd(n.py, (float) n.qhiy[i] * sy);
-	hiz = fadd(n.pz, (float) n.qhiz[i] * sz);
-}
-
 RGL_HD int popc8(uint32_t x)
 {
 #if defined(__CUDA_ARCH__)
@@ -173,10 +128,15 @@ RGL_HD int popc8(uint32_t x)
 
 // ---------------------------------------------------------------- wide-node traversal
 //
-// Stack entries are two 32-bit words. BLAS entries are node groups (after Ylitie et al., HPG 2017):
-// (childBase, imask | remaining-hits << 8), where bit j of the hits selects slot j ^ octant. TLAS
-// entries are (node or ~instance, entry distance bits). `Stack` provides push(a, b), pop(a&, b&),
-// size().
+// One loop walks both levels: the TLAS and every BLAS are 8-wide nodes of the same format, so lanes
+// of a warp at different levels execute the same node-visit code. Stack entries are two 32-bit words
+// (after Ylitie et al., HPG 2017), told apart by the second word:
+//   node group      (childBase, imask | remaining-hits << 8), remaining hits != 0, so >= 256;
+//                   bit j of the hits selects slot j ^ octant of the frame the group was pushed in;
+//   enter instance  (instance index, kEnterInstance): transform the ray into the instance's frame;
+//   leave instance  (0, kLeaveInstance): back to the world frame.
+// Entries pushed inside an instance sit above its leave entry, so each group is popped in the frame
+// it was pushed in. `Stack` provides push(a, b), pop(a&, b&), size().
 
 // Slab test of a dequantised child box in the FMA form t = q * (s * inv) + (p - o) * inv. The computed
 // t differs from the exact plane distance by at most 4u|t| + 3u * 255 * s * |inv| (u = 2^-24), plus
@@ -265,25 +225,62 @@ RGL_HD float min4(float a, float b, float c, float d)
 #endif
 }
 
-template<class Stack, class NodeLoader>
-RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 d, Stack& st, HitRec& best,
-                         const NodeLoader& load)
+constexpr uint32_t kLeaveInstance = 0u;
+constexpr uint32_t kEnterInstance = 1u;
+
+RGL_HD uint32_t highestBit(uint32_t x)
 {
-	const Watertight wt = setupWatertight(d);
-	const Vec3 inv = {safeInv(d.x), safeInv(d.y), safeInv(d.z)};
-	const bool negx = inv.x < 0.0f, negy = inv.y < 0.0f, negz = inv.z < 0.0f;
-	const uint32_t oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);
+#if defined(__CUDA_ARCH__)
+	return (uint32_t) (31 - __clz((int) x));
+#else
+	return (uint32_t) (31 - __builtin_clz(x));
+#endif
+}
+
+// A ray in the frame being traversed: origin, direction, inverse direction and its octant.
+struct FrameRay
+{
+	Vec3 o, d, inv;
+	uint32_t oct;
+};
+
+RGL_HD FrameRay frameRay(Vec3 o, Vec3 d)
+{
+	FrameRay r;
+	r.o = o;
+	r.d = d;
+	r.inv = {safeInv(d.x), safeInv(d.y), safeInv(d.z)};
+	r.oct = (r.inv.x < 0.0f ? 1u : 0u) | (r.inv.y < 0.0f ? 2u : 0u) | (r.inv.z < 0.0f ? 4u : 0u);
+	return r;
+}
+
+// Closest hit over all instances for a world-space ray o + t d, t in (0, tmax].
+template<class Stack, class NodeLoader>
+RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, Stack& st, const NodeLoader& load)
+{
+	HitRec best;
+	best.t = tmax; // hits with t == tmax are accepted
+	best.inst = -1;
+	best.tri = -1;
+	if (sc.nInstances <= 0) {
+		return best;
+	}
 	const int base = st.size();
+	FrameRay r = frameRay(oW, dW);
+	Watertight wt = setupWatertight(dW); // valid inside an instance
+	const WideNode* nodes = sc.tlas;
+	const TriRecord* leaves = sc.tlasLeaves;
+	int32_t inst = -1; // -1: the TLAS (world frame)
 	uint32_t node = 0;
 	for (;;) {
 		uint4 w0, w1, w2, w3, w4;
-		load.nodeWords(inst.nodes, node, w0, w1, w2, w3, w4);
+		load.nodeWords(nodes, node, w0, w1, w2, w3, w4);
 		const float sx = exp2Byte((uint8_t) (w0.w & 0xffu)), sy = exp2Byte((uint8_t) ((w0.w >> 8) & 0xffu)),
 		            sz = exp2Byte((uint8_t) ((w0.w >> 16) & 0xffu));
 		const uint32_t imask = w0.w >> 24;
 		const uint32_t childBase = w1.x, triBase = w1.y;
-		const float Ax = sx * inv.x, Ay = sy * inv.y, Az = sz * inv.z;
-		const float Cx = (asFloat(w0.x) - o.x) * inv.x, Cy = (asFloat(w0.y) - o.y) * inv.y, Cz = (asFloat(w0.z) - o.z) * inv.z;
+		const float Ax = sx * r.inv.x, Ay = sy * r.inv.y, Az = sz * r.inv.z;
+		const float Cx = (asFloat(w0.x) - r.o.x) * r.inv.x, Cy = (asFloat(w0.y) - r.o.y) * r.inv.y, Cz = (asFloat(w0.z) - r.o.z) * r.inv.z;
 		// Plane distance q * A + C evaluated as fma(1 + q * 2^-15, 2^15 * A, C - 2^15 * A): 2^15 * A is
 		// exact and the product term is exact, so the only extra rounding is that of C - 2^15 * A,
 		// at most u|C| + 2^-9 |A|. With |C| <= |t| + 255 |A|, the relative slack (5u of 8.4u used) and
@@ -291,6 +288,7 @@ RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 
 		const float Sx = 32768.0f * Ax, Sy = 32768.0f * Ay, Sz = 32768.0f * Az;
 		const float Dx = Cx - Sx, Dy = Cy - Sy, Dz = Cz - Sz;
 		// near/far quantised planes per axis (packed bytes), swapped for negative directions
+		const bool negx = (r.oct & 1u) != 0, negy = (r.oct & 2u) != 0, negz = (r.oct & 4u) != 0;
 		const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y, fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
 		const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w, fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
 		const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y, fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
@@ -309,108 +307,79 @@ RGL_HD void traverseBlas(const InstanceRec& inst, int32_t instIdx, Vec3 o, Vec3 
 			hitSlots |= (tEntry <= tExit * kSlabRelSlack) ? (1u << s) : 0u;
 		}
 		// Internal and leaf hits in traversal order j (slot = j ^ oct): one permutation for both.
-		const uint32_t ordered = octantPermute((hitSlots & imask) | ((hitSlots & ~imask & 0xffu) << 8), oct);
+		const uint32_t ordered = octantPermute((hitSlots & imask) | ((hitSlots & ~imask & 0xffu) << 8), r.oct);
 		uint32_t internalHits = ordered & 0xffu, leafHits = ordered >> 8;
-		// Triangles of hit leaf children, in ray order.
 		const uint32_t metaLo = w1.z, metaHi = w1.w;
-		while (leafHits) {
-			const uint32_t s = lowestBit(leafHits) ^ oct;
-			leafHits &= leafHits - 1u;
-			const uint32_t meta = ((s < 4 ? metaLo : metaHi) >> ((s & 3) * 8)) & 0xffu;
-			const int first = (int) triBase + (int) (meta & 31u);
-			const int cnt = (int) (meta >> 5);
-			for (int k = 0; k < cnt; ++k) {
-				TriRecord tr = load.tri(inst.tris, first + k);
-				float t;
-				if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), o, wt,
-				                      best.t, t)) {
-					best.t = t;
-					best.inst = instIdx;
-					best.tri = first + k;
+		if (inst < 0) {
+			// TLAS leaves are instances (one per leaf child): queued, the nearest on top.
+			while (leafHits) {
+				const uint32_t j = highestBit(leafHits);
+				leafHits &= ~(1u << j);
+				const uint32_t s = j ^ r.oct;
+				const uint32_t meta = ((s < 4 ? metaLo : metaHi) >> ((s & 3) * 8)) & 0xffu;
+				st.push((uint32_t) load.leafPrim(leaves, (int) triBase + (int) (meta & 31u)), kEnterInstance);
+			}
+		} else {
+			// BLAS leaves: their triangles now, in ray order.
+			while (leafHits) {
+				const uint32_t s = lowestBit(leafHits) ^ r.oct;
+				leafHits &= leafHits - 1u;
+				const uint32_t meta = ((s < 4 ? metaLo : metaHi) >> ((s & 3) * 8)) & 0xffu;
+				const int first = (int) triBase + (int) (meta & 31u);
+				const int cnt = (int) (meta >> 5);
+				for (int k = 0; k < cnt; ++k) {
+					TriRecord tr = load.tri(leaves, first + k);
+					float t;
+					if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), r.o, wt,
+					                      best.t, t)) {
+						best.t = t;
+						best.inst = inst;
+						best.tri = first + k;
+					}
 				}
 			}
 		}
 		uint32_t groupBase = childBase, groupMask = imask, hits = internalHits;
-		if (hits == 0) {
+		bool enterRoot = false;
+		while (hits == 0) {
 			if (st.size() == base) {
-				break;
+				return best;
 			}
-			uint32_t b;
-			st.pop(groupBase, b);
-			groupMask = b & 0xffu;
-			hits = b >> 8;
+			uint32_t a, b;
+			st.pop(a, b);
+			if (b == kLeaveInstance) {
+				r = frameRay(oW, dW);
+				nodes = sc.tlas;
+				leaves = sc.tlasLeaves;
+				inst = -1;
+			} else if (b == kEnterInstance) {
+				const InstanceRec& ir = load.instance(sc.instances, (int32_t) a);
+				st.push(0u, kLeaveInstance);
+				const Vec3 od = ir.worldToObject.vector(dW);
+				r = frameRay(ir.worldToObject.point(oW), od);
+				wt = setupWatertight(od);
+				nodes = ir.nodes;
+				leaves = ir.tris;
+				inst = (int32_t) a;
+				enterRoot = true;
+				break;
+			} else {
+				groupBase = a;
+				groupMask = b & 0xffu;
+				hits = b >> 8;
+			}
 		}
-		const uint32_t s = lowestBit(hits) ^ oct;
+		if (enterRoot) {
+			node = 0;
+			continue;
+		}
+		const uint32_t s = lowestBit(hits) ^ r.oct;
 		hits &= hits - 1u;
 		if (hits) {
 			st.push(groupBase, groupMask | (hits << 8));
 		}
 		node = groupBase + (uint32_t) popc8(groupMask & ((1u << s) - 1u));
 	}
-}
-
-// Closest hit over all instances for a world-space ray o + t d, t in (0, tmax].
-template<class Stack, class NodeLoader>
-RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 o, Vec3 d, float tmax, Stack& st, const NodeLoader& load)
-{
-	HitRec best;
-	best.t = tmax; // hits with t == tmax are accepted
-	best.inst = -1;
-	best.tri = -1;
-	if (sc.nInstances <= 0) {
-		return best;
-	}
-	const BoxRay br = makeBoxRay(o, d);
-	const int base = st.size();
-	// TLAS entries: (value >= 0 internal node | value < 0 instance ~value, entry distance bits).
-	st.push((uint32_t) (sc.nInstances == 1 ? ~0 : 0), 0u);
-	while (st.size() > base) {
-		uint32_t ev, tb;
-		st.pop(ev, tb);
-		const int32_t e = (int32_t) ev;
-		if (asFloat(tb) > best.t) {
-			continue;
-		}
-		if (e < 0) {
-			const int32_t ii = ~e;
-			const InstanceRec& inst = load.instance(sc.instances, ii);
-			traverseBlas(inst, ii, inst.worldToObject.point(o), inst.worldToObject.vector(d), st, best, load);
-			continue;
-		}
-		const BinNode bn = load.bin(sc.tlas, e);
-		const int32_t ch[2] = {bn.left, bn.right};
-		float te[2];
-		for (int k = 0; k < 2; ++k) {
-			const int32_t c = ch[k];
-			float lx, ly, lz, hx, hy, hz;
-			if (c >= 0) {
-				const BinNode cn = load.bin(sc.tlas, c);
-				lx = cn.lox;
-				ly = cn.loy;
-				lz = cn.loz;
-				hx = cn.hix;
-				hy = cn.hiy;
-				hz = cn.hiz;
-			} else {
-				const InstanceRec& ci = load.instance(sc.instances, ~c);
-				lx = ci.lox;
-				ly = ci.loy;
-				lz = ci.loz;
-				hx = ci.hix;
-				hy = ci.hiy;
-				hz = ci.hiz;
-			}
-			te[k] = slabEnter(br, lx, ly, lz, hx, hy, hz, best.t);
-		}
-		const int farK = (te[0] >= 0.0f && te[1] >= 0.0f && te[1] < te[0]) ? 0 : 1;
-		for (int q = 0; q < 2; ++q) {
-			const int k = (q == 0) ? farK : 1 - farK;
-			if (te[k] >= 0.0f) {
-				st.push((uint32_t) ch[k], asUint(te[k]));
-			}
-		}
-	}
-	return best;
 }
 
 } // namespace rgl

@@ -1,6 +1,5 @@
-// Device pieces shared by the single-sensor traversal kernel (trace.cu) and the batched
-// multi-sensor kernel (trace_batch.cu): the traversal stack, the loaders, one traced sample, the
-// in-order return selection and the per-point field writes.
+// Device pieces of the persistent traversal kernel (trace_batch.cu): the traversal stack, the
+// loaders, one traced sample, the in-order return selection and the per-point field writes.
 //
 // Return selection restates reference src/gpu/nodeKernels.cu:334-422 (kReduceDivergentBeams) with
 // its quirks:
@@ -88,21 +87,8 @@ struct DevLoader
 		return t;
 	}
 	__device__ __forceinline__ const InstanceRec& instance(const InstanceRec* base, int32_t i) const { return base[i]; }
-	__device__ __forceinline__ BinNode bin(const BinNode* base, int32_t i) const
-	{
-		const float4* p = reinterpret_cast<const float4*>(base + i);
-		const float4 a = __ldg(p), b = __ldg(p + 1);
-		BinNode n;
-		n.lox = a.x;
-		n.loy = a.y;
-		n.loz = a.z;
-		n.left = __float_as_int(a.w);
-		n.hix = b.x;
-		n.hiy = b.y;
-		n.hiz = b.z;
-		n.right = __float_as_int(b.w);
-		return n;
-	}
+	// primId of a leaf record (a TLAS leaf's instance index).
+	__device__ __forceinline__ int32_t leafPrim(const TriRecord* base, int32_t i) const { return __ldg(&base[i].primId); }
 };
 
 // One traced sample. For non-hits `dist` holds the non-hit distance (near or far).

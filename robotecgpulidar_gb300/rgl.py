@@ -209,7 +209,7 @@ def _proto(l):
         "rgl_gb300_server_get_result_host": [vp, C.c_int64, i32, P(vp), P(i32)],
         "rgl_gb300_server_release": [vp, C.c_int64],
         "rgl_gb300_server_drain": [vp],
-        "rgl_gb300_server_get_stats": [vp, P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)],
+        "rgl_gb300_server_get_stats": [vp] + [P(C.c_int64)] * 7,
     }
     for name, args in sigs.items():
         fn = getattr(l, name)
@@ -551,7 +551,7 @@ class Server:
         check(lib().rgl_gb300_server_drain(self.h))
 
     def stats(self) -> dict:
-        v = [C.c_int64() for _ in range(6)]
+        v = [C.c_int64() for _ in range(7)]
         check(lib().rgl_gb300_server_get_stats(self.h, *[C.byref(x) for x in v]))
-        return dict(zip(["submitted", "completed", "failed", "batches", "requests_in_batches", "peak_reserved_bytes"],
+        return dict(zip(["submitted", "completed", "failed", "batches", "requests_in_batches", "peak_reserved_bytes", "device_us"],
                         [x.value for x in v]))

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "bvh_core.hpp"
+#include "tlas_sah.hpp"
 #include "trace_core.hpp"
 
 using namespace rgl;
@@ -71,18 +72,14 @@ void bottomUp(std::vector<BinNode>& bin, const std::vector<int32_t>& parentInt, 
 	}
 }
 
-Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
+// Wide BVH over primitive boxes lo/hi, as the device builder makes it (bvh.cu buildWide): leaf records
+// are triangles (v/idx given) or primitive indices (v null, the TLAS).
+Blas buildWideHost(std::vector<float4> lo, std::vector<float4> hi, const float* v, const int32_t* idx, int leafMax)
 {
-	(void) nv;
-	std::vector<float4> lo(nt), hi(nt);
+	const int nt = (int) lo.size();
 	Box cb = emptyBox();
 	std::vector<float> cx(nt), cy(nt), cz(nt);
 	for (int t = 0; t < nt; ++t) {
-		const float* a = v + 3 * idx[3 * t];
-		const float* b = v + 3 * idx[3 * t + 1];
-		const float* c = v + 3 * idx[3 * t + 2];
-		lo[t] = make_float4(std::min({a[0], b[0], c[0]}), std::min({a[1], b[1], c[1]}), std::min({a[2], b[2], c[2]}), 0);
-		hi[t] = make_float4(std::max({a[0], b[0], c[0]}), std::max({a[1], b[1], c[1]}), std::max({a[2], b[2], c[2]}), 0);
 		cx[t] = 0.5f * (lo[t].x + hi[t].x);
 		cy[t] = 0.5f * (lo[t].y + hi[t].y);
 		cz[t] = 0.5f * (lo[t].z + hi[t].z);
@@ -115,10 +112,10 @@ Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
 	std::vector<int2> qa(std::max(1, nt)), qb(std::max(1, nt));
 	uint32_t qaCount = 1, qbCount = 0;
 	qa[0] = make_int2(nt == 1 ? ~0 : 0, 0);
-	CollapseInputs in{bin.data(), rf.data(), rl.data(), ids.data(), lo.data(), hi.data(), v, idx};
+	CollapseInputs in{bin.data(), rf.data(), rl.data(), ids.data(), lo.data(), hi.data(), v, idx, leafMax};
 	while (qaCount > 0) {
 		qbCount = 0;
-		CollapseOutputs o{out.wide.data(), out.tris.data(), &wideCounter, &triCounter, qb.data(), &qbCount};
+		CollapseOutputs o{out.wide.data(), out.tris.data(), &wideCounter, &triCounter, qb.data(), &qbCount, nullptr};
 		for (uint32_t i = 0; i < qaCount; ++i)
 			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
 		std::swap(qa, qb);
@@ -127,6 +124,51 @@ Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
 	out.wide.resize(wideCounter);
 	out.bounds = nt == 1 ? leafBox[0] : binBox(bin[0]);
 	return out;
+}
+
+// Wide TLAS from a host SAH topology (tlas_sah.hpp), collapsed like the device build.
+Blas buildTlasSah(const std::vector<float4>& lo, const std::vector<float4>& hi)
+{
+	const int n = (int) lo.size();
+	std::vector<Box> boxes(n);
+	for (int i = 0; i < n; ++i) {
+		boxes[i] = Box{lo[i].x, lo[i].y, lo[i].z, hi[i].x, hi[i].y, hi[i].z};
+	}
+	SahTree t = buildSahTree(boxes);
+	Blas out;
+	out.wide.resize(std::max(1, n));
+	out.tris.resize(n);
+	uint32_t wideCounter = 1, triCounter = 0;
+	std::vector<int2> qa(std::max(1, n)), qb(std::max(1, n));
+	uint32_t qaCount = 1, qbCount = 0;
+	qa[0] = make_int2(n == 1 ? ~0 : 0, 0);
+	CollapseInputs in{t.bin.data(), t.rangeFirst.data(), t.rangeLast.data(), t.sortedIds.data(), lo.data(), hi.data(), nullptr, nullptr, 1};
+	while (qaCount > 0) {
+		qbCount = 0;
+		CollapseOutputs o{out.wide.data(), out.tris.data(), &wideCounter, &triCounter, qb.data(), &qbCount, nullptr};
+		for (uint32_t i = 0; i < qaCount; ++i)
+			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
+		std::swap(qa, qb);
+		qaCount = qbCount;
+	}
+	out.wide.resize(wideCounter);
+	return out;
+}
+
+int gTlasSah = 1; // the product builds the TLAS topology by SAH (tlas_sah.hpp)
+
+Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
+{
+	(void) nv;
+	std::vector<float4> lo(nt), hi(nt);
+	for (int t = 0; t < nt; ++t) {
+		const float* a = v + 3 * idx[3 * t];
+		const float* b = v + 3 * idx[3 * t + 1];
+		const float* c = v + 3 * idx[3 * t + 2];
+		lo[t] = make_float4(std::min({a[0], b[0], c[0]}), std::min({a[1], b[1], c[1]}), std::min({a[2], b[2], c[2]}), 0);
+		hi[t] = make_float4(std::max({a[0], b[0], c[0]}), std::max({a[1], b[1], c[1]}), std::max({a[2], b[2], c[2]}), 0);
+	}
+	return buildWideHost(lo, hi, v, idx, kLeafMaxTris);
 }
 
 struct HostStack
@@ -156,13 +198,15 @@ struct HostStack
 };
 
 int gNodeVisits = 0;
-long gTriTests = 0, gBinLoads = 0, gInstLoads = 0;
+long gTriTests = 0, gBinLoads = 0, gInstLoads = 0, gTlasVisits = 0;
+const WideNode* gTlasBase = nullptr;
 
 struct HostLoader
 {
 	void nodeWords(const WideNode* base, uint32_t i, uint4& w0, uint4& w1, uint4& w2, uint4& w3, uint4& w4) const
 	{
 		++gNodeVisits;
+		gTlasVisits += base == gTlasBase ? 1 : 0;
 		const uint4* p = reinterpret_cast<const uint4*>(base + i);
 		w0 = p[0];
 		w1 = p[1];
@@ -180,10 +224,10 @@ struct HostLoader
 		++gInstLoads;
 		return base[i];
 	}
-	BinNode bin(const BinNode* base, int32_t i) const
+	int32_t leafPrim(const TriRecord* base, int32_t i) const
 	{
 		++gBinLoads;
-		return base[i];
+		return base[i].primId;
 	}
 };
 
@@ -196,15 +240,19 @@ int gMaxNodeVisits = 0;
 long gTotalNodeVisits = 0;
 int gMaxStackDepth = 0;
 int harness_max_node_visits() { return gMaxNodeVisits; }
+// 1: build the TLAS topology with the host SAH builder instead of the Morton-ordered LBVH.
+void harness_set_tlas_sah(int on) { gTlasSah = on; }
 // Deepest traversal stack of a single ray in the last harness_cast call.
 int harness_max_stack_depth() { return gMaxStackDepth; }
 long harness_total_node_visits() { return gTotalNodeVisits; }
-// Totals of the last harness_cast call: triangle tests, TLAS node loads, instance record loads.
+// Totals of the last harness_cast call: triangle tests, TLAS leaf reads, instance entries, TLAS
+// node visits.
 void harness_work_counters(long* out)
 {
 	out[0] = gTriTests;
 	out[1] = gBinLoads;
 	out[2] = gInstLoads;
+	out[3] = gTlasVisits;
 }
 
 // Builds BLASes for `nMeshes` meshes and a TLAS over `nInst` instances, then casts `nRays` world
@@ -247,35 +295,20 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 		float c3[3] = {0.5f * (w.lox + w.hix), 0.5f * (w.loy + w.hiy), 0.5f * (w.loz + w.hiz)};
 		cb = unite(cb, Box{c3[0], c3[1], c3[2], c3[0], c3[1], c3[2]});
 	}
-	std::vector<uint32_t> code(nInst);
-	std::vector<int32_t> ids(nInst);
+	std::vector<float4> ilo(nInst), ihi(nInst);
 	for (int i = 0; i < nInst; ++i) {
-		code[i] = morton30(0.5f * (ib[i].lox + ib[i].hix), 0.5f * (ib[i].loy + ib[i].hiy), 0.5f * (ib[i].loz + ib[i].hiz), cb);
-		ids[i] = i;
+		ilo[i] = make_float4(ib[i].lox, ib[i].loy, ib[i].loz, 0);
+		ihi[i] = make_float4(ib[i].hix, ib[i].hiy, ib[i].hiz, 0);
 	}
-	std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return code[a] < code[b]; });
-	std::vector<uint32_t> sc(nInst);
-	for (int k = 0; k < nInst; ++k)
-		sc[k] = code[ids[k]];
-	std::vector<BinNode> tlas;
-	std::vector<int32_t> rf, rl, pi, pl;
-	buildLbvh(sc, tlas, rf, rl, pi, pl);
-	std::vector<Box> leafBox(nInst);
-	for (int k = 0; k < nInst; ++k)
-		leafBox[k] = ib[ids[k]];
-	bottomUp(tlas, pi, pl, leafBox);
-	for (auto& n : tlas) { // leaves reference original instance indices
-		if (n.left < 0)
-			n.left = ~ids[~n.left];
-		if (n.right < 0)
-			n.right = ~ids[~n.right];
-	}
-	SceneView sv{tlas.data(), inst.data(), nInst, 0};
+	(void) cb;
+	Blas tlas = gTlasSah ? buildTlasSah(ilo, ihi) : buildWideHost(ilo, ihi, nullptr, nullptr, 1);
+	SceneView sv{tlas.wide.data(), tlas.tris.data(), inst.data(), nInst, 0};
+	gTlasBase = tlas.wide.data();
 	HostLoader ld;
 	bool overflow = false;
 	gMaxNodeVisits = 0;
 	gTotalNodeVisits = 0;
-	gTriTests = gBinLoads = gInstLoads = 0;
+	gTriTests = gBinLoads = gInstLoads = gTlasVisits = 0;
 	gMaxStackDepth = 0;
 	for (int r = 0; r < nRays; ++r) {
 		const float* p = rays + 7 * r;
