@@ -43,8 +43,9 @@ RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t*
 /*
  * Traversal schedule of graph runs (rgl_graph_run). Every raytrace runs on the persistent traversal
  * kernel of batched frames as a one-job launch; this sets its block size (64, 128, 256), packing
- * (0: a beam's sub-rays on adjacent lanes, 1: one lane per beam), tasks per fetch (1..64) and
- * register budget (64, 80, 96, 128). The default is 256, 0, 1, 80. Changes speed only, never results.
+ * (0: a beam's sub-rays on adjacent lanes, walking the scene together; 1: one lane per beam), tasks
+ * per fetch (1..64) and register budget (64, 80, 96, 128). The default is 256, 0, 1, 80. Changes speed
+ * only, never results.
  */
 RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs);
 
@@ -107,7 +108,8 @@ RGL_API rgl_status_t rgl_gb300_batch_destroy(rgl_gb300_batch_t batch);
  * candidates on the first frame of every new batch shape (per-graph ray and sample counts) and keeps
  * the fastest; otherwise the given schedule is used:
  *   block    threads per block: 64, 128 or 256
- *   packing  0: a beam's sub-rays on adjacent lanes; 1: one lane per beam, sub-rays in turn
+ *   packing  0: a beam's sub-rays on adjacent lanes, walking the scene together; 1: one lane per
+ *            beam, sub-rays in turn
  *   order    beam visiting order. 0: as given; 1: sorted by octahedral direction; 2: by Morton code
  *   chunk    tasks (one warp's beams each) taken per fetch from the shared work counter, 1..64
  *   regs     registers per thread: 64, 80, 96 or 128 (fewer registers, more resident warps)
@@ -190,6 +192,16 @@ RGL_API rgl_status_t rgl_gb300_server_get_request_timing(rgl_gb300_server_t serv
 RGL_API rgl_status_t rgl_gb300_server_release(rgl_gb300_server_t server, int64_t request);
 /* Waits until no request is pending or running. */
 RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server);
+
+/*
+ * Traversal schedule of the server's batches (block, order, chunk and regs as for
+ * rgl_gb300_batch_configure_schedule; order 0 casts a pattern's beams in the given order, 1 and 2 in
+ * its octahedral direction order) and the most beams coalesced into one batch (>= 1; a single larger
+ * request still forms a batch of its own). Applies to batches launched afterwards; changes speed only,
+ * never results. Defaults: 256, 1, 1, 80 and 32 Mi beams.
+ */
+RGL_API rgl_status_t rgl_gb300_server_configure_schedule(rgl_gb300_server_t server, int32_t block, int32_t order, int32_t chunk,
+                                                         int32_t regs, int64_t max_batch_beams);
 /* Counters: requests submitted, completed (including failed), failed; batches launched and the requests
  * they held; the largest admitted byte total; the summed device time of the batches in microseconds. */
 RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64_t* out_submitted, int64_t* out_completed,

@@ -225,3 +225,23 @@ def inv34(m34):
 
 def mul34(a, b):
     return (mat4(a) @ mat4(b))[:3, :]
+
+
+# ---------------------------------------------------------------- fields every return of a beam shares
+
+def beam_shared_fields(rays_world, sensor_to_world, return_count=1, ring_ids=None):
+    """Azimuth, elevation and ring id per return point (reference src/gpu/optixPrograms.cu:288-326,
+    src/math/Mat3x4f.hpp:146-175), in FP64: the sensor-frame pose is inverse(sensor_to_world) @ ray;
+    elevation = asin(m[1][2]) (clamped to +-pi/2 outside (-1, 1)), azimuth = atan2(-m[2][0], m[2][2])
+    (0 outside (-1, 1) of m[2][1]); beam b's ring id is ring_ids[b % len(ring_ids)] as uint16."""
+    rays = np.asarray(rays_world, dtype=np.float64).reshape(-1, 3, 4)
+    inv = inv34(sensor_to_world)
+    local = np.einsum("ij,njk->nik", inv[:, :3], rays[:, :, :3])
+    m12, m21 = local[:, 1, 2], local[:, 2, 1]
+    elev = np.where(m12 < 1.0, np.where(m12 > -1.0, np.arcsin(np.clip(m12, -1.0, 1.0)), -np.pi / 2), np.pi / 2)
+    az = np.where((m21 < 1.0) & (m21 > -1.0), np.arctan2(-local[:, 2, 0], local[:, 2, 2]), 0.0)
+    out = {"azimuth": np.repeat(az, return_count), "elevation": np.repeat(elev, return_count)}
+    if ring_ids is not None:
+        ids = np.asarray(ring_ids, dtype=np.int64)
+        out["ring_id"] = np.repeat(ids[np.arange(rays.shape[0]) % len(ids)].astype(np.uint16), return_count)
+    return out

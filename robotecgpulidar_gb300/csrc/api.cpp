@@ -19,9 +19,12 @@
 #include <rgl/api/extensions/tape.h>
 
 #include "batch.hpp"
+#include "tape.hpp"
 #include "serve.hpp"
 #include "graph.hpp"
 #include "scene.hpp"
+
+namespace T = rgl::tape;
 
 using namespace rgl;
 
@@ -93,6 +96,12 @@ rgl_status_t safeCall(Fn&& fn)
 	}
 	catch (InvalidAPIObject& e) {
 		return updateState(RGL_INVALID_API_OBJECT, std::string(e.what()));
+	}
+	catch (rgl::tape::RecordError& e) {
+		return updateState(RGL_TAPE_ERROR, std::string(e.what()));
+	}
+	catch (rgl::tape::InvalidFilePath& e) {
+		return updateState(RGL_INVALID_FILE_PATH, std::string(e.what()));
 	}
 	catch (InvalidPipeline& e) {
 		return updateState(RGL_INVALID_PIPELINE, std::string(e.what()));
@@ -220,6 +229,20 @@ void releaseGraph(const std::shared_ptr<Node>& node)
 	}
 }
 
+// Bytes of a points-from-array input, as the tape stores it (0 when the arguments are invalid).
+size_t tapePointBytes(const void* points, int32_t count, const rgl_field_t* fields, int32_t fieldCount)
+{
+	if (points == nullptr || fields == nullptr || count <= 0 || fieldCount <= 0) {
+		return 0;
+	}
+	try {
+		return (size_t) count * rgl::pointSize(std::vector<rgl_field_t>(fields, fields + fieldCount));
+	}
+	catch (std::exception&) {
+		return 0;
+	}
+}
+
 [[noreturn]] void notImplemented(const char* what)
 {
 	throw NotImplemented(format("%s is not implemented by this GB300 build", what));
@@ -238,7 +261,7 @@ uint64_t randomSeed()
 
 RGL_API rgl_status_t rgl_get_version_info(int32_t* out_major, int32_t* out_minor, int32_t* out_patch)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_major != nullptr);
 		CHECK_ARG(out_minor != nullptr);
 		CHECK_ARG(out_patch != nullptr);
@@ -246,23 +269,29 @@ RGL_API rgl_status_t rgl_get_version_info(int32_t* out_major, int32_t* out_minor
 		*out_minor = RGL_VERSION_MINOR;
 		*out_patch = RGL_VERSION_PATCH;
 	});
+	RGL_TAPE_RECORD(T::num(out_major ? *out_major : 0), T::num(out_minor ? *out_minor : 0), T::num(out_patch ? *out_patch : 0));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_get_extension_info(rgl_extension_t extension, int32_t* out_available)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(0 <= extension && extension < RGL_EXTENSION_COUNT);
 		CHECK_ARG(out_available != nullptr);
 		*out_available = 0; // PCL, ROS2, UDP and weather extensions are not part of this build
 	});
+	RGL_TAPE_RECORD(T::num(extension), T::num(out_available ? *out_available : 0));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_configure_logging(rgl_log_level_t log_level, const char* log_file_path, bool use_stdout)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(0 <= log_level && log_level <= 6);
 		logConfigure((int) log_level, log_file_path, use_stdout);
 	});
+	RGL_TAPE_RECORD(T::num(log_level), T::text(log_file_path), T::flag(use_stdout));
+	return status;
 }
 
 RGL_API void rgl_get_last_error_string(const char** out_error_string)
@@ -275,7 +304,7 @@ RGL_API void rgl_get_last_error_string(const char** out_error_string)
 
 RGL_API rgl_status_t rgl_cleanup(void)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		Batches::map().clear();
 		Servers::map().clear();
 		while (!Nodes::map().empty()) {
@@ -295,6 +324,8 @@ RGL_API rgl_status_t rgl_cleanup(void)
 		Meshes::map().clear();
 		Textures::map().clear();
 	});
+	RGL_TAPE_RECORD();
+	return status;
 }
 
 // ================================================================ mesh
@@ -302,7 +333,7 @@ RGL_API rgl_status_t rgl_cleanup(void)
 RGL_API rgl_status_t rgl_mesh_create(rgl_mesh_t* out_mesh, const rgl_vec3f* vertices, int32_t vertex_count,
                                      const rgl_vec3i* indices, int32_t index_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_mesh != nullptr);
 		CHECK_ARG(vertices != nullptr);
 		CHECK_ARG(vertex_count > 0);
@@ -311,16 +342,20 @@ RGL_API rgl_status_t rgl_mesh_create(rgl_mesh_t* out_mesh, const rgl_vec3f* vert
 		GraphRunCtx::synchronizeAll();
 		*out_mesh = Meshes::add(std::make_shared<Mesh>(vertices, vertex_count, indices, index_count));
 	});
+	RGL_TAPE_RECORD(T::handle(out_mesh ? *out_mesh : nullptr), T::arr(vertices, vertex_count), T::num(vertex_count), T::arr(indices, index_count), T::num(index_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_mesh_set_texture_coords(rgl_mesh_t mesh, const rgl_vec2f* uvs, int32_t uv_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(mesh != nullptr);
 		CHECK_ARG(uvs != nullptr);
 		CHECK_ARG(uv_count > 0);
 		notImplemented("rgl_mesh_set_texture_coords");
 	});
+	RGL_TAPE_RECORD(T::handle(mesh), T::arr(uvs, uv_count), T::num(uv_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_mesh_set_bone_weights(rgl_mesh_t mesh, const rgl_bone_weights_t* bone_weights, int32_t bone_weights_count)
@@ -345,26 +380,30 @@ RGL_API rgl_status_t rgl_mesh_set_restposes(rgl_mesh_t mesh, const rgl_mat3x4f* 
 
 RGL_API rgl_status_t rgl_mesh_destroy(rgl_mesh_t mesh)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(mesh != nullptr);
 		GraphRunCtx::synchronizeAll();
 		Meshes::release(mesh, "Mesh");
 	});
+	RGL_TAPE_RECORD(T::handle(mesh));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_mesh_is_alive(rgl_mesh_t mesh, bool* out_alive)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_alive != nullptr);
 		*out_alive = Meshes::contains(mesh);
 	});
+	RGL_TAPE_RECORD(T::handle(mesh), T::flag(out_alive && *out_alive));
+	return status;
 }
 
 // ================================================================ entity
 
 RGL_API rgl_status_t rgl_entity_create(rgl_entity_t* out_entity, rgl_scene_t scene, rgl_mesh_t mesh)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_entity != nullptr);
 		CHECK_ARG(mesh != nullptr);
 		GraphRunCtx::synchronizeAll();
@@ -374,27 +413,33 @@ RGL_API rgl_status_t rgl_entity_create(rgl_entity_t* out_entity, rgl_scene_t sce
 		sc->addEntity(e);
 		*out_entity = Entities::add(e);
 	});
+	RGL_TAPE_RECORD(T::handle(out_entity ? *out_entity : nullptr), T::handle(scene), T::handle(mesh));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_destroy(rgl_entity_t entity)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
 		GraphRunCtx::synchronizeAll();
 		auto e = Entities::get(entity, "Entity");
 		e->scene->removeEntity(e.get());
 		Entities::release(entity, "Entity");
 	});
+	RGL_TAPE_RECORD(T::handle(entity));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_set_transform(rgl_entity_t entity, const rgl_mat3x4f* transform)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
 		CHECK_ARG(transform != nullptr);
 		GraphRunCtx::synchronizeAll();
 		Entities::get(entity, "Entity")->setTransform(toMat(*transform));
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::arr(transform, 1));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_set_pose_world(rgl_entity_t entity, const rgl_mat3x4f* pose, int32_t bones_count)
@@ -409,12 +454,14 @@ RGL_API rgl_status_t rgl_entity_set_pose_world(rgl_entity_t entity, const rgl_ma
 
 RGL_API rgl_status_t rgl_entity_set_id(rgl_entity_t entity, int32_t id)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
 		CHECK_ARG(id != RGL_ENTITY_INVALID_ID);
 		GraphRunCtx::synchronizeAll();
 		Entities::get(entity, "Entity")->setId(id);
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::num(id));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_set_intensity_texture(rgl_entity_t entity, rgl_texture_t texture)
@@ -428,10 +475,13 @@ RGL_API rgl_status_t rgl_entity_set_intensity_texture(rgl_entity_t entity, rgl_t
 
 RGL_API rgl_status_t rgl_entity_set_laser_retro(rgl_entity_t entity, float retro)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
-		Entities::get(entity, "Entity")->laserRetro = retro;
+		GraphRunCtx::synchronizeAll();
+		Entities::get(entity, "Entity")->setLaserRetro(retro);
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::real(retro));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_apply_external_animation(rgl_entity_t entity, const rgl_vec3f* vertices, int32_t vertex_count)
@@ -446,10 +496,12 @@ RGL_API rgl_status_t rgl_entity_apply_external_animation(rgl_entity_t entity, co
 
 RGL_API rgl_status_t rgl_entity_is_alive(rgl_entity_t entity, bool* out_alive)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_alive != nullptr);
 		*out_alive = Entities::contains(entity);
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::flag(out_alive && *out_alive));
+	return status;
 }
 
 // ================================================================ texture
@@ -485,19 +537,21 @@ RGL_API rgl_status_t rgl_texture_is_alive(rgl_texture_t texture, bool* out_alive
 
 RGL_API rgl_status_t rgl_scene_set_time(rgl_scene_t scene, uint64_t nanoseconds)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		GraphRunCtx::synchronizeAll();
 		auto sc = sceneOf(scene);
 		sc->timeNs = nanoseconds;
 		sc->timeSet = true;
 	});
+	RGL_TAPE_RECORD(T::handle(scene), T::unum(nanoseconds));
+	return status;
 }
 
 // ================================================================ graph
 
 RGL_API rgl_status_t rgl_graph_run(rgl_node_t raw_node)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(raw_node != nullptr);
 		auto node = getNode(raw_node);
 		if (!node->ctx) {
@@ -505,19 +559,23 @@ RGL_API rgl_status_t rgl_graph_run(rgl_node_t raw_node)
 		}
 		node->ctx->run();
 	});
+	RGL_TAPE_RECORD(T::handle(raw_node));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_destroy(rgl_node_t raw_node)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(raw_node != nullptr);
 		releaseGraph(getNode(raw_node));
 	});
+	RGL_TAPE_RECORD(T::handle(raw_node));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_get_result_size(rgl_node_t node, rgl_field_t field, int32_t* out_count, int32_t* out_size_of)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		auto pn = getNodeAs<PointsNode>(node, "IPointsNode");
 		if (pn->dirty || !pn->ctx) {
@@ -533,11 +591,13 @@ RGL_API rgl_status_t rgl_graph_get_result_size(rgl_node_t node, rgl_field_t fiel
 			*out_size_of = size;
 		}
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::num(field), T::num(out_count ? *out_count : 0), T::num(out_size_of ? *out_size_of : 0));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_get_result_data(rgl_node_t node, rgl_field_t field, void* dst)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(dst != nullptr);
 		auto pn = getNodeAs<PointsNode>(node, "IPointsNode");
@@ -556,30 +616,36 @@ RGL_API rgl_status_t rgl_graph_get_result_data(rgl_node_t node, rgl_field_t fiel
 		const void* src = pn->fieldDev(field);
 		RGL_CHECK_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::num(field), T::handle(dst));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_node_add_child(rgl_node_t parent, rgl_node_t child)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(parent != nullptr);
 		CHECK_ARG(child != nullptr);
 		CHECK_ARG(parent != child);
 		getNode(parent)->addChild(getNode(child));
 	});
+	RGL_TAPE_RECORD(T::handle(parent), T::handle(child));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_node_remove_child(rgl_node_t parent, rgl_node_t child)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(parent != nullptr);
 		CHECK_ARG(child != nullptr);
 		getNode(parent)->removeChild(getNode(child));
 	});
+	RGL_TAPE_RECORD(T::handle(parent), T::handle(child));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_node_set_priority(rgl_node_t node, int32_t priority)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		auto n = getNode(node);
 		if (n->ctx) {
@@ -587,86 +653,104 @@ RGL_API rgl_status_t rgl_graph_node_set_priority(rgl_node_t node, int32_t priori
 		}
 		n->setPriority(priority);
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::num(priority));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_graph_node_get_priority(rgl_node_t node, int32_t* out_priority)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(out_priority != nullptr);
 		*out_priority = getNode(node)->priority;
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::num(out_priority ? *out_priority : 0));
+	return status;
 }
 
 // ================================================================ ray nodes
 
 RGL_API rgl_status_t rgl_node_rays_from_mat3x4f(rgl_node_t* node, const rgl_mat3x4f* rays, int32_t ray_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(rays != nullptr);
 		CHECK_ARG(ray_count > 0);
 		createOrUpdateNode<FromMat3x4fRaysNode>(node, "FromMat3x4fRaysNode",
 		                                        [&](FromMat3x4fRaysNode& n) { n.setParameters(rays, (size_t) ray_count); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(rays, ray_count), T::num(ray_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_rays_set_ring_ids(rgl_node_t* node, const int32_t* ring_ids, int32_t ring_ids_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(ring_ids != nullptr);
 		CHECK_ARG(ring_ids_count > 0);
-		notImplemented("rgl_node_rays_set_ring_ids");
+		createOrUpdateNode<SetRingIdsRaysNode>(node, "SetRingIdsRaysNode",
+		                                       [&](SetRingIdsRaysNode& n) { n.setParameters(ring_ids, (size_t) ring_ids_count); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(ring_ids, ring_ids_count), T::num(ring_ids_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_rays_set_range(rgl_node_t* node, const rgl_vec2f* ranges, int32_t ranges_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(ranges != nullptr);
 		CHECK_ARG(ranges_count > 0);
 		createOrUpdateNode<SetRangeRaysNode>(node, "SetRangeRaysNode",
 		                                     [&](SetRangeRaysNode& n) { n.setParameters(ranges, (size_t) ranges_count); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(ranges, ranges_count), T::num(ranges_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_rays_set_time_offsets(rgl_node_t* node, const float* offsets, int32_t offsets_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(offsets != nullptr);
 		CHECK_ARG(offsets_count > 0);
-		notImplemented("rgl_node_rays_set_time_offsets");
+		createOrUpdateNode<SetTimeOffsetsRaysNode>(node, "SetTimeOffsetsRaysNode",
+		                                           [&](SetTimeOffsetsRaysNode& n) { n.setParameters(offsets, (size_t) offsets_count); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(offsets, offsets_count), T::num(offsets_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_rays_transform(rgl_node_t* node, const rgl_mat3x4f* transform)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(transform != nullptr);
 		Mat34 tf = toMat(*transform);
 		createOrUpdateNode<TransformRaysNode>(node, "TransformRaysNode", [&](TransformRaysNode& n) { n.setParameters(tf); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(transform, 1));
+	return status;
 }
 
 // ================================================================ point nodes
 
 RGL_API rgl_status_t rgl_node_points_transform(rgl_node_t* node, const rgl_mat3x4f* transform)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(transform != nullptr);
 		Mat34 tf = toMat(*transform);
 		createOrUpdateNode<TransformPointsNode>(node, "TransformPointsNode", [&](TransformPointsNode& n) { n.setParameters(tf); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(transform, 1));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace(rgl_node_t* node, rgl_scene_t scene)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		auto sc = sceneOf(scene);
 		createOrUpdateNode<RaytraceNode>(node, "RaytraceNode", [&](RaytraceNode& n) {
@@ -674,12 +758,14 @@ RGL_API rgl_status_t rgl_node_raytrace(rgl_node_t* node, rgl_scene_t scene)
 			n.scene = sc.get();
 		});
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::handle(scene));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_velocity(rgl_node_t node, const rgl_vec3f* linear_velocity,
                                                           const rgl_vec3f* angular_velocity)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(linear_velocity != nullptr);
 		CHECK_ARG(angular_velocity != nullptr);
@@ -687,22 +773,26 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_velocity(rgl_node_t node, const
 		// Velocity only feeds velocity/distortion fields, which this build does not compute; the
 		// configuration is accepted and has no effect on the computed fields.
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::arr(linear_velocity, 1), T::arr(angular_velocity, 1));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_distortion(rgl_node_t node, bool enable)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		getNodeAs<RaytraceNode>(node, "RaytraceNode");
 		if (enable) {
 			notImplemented("velocity distortion");
 		}
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::flag(enable));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_non_hits(rgl_node_t node, float nearDistance, float farDistance)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
 		if (n->ctx) {
@@ -711,22 +801,26 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_non_hits(rgl_node_t node, float
 		n->setNonHits(nearDistance, farDistance);
 		n->markParamsChanged();
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::real(nearDistance), T::real(farDistance));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_mask(rgl_node_t node, const int8_t* rays_mask, int32_t rays_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(rays_mask != nullptr);
 		CHECK_ARG(rays_count > 0);
 		notImplemented("rgl_node_raytrace_configure_mask");
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::arr(rays_mask, rays_count), T::num(rays_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_beam_divergence(rgl_node_t node, float horizontal_beam_divergence,
                                                                  float vertical_beam_divergence)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG((horizontal_beam_divergence > 0.0f && vertical_beam_divergence > 0.0f) ||
 		          (horizontal_beam_divergence == 0.0f && vertical_beam_divergence == 0.0f));
@@ -737,11 +831,13 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_beam_divergence(rgl_node_t node
 		n->setBeamDivergence(horizontal_beam_divergence, vertical_beam_divergence);
 		n->markParamsChanged();
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::real(horizontal_beam_divergence), T::real(vertical_beam_divergence));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_default_intensity(rgl_node_t node, float default_intensity)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(default_intensity >= 0.0f);
 		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
@@ -751,11 +847,13 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_default_intensity(rgl_node_t no
 		n->setDefaultIntensity(default_intensity);
 		n->markParamsChanged();
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::real(default_intensity));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_raytrace_configure_return_mode(rgl_node_t node, rgl_return_mode_t return_mode)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(return_mode != RGL_RETURN_UNKNOWN);
 		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
@@ -766,64 +864,78 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_return_mode(rgl_node_t node, rg
 		n->dirty = true;
 		n->markParamsChanged();
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::num(return_mode));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_format(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(fields != nullptr);
 		CHECK_ARG(field_count > 0);
 		std::vector<rgl_field_t> f(fields, fields + field_count);
 		createOrUpdateNode<FormatPointsNode>(node, "FormatPointsNode", [&](FormatPointsNode& n) { n.setParameters(f); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(fields, field_count), T::num(field_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_yield(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(fields != nullptr);
 		CHECK_ARG(field_count > 0);
 		std::vector<rgl_field_t> f(fields, fields + field_count);
 		createOrUpdateNode<YieldPointsNode>(node, "YieldPointsNode", [&](YieldPointsNode& n) { n.setParameters(f); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(fields, field_count), T::num(field_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_compact_by_field(rgl_node_t* node, rgl_field_t field)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(field == RGL_FIELD_IS_HIT_I32 || field == RGL_FIELD_IS_GROUND_I32);
 		createOrUpdateNode<CompactByFieldPointsNode>(node, "CompactByFieldPointsNode",
 		                                             [&](CompactByFieldPointsNode& n) { n.setParameters(field); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::num(field));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_spatial_merge(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(fields != nullptr);
 		CHECK_ARG(field_count > 0);
-		notImplemented("rgl_node_points_spatial_merge");
+		std::vector<rgl_field_t> f(fields, fields + field_count);
+		createOrUpdateNode<SpatialMergePointsNode>(node, "SpatialMergePointsNode", [&](SpatialMergePointsNode& n) { n.setParameters(f); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(fields, field_count), T::num(field_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_temporal_merge(rgl_node_t* node, const rgl_field_t* fields, int32_t field_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(fields != nullptr);
 		CHECK_ARG(field_count > 0);
-		notImplemented("rgl_node_points_temporal_merge");
+		std::vector<rgl_field_t> f(fields, fields + field_count);
+		createOrUpdateNode<TemporalMergePointsNode>(node, "TemporalMergePointsNode", [&](TemporalMergePointsNode& n) { n.setParameters(f); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(fields, field_count), T::num(field_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_from_array(rgl_node_t* node, const void* points, int32_t points_count, const rgl_field_t* fields,
                                                 int32_t field_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(points != nullptr);
 		CHECK_ARG(points_count > 0);
@@ -833,6 +945,8 @@ RGL_API rgl_status_t rgl_node_points_from_array(rgl_node_t* node, const void* po
 		createOrUpdateNode<FromArrayPointsNode>(node, "FromArrayPointsNode",
 		                                        [&](FromArrayPointsNode& n) { n.setParameters(points, (size_t) points_count, f); });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::bin(points, tapePointBytes(points, points_count, fields, field_count)), T::num(points_count), T::arr(fields, field_count), T::num(field_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_points_radar_postprocess(rgl_node_t* node, const rgl_radar_scope_t* radar_scopes,
@@ -869,16 +983,18 @@ RGL_API rgl_status_t rgl_node_points_radar_set_classes(rgl_node_t node, const in
 
 RGL_API rgl_status_t rgl_node_points_filter_ground(rgl_node_t* node, const rgl_vec3f* sensor_up_vector, float ground_angle_threshold)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(ground_angle_threshold >= 0);
 		notImplemented("rgl_node_points_filter_ground");
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(sensor_up_vector, 1), T::real(ground_angle_threshold));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_gaussian_noise_angular_ray(rgl_node_t* node, float mean, float st_dev, rgl_axis_t rotation_axis)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(st_dev >= 0);
 		CHECK_ARG((rotation_axis == RGL_AXIS_X) || (rotation_axis == RGL_AXIS_Y) || (rotation_axis == RGL_AXIS_Z));
@@ -890,11 +1006,13 @@ RGL_API rgl_status_t rgl_node_gaussian_noise_angular_ray(rgl_node_t* node, float
 			}
 		});
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::real(mean), T::real(st_dev), T::num(rotation_axis));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_gaussian_noise_angular_hitpoint(rgl_node_t* node, float mean, float st_dev, rgl_axis_t rotation_axis)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(st_dev >= 0);
 		CHECK_ARG((rotation_axis == RGL_AXIS_X) || (rotation_axis == RGL_AXIS_Y) || (rotation_axis == RGL_AXIS_Z));
@@ -907,11 +1025,13 @@ RGL_API rgl_status_t rgl_node_gaussian_noise_angular_hitpoint(rgl_node_t* node, 
 			                                                     }
 		                                                     });
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::real(mean), T::real(st_dev), T::num(rotation_axis));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_gaussian_noise_distance(rgl_node_t* node, float mean, float st_dev_base, float st_dev_rise_per_meter)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(st_dev_base >= 0);
 		CHECK_ARG(st_dev_rise_per_meter >= 0);
@@ -923,14 +1043,18 @@ RGL_API rgl_status_t rgl_node_gaussian_noise_distance(rgl_node_t* node, float me
 			}
 		});
 	});
+	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::real(mean), T::real(st_dev_base), T::real(st_dev_rise_per_meter));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_node_is_alive(rgl_node_t node, bool* out_alive)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_alive != nullptr);
 		*out_alive = Nodes::contains(node);
 	});
+	RGL_TAPE_RECORD(T::handle(node), T::flag(out_alive && *out_alive));
+	return status;
 }
 
 // ================================================================ tape extension (not part of this build)
@@ -940,17 +1064,20 @@ RGL_API rgl_status_t rgl_tape_record_begin(const char* path)
 	return safeCall([&]() {
 		CHECK_ARG(path != nullptr);
 		CHECK_ARG(path[0] != '\0');
-		notImplemented("rgl_tape_record_begin");
+		T::beginRecording(path);
 	});
 }
 
-RGL_API rgl_status_t rgl_tape_record_end() { return safeCall([&]() { notImplemented("rgl_tape_record_end"); }); }
+RGL_API rgl_status_t rgl_tape_record_end()
+{
+	return safeCall([&]() { T::endRecording(); });
+}
 
 RGL_API rgl_status_t rgl_tape_record_is_active(bool* is_active)
 {
 	return safeCall([&]() {
 		CHECK_ARG(is_active != nullptr);
-		*is_active = false;
+		*is_active = T::recording();
 	});
 }
 
@@ -959,7 +1086,7 @@ RGL_API rgl_status_t rgl_tape_play(const char* path)
 	return safeCall([&]() {
 		CHECK_ARG(path != nullptr);
 		CHECK_ARG(path[0] != '\0');
-		notImplemented("rgl_tape_play");
+		T::play(path);
 	});
 }
 
@@ -1395,6 +1522,20 @@ RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server)
 	return safeCall([&]() {
 		CHECK_ARG(server != nullptr);
 		Servers::get(server, "Server")->drain();
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_server_configure_schedule(rgl_gb300_server_t server, int32_t block, int32_t order, int32_t chunk,
+                                                         int32_t regs, int64_t max_batch_beams)
+{
+	return safeCall([&]() {
+		CHECK_ARG(server != nullptr);
+		CHECK_ARG(block == 64 || block == 128 || block == 256);
+		CHECK_ARG(order == rgl::kOrderNatural || order == rgl::kOrderOctahedral || order == rgl::kOrderMorton);
+		CHECK_ARG(chunk >= 1 && chunk <= 64);
+		CHECK_ARG(regs == 64 || regs == 80 || regs == 96 || regs == 128);
+		CHECK_ARG(max_batch_beams >= 1);
+		Servers::get(server, "Server")->configure(rgl::BatchSchedule{block, rgl::kPackLaneGroup, order, chunk, regs}, max_batch_beams);
 	});
 }
 

@@ -77,7 +77,8 @@ struct alignas(16) InstanceRec
 	int32_t entityId;
 	int32_t blasRootIsLeaf;    // unused by traversal, kept for alignment/debug
 	float lox, loy, loz, hix, hiy, hiz; // world-space box (TLAS leaf bounds)
-	int32_t pad[2];
+	float laserRetro;          // rgl_entity_set_laser_retro
+	int32_t pad;
 };
 
 // Device view of a scene, read by the traversal kernel through one pointer so a captured CUDA graph
@@ -124,6 +125,11 @@ struct TraceOutputs
 	float* normal;     // 3 floats per point
 	float* incidentAngle;
 	float* laserRetro;
+	uint16_t* ringId;
+	float* azimuth;
+	float* elevation;
+	double* timeStampF64;
+	uint32_t* timeStampU32;
 };
 
 struct TraceParams
@@ -142,6 +148,10 @@ struct TraceParams
 	int32_t* errorFlag;         // set when a traversal stack overflows
 	const SceneView* scene;
 	TraceOutputs out;
+	const int32_t* ringIds;     // rays-set-ring-ids values (beam b gets ringIds[b % nRingIds]), or null
+	int32_t nRingIds;
+	int32_t pad;
+	Mat34 worldToSensor;        // inverse of the rays' cumulative transform (azimuth, elevation)
 };
 
 // One sensor (or served request) of a batched traversal launch (trace_batch.cu): its raytrace

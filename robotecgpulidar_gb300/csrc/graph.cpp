@@ -231,6 +231,36 @@ void SetRangeRaysNode::validateImpl()
 	}
 }
 
+void SetRingIdsRaysNode::setParameters(const int32_t* r, size_t n)
+{
+	RGL_CHECK_CUDA(cudaMemcpy(ids.ensure(sizeof(int32_t) * n), r, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+	count = n;
+}
+
+void SetRingIdsRaysNode::validateImpl()
+{
+	RaysNodeSingleInput::validateImpl();
+	if (input->rayCount() % count != 0) {
+		throw InvalidPipeline(format("ring ids doesn't match number of rays. RayCount(%zu) mod RingIdsCount(%zu) should be zero",
+		                             input->rayCount(), count));
+	}
+}
+
+void SetTimeOffsetsRaysNode::setParameters(const float* o, size_t n)
+{
+	RGL_CHECK_CUDA(cudaMemcpy(offsets.ensure(sizeof(float) * n), o, sizeof(float) * n, cudaMemcpyHostToDevice));
+	count = n;
+}
+
+void SetTimeOffsetsRaysNode::validateImpl()
+{
+	RaysNodeSingleInput::validateImpl();
+	if (input->rayCount() != count) {
+		throw InvalidPipeline(format("time offsets don't match number of rays. RayCount(%zu) and TimeOffsetsCount(%zu) should be equal",
+		                             input->rayCount(), count));
+	}
+}
+
 void GaussianNoiseAngularRaysNode::setParameters(float m, float sd, rgl_axis_t a)
 {
 	mean = m;
@@ -311,7 +341,13 @@ static bool raytraceSupports(rgl_field_t f)
 		case RGL_FIELD_INTENSITY_U8:
 		case RGL_FIELD_RAY_IDX_U32:
 		case RGL_FIELD_NORMAL_VEC3_F32:
-		case RGL_FIELD_INCIDENT_ANGLE_F32: return true;
+		case RGL_FIELD_INCIDENT_ANGLE_F32:
+		case RGL_FIELD_LASER_RETRO_F32:
+		case RGL_FIELD_AZIMUTH_F32:
+		case RGL_FIELD_ELEVATION_F32:
+		case RGL_FIELD_RING_ID_U16:
+		case RGL_FIELD_TIME_STAMP_F64:
+		case RGL_FIELD_TIME_STAMP_U32: return true;
 		default: return false;
 	}
 }
@@ -355,6 +391,16 @@ void RaytraceNode::validateImpl()
 		}
 	}
 	rays = exactlyOneInput<RaysNode>("IRaysNode");
+	if (scene == nullptr) {
+		scene = &Scene::defaultScene();
+	}
+	// Reference src/graph/RaytraceNode.cpp:37-45.
+	if (fields.count(RGL_FIELD_RING_ID_U16) && rays->ringIdsDev() == nullptr) {
+		throw InvalidPipeline("requested for field RING_ID_U16, but RaytraceNode cannot get ring ids");
+	}
+	if (fields.count(RGL_FIELD_TIME_STAMP_F64) && !scene->timeSet) {
+		throw InvalidPipeline("requested for field TIME_STAMP_F64, but RaytraceNode cannot get time from scene");
+	}
 	if (sampleCount() > rgl::kMaxBeamSamples) {
 		throw rgl::InvalidAPIArgument(format("beam sample pattern of %d rays exceeds %d", sampleCount(), rgl::kMaxBeamSamples));
 	}
@@ -451,7 +497,17 @@ rgl::TraceParams RaytraceNode::traceParams()
 	p.out.intensityU8 = static_cast<uint8_t*>(ptr(RGL_FIELD_INTENSITY_U8));
 	p.out.normal = static_cast<float*>(ptr(RGL_FIELD_NORMAL_VEC3_F32));
 	p.out.incidentAngle = static_cast<float*>(ptr(RGL_FIELD_INCIDENT_ANGLE_F32));
-	p.out.laserRetro = nullptr;
+	p.out.laserRetro = static_cast<float*>(ptr(RGL_FIELD_LASER_RETRO_F32));
+	p.out.ringId = static_cast<uint16_t*>(ptr(RGL_FIELD_RING_ID_U16));
+	p.out.azimuth = static_cast<float*>(ptr(RGL_FIELD_AZIMUTH_F32));
+	p.out.elevation = static_cast<float*>(ptr(RGL_FIELD_ELEVATION_F32));
+	p.out.timeStampF64 = static_cast<double*>(ptr(RGL_FIELD_TIME_STAMP_F64));
+	p.out.timeStampU32 = static_cast<uint32_t*>(ptr(RGL_FIELD_TIME_STAMP_U32));
+	p.ringIds = rays->ringIdsDev();
+	p.nRingIds = (int32_t) rays->ringIdsCount();
+	if (p.out.azimuth || p.out.elevation) {
+		p.worldToSensor = rgl::inverse(rays->cumulativeRayTransform());
+	}
 	return p;
 }
 
@@ -809,6 +865,203 @@ const void* FromArrayPointsNode::fieldDev(rgl_field_t f)
 		throw InvalidPipeline(format("FromArrayPointsNode does not provide field %s", rgl::fieldName(f)));
 	}
 	return it->second.get();
+}
+
+// ---- SpatialMergePointsNode
+
+static std::vector<rgl_field_t> mergeFields(const std::vector<rgl_field_t>& f, const char* what)
+{
+	if (std::find(f.begin(), f.end(), RGL_FIELD_DYNAMIC_FORMAT) != f.end()) {
+		throw rgl::InvalidAPIArgument(format("cannot perform %s merge on field 'RGL_FIELD_DYNAMIC_FORMAT'", what));
+	}
+	std::vector<rgl_field_t> out;
+	for (auto x : f) {
+		(void) rgl::fieldSize(x);
+		if (!rgl::isDummy(x) && std::find(out.begin(), out.end(), x) == out.end()) {
+			out.push_back(x);
+		}
+	}
+	if (out.size() > (size_t) rgl::kMaxFieldCopies) {
+		throw rgl::InvalidAPIArgument(format("merge of more than %d fields", rgl::kMaxFieldCopies));
+	}
+	return out;
+}
+
+void SpatialMergePointsNode::setParameters(const std::vector<rgl_field_t>& f)
+{
+	fields = mergeFields(f, "spatial");
+	outputs.clear();
+	for (auto x : fields) {
+		outputs[x];
+	}
+}
+
+void SpatialMergePointsNode::validateImpl()
+{
+	pointInputs.clear();
+	for (auto& in : inputs) {
+		if (auto p = std::dynamic_pointer_cast<PointsNode>(in)) {
+			pointInputs.push_back(p);
+		}
+	}
+	if (pointInputs.size() < 2) {
+		// One input would make the node a no-op (reference SpatialMergePointsNode.cpp:39-43).
+		throw InvalidPipeline(format("%s requires >= 2 input nodes, found %zu", name(), pointInputs.size()));
+	}
+	onDevice = false;
+	for (auto& in : pointInputs) {
+		for (auto f : fields) {
+			if (!in->hasField(f)) {
+				throw InvalidPipeline(format("%s input does not have required field '%s'", name(), rgl::fieldName(f)));
+			}
+		}
+		onDevice = onDevice || in->deviceCount() != nullptr;
+	}
+	count.ensure(sizeof(int32_t));
+	hCount.ensure(sizeof(int32_t));
+}
+
+bool SpatialMergePointsNode::isDense() const
+{
+	for (auto& in : pointInputs) {
+		if (!in->isDense()) {
+			return false;
+		}
+	}
+	return true;
+}
+
+size_t SpatialMergePointsNode::capacity() const
+{
+	size_t c = 0;
+	for (auto& in : pointInputs) {
+		c += in->capacity();
+	}
+	return c;
+}
+
+void SpatialMergePointsNode::prepareImpl(cudaStream_t s)
+{
+	const size_t cap = capacity();
+	if (cap > (size_t) INT32_MAX) {
+		throw rgl::InvalidAPIArgument(format("%s: %zu points exceed the 32-bit point count", name(), cap));
+	}
+	std::vector<rgl::MergeInput> ins;
+	std::vector<const void*> src;
+	std::vector<rgl::FieldCopy> fl;
+	maxCount = 0;
+	for (auto& in : pointInputs) {
+		ins.push_back({in->deviceCount(), (int32_t) in->capacity(), 0});
+		maxCount = std::max(maxCount, (int) in->capacity());
+		for (auto f : fields) {
+			src.push_back(in->fieldDev(f));
+		}
+	}
+	for (auto f : fields) {
+		rgl::FieldCopy c{};
+		c.size = (int32_t) rgl::fieldSize(f);
+		c.dst = outputs[f].ensure(std::max<size_t>(1, rgl::fieldSize(f) * cap));
+		fl.push_back(c);
+	}
+	const size_t bytes = rgl::mergeTableBytes((int) ins.size(), (int) fl.size());
+	rgl::fillMergeTable(hTable.ensure(bytes), ins, src, fl);
+	// The previous run has completed (runs synchronise first), so the pinned table is free to reuse.
+	RGL_CHECK_CUDA(cudaMemcpyAsync(table.ensure(bytes), hTable.get(), bytes, cudaMemcpyHostToDevice, s));
+}
+
+void SpatialMergePointsNode::enqueueImpl(cudaStream_t s)
+{
+	rgl::launchMergePoints(table.get(), (int) pointInputs.size(), (int) fields.size(), maxCount, nullptr, count.as<int32_t>(), s);
+	if (onDevice) {
+		RGL_CHECK_CUDA(cudaMemcpyAsync(hCount.get(), count.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+	}
+}
+
+const void* SpatialMergePointsNode::fieldDev(rgl_field_t f)
+{
+	auto it = outputs.find(f);
+	if (it == outputs.end()) {
+		throw InvalidPipeline(format("%s does not provide field %s", name(), rgl::fieldName(f)));
+	}
+	return it->second.get();
+}
+
+// ---- TemporalMergePointsNode
+
+void TemporalMergePointsNode::setParameters(const std::vector<rgl_field_t>& f)
+{
+	fields = mergeFields(f, "temporal");
+	outputs.clear();
+	for (auto x : fields) {
+		outputs[x] = std::make_unique<rgl::DeviceBuffer>();
+	}
+	bound = 0;
+	allocated = 0;
+	reset = true;
+}
+
+void TemporalMergePointsNode::validateImpl()
+{
+	PointsNodeSingleInput::validateImpl();
+	count.ensure(sizeof(int32_t));
+	hCount.ensure(sizeof(int32_t));
+}
+
+void TemporalMergePointsNode::prepareImpl(cudaStream_t s)
+{
+	if (reset) {
+		RGL_CHECK_CUDA(cudaMemsetAsync(count.get(), 0, sizeof(int32_t), s));
+		reset = false;
+	}
+	const size_t kept = bound;
+	bound += input->capacity();
+	if (bound > (size_t) INT32_MAX) {
+		throw rgl::InvalidAPIArgument(format("%s: %zu accumulated points exceed the 32-bit point count", name(), bound));
+	}
+	if (bound > allocated) {
+		const size_t want = std::max(bound, 2 * allocated);
+		for (auto f : fields) {
+			auto grown = std::make_unique<rgl::DeviceBuffer>();
+			grown->ensure(std::max<size_t>(1, rgl::fieldSize(f) * want));
+			if (kept > 0) {
+				RGL_CHECK_CUDA(cudaMemcpyAsync(grown->get(), outputs[f]->get(), rgl::fieldSize(f) * kept, cudaMemcpyDeviceToDevice, s));
+			}
+			// The old storage may be freed only after the copy has read it.
+			RGL_CHECK_CUDA(cudaStreamSynchronize(s));
+			outputs[f] = std::move(grown);
+		}
+		allocated = want;
+	}
+	std::vector<const void*> src;
+	std::vector<rgl::FieldCopy> fl;
+	for (auto f : fields) {
+		src.push_back(input->fieldDev(f));
+		rgl::FieldCopy c{};
+		c.size = (int32_t) rgl::fieldSize(f);
+		c.dst = outputs[f]->get();
+		fl.push_back(c);
+	}
+	const std::vector<rgl::MergeInput> ins{{input->deviceCount(), (int32_t) input->capacity(), 0}};
+	const size_t bytes = rgl::mergeTableBytes(1, (int) fl.size());
+	rgl::fillMergeTable(hTable.ensure(bytes), ins, src, fl);
+	RGL_CHECK_CUDA(cudaMemcpyAsync(table.ensure(bytes), hTable.get(), bytes, cudaMemcpyHostToDevice, s));
+}
+
+void TemporalMergePointsNode::enqueueImpl(cudaStream_t s)
+{
+	const int32_t inCap = (int32_t) input->capacity();
+	rgl::launchMergePoints(table.get(), 1, (int) fields.size(), inCap, count.as<int32_t>(), nullptr, s);
+	rgl::launchAddCount(count.as<int32_t>(), input->deviceCount(), inCap, s);
+	RGL_CHECK_CUDA(cudaMemcpyAsync(hCount.get(), count.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+}
+
+const void* TemporalMergePointsNode::fieldDev(rgl_field_t f)
+{
+	auto it = outputs.find(f);
+	if (it == outputs.end()) {
+		throw InvalidPipeline(format("%s does not provide field %s", name(), rgl::fieldName(f)));
+	}
+	return it->second->get();
 }
 
 // ================================================================ GraphRunCtx

@@ -75,6 +75,10 @@ struct RaysNode : virtual Node
 	virtual const float* rangesDev() const { return nullptr; } // 2 floats per entry
 	virtual size_t rangesCount() const { return 0; }
 	virtual rgl::Mat34 cumulativeRayTransform() const { return rgl::Mat34::identity(); }
+	virtual const int32_t* ringIdsDev() const { return nullptr; } // null: no ring ids upstream
+	virtual size_t ringIdsCount() const { return 0; }
+	virtual const float* timeOffsetsDev() const { return nullptr; }
+	virtual size_t timeOffsetsCount() const { return 0; }
 };
 
 struct RaysNodeSingleInput : RaysNode
@@ -85,6 +89,10 @@ struct RaysNodeSingleInput : RaysNode
 	const float* rangesDev() const override { return input->rangesDev(); }
 	size_t rangesCount() const override { return input->rangesCount(); }
 	rgl::Mat34 cumulativeRayTransform() const override { return input->cumulativeRayTransform(); }
+	const int32_t* ringIdsDev() const override { return input->ringIdsDev(); }
+	size_t ringIdsCount() const override { return input->ringIdsCount(); }
+	const float* timeOffsetsDev() const override { return input->timeOffsetsDev(); }
+	size_t timeOffsetsCount() const override { return input->timeOffsetsCount(); }
 
 protected:
 	std::shared_ptr<RaysNode> input;
@@ -133,6 +141,38 @@ struct SetRangeRaysNode : RaysNodeSingleInput
 
 private:
 	rgl::DeviceBuffer ranges;
+	size_t count = 0;
+};
+
+// Ring ids of the rays (reference src/graph/SetRaysRingIdsRaysNode.cpp:17-33): beam b gets
+// ids[b % count]; the ray count must be a multiple of the id count.
+struct SetRingIdsRaysNode : RaysNodeSingleInput
+{
+	const char* name() const override { return "SetRingIdsRaysNode"; }
+	void setParameters(const int32_t* ids, size_t n);
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t) override {}
+	const int32_t* ringIdsDev() const override { return ids.as<int32_t>(); }
+	size_t ringIdsCount() const override { return count; }
+
+private:
+	rgl::DeviceBuffer ids;
+	size_t count = 0;
+};
+
+// Per-ray time offsets in milliseconds (reference src/graph/SetTimeOffsetsRaysNode.cpp:17-33), one per
+// ray. They feed velocity distortion, which this build does not apply.
+struct SetTimeOffsetsRaysNode : RaysNodeSingleInput
+{
+	const char* name() const override { return "SetTimeOffsetsRaysNode"; }
+	void setParameters(const float* offsets, size_t n);
+	void validateImpl() override;
+	void enqueueImpl(cudaStream_t) override {}
+	const float* timeOffsetsDev() const override { return offsets.as<float>(); }
+	size_t timeOffsetsCount() const override { return count; }
+
+private:
+	rgl::DeviceBuffer offsets;
 	size_t count = 0;
 };
 
@@ -398,6 +438,63 @@ struct FromArrayPointsNode : PointsNode
 private:
 	size_t count = 0;
 	std::map<rgl_field_t, rgl::DeviceBuffer> data;
+};
+
+// Concatenation of >= 2 unorganised point clouds, inputs in the order they were linked (reference
+// src/graph/SpatialMergePointsNode.cpp:18-82). One kernel copies every field of every input; when an
+// input's count lives on the device (after compaction) the offsets and the merged count are found on
+// the device too, so the merge needs no host synchronisation.
+struct SpatialMergePointsNode : PointsNode
+{
+	const char* name() const override { return "SpatialMergePointsNode"; }
+	void setParameters(const std::vector<rgl_field_t>& f);
+	std::vector<rgl_field_t> requiredFields() const override { return fields; }
+	void validateImpl() override;
+	void prepareImpl(cudaStream_t s) override;
+	void enqueueImpl(cudaStream_t s) override;
+	bool isDense() const override;
+	bool hasField(rgl_field_t f) const override { return outputs.count(f) != 0; }
+	size_t capacity() const override;
+	const int32_t* deviceCount() const override { return onDevice ? count.as<int32_t>() : nullptr; }
+	const int32_t* hostCount() const override { return onDevice ? static_cast<const int32_t*>(hCount.get()) : nullptr; }
+	const void* fieldDev(rgl_field_t f) override;
+
+private:
+	std::vector<rgl_field_t> fields;
+	std::map<rgl_field_t, rgl::DeviceBuffer> outputs;
+	std::vector<std::shared_ptr<PointsNode>> pointInputs;
+	bool onDevice = false;
+	rgl::DeviceBuffer count, table;
+	rgl::PinnedBuffer hCount, hTable;
+	int maxCount = 0;
+};
+
+// Accumulates the input's points over runs until its fields are set again (reference
+// src/graph/TemporalMergePointsNode.cpp:18-48, which appends into host arrays). Here the accumulated
+// cloud stays on the device: each run appends at the device-resident count; storage grows
+// geometrically in the prepare phase.
+struct TemporalMergePointsNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "TemporalMergePointsNode"; }
+	void setParameters(const std::vector<rgl_field_t>& f);
+	std::vector<rgl_field_t> requiredFields() const override { return fields; }
+	bool hasField(rgl_field_t f) const override { return outputs.count(f) != 0; }
+	void validateImpl() override;
+	void prepareImpl(cudaStream_t s) override;
+	void enqueueImpl(cudaStream_t s) override;
+	size_t capacity() const override { return bound; }
+	const int32_t* deviceCount() const override { return count.as<int32_t>(); }
+	const int32_t* hostCount() const override { return static_cast<const int32_t*>(hCount.get()); }
+	const void* fieldDev(rgl_field_t f) override;
+
+private:
+	std::vector<rgl_field_t> fields;
+	std::map<rgl_field_t, std::unique_ptr<rgl::DeviceBuffer>> outputs;
+	size_t bound = 0;     // upper bound of the accumulated count, including the current run
+	size_t allocated = 0; // points each output buffer holds
+	bool reset = true;
+	rgl::DeviceBuffer count, table;
+	rgl::PinnedBuffer hCount, hTable;
 };
 
 // ---------------------------------------------------------------- run context

@@ -1,6 +1,8 @@
 // Host-side launchers of the CUDA kernels (defined in the .cu files of this directory).
 #pragma once
 
+#include <vector>
+
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
@@ -142,6 +144,27 @@ struct FieldCopies
 	FieldCopy f[kMaxFieldCopies];
 	int32_t count;
 };
+
+// Concatenation of point clouds (spatial and temporal merge). Input i contributes its first count_i
+// points (count_i = *count when count is set, else staticCount).
+struct MergeInput
+{
+	const int32_t* count;
+	int32_t staticCount;
+	int32_t pad;
+};
+// Device table of a merge: MergeInput[nInputs] | const void* src[nInputs * nFields] | FieldCopy[nFields]
+// (dst and size used), each part 16-byte aligned.
+size_t mergeTableBytes(int nInputs, int nFields);
+void fillMergeTable(void* table, const std::vector<MergeInput>& inputs, const std::vector<const void*>& src,
+                    const std::vector<FieldCopy>& fields);
+// Writes input i's points at base + sum_{j<i} count_j of every field's dst (base = *dBase when dBase is
+// set, else 0) and, when dOutCount is set, base + sum of all counts to *dOutCount. maxCount bounds every
+// count_i.
+void launchMergePoints(const void* dTable, int nInputs, int nFields, int maxCount, const int32_t* dBase, int32_t* dOutCount,
+                       cudaStream_t s);
+// *dAcc += (dAdd ? *dAdd : addStatic), one thread.
+void launchAddCount(int32_t* dAcc, const int32_t* dAdd, int32_t addStatic, cudaStream_t s);
 
 size_t compactScratchBytes(int cap);
 // Stable compaction of `cap` points (first *dInCount valid when dInCount != null) by int32 flags.

@@ -8,6 +8,8 @@
 // and formatting writes the packed output word by word (coalesced 4-byte stores).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.hpp"
 #include "philox.hpp"
 
@@ -316,7 +318,128 @@ __global__ void kAosToSoa(const uint8_t* __restrict__ in, int pointSize, int n, 
 	}
 }
 
+// Point clouds concatenated: blockIdx.y is the input, blockIdx.x a tile of its points. Every block
+// finds its input's offset by summing the counts before it (inputs are few); the copy moves whole
+// 4-byte words when the element size allows (all but 1- and 2-byte fields).
+constexpr int kMergeTile = 2048;
+
+struct MergeTableView
+{
+	const MergeInput* in;
+	const void* const* src;
+	const FieldCopy* fld;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t{15}; }
+
+__host__ __device__ inline MergeTableView mergeView(const void* table, int nIn, int nF)
+{
+	const uint8_t* b = static_cast<const uint8_t*>(table);
+	const size_t offSrc = align16(sizeof(MergeInput) * (size_t) nIn);
+	const size_t offFld = offSrc + align16(sizeof(void*) * (size_t) nIn * (size_t) nF);
+	return {reinterpret_cast<const MergeInput*>(b), reinterpret_cast<const void* const*>(b + offSrc),
+	        reinterpret_cast<const FieldCopy*>(b + offFld)};
+}
+
+__device__ __forceinline__ int mergeCount(const MergeInput& m) { return m.count ? *m.count : m.staticCount; }
+
+template<class W>
+__device__ __forceinline__ void copyRange(const void* src, void* dst, long srcFirst, long dstFirst, long n)
+{
+	const W* s = static_cast<const W*>(src) + srcFirst;
+	W* d = static_cast<W*>(dst) + dstFirst;
+	for (long k = threadIdx.x; k < n; k += blockDim.x) {
+		d[k] = s[k];
+	}
+}
+
+__global__ void __launch_bounds__(kBlock) kMergePoints(const void* table, int nIn, int nF, const int32_t* dBase, int32_t* dOutCount)
+{
+	const MergeTableView t = mergeView(table, nIn, nF);
+	const int i = blockIdx.y;
+	__shared__ long long sOffset;
+	__shared__ int sCount;
+	if (threadIdx.x < 32) {
+		const int lane = threadIdx.x;
+		const bool total = dOutCount != nullptr && i == 0 && blockIdx.x == 0;
+		const int upTo = total ? nIn : i;
+		long long before = 0, all = 0;
+		for (int j = lane; j < upTo; j += 32) {
+			const long long c = mergeCount(t.in[j]);
+			all += c;
+			before += j < i ? c : 0;
+		}
+		for (int o = 16; o > 0; o >>= 1) {
+			before += __shfl_down_sync(0xffffffffu, before, o);
+			all += __shfl_down_sync(0xffffffffu, all, o);
+		}
+		if (lane == 0) {
+			const long long base = dBase ? *dBase : 0;
+			sOffset = base + before;
+			sCount = mergeCount(t.in[i]);
+			if (total) {
+				*dOutCount = (int32_t) (base + all);
+			}
+		}
+	}
+	__syncthreads();
+	const long first = (long) blockIdx.x * kMergeTile;
+	const long last = min((long) sCount, first + kMergeTile);
+	if (first >= last) {
+		return;
+	}
+	for (int f = 0; f < nF; ++f) {
+		const int sz = t.fld[f].size;
+		const void* src = t.src[(size_t) i * nF + f];
+		void* dst = t.fld[f].dst;
+		if (sz % 4 == 0) {
+			const int w = sz / 4;
+			copyRange<uint32_t>(src, dst, first * w, (sOffset + first) * w, (last - first) * w);
+		} else if (sz % 2 == 0) {
+			const int w = sz / 2;
+			copyRange<uint16_t>(src, dst, first * w, (sOffset + first) * w, (last - first) * w);
+		} else {
+			copyRange<uint8_t>(src, dst, first * sz, (sOffset + first) * sz, (last - first) * sz);
+		}
+	}
+}
+
+__global__ void kAddCount(int32_t* acc, const int32_t* add, int32_t addStatic) { *acc += add ? *add : addStatic; }
+
 } // namespace
+
+size_t mergeTableBytes(int nInputs, int nFields)
+{
+	return align16(sizeof(MergeInput) * (size_t) nInputs) + align16(sizeof(void*) * (size_t) nInputs * (size_t) nFields) +
+	       sizeof(FieldCopy) * (size_t) nFields;
+}
+
+void fillMergeTable(void* table, const std::vector<MergeInput>& inputs, const std::vector<const void*>& src,
+                    const std::vector<FieldCopy>& fields)
+{
+	const int nIn = (int) inputs.size(), nF = (int) fields.size();
+	const MergeTableView v = mergeView(table, nIn, nF);
+	std::copy(inputs.begin(), inputs.end(), const_cast<MergeInput*>(v.in));
+	std::copy(src.begin(), src.end(), const_cast<const void**>(v.src));
+	std::copy(fields.begin(), fields.end(), const_cast<FieldCopy*>(v.fld));
+}
+
+void launchMergePoints(const void* dTable, int nInputs, int nFields, int maxCount, const int32_t* dBase, int32_t* dOutCount,
+                       cudaStream_t s)
+{
+	if (nInputs <= 0) {
+		return;
+	}
+	const dim3 grid((unsigned) std::max(1, blocks(maxCount, kMergeTile)), (unsigned) nInputs);
+	kMergePoints<<<grid, kBlock, 0, s>>>(dTable, nInputs, nFields, dBase, dOutCount);
+	countLaunch();
+}
+
+void launchAddCount(int32_t* dAcc, const int32_t* dAdd, int32_t addStatic, cudaStream_t s)
+{
+	kAddCount<<<1, 1, 0, s>>>(dAcc, dAdd, addStatic);
+	countLaunch();
+}
 
 void launchTransformRays(const Mat34* in, Mat34* out, int n, const Mat34* dTf, cudaStream_t s)
 {

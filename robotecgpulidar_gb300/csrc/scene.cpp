@@ -58,6 +58,12 @@ void Entity::setId(int32_t newId)
 	scene->markPosesDirty();
 }
 
+void Entity::setLaserRetro(float retro)
+{
+	laserRetro = retro;
+	scene->markPosesDirty(); // the value travels in the instance record
+}
+
 Scene& Scene::defaultScene()
 {
 	static Scene scene;
@@ -145,6 +151,7 @@ rgl::InstanceRec* Scene::fillInstanceRecords()
 		r.nodes = e.mesh->blas.nodes;
 		r.tris = e.mesh->blas.tris;
 		r.entityId = e.id;
+		r.laserRetro = e.laserRetro;
 		const float* b = e.mesh->blas.bounds;
 		float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
 		for (int c = 0; c < 8; ++c) {

@@ -33,6 +33,7 @@ struct Entity
 	Entity(std::shared_ptr<Mesh> m, Scene* s);
 	void setTransform(const rgl::Mat34& tf);
 	void setId(int32_t id);
+	void setLaserRetro(float retro);
 
 	std::shared_ptr<Mesh> mesh;
 	Scene* scene;

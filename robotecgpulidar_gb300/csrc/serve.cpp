@@ -27,6 +27,10 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 	RGL_CHECK_CUDA(cudaHostGetDevicePointer(&d, h, 0));
 	arena.host = static_cast<uint8_t*>(h);
 	arena.dev = static_cast<uint8_t*>(d);
+	// The device writes every page of the arena once now, so the first batches that land in a page
+	// do not pay the device's first access to it.
+	RGL_CHECK_CUDA(cudaMemsetAsync(d, 0, Arena::kMinBlock << order, stream));
+	RGL_CHECK_CUDA(cudaStreamSynchronize(stream));
 	for (int i = 0; i < maxInFlight; ++i) {
 		auto s = std::make_unique<Slot>();
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
@@ -323,7 +327,14 @@ Server::Stats Server::stats()
 }
 
 // Builds and enqueues one batch from slot.reqs (already admitted, outputs allocated).
-void Server::launch(Slot& slot)
+void Server::configure(const rgl::BatchSchedule& s, int64_t maxBeams)
+{
+	std::lock_guard<std::mutex> g(m);
+	schedule = s;
+	maxBatchBeams = maxBeams;
+}
+
+void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 {
 	const int n = (int) slot.reqs.size();
 	int64_t points = 0;
@@ -371,7 +382,7 @@ void Server::launch(Slot& slot)
 		b.p.out.isHit = flags + pointBase;
 		b.p.out.entityId = ent + pointBase;
 		b.samples = nullptr; // one sample per beam: never read
-		b.order = patterns[r.pattern]->order.as<uint32_t>();
+		b.order = sched.order == rgl::kOrderNatural ? nullptr : patterns[r.pattern]->order.as<uint32_t>();
 		b.groupSize = 1;
 		b.hasRayTransform = 1;
 		b.rayTransform = r.pose;
@@ -404,7 +415,7 @@ void Server::launch(Slot& slot)
 	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, stream));
 	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, stream));
 	rgl::launchTraceBatch(reinterpret_cast<const rgl::BatchJob*>(dBase), reinterpret_cast<const int32_t*>(dBase + offTask), n, 1, false,
-	                      schedule, slot.counter.as<uint32_t>(), stream);
+	                      sched, slot.counter.as<uint32_t>(), stream);
 	rgl::launchSegCompact(reinterpret_cast<const rgl::SegCompactJob*>(dBase + offSeg), reinterpret_cast<const int32_t*>(dBase + offTile), n,
 	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, stream);
 	auto* hResults = static_cast<int32_t*>(slot.hResults.ensure(sizeof(int32_t) * 2 * n));
@@ -516,6 +527,7 @@ void Server::loop()
 				inFlight.push_back(freeSlot);
 				++st.batches;
 				st.jobsInBatches += (int64_t) batch.size();
+				const rgl::BatchSchedule sched = schedule;
 				lk.unlock();
 				bool ok = true;
 				std::string why;
@@ -528,7 +540,7 @@ void Server::loop()
 						}
 
 					}
-					launch(*freeSlot);
+					launch(*freeSlot, sched);
 				}
 				catch (std::exception& e) {
 					ok = false;

@@ -60,8 +60,8 @@ struct Server
 	void release(int64_t id);
 	void drain();
 
-	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 80};
-	int64_t maxBatchBeams = 32 << 20;
+	// Schedule and batch size limit of batches launched from now on.
+	void configure(const rgl::BatchSchedule& s, int64_t maxBeams);
 
 	struct Stats
 	{
@@ -139,13 +139,15 @@ private:
 	Arena arena;
 
 	void loop();
-	void launch(Slot& slot);
+	void launch(Slot& slot, const rgl::BatchSchedule& sched);
 	void retire(Slot& slot);
 	Request& get(int64_t id);
 	static void CUDART_CB batchDone(void* self);
 
 	int64_t budget;
 	int maxInFlight;
+	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 80}; // guarded by m
+	int64_t maxBatchBeams = 32 << 20;                                                     // guarded by m
 	cudaStream_t stream = nullptr;
 	std::vector<std::unique_ptr<Pattern>> patterns;
 	std::vector<std::unique_ptr<Slot>> slots;

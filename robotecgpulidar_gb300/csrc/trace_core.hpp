@@ -237,6 +237,17 @@ RGL_HD uint32_t highestBit(uint32_t x)
 #endif
 }
 
+// Closest-hit order: smaller t first; equal t goes to the smaller (instance, triangle) pair. The order
+// does not depend on the traversal order, so every traversal that tests all triangles at the minimal
+// t (every correct one does: their boxes are never culled) returns the same hit.
+RGL_HD bool closerHit(float t, int32_t inst, int32_t tri, const HitRec& best)
+{
+	if (t != best.t) {
+		return t < best.t;
+	}
+	return (uint32_t) inst != (uint32_t) best.inst ? (uint32_t) inst < (uint32_t) best.inst : (uint32_t) tri < (uint32_t) best.tri;
+}
+
 // A ray in the frame being traversed: origin, direction, inverse direction and its octant.
 struct FrameRay
 {
@@ -331,7 +342,8 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 					TriRecord tr = load.tri(leaves, first + k);
 					float t;
 					if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), r.o, wt,
-					                      best.t, t)) {
+					                      best.t, t) &&
+					    closerHit(t, inst, first + k, best)) {
 						best.t = t;
 						best.inst = inst;
 						best.tri = first + k;

@@ -97,7 +97,7 @@ struct SampleVal
 	uint32_t hit;
 	float dist;
 	float intensity;
-	int32_t entity;
+	int32_t inst; // instance index of a hit (its entity id and laser retro are read when written)
 	float nx, ny, nz, cosInc;
 };
 
@@ -105,7 +105,7 @@ struct Selected
 {
 	float dist;
 	float intensity;
-	int32_t entity;
+	int32_t inst;
 	float nx, ny, nz, cosInc;
 };
 
@@ -123,13 +123,10 @@ __device__ __forceinline__ Mat34 loadMat(const Mat34* p)
 // min-range rule turns a closer hit into the near non-hit without continuing, a miss gives the far
 // non-hit distance. With SHADING the world normal, |cos| of the incidence and intensity are added.
 template<bool SHADING>
-__device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
-                                                 const Mat34& sr, float minRange, float maxRange, DevStack& st)
+__device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
+                                                   const HitRec& h, Vec3 d, float minRange)
 {
 	DevLoader ld;
-	const Vec3 o = sr.rayOrigin();
-	const Vec3 d = sr.rayDir();
-	const HitRec h = traceClosest(sc, o, d, maxRange, st, ld);
 	SampleVal v = emptySample();
 	v.dist = farNonHit;
 	if (h.inst >= 0) {
@@ -140,7 +137,7 @@ __device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonH
 			const InstanceRec& inst = sc.instances[h.inst];
 			v.hit = 1;
 			v.dist = dist;
-			v.entity = inst.entityId;
+			v.inst = h.inst;
 			if (SHADING) {
 				const TriRecord tr = ld.tri(inst.tris, h.tri);
 				const Vec3 wa = inst.objectToWorld.point(v3(tr.v0x, tr.v0y, tr.v0z));
@@ -159,9 +156,19 @@ __device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonH
 	return v;
 }
 
+template<bool SHADING>
+__device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
+                                                 const Mat34& sr, float minRange, float maxRange, DevStack& st)
+{
+	DevLoader ld;
+	const Vec3 d = sr.rayDir();
+	const HitRec h = traceClosest(sc, sr.rayOrigin(), d, maxRange, st, ld);
+	return sampleFromHit<SHADING>(nearNonHit, farNonHit, defaultIntensity, sc, h, d, minRange);
+}
+
 __device__ __forceinline__ Selected toSelected(const SampleVal& v)
 {
-	return Selected{v.dist, v.intensity, v.entity, v.nx, v.ny, v.nz, v.cosInc};
+	return Selected{v.dist, v.intensity, v.inst, v.nx, v.ny, v.nz, v.cosInc};
 }
 
 // In-order selection over a beam's samples; add() must see samples 0, 1, 2, ... in order.
@@ -208,18 +215,49 @@ struct ReturnReducer
 	}
 };
 
-// Writes beam `beam`'s returns at points beam * returnCount + r. `ray` is the primary ray pose.
-__device__ __forceinline__ void writeReturns(const TraceOutputs& out, uint32_t beam, int32_t returnMode, int returnCount,
-                                             const Mat34& ray, const ReturnReducer& red)
+// Azimuth and elevation of a sensor-frame ray pose, for rays generated in a left-handed frame with the
+// rotation applied in ZXY order, Y up and Z forward (reference Mat3x4f.hpp:146-175).
+__device__ __forceinline__ float rayElevation(const Mat34& m)
 {
+	const float v = m.m[1][2];
+	return v < 1.0f ? (v > -1.0f ? asinf(v) : -1.57079632679489661923f) : 1.57079632679489661923f;
+}
+__device__ __forceinline__ float rayAzimuth(const Mat34& m)
+{
+	const float v = m.m[2][1];
+	return (v < 1.0f && v > -1.0f) ? atan2f(-m.m[2][0], m.m[2][2]) : 0.0f;
+}
+
+// Writes beam `beam`'s returns at points beam * returnCount + r. `ray` is the primary ray pose. Per
+// return point it also writes the beam's shared fields (reference optixPrograms.cu:288-326): ray
+// index, azimuth and elevation of the sensor-frame pose, ring id and time stamps (zero: this build
+// applies no velocity distortion).
+__device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneView& sc, uint32_t beam, const Mat34& ray,
+                                             const ReturnReducer& red)
+{
+	const TraceOutputs& out = p.out;
+	const int32_t returnMode = p.returnMode;
+	const int returnCount = p.returnCount;
 	const Vec3 org = ray.rayOrigin();
 	const Vec3 dn = normalized(ray.rayDir());
+	float azimuth = 0.0f, elevation = 0.0f;
+	if (out.azimuth || out.elevation) {
+		const Mat34 local = mul(p.worldToSensor, ray);
+		azimuth = rayAzimuth(local);
+		elevation = rayElevation(local);
+	}
+	const uint16_t ring = (out.ringId && p.ringIds) ? (uint16_t) p.ringIds[beam % (uint32_t) p.nRingIds] : (uint16_t) 0;
 	for (int r = 0; r < returnCount; ++r) {
 		const size_t pi = (size_t) beam * returnCount + r;
 		const uint32_t type = (((uint32_t) returnMode) >> (8 * r)) & 0xffu;
 		if (out.rayIdx) {
 			out.rayIdx[pi] = beam;
 		}
+		if (out.azimuth) out.azimuth[pi] = azimuth;
+		if (out.elevation) out.elevation[pi] = elevation;
+		if (out.ringId) out.ringId[pi] = ring;
+		if (out.timeStampF64) out.timeStampF64[pi] = 0.0;
+		if (out.timeStampU32) out.timeStampU32[pi] = 0u;
 		if (!red.haveFirst) {
 			const float nonHitDist = red.nonHitDist;
 			Vec3 disp = dn * nonHitDist;
@@ -262,7 +300,8 @@ __device__ __forceinline__ void writeReturns(const TraceOutputs& out, uint32_t b
 		}
 		if (out.distance) out.distance[pi] = sel.dist;
 		if (out.isHit) out.isHit[pi] = 1;
-		if (out.entityId) out.entityId[pi] = sel.entity;
+		const InstanceRec& hitInst = sc.instances[sel.inst];
+		if (out.entityId) out.entityId[pi] = hitInst.entityId;
 		if (out.returnType) out.returnType[pi] = (uint8_t) type;
 		if (out.intensityF32) out.intensityF32[pi] = sel.intensity;
 		if (out.intensityU8) out.intensityU8[pi] = sel.intensity < 255.0f ? (uint8_t) roundf(sel.intensity) : (uint8_t) 255;
@@ -272,7 +311,7 @@ __device__ __forceinline__ void writeReturns(const TraceOutputs& out, uint32_t b
 			out.normal[3 * pi + 2] = sel.nz;
 		}
 		if (out.incidentAngle) out.incidentAngle[pi] = acosf(sel.cosInc);
-		if (out.laserRetro) out.laserRetro[pi] = 0.0f;
+		if (out.laserRetro) out.laserRetro[pi] = hitInst.laserRetro;
 	}
 }
 
@@ -292,7 +331,7 @@ __device__ __forceinline__ void reduceGroup(const SampleVal (&sv)[ROUNDS], int n
 		const uint32_t hit = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].hit : pickU(r, sv[0].hit, sv[ROUNDS - 1].hit), src);
 		const float dist = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].dist : pick(r, sv[0].dist, sv[ROUNDS - 1].dist), src);
 		const int32_t ent = __shfl_sync(
-		    0xffffffffu, ROUNDS == 1 ? sv[0].entity : (int32_t) pickU(r, (uint32_t) sv[0].entity, (uint32_t) sv[ROUNDS - 1].entity), src);
+		    0xffffffffu, ROUNDS == 1 ? sv[0].inst : (int32_t) pickU(r, (uint32_t) sv[0].inst, (uint32_t) sv[ROUNDS - 1].inst), src);
 		Selected cur{dist, 0.0f, ent, 0.0f, 0.0f, 0.0f, 0.0f};
 		if (SHADING) {
 			cur.intensity = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].intensity : pick(r, sv[0].intensity, sv[ROUNDS - 1].intensity), src);

@@ -158,6 +158,10 @@ def _proto(l):
         "rgl_node_points_format": [P(vp), vp, i32],
         "rgl_node_points_yield": [P(vp), vp, i32],
         "rgl_node_points_compact_by_field": [P(vp), i32],
+        "rgl_tape_record_begin": [C.c_char_p],
+        "rgl_tape_record_end": [],
+        "rgl_tape_record_is_active": [P(C.c_bool)],
+        "rgl_tape_play": [C.c_char_p],
         "rgl_node_points_spatial_merge": [P(vp), vp, i32],
         "rgl_node_points_temporal_merge": [P(vp), vp, i32],
         "rgl_node_points_from_array": [P(vp), vp, i32, vp, i32],
@@ -209,6 +213,7 @@ def _proto(l):
         "rgl_gb300_server_get_result_host": [vp, C.c_int64, i32, P(vp), P(i32)],
         "rgl_gb300_server_release": [vp, C.c_int64],
         "rgl_gb300_server_drain": [vp],
+        "rgl_gb300_server_configure_schedule": [vp, i32, i32, i32, i32, C.c_int64],
         "rgl_gb300_server_get_stats": [vp] + [P(C.c_int64)] * 7,
     }
     for name, args in sigs.items():
@@ -351,6 +356,18 @@ def points_from_array(node_ref, data: np.ndarray, count: int, fields):
     f = _fields(fields)
     d = np.ascontiguousarray(data)
     check(lib().rgl_node_points_from_array(C.byref(node_ref), ptr(d), count, ptr(f), f.shape[0]))
+    return node_ref
+
+
+def points_spatial_merge(node_ref, fields):
+    f = _fields(fields)
+    check(lib().rgl_node_points_spatial_merge(C.byref(node_ref), ptr(f), f.shape[0]))
+    return node_ref
+
+
+def points_temporal_merge(node_ref, fields):
+    f = _fields(fields)
+    check(lib().rgl_node_points_temporal_merge(C.byref(node_ref), ptr(f), f.shape[0]))
     return node_ref
 
 
@@ -549,6 +566,9 @@ class Server:
 
     def drain(self):
         check(lib().rgl_gb300_server_drain(self.h))
+
+    def configure_schedule(self, block=256, order=1, chunk=1, regs=80, max_batch_beams=32 << 20):
+        check(lib().rgl_gb300_server_configure_schedule(self.h, block, order, chunk, regs, max_batch_beams))
 
     def stats(self) -> dict:
         v = [C.c_int64() for _ in range(7)]

@@ -231,6 +231,249 @@ struct HostLoader
 	}
 };
 
+// ---------------------------------------------------------------- union traversal (test only)
+//
+// A second traversal order for the order-independence test: up to P rays sharing an origin walk the
+// hierarchy together; every ray is tested against each visited node and a child is entered when any
+// ray hits it, so the walk visits the union of the rays' nodes (in the first ray's octant order) and
+// each ray tests at least the triangles its own traversal would. With closerHit() (trace_core.hpp)
+// each ray's hit must then equal traceClosest's, bit for bit. Built only from the library's node
+// decode, slab and triangle primitives.
+
+// The set is held by one thread: nothing to share between lanes.
+struct SoloGroup
+{
+	RGL_HD uint32_t unite(uint32_t v) const { return v; }
+	RGL_HD uint32_t orderOctant(uint32_t oct) const { return oct; }
+};
+
+template<int P>
+struct PacketFrame
+{
+	Vec3 o;
+	Vec3 inv[P];
+	uint32_t selOct; // octant of ray 0: near/far plane selection when the rays share it
+	uint32_t ordOct; // child visiting order, common to the whole set
+	bool mixed;      // the rays' octants differ: near and far planes are found per ray
+};
+
+// World directions and per-frame watertight constants of the set's rays are kept by `Scratch`
+// (registers for one ray, shared memory or arrays for more), read once per frame change and once per
+// triangle test. Scratch provides dir(r), setDir(r, v), wt(r) and setWt(r, w).
+template<int P, class Scratch, class Group>
+RGL_HD void setPacketFrame(PacketFrame<P>& f, Vec3 o, const Mat34* worldToObject, Scratch& sp, const Group& grp)
+{
+	f.o = o;
+	uint32_t any = 0u, all = 7u;
+	for (int r = 0; r < P; ++r) {
+		const Vec3 d = worldToObject ? worldToObject->vector(sp.dir(r)) : sp.dir(r);
+		f.inv[r] = {safeInv(d.x), safeInv(d.y), safeInv(d.z)};
+		const uint32_t oc = (f.inv[r].x < 0.0f ? 1u : 0u) | (f.inv[r].y < 0.0f ? 2u : 0u) | (f.inv[r].z < 0.0f ? 4u : 0u);
+		any |= oc;
+		all &= oc;
+		if (r == 0) {
+			f.selOct = oc;
+		}
+		if (worldToObject) {
+			sp.setWt(r, setupWatertight(d));
+		}
+	}
+	f.mixed = any != all;
+	f.ordOct = grp.orderOctant(f.selOct);
+}
+
+// Closest hits of the rays oW + t sp.dir(r), t in (0, tmax], r < n (n <= P; directions r >= n must be
+// finite, e.g. copies of ray 0's, and get t = -1 with no hit). Every member of `grp` must make the
+// call with the same oW, scene and stack depth.
+template<int P, class Stack, class NodeLoader, class Scratch, class Group>
+RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, Stack& st, const NodeLoader& load, Scratch& sp,
+                               const Group& grp, HitRec (&best)[P])
+{
+	for (int r = 0; r < P; ++r) {
+		best[r].t = r < n ? tmax : -1.0f; // an inactive ray culls every box and triangle
+		best[r].inst = -1;
+		best[r].tri = -1;
+	}
+	if (sc.nInstances <= 0) {
+		return;
+	}
+	const int base = st.size();
+	PacketFrame<P> f;
+	setPacketFrame<P>(f, oW, nullptr, sp, grp);
+	const WideNode* nodes = sc.tlas;
+	const TriRecord* leaves = sc.tlasLeaves;
+	int32_t inst = -1;
+	uint32_t node = 0;
+	for (;;) {
+		uint4 w0, w1, w2, w3, w4;
+		load.nodeWords(nodes, node, w0, w1, w2, w3, w4);
+		const float sx = exp2Byte((uint8_t) (w0.w & 0xffu)), sy = exp2Byte((uint8_t) ((w0.w >> 8) & 0xffu)),
+		            sz = exp2Byte((uint8_t) ((w0.w >> 16) & 0xffu));
+		const uint32_t imask = w0.w >> 24;
+		const uint32_t childBase = w1.x, triBase = w1.y;
+		const float px = asFloat(w0.x) - f.o.x, py = asFloat(w0.y) - f.o.y, pz = asFloat(w0.z) - f.o.z;
+		// Per ray the slab form of traceClosest: t = fma(1 + q 2^-15, 2^15 A, C - 2^15 A).
+		float Sx[P], Sy[P], Sz[P], Dx[P], Dy[P], Dz[P];
+		for (int r = 0; r < P; ++r) {
+			Sx[r] = 32768.0f * (sx * f.inv[r].x);
+			Sy[r] = 32768.0f * (sy * f.inv[r].y);
+			Sz[r] = 32768.0f * (sz * f.inv[r].z);
+			Dx[r] = px * f.inv[r].x - Sx[r];
+			Dy[r] = py * f.inv[r].y - Sy[r];
+			Dz[r] = pz * f.inv[r].z - Sz[r];
+		}
+		uint32_t hitSlots = 0;
+		if (!f.mixed) {
+			// One octant: near/far planes selected once for the packet.
+			const bool negx = (f.selOct & 1u) != 0, negy = (f.selOct & 2u) != 0, negz = (f.selOct & 4u) != 0;
+			const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y, fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
+			const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w, fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
+			const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y, fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
+			for (int s = 0; s < kWideArity; ++s) {
+				const int k = s & 3;
+				const bool hiw = s >= 4;
+				const float bnx = byteMantissa(hiw ? nx1 : nx0, k), bfx = byteMantissa(hiw ? fx1 : fx0, k);
+				const float bny = byteMantissa(hiw ? ny1 : ny0, k), bfy = byteMantissa(hiw ? fy1 : fy0, k);
+				const float bnz = byteMantissa(hiw ? nz1 : nz0, k), bfz = byteMantissa(hiw ? fz1 : fz0, k);
+				uint32_t h = 0u; // no short circuit: every ray's test is straight-line code
+				for (int r = 0; r < P; ++r) {
+					const float tEntry = max4(fmaf(bnx, Sx[r], Dx[r]), fmaf(bny, Sy[r], Dy[r]), fmaf(bnz, Sz[r], Dz[r]), 0.0f);
+					const float tExit = min4(fmaf(bfx, Sx[r], Dx[r]), fmaf(bfy, Sy[r], Dy[r]), fmaf(bfz, Sz[r], Dz[r]), best[r].t);
+					h |= (tEntry <= tExit * kSlabRelSlack) ? 1u : 0u;
+				}
+				hitSlots |= h << s;
+			}
+		} else {
+			// Mixed octants: both planes per axis, near = min, far = max, per ray.
+			for (int s = 0; s < kWideArity; ++s) {
+				const int k = s & 3;
+				const bool hiw = s >= 4;
+				const float lx = byteMantissa(hiw ? w2.y : w2.x, k), hx = byteMantissa(hiw ? w3.w : w3.z, k);
+				const float ly = byteMantissa(hiw ? w2.w : w2.z, k), hy = byteMantissa(hiw ? w4.y : w4.x, k);
+				const float lz = byteMantissa(hiw ? w3.y : w3.x, k), hz = byteMantissa(hiw ? w4.w : w4.z, k);
+				uint32_t h = 0u;
+				for (int r = 0; r < P; ++r) {
+					const float ax = fmaf(lx, Sx[r], Dx[r]), bx = fmaf(hx, Sx[r], Dx[r]);
+					const float ay = fmaf(ly, Sy[r], Dy[r]), by = fmaf(hy, Sy[r], Dy[r]);
+					const float az = fmaf(lz, Sz[r], Dz[r]), bz = fmaf(hz, Sz[r], Dz[r]);
+					const float tEntry = max4(minf_(ax, bx), minf_(ay, by), minf_(az, bz), 0.0f);
+					const float tExit = min4(maxf_(ax, bx), maxf_(ay, by), maxf_(az, bz), best[r].t);
+					h |= (tEntry <= tExit * kSlabRelSlack) ? 1u : 0u;
+				}
+				hitSlots |= h << s;
+			}
+		}
+		hitSlots = grp.unite(hitSlots);
+		const uint32_t ordered = octantPermute((hitSlots & imask) | ((hitSlots & ~imask & 0xffu) << 8), f.ordOct);
+		uint32_t internalHits = ordered & 0xffu, leafHits = ordered >> 8;
+		const uint32_t metaLo = w1.z, metaHi = w1.w;
+		if (inst < 0) {
+			while (leafHits) {
+				const uint32_t j = highestBit(leafHits);
+				leafHits &= ~(1u << j);
+				const uint32_t s = j ^ f.ordOct;
+				const uint32_t meta = ((s < 4 ? metaLo : metaHi) >> ((s & 3) * 8)) & 0xffu;
+				st.push((uint32_t) load.leafPrim(leaves, (int) triBase + (int) (meta & 31u)), kEnterInstance);
+			}
+		} else {
+			while (leafHits) {
+				const uint32_t s = lowestBit(leafHits) ^ f.ordOct;
+				leafHits &= leafHits - 1u;
+				const uint32_t meta = ((s < 4 ? metaLo : metaHi) >> ((s & 3) * 8)) & 0xffu;
+				const int first = (int) triBase + (int) (meta & 31u);
+				const int cnt = (int) (meta >> 5);
+				for (int k = 0; k < cnt; ++k) {
+					const TriRecord tr = load.tri(leaves, first + k);
+					const Vec3 a = v3(tr.v0x, tr.v0y, tr.v0z), b = v3(tr.v1x, tr.v1y, tr.v1z), c = v3(tr.v2x, tr.v2y, tr.v2z);
+					for (int r = 0; r < P; ++r) {
+						float t;
+						if (r < n && intersectTriangle(a, b, c, f.o, sp.wt(r), best[r].t, t) && closerHit(t, inst, first + k, best[r])) {
+							best[r].t = t;
+							best[r].inst = inst;
+							best[r].tri = first + k;
+						}
+					}
+				}
+			}
+		}
+		uint32_t groupBase = childBase, groupMask = imask, hits = internalHits;
+		bool enterRoot = false;
+		while (hits == 0) {
+			if (st.size() == base) {
+				return;
+			}
+			uint32_t a, b;
+			st.pop(a, b);
+			if (b == kLeaveInstance) {
+				setPacketFrame<P>(f, oW, nullptr, sp, grp);
+				nodes = sc.tlas;
+				leaves = sc.tlasLeaves;
+				inst = -1;
+			} else if (b == kEnterInstance) {
+				const InstanceRec& ir = load.instance(sc.instances, (int32_t) a);
+				st.push(0u, kLeaveInstance);
+				setPacketFrame<P>(f, ir.worldToObject.point(oW), &ir.worldToObject, sp, grp);
+				nodes = ir.nodes;
+				leaves = ir.tris;
+				inst = (int32_t) a;
+				enterRoot = true;
+				break;
+			} else {
+				groupBase = a;
+				groupMask = b & 0xffu;
+				hits = b >> 8;
+			}
+		}
+		if (enterRoot) {
+			node = 0;
+			continue;
+		}
+		const uint32_t s = lowestBit(hits) ^ f.ordOct;
+		hits &= hits - 1u;
+		if (hits) {
+			st.push(groupBase, groupMask | (hits << 8));
+		}
+		node = groupBase + (uint32_t) popc8(groupMask & ((1u << s) - 1u));
+	}
+}
+
+template<int P>
+struct HostPacketScratch
+{
+	Vec3 d[P];
+	Watertight w[P];
+	Vec3 dir(int r) const { return d[r]; }
+	void setDir(int r, Vec3 v) { d[r] = v; }
+	Watertight wt(int r) const { return w[r]; }
+	void setWt(int r, const Watertight& x) { w[r] = x; }
+};
+
+// Casts groups of `group` consecutive rays (same origin) as packets; returns false on stack overflow.
+template<int P>
+bool castPackets(const SceneView& sv, int nRays, int group, const float* rays, HitRec* out)
+{
+	HostLoader ld;
+	for (int g0 = 0; g0 < nRays; g0 += group) {
+		const int n = std::min(group, nRays - g0);
+		HostPacketScratch<P> sp;
+		for (int r = 0; r < P; ++r) {
+			const float* p = rays + 7 * (g0 + (r < n ? r : 0));
+			sp.setDir(r, v3(p[3], p[4], p[5]));
+		}
+		const float* p0 = rays + 7 * g0;
+		HostStack st;
+		HitRec h[P];
+		traceClosestPacket<P>(sv, v3(p0[0], p0[1], p0[2]), n, p0[6], st, ld, sp, SoloGroup{}, h);
+		if (st.overflow) {
+			return false;
+		}
+		for (int r = 0; r < n; ++r) {
+			out[g0 + r] = h[r];
+		}
+	}
+	return true;
+}
+
 } // namespace
 
 extern "C" {
@@ -254,6 +497,11 @@ void harness_work_counters(long* out)
 	out[2] = gInstLoads;
 	out[3] = gTlasVisits;
 }
+
+// 0: every ray alone (traceClosest); g in 1..8: groups of g consecutive rays, which must share their
+// origin and tmax, walk together (traceClosestPacket with the packet size the device uses for g).
+int gPacketGroup = 0;
+void harness_set_packet_group(int g) { gPacketGroup = g; }
 
 // Builds BLASes for `nMeshes` meshes and a TLAS over `nInst` instances, then casts `nRays` world
 // rays (origin, direction, tmax: 7 floats each). Outputs per ray: t, instance, original triangle id.
@@ -310,6 +558,20 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	gTotalNodeVisits = 0;
 	gTriTests = gBinLoads = gInstLoads = gTlasVisits = 0;
 	gMaxStackDepth = 0;
+	if (gPacketGroup > 0) {
+		gNodeVisits = 0;
+		std::vector<HitRec> hits(nRays);
+		const bool ok = gPacketGroup <= 4 ? castPackets<4>(sv, nRays, gPacketGroup, rays, hits.data())
+		                : gPacketGroup == 5 ? castPackets<5>(sv, nRays, gPacketGroup, rays, hits.data())
+		                                    : castPackets<8>(sv, nRays, gPacketGroup, rays, hits.data());
+		gTotalNodeVisits = gNodeVisits;
+		for (int r = 0; r < nRays; ++r) {
+			outT[r] = hits[r].t;
+			outInst[r] = hits[r].inst;
+			outPrim[r] = hits[r].inst >= 0 ? inst[hits[r].inst].tris[hits[r].tri].primId : -1;
+		}
+		return ok ? (nMeshes > 0 ? (int) blas[0].wide.size() : 0) : -1;
+	}
 	for (int r = 0; r < nRays; ++r) {
 		const float* p = rays + 7 * r;
 		HostStack st;

@@ -163,8 +163,8 @@ def test_entity_id_limit(rgl):
 
 def test_not_implemented_calls_are_recoverable(rgl):
     n = rgl.node()
-    ids = np.array([1, 2], np.int32)
-    assert rgl.lib().rgl_node_rays_set_ring_ids(C.byref(n), rgl.ptr(ids), 2) == rgl.RGL_NOT_IMPLEMENTED
+    up = np.array([0, 0, 1], np.float32)
+    assert rgl.lib().rgl_node_points_filter_ground(C.byref(n), rgl.ptr(up), 0.3) == rgl.RGL_NOT_IMPLEMENTED
     # the library keeps working afterwards
     rgl.raytrace(rgl.node())
 

@@ -148,6 +148,30 @@ def test_batched_frame_equals_solo_runs(rgl, sched):
     rgl.batch_destroy(batch)
 
 
+MIXED_SCHEDULES = [
+    dict(autotune=False, block=256, packing=0, order=1, chunk=1, regs=80),
+    dict(autotune=False, block=128, packing=1, order=0, chunk=2, regs=96),
+    dict(autotune=False, block=64, packing=0, order=2, chunk=4, regs=64),
+]
+
+
+@pytest.mark.parametrize("sched", MIXED_SCHEDULES, ids=lambda s: f"b{s['block']}-p{s['packing']}-o{s['order']}-c{s['chunk']}-r{s['regs']}")
+def test_mixed_sample_counts_batch_equals_solo_runs(rgl, sched):
+    """Sensors of 1 and 5 samples in one launch (lane groups of 1 and 5 lanes walking the scene
+    together, or one lane per beam) write what their solo runs write."""
+    scene = small_multi_entity_scene()
+    rgl.spawn_scene(scene)
+    cfgs = [SENSORS[k] for k in (0, 1, 4, 5)]
+    graphs = [make_graph(rgl, cfg, sensor_pose(k)) for k, cfg in enumerate(cfgs)]
+    batch = rgl.batch_create([g["rays"] for g in graphs])
+    rgl.batch_configure_schedule(batch, **sched)
+    reseed(rgl, graphs)
+    rgl.batch_run(batch)
+    batched = [collect(rgl, g) for g in graphs]
+    assert_same(rgl, batched, solo_results(rgl, graphs))
+    rgl.batch_destroy(batch)
+
+
 def test_repose_frames_equal_solo_runs(rgl):
     scene, ents, graphs, batch = build_batch(rgl)
     rng = np.random.default_rng(9)

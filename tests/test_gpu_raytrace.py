@@ -7,6 +7,7 @@ Tolerances: hit/miss and entity id exact except on rays the oracle flags as ambi
 relative of an edge or range bound), distance within 1e-5 relative, XYZ within 1e-5 of the
 coordinate magnitude.
 """
+import ctypes as C
 import json
 import math
 import os
@@ -242,3 +243,134 @@ def test_parity_million_scene_dual_return_5_subrays(rgl, oracle):
                        [[0.1, 100.0]], rgl.RGL_RETURN_FIRST_LAST, h_div=math.radians(0.2), v_div=math.radians(0.2),
                        layers=1, vertices=4)
     _check(rgl, got, exp)
+
+
+@pytest.mark.parametrize("layers,vertices", [(1, 4), (1, 7), (1, 2)])
+def test_union_and_single_ray_traversals_agree(rgl, layers, vertices):
+    """Lane groups (a beam's sub-rays on adjacent lanes walking the union of their nodes) and one lane
+    per beam (each sub-ray alone) give byte-identical points: the closest-hit order does not depend on
+    the traversal."""
+    scene = scenes.million_scene(seed=3, instances=30, spheres=3, cells=128, extent=150.0)
+    rgl.spawn_scene(scene)
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], scenes.lidar_rays(32, 360))
+    rgl.rays_transform(n["pose"], scenes.translation(3.0, -2.0, 6.0))
+    rgl.raytrace(n["trace"])
+    lib = rgl.lib()
+    rgl.check(lib.rgl_node_raytrace_configure_return_mode(n["trace"], rgl.RGL_RETURN_FIRST_LAST))
+    rgl.check(lib.rgl_node_raytrace_configure_beam_divergence(n["trace"], math.radians(0.4), math.radians(0.4)))
+    rgl.configure_beam_samples(n["trace"], layers, vertices)
+    fields = [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32,
+              rgl.RGL_FIELD_NORMAL_VEC3_F32]
+    rgl.points_yield(n["out"], fields)
+    rgl.chain(n["rays"], n["pose"], n["trace"], n["out"])
+    got = {}
+    for packing, regs in ((0, 80), (1, 128), (0, 96), (1, 64)):
+        rgl.check(lib.rgl_gb300_configure_trace_schedule(256, packing, 1, regs))
+        rgl.graph_run(n["rays"])
+        got[(packing, regs)] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
+    rgl.check(lib.rgl_gb300_configure_trace_schedule(256, 0, 1, 80))
+    ref = got[(1, 128)]
+    for k, v in got.items():
+        assert v == ref, f"schedule {k} differs from single-ray traversal"
+
+
+def _beam_field_graph(rgl, rays, pose, fields, ring_ids=None, offsets=None):
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], rays)
+    rgl.rays_transform(n["pose"], pose)
+    chain = [n["rays"], n["pose"]]
+    lib = rgl.lib()
+    if ring_ids is not None:
+        n["ring"] = rgl.node()
+        ids = np.ascontiguousarray(ring_ids, dtype=np.int32)
+        rgl.check(lib.rgl_node_rays_set_ring_ids(C.byref(n["ring"]), rgl.ptr(ids), len(ids)))
+        chain.append(n["ring"])
+    if offsets is not None:
+        n["off"] = rgl.node()
+        o = np.ascontiguousarray(offsets, dtype=np.float32)
+        rgl.check(lib.rgl_node_rays_set_time_offsets(C.byref(n["off"]), rgl.ptr(o), len(o)))
+        chain.append(n["off"])
+    rgl.raytrace(n["trace"])
+    rgl.points_yield(n["out"], fields)
+    rgl.chain(*chain, n["trace"], n["out"])
+    return n
+
+
+def test_azimuth_elevation_ring_ids_match_oracle(rgl, oracle):
+    """Fields a beam's returns share (reference optixPrograms.cu:288-326): azimuth and elevation of the
+    sensor-frame ray pose, ring id = ids[beam % count], time stamps 0 without velocity distortion."""
+    cube = scenes.cube_mesh(2.0)
+    e = rgl.entity_create(rgl.mesh_create(cube.vertices, cube.indices))
+    rgl.entity_set_transform(e, scenes.translation(0, 0, 5))
+    rays = scenes.lidar_rays(16, 90)
+    pose = scenes.trs((1.0, -2.0, 0.5), (0.1, -0.2, 0.7))
+    ids = np.arange(16, dtype=np.int32) * 7 + 70000  # wraps in uint16
+    fields = [rgl.RGL_FIELD_AZIMUTH_F32, rgl.RGL_FIELD_ELEVATION_F32, rgl.RGL_FIELD_RING_ID_U16, rgl.RGL_FIELD_TIME_STAMP_U32,
+              rgl.RGL_FIELD_RAY_IDX_U32]
+    n = _beam_field_graph(rgl, rays, pose, fields, ring_ids=ids)
+    rgl.check(rgl.lib().rgl_node_raytrace_configure_return_mode(n["trace"], rgl.RGL_RETURN_FIRST_LAST))
+    rgl.graph_run(n["rays"])
+    world = oracle.transform_rays(pose, rays)
+    exp = oracle.beam_shared_fields(world, pose, return_count=2, ring_ids=ids)
+    az, el = rgl.result(n["out"], rgl.RGL_FIELD_AZIMUTH_F32), rgl.result(n["out"], rgl.RGL_FIELD_ELEVATION_F32)
+    assert az.shape == (2 * len(rays),)
+    assert np.abs(az - exp["azimuth"]).max() <= 1e-5
+    assert np.abs(el - exp["elevation"]).max() <= 1e-5
+    assert np.array_equal(rgl.result(n["out"], rgl.RGL_FIELD_RING_ID_U16), exp["ring_id"])
+    assert not rgl.result(n["out"], rgl.RGL_FIELD_TIME_STAMP_U32).any()
+    assert np.array_equal(rgl.result(n["out"], rgl.RGL_FIELD_RAY_IDX_U32), np.repeat(np.arange(len(rays), dtype=np.uint32), 2))
+
+
+def test_beam_field_pipeline_errors(rgl):
+    rays = scenes.lidar_rays(4, 10)
+    n = _beam_field_graph(rgl, rays, scenes.translation(0, 0, 0), [rgl.RGL_FIELD_RING_ID_U16])
+    with pytest.raises(rgl.RGLError) as e:
+        rgl.graph_run(n["rays"])
+    assert e.value.status == rgl.RGL_INVALID_PIPELINE and "cannot get ring ids" in str(e.value)
+    n = _beam_field_graph(rgl, rays, scenes.translation(0, 0, 0), [rgl.RGL_FIELD_RING_ID_U16], ring_ids=np.arange(3))
+    with pytest.raises(rgl.RGLError) as e:
+        rgl.graph_run(n["rays"])
+    assert e.value.status == rgl.RGL_INVALID_PIPELINE and "ring ids doesn't match number of rays" in str(e.value)
+    n = _beam_field_graph(rgl, rays, scenes.translation(0, 0, 0), [rgl.RGL_FIELD_DISTANCE_F32], offsets=np.zeros(7))
+    with pytest.raises(rgl.RGLError) as e:
+        rgl.graph_run(n["rays"])
+    assert e.value.status == rgl.RGL_INVALID_PIPELINE and "time offsets don't match number of rays" in str(e.value)
+    n = _beam_field_graph(rgl, rays, scenes.translation(0, 0, 0), [rgl.RGL_FIELD_TIME_STAMP_F64], offsets=np.zeros(40))
+    with pytest.raises(rgl.RGLError) as e:
+        rgl.graph_run(n["rays"])
+    assert e.value.status == rgl.RGL_INVALID_PIPELINE and "cannot get time from scene" in str(e.value)
+    rgl.check(rgl.lib().rgl_scene_set_time(None, 1_000_000))
+    rgl.graph_run(n["rays"])
+    assert not rgl.result(n["out"], rgl.RGL_FIELD_TIME_STAMP_F64).any()
+
+
+def test_laser_retro_of_hit_entity(rgl, oracle):
+    scene = scenes.million_scene(seed=4, instances=10, spheres=2, cells=32, extent=60.0)
+    _, ents = rgl.spawn_scene(scene)
+    retro = {e.entity_id: 0.05 * (k + 1) for k, e in enumerate(scene.entities)}
+    for h, e in zip(ents, scene.entities):
+        rgl.check(rgl.lib().rgl_entity_set_laser_retro(h, retro[e.entity_id]))
+    rays = scenes.lidar_rays(32, 256)
+    pose = scenes.translation(0, 0, 6.0)
+    n = _beam_field_graph(rgl, rays, pose, [rgl.RGL_FIELD_LASER_RETRO_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32])
+    rgl.graph_run(n["rays"])
+    got = rgl.result(n["out"], rgl.RGL_FIELD_LASER_RETRO_F32)
+    ent = rgl.result(n["out"], rgl.RGL_FIELD_ENTITY_ID_I32)
+    hit = rgl.result(n["out"], rgl.RGL_FIELD_IS_HIT_I32) == 1
+    exp = oracle.OracleScene(scene).raytrace(rays, ray_transform=pose, ranges=[[0.0, 1e30]])
+    ok = ~(exp["ambiguous"] != 0)
+    assert np.array_equal(ent[ok], exp["entity_id"][ok])
+    want = np.array([retro.get(int(x), 0.0) for x in exp["entity_id"]], np.float32)
+    assert np.array_equal(got[ok & hit], want[ok & hit])
+    assert not got[~hit].any()
+    # A new value reaches the next run (on the entity hit most often).
+    ids, counts = np.unique(ent[hit], return_counts=True)
+    top = int(ids[np.argmax(counts)])
+    k = [e.entity_id for e in scene.entities].index(top)
+    rgl.check(rgl.lib().rgl_entity_set_laser_retro(ents[k], 0.9))
+    rgl.graph_run(n["rays"])
+    got2 = rgl.result(n["out"], rgl.RGL_FIELD_LASER_RETRO_F32)
+    sel = (rgl.result(n["out"], rgl.RGL_FIELD_ENTITY_ID_I32) == top) & hit
+    assert sel.any() and np.all(got2[sel] == np.float32(0.9))
+    assert np.array_equal(got2[hit & ~sel], got[hit & ~sel])

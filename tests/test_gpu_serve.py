@@ -233,3 +233,30 @@ def test_batches_of_varying_size_complete_and_host_results_match(rgl):
         assert srv.stats()["failed"] == 0
     finally:
         srv.destroy()
+
+
+def test_server_schedule_changes_speed_only(rgl):
+    """Natural and octahedral beam order, other block/register shapes and batches capped at a few
+    thousand beams (every request its own batch) give byte-identical results."""
+    (sa, _), (sb, _) = two_scenes(rgl)
+    srv = rgl.Server(8 << 30, 2)
+    try:
+        pats = [srv.add_pattern(pattern_rays(p)) for p in PATTERNS]
+        specs = [(sa if k % 2 else sb, pats[k % len(pats)], pose(300 + k), rgl.RGL_RETURN_FIRST_LAST if k % 3 else rgl.RGL_RETURN_FIRST)
+                 for k in range(16)]
+        runs = []
+        for sched in (dict(), dict(order=0), dict(block=128, regs=64, chunk=4), dict(order=2, regs=128, max_batch_beams=4096)):
+            srv.configure_schedule(**sched)
+            reqs = [srv.submit(sc, p, tf, mode, 0.1, 90.0) for sc, p, tf, mode in specs]
+            for r in reqs:
+                assert srv.wait(r, 20000.0)
+            runs.append([served(rgl, srv, r) for r in reqs])
+            for r in reqs:
+                srv.release(r)
+        for other in runs[1:]:
+            assert other == runs[0]
+        with pytest.raises(rgl.RGLError) as e:
+            srv.configure_schedule(block=96)
+        assert e.value.status == rgl.RGL_INVALID_ARGUMENT
+    finally:
+        srv.destroy()
