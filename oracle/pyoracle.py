@@ -245,3 +245,75 @@ def beam_shared_fields(rays_world, sensor_to_world, return_count=1, ring_ids=Non
         ids = np.asarray(ring_ids, dtype=np.int64)
         out["ring_id"] = np.repeat(ids[np.arange(rays.shape[0]) % len(ids)].astype(np.uint16), return_count)
     return out
+
+
+# ---------------------------------------------------------------- velocities and velocity distortion (FP64)
+
+def hit_velocities(hit_world, entity_now, entity_prev, dt, sensor_to_world, lin_vel, ang_vel):
+    """Velocities of hit points (reference src/gpu/optixPrograms.cu:169-212): the point fixed in its
+    entity moves from entity_prev @ p_obj to entity_now @ p_obj over dt (entity_prev None: no known
+    previous pose, zero displacement); relative velocity = that velocity in the sensor frame minus the
+    sensor's linear velocity minus angular x (hit in the sensor frame); radial speed = its component
+    along the sensor-to-hit direction. Per point arrays: entity_now / entity_prev are (n, 3, 4)."""
+    n = len(hit_world)
+    absv = np.zeros((n, 3))
+    for i in range(n):
+        now = mat4(entity_now[i])
+        p_obj = np.linalg.solve(now, np.append(np.asarray(hit_world[i], np.float64), 1.0))
+        if entity_prev[i] is not None:
+            absv[i] = (now @ p_obj - mat4(entity_prev[i]) @ p_obj)[:3] / dt
+    s2w = mat4(sensor_to_world)
+    rot_inv = np.linalg.inv(s2w[:3, :3])
+    hit_s = (np.linalg.inv(s2w) @ np.c_[np.asarray(hit_world, np.float64), np.ones(n)].T).T[:, :3]
+    rel = (rot_inv @ absv.T).T - np.asarray(lin_vel, np.float64) - np.cross(np.asarray(ang_vel, np.float64), hit_s)
+    radial = np.einsum("ij,ij->i", hit_s / np.linalg.norm(hit_s, axis=1, keepdims=True), rel)
+    return absv, rel, radial
+
+
+def distort_rays(rays_world, sensor_to_world, offsets_ms, lin_vel, ang_vel):
+    """Ray poses under velocity distortion (reference src/gpu/optixPrograms.cu:60-70): in the sensor
+    frame each ray is moved by translation offset*lin/1000 and rotation Rz Ry Rx of offset*ang/1000
+    rad, then returned to the world frame."""
+    s2w = mat4(sensor_to_world)
+    w2s = np.linalg.inv(s2w)
+    out = np.zeros((len(rays_world), 3, 4))
+    for i, r in enumerate(np.asarray(rays_world, np.float64).reshape(-1, 3, 4)):
+        t = offsets_ms[i] * np.asarray(lin_vel, np.float64) * 1e-3
+        rx, ry, rz = offsets_ms[i] * np.asarray(ang_vel, np.float64) * 1e-3
+        cx, sx, cy, sy, cz, sz = np.cos(rx), np.sin(rx), np.cos(ry), np.sin(ry), np.cos(rz), np.sin(rz)
+        R = (np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]]) @ np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+             @ np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]]))
+        m = np.eye(4)
+        m[:3, :3] = R
+        m[:3, 3] = t
+        out[i] = (s2w @ m @ w2s @ mat4(r))[:3, :]
+    return out.astype(np.float32)
+
+
+# ---------------------------------------------------------------- mesh animation (FP64)
+
+def skinned_vertices(rest, weights, bones, pose, restposes):
+    """Linear blend skinning (reference src/gpu/sceneKernels.cu:17-38): vertex i moves to
+    sum_k weights[i, k] * (pose[b] @ restposes[b]) @ rest[i] with b = bones[i, k]."""
+    rest = np.asarray(rest, np.float64)
+    mats = [mat4(p) @ mat4(r) for p, r in zip(pose, restposes)]
+    out = np.zeros_like(rest)
+    for i, v in enumerate(rest):
+        for k in range(4):
+            if weights[i][k] != 0.0:
+                out[i] += weights[i][k] * (mats[bones[i][k]] @ np.append(v, 1.0))[:3]
+    return out.astype(np.float32)
+
+
+def animation_velocity(hit_world, entity_tf, tri_vertices, tri_displacements, dt):
+    """Velocity of a hit on an animated mesh whose pose did not change (reference
+    src/gpu/optixPrograms.cu:185-195): the triangle's vertex displacements since the previous step,
+    rotated into the world and interpolated at the hit's barycentric coordinates, over dt."""
+    m = mat4(entity_tf)
+    p = (np.linalg.inv(m) @ np.append(np.asarray(hit_world, np.float64), 1.0))[:3]
+    a, b, c = (np.asarray(x, np.float64) for x in tri_vertices)
+    n = np.cross(b - a, c - a)
+    u = np.dot(np.cross(p - a, c - a), n) / np.dot(n, n)
+    w = np.dot(np.cross(b - a, p - a), n) / np.dot(n, n)
+    da, db, dc = (m[:3, :3] @ np.asarray(x, np.float64) for x in tri_displacements)
+    return ((1 - u - w) * da + u * db + w * dc) / dt

@@ -360,22 +360,28 @@ RGL_API rgl_status_t rgl_mesh_set_texture_coords(rgl_mesh_t mesh, const rgl_vec2
 
 RGL_API rgl_status_t rgl_mesh_set_bone_weights(rgl_mesh_t mesh, const rgl_bone_weights_t* bone_weights, int32_t bone_weights_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(mesh != nullptr);
 		CHECK_ARG(bone_weights != nullptr);
 		CHECK_ARG(bone_weights_count > 0);
-		notImplemented("rgl_mesh_set_bone_weights");
+		GraphRunCtx::synchronizeAll();
+		Meshes::get(mesh, "Mesh")->setBoneWeights(bone_weights, bone_weights_count);
 	});
+	RGL_TAPE_RECORD(T::handle(mesh), T::arr(bone_weights, bone_weights_count), T::num(bone_weights_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_mesh_set_restposes(rgl_mesh_t mesh, const rgl_mat3x4f* restposes, int32_t bones_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(mesh != nullptr);
 		CHECK_ARG(restposes != nullptr);
 		CHECK_ARG(bones_count > 0);
-		notImplemented("rgl_mesh_set_restposes");
+		GraphRunCtx::synchronizeAll();
+		Meshes::get(mesh, "Mesh")->setRestposes(restposes, bones_count);
 	});
+	RGL_TAPE_RECORD(T::handle(mesh), T::arr(restposes, bones_count), T::num(bones_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_mesh_destroy(rgl_mesh_t mesh)
@@ -444,12 +450,17 @@ RGL_API rgl_status_t rgl_entity_set_transform(rgl_entity_t entity, const rgl_mat
 
 RGL_API rgl_status_t rgl_entity_set_pose_world(rgl_entity_t entity, const rgl_mat3x4f* pose, int32_t bones_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
 		CHECK_ARG(pose != nullptr);
 		CHECK_ARG(bones_count > 0);
-		notImplemented("rgl_entity_set_pose_world (skeletal animation)");
+		// The entity's BLAS is rebuilt in place: nothing may still be reading it.
+		GraphRunCtx::synchronizeAll();
+		RGL_CHECK_CUDA(cudaDeviceSynchronize());
+		Entities::get(entity, "Entity")->setPoseAndAnimate(pose, bones_count);
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::arr(pose, bones_count), T::num(bones_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_set_id(rgl_entity_t entity, int32_t id)
@@ -486,12 +497,16 @@ RGL_API rgl_status_t rgl_entity_set_laser_retro(rgl_entity_t entity, float retro
 
 RGL_API rgl_status_t rgl_entity_apply_external_animation(rgl_entity_t entity, const rgl_vec3f* vertices, int32_t vertex_count)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
 		CHECK_ARG(vertices != nullptr);
 		CHECK_ARG(vertex_count > 0);
-		notImplemented("rgl_entity_apply_external_animation");
+		GraphRunCtx::synchronizeAll();
+		RGL_CHECK_CUDA(cudaDeviceSynchronize());
+		Entities::get(entity, "Entity")->applyExternalAnimation(vertices, vertex_count);
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::arr(vertices, vertex_count), T::num(vertex_count));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_is_alive(rgl_entity_t entity, bool* out_alive)
@@ -539,9 +554,7 @@ RGL_API rgl_status_t rgl_scene_set_time(rgl_scene_t scene, uint64_t nanoseconds)
 {
 	const rgl_status_t status = safeCall([&]() {
 		GraphRunCtx::synchronizeAll();
-		auto sc = sceneOf(scene);
-		sc->timeNs = nanoseconds;
-		sc->timeSet = true;
+		sceneOf(scene)->setTime(nanoseconds);
 	});
 	RGL_TAPE_RECORD(T::handle(scene), T::unum(nanoseconds));
 	return status;
@@ -769,9 +782,12 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_velocity(rgl_node_t node, const
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(linear_velocity != nullptr);
 		CHECK_ARG(angular_velocity != nullptr);
-		getNodeAs<RaytraceNode>(node, "RaytraceNode");
-		// Velocity only feeds velocity/distortion fields, which this build does not compute; the
-		// configuration is accepted and has no effect on the computed fields.
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setVelocity(rgl::v3(linear_velocity->value[0], linear_velocity->value[1], linear_velocity->value[2]),
+		               rgl::v3(angular_velocity->value[0], angular_velocity->value[1], angular_velocity->value[2]));
 	});
 	RGL_TAPE_RECORD(T::handle(node), T::arr(linear_velocity, 1), T::arr(angular_velocity, 1));
 	return status;
@@ -781,10 +797,11 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_distortion(rgl_node_t node, boo
 {
 	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
-		getNodeAs<RaytraceNode>(node, "RaytraceNode");
-		if (enable) {
-			notImplemented("velocity distortion");
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
 		}
+		n->setDistortion(enable);
 	});
 	RGL_TAPE_RECORD(T::handle(node), T::flag(enable));
 	return status;

@@ -114,7 +114,7 @@ void BatchRun::buildJobs()
 		b.samples = members[j].trace->sampleTableDev();
 		b.order = nullptr;
 		b.groupSize = std::min(p.nSamples, 32);
-		shading = shading || p.needIntensity != 0 || p.out.normal != nullptr || p.out.incidentAngle != nullptr;
+		shading = shading || rgl::needsShadingKernel(p);
 		maxSamples = std::max(maxSamples, (int) p.nSamples);
 		beamBase[j] = beams;
 		beams += p.nRays;

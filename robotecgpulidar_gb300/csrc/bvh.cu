@@ -4,13 +4,15 @@
 // Replaces the OptiX acceleration-structure builds of reference src/scene/GASBuilder.hpp:31-100 and
 // src/scene/Scene.cpp:131-190 (where any pose change triggers a full IAS rebuild plus a stream sync).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "bvh_core.hpp"
 #include "kernels.hpp"
-#include "tlas_sah.hpp"
+#include "sah_build.hpp"
 
 namespace rgl {
 
@@ -290,10 +292,16 @@ void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, i
 	float4* lo = mallocAsync<float4>(T, s);
 	float4* hi = mallocAsync<float4>(T, s);
 	uint32_t* cb = mallocAsync<uint32_t>(8, s);
-	out.nodeCapacity = (uint32_t) T;
+	// A rebuild (an animated entity) reuses the previous storage when it is large enough.
+	if (out.nodes == nullptr || out.nodeCapacity < (uint32_t) T) {
+		if (out.nodes != nullptr) {
+			freeBlas(out);
+		}
+		RGL_CUDA_OK(cudaMalloc(&out.nodes, sizeof(WideNode) * (size_t) T));
+		RGL_CUDA_OK(cudaMalloc(&out.tris, sizeof(TriRecord) * (size_t) T));
+		out.nodeCapacity = (uint32_t) T;
+	}
 	out.triCount = T;
-	RGL_CUDA_OK(cudaMalloc(&out.nodes, sizeof(WideNode) * (size_t) T));
-	RGL_CUDA_OK(cudaMalloc(&out.tris, sizeof(TriRecord) * (size_t) T));
 	uint32_t cbInit[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
 	RGL_CUDA_OK(cudaMemcpyAsync(cb, cbInit, sizeof(cbInit), cudaMemcpyHostToDevice, s));
 	kTriBounds<<<blocks(T, 256), 256, 0, s>>>(dVertices, dIndices, T, lo, hi, cb);
@@ -306,6 +314,67 @@ void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, i
 	out.bounds[3] = r.bounds.hix;
 	out.bounds[4] = r.bounds.hiy;
 	out.bounds[5] = r.bounds.hiz;
+}
+
+void buildBlasHost(const float* hVertices, int nVertices, const int32_t* hIndices, int nTris, BlasBuild& out)
+{
+	(void) nVertices;
+	if (nTris <= 0) {
+		throw std::invalid_argument("mesh without triangles");
+	}
+	const int T = nTris;
+	std::vector<Box> boxes(T);
+	std::vector<float4> lo(T), hi(T);
+	for (int t = 0; t < T; ++t) {
+		const float* a = hVertices + 3 * hIndices[3 * t];
+		const float* b = hVertices + 3 * hIndices[3 * t + 1];
+		const float* c = hVertices + 3 * hIndices[3 * t + 2];
+		Box bx{std::min(a[0], std::min(b[0], c[0])), std::min(a[1], std::min(b[1], c[1])), std::min(a[2], std::min(b[2], c[2])),
+		       std::max(a[0], std::max(b[0], c[0])), std::max(a[1], std::max(b[1], c[1])), std::max(a[2], std::max(b[2], c[2]))};
+		boxes[t] = bx;
+		lo[t] = make_float4(bx.lox, bx.loy, bx.loz, 0.0f);
+		hi[t] = make_float4(bx.hix, bx.hiy, bx.hiz, 0.0f);
+	}
+	const SahTree tree = buildBinnedSahTree(boxes);
+	std::vector<WideNode> wide(T);
+	std::vector<TriRecord> tris(T);
+	uint32_t wideCounter = 1, triCounter = 0;
+	std::vector<int2> qa(T), qb(T);
+	uint32_t qaCount = 1, qbCount = 0;
+	qa[0] = make_int2(T == 1 ? ~0 : 0, 0);
+	CollapseInputs in{tree.bin.data(), tree.rangeFirst.data(), tree.rangeLast.data(), tree.sortedIds.data(), lo.data(), hi.data(),
+	                  hVertices, hIndices, kLeafMaxTris};
+	while (qaCount > 0) {
+		qbCount = 0;
+		CollapseOutputs o{wide.data(), tris.data(), &wideCounter, &triCounter, qb.data(), &qbCount, nullptr};
+		for (uint32_t i = 0; i < qaCount; ++i) {
+			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
+		}
+		std::swap(qa, qb);
+		qaCount = qbCount;
+	}
+	if (triCounter != (uint32_t) T || wideCounter > (uint32_t) T) {
+		throw std::runtime_error("BLAS build: collapse produced an inconsistent tree");
+	}
+	if (out.nodes == nullptr || out.nodeCapacity < (uint32_t) T) {
+		if (out.nodes != nullptr) {
+			freeBlas(out);
+		}
+		RGL_CUDA_OK(cudaMalloc(&out.nodes, sizeof(WideNode) * (size_t) T));
+		RGL_CUDA_OK(cudaMalloc(&out.tris, sizeof(TriRecord) * (size_t) T));
+		out.nodeCapacity = (uint32_t) T;
+	}
+	RGL_CUDA_OK(cudaMemcpy(out.nodes, wide.data(), sizeof(WideNode) * wideCounter, cudaMemcpyHostToDevice));
+	RGL_CUDA_OK(cudaMemcpy(out.tris, tris.data(), sizeof(TriRecord) * (size_t) T, cudaMemcpyHostToDevice));
+	out.nodeCount = wideCounter;
+	out.triCount = T;
+	const Box root = T == 1 ? boxes[0] : Box{tree.bin[0].lox, tree.bin[0].loy, tree.bin[0].loz, tree.bin[0].hix, tree.bin[0].hiy, tree.bin[0].hiz};
+	out.bounds[0] = root.lox;
+	out.bounds[1] = root.loy;
+	out.bounds[2] = root.loz;
+	out.bounds[3] = root.hix;
+	out.bounds[4] = root.hiy;
+	out.bounds[5] = root.hiz;
 }
 
 void freeBlas(BlasBuild& b)
@@ -365,7 +434,7 @@ __global__ void __launch_bounds__(256) kRefitTlas(WideNode* nodes, const TriReco
 
 // The TLAS is a wide BVH over the instances' world boxes, one instance per leaf child. Its topology is
 // built on the host by a full sweep SAH over the (few) instance boxes and collapsed with the BLAS
-// collapse (tlas_sah.hpp); node depths (contiguous per depth: the collapse allocates nodes level by
+// collapse (sah_build.hpp); node depths (contiguous per depth: the collapse allocates nodes level by
 // level) drive the refit kernel, which keeps the topology on pose changes.
 void buildTlas(const InstanceRec* hInst, int n, TlasBuild& t, cudaStream_t s)
 {

@@ -75,10 +75,13 @@ struct alignas(16) InstanceRec
 	const WideNode* nodes;     // BLAS of the entity's mesh
 	const TriRecord* tris;
 	int32_t entityId;
-	int32_t blasRootIsLeaf;    // unused by traversal, kept for alignment/debug
+	int32_t hasPrev;           // prevObjectToWorld holds the pose of the scene's previous time step
 	float lox, loy, loz, hix, hiy, hiz; // world-space box (TLAS leaf bounds)
 	float laserRetro;          // rgl_entity_set_laser_retro
 	int32_t pad;
+	Mat34 prevObjectToWorld;   // 48 B, for hit-point velocities
+	const float* vertexDisplacement; // animated entity: per-vertex motion since the previous time step, or null
+	const int32_t* indices;          // the mesh's triangle vertex indices (with vertexDisplacement)
 };
 
 // Device view of a scene, read by the traversal kernel through one pointer so a captured CUDA graph
@@ -130,6 +133,9 @@ struct TraceOutputs
 	float* elevation;
 	double* timeStampF64;
 	uint32_t* timeStampU32;
+	float* absVelocity;  // 3 floats per point
+	float* relVelocity;  // 3 floats per point
+	float* radialSpeed;
 };
 
 struct TraceParams
@@ -150,8 +156,14 @@ struct TraceParams
 	TraceOutputs out;
 	const int32_t* ringIds;     // rays-set-ring-ids values (beam b gets ringIds[b % nRingIds]), or null
 	int32_t nRingIds;
-	int32_t pad;
-	Mat34 worldToSensor;        // inverse of the rays' cumulative transform (azimuth, elevation)
+	int32_t distortion;         // velocity distortion: rays shifted by their time offset (needs timeOffsetsMs)
+	Mat34 worldToSensor;        // inverse of the rays' cumulative transform (azimuth, elevation, distortion)
+	Mat34 sensorToWorld;        // the rays' cumulative transform
+	Mat34 worldToSensorRotation; // inverse of the rotation part of sensorToWorld
+	const float* timeOffsetsMs; // per ray, or null
+	float sceneDeltaTime;       // seconds between the scene's last two time steps, 0 when unknown
+	Vec3 sensorLinearVelocity;  // rgl_node_raytrace_configure_velocity, sensor frame
+	Vec3 sensorAngularVelocity; // roll, pitch, yaw rates in rad/s
 };
 
 // One sensor (or served request) of a batched traversal launch (trace_batch.cu): its raytrace

@@ -347,7 +347,10 @@ static bool raytraceSupports(rgl_field_t f)
 		case RGL_FIELD_ELEVATION_F32:
 		case RGL_FIELD_RING_ID_U16:
 		case RGL_FIELD_TIME_STAMP_F64:
-		case RGL_FIELD_TIME_STAMP_U32: return true;
+		case RGL_FIELD_TIME_STAMP_U32:
+		case RGL_FIELD_ABSOLUTE_VELOCITY_VEC3_F32:
+		case RGL_FIELD_RELATIVE_VELOCITY_VEC3_F32:
+		case RGL_FIELD_RADIAL_SPEED_F32: return true;
 		default: return false;
 	}
 }
@@ -400,6 +403,9 @@ void RaytraceNode::validateImpl()
 	}
 	if (fields.count(RGL_FIELD_TIME_STAMP_F64) && !scene->timeSet) {
 		throw InvalidPipeline("requested for field TIME_STAMP_F64, but RaytraceNode cannot get time from scene");
+	}
+	if (distortion && rays->timeOffsetsDev() == nullptr) {
+		throw InvalidPipeline("requested for raytrace with velocity distortion, but RaytraceNode cannot get time offsets");
 	}
 	if (sampleCount() > rgl::kMaxBeamSamples) {
 		throw rgl::InvalidAPIArgument(format("beam sample pattern of %d rays exceeds %d", sampleCount(), rgl::kMaxBeamSamples));
@@ -503,11 +509,21 @@ rgl::TraceParams RaytraceNode::traceParams()
 	p.out.elevation = static_cast<float*>(ptr(RGL_FIELD_ELEVATION_F32));
 	p.out.timeStampF64 = static_cast<double*>(ptr(RGL_FIELD_TIME_STAMP_F64));
 	p.out.timeStampU32 = static_cast<uint32_t*>(ptr(RGL_FIELD_TIME_STAMP_U32));
+	p.out.absVelocity = static_cast<float*>(ptr(RGL_FIELD_ABSOLUTE_VELOCITY_VEC3_F32));
+	p.out.relVelocity = static_cast<float*>(ptr(RGL_FIELD_RELATIVE_VELOCITY_VEC3_F32));
+	p.out.radialSpeed = static_cast<float*>(ptr(RGL_FIELD_RADIAL_SPEED_F32));
 	p.ringIds = rays->ringIdsDev();
 	p.nRingIds = (int32_t) rays->ringIdsCount();
-	if (p.out.azimuth || p.out.elevation) {
-		p.worldToSensor = rgl::inverse(rays->cumulativeRayTransform());
-	}
+	p.sensorToWorld = rays->cumulativeRayTransform();
+	p.worldToSensor = rgl::inverse(p.sensorToWorld);
+	Mat34 rot = p.sensorToWorld;
+	rot.m[0][3] = rot.m[1][3] = rot.m[2][3] = 0.0f;
+	p.worldToSensorRotation = rgl::inverse(rot);
+	p.distortion = distortion ? 1 : 0;
+	p.timeOffsetsMs = rays->timeOffsetsDev();
+	p.sceneDeltaTime = scene->deltaTimeSeconds();
+	p.sensorLinearVelocity = sensorLinearVelocity;
+	p.sensorAngularVelocity = sensorAngularVelocity;
 	return p;
 }
 
@@ -529,7 +545,7 @@ void RaytraceNode::stageJob()
 	tr.base[0] = 0;
 	tr.base[1] = (p.nRays + per - 1) / per;
 	(void) tasks.device();
-	shading = p.needIntensity != 0 || p.out.normal != nullptr || p.out.incidentAngle != nullptr;
+	shading = rgl::needsShadingKernel(p);
 	if (counter.get() == nullptr) {
 		RGL_CHECK_CUDA(cudaMemset(counter.ensure(sizeof(uint32_t)), 0, sizeof(uint32_t)));
 	}

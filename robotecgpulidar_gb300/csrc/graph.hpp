@@ -267,6 +267,12 @@ struct RaytraceNode : PointsNode
 		farDistance = farD;
 	}
 	void setDefaultIntensity(float i) { defaultIntensity = i; }
+	void setVelocity(rgl::Vec3 linear, rgl::Vec3 angular)
+	{
+		sensorLinearVelocity = linear;
+		sensorAngularVelocity = angular;
+	}
+	void setDistortion(bool on) { distortion = on; }
 	int sampleCount() const;
 	void checkErrors() override;
 	std::shared_ptr<Scene> sceneRef; // keeps a scene made by rgl_gb300_scene_create alive
@@ -293,6 +299,8 @@ private:
 	int sampleLayers = 3, sampleVertices = 19; // reference pattern: 1 + 3 * 19 = 58 samples
 	float nearDistance = INFINITY, farDistance = INFINITY;
 	float defaultIntensity = 0.0f;
+	rgl::Vec3 sensorLinearVelocity{0.0f, 0.0f, 0.0f}, sensorAngularVelocity{0.0f, 0.0f, 0.0f};
+	bool distortion = false;
 	rgl::ErrorSlot errorFlag;
 	// The node's traversal as a one-job persistent launch.
 	rgl::StagedParam<rgl::BatchJob> job;

@@ -29,8 +29,12 @@ struct BlasBuild
 	int32_t triCount = 0;
 	float bounds[6] = {0, 0, 0, 0, 0, 0}; // object-space box lo.xyz, hi.xyz (host copy)
 };
-// Builds the BLAS of a mesh (device vertices/indices); synchronises `stream` at the end (one-off).
+// Builds a BLAS on the device from device vertices/indices (Morton LBVH + wide collapse); synchronises
+// `stream` at the end. Used for animated entities, whose BLAS is rebuilt at every animation.
 void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, int nTris, BlasBuild& out, cudaStream_t stream);
+// Builds the BLAS of a mesh on the host from host vertices/indices (binned SAH topology, the same wide
+// collapse) and uploads it; storage of `out` is reused when large enough.
+void buildBlasHost(const float* hVertices, int nVertices, const int32_t* hIndices, int nTris, BlasBuild& out);
 void freeBlas(BlasBuild& b);
 
 struct TlasBuild
@@ -50,6 +54,20 @@ void buildTlas(const InstanceRec* hInstances, int nInstances, TlasBuild& t, cuda
 // Refits the TLAS after instance boxes changed (same instance set): one single-block launch.
 void refitTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);
 void freeTlas(TlasBuild& t);
+
+// ---- animate.cu: mesh animation of entities
+// Four bone influences of a vertex (layout of rgl_bone_weights_t).
+struct BoneWeights
+{
+	float weight[4];
+	int32_t bone[4];
+};
+// Skinned vertices out[i] = sum_k weight_k * (pose[b_k] * restposes[b_k]) * rest[i]; boneMatrices is
+// scratch for nBones matrices. A non-zero weight on a bone outside [0, nBones) raises *errorFlag.
+void launchSkin(int nVertices, const float* restVertices, const BoneWeights* weights, const Mat34* pose, const Mat34* restposes,
+                int nBones, Mat34* boneMatrices, float* out, int32_t* errorFlag, cudaStream_t s);
+// newToDisplacement holds the new vertices and receives new - old; oldToNew receives the new ones.
+void launchUpdateVertices(int nVertices, float* newToDisplacement, float* oldToNew, cudaStream_t s);
 
 // ---- trace_batch.cu: the traversal, one persistent launch over one or many sensors
 constexpr int kMaxBatchJobs = 1024;
@@ -77,6 +95,13 @@ struct TaskRange
 {
 	int32_t base[2];
 };
+// Whether a raytrace needs the SHADING variant of the traversal kernel: intensity, normals, incident
+// angles, velocities or velocity distortion (the plain variant carries none of that code).
+inline bool needsShadingKernel(const TraceParams& p)
+{
+	return p.needIntensity != 0 || p.out.normal != nullptr || p.out.incidentAngle != nullptr || p.out.absVelocity != nullptr ||
+	       p.out.relVelocity != nullptr || p.out.radialSpeed != nullptr || p.distortion != 0;
+}
 // Beams covered by one task (one warp's worth of work) of a sensor with `nSamples` samples.
 int batchBeamsPerTask(int packing, int nSamples);
 // Resolves and caches the launch configuration (occupancy, shared-memory opt-in) of a schedule;

@@ -196,4 +196,28 @@ RGL_HD Mat34 beamSampleRotation(float hAngle, float vAngle)
 	return r;
 }
 
+// Pose of a ray shifted by velocity distortion: translation t times the rotation Rz(z) Ry(y) Rx(x)
+// given in degrees (reference Mat3x4f.hpp:38-97, TRS with unit scale; the entries of the rotation
+// product are evaluated left to right as written there, so host and device agree bit for bit).
+RGL_HD Mat34 translationRotationDeg(Vec3 t, Vec3 rDeg)
+{
+	const float toRad = 3.14159265358979323846f / 180.0f;
+	const float x = fmul(rDeg.x, toRad), y = fmul(rDeg.y, toRad), z = fmul(rDeg.z, toRad);
+	const float cr = cosf(x), sr = sinf(x), cp = cosf(y), sp = sinf(y), cy = cosf(z), sy = sinf(z);
+	Mat34 m;
+	m.m[0][0] = fmul(cp, cy);
+	m.m[0][1] = fsub(fmul(fmul(sr, sp), cy), fmul(cr, sy));
+	m.m[0][2] = fadd(fmul(sr, sy), fmul(fmul(cr, sp), cy));
+	m.m[0][3] = t.x;
+	m.m[1][0] = fmul(cp, sy);
+	m.m[1][1] = fadd(fmul(cr, cy), fmul(fmul(sr, sp), sy));
+	m.m[1][2] = fsub(fmul(fmul(cr, sp), sy), fmul(sr, cy));
+	m.m[1][3] = t.y;
+	m.m[2][0] = -sp;
+	m.m[2][1] = fmul(sr, cp);
+	m.m[2][2] = fmul(cr, cp);
+	m.m[2][3] = t.z;
+	return m;
+}
+
 } // namespace rgl

@@ -21,6 +21,8 @@ Mesh::Mesh(const rgl_vec3f* vertices, int32_t vc, const rgl_vec3i* indices, int3
 	}
 	RGL_CHECK_CUDA(cudaMemcpy(dVertices.ensure(sizeof(rgl_vec3f) * vc), vertices, sizeof(rgl_vec3f) * vc, cudaMemcpyHostToDevice));
 	RGL_CHECK_CUDA(cudaMemcpy(dIndices.ensure(sizeof(rgl_vec3i) * ic), indices, sizeof(rgl_vec3i) * ic, cudaMemcpyHostToDevice));
+	hVertices.assign(&vertices[0].value[0], &vertices[0].value[0] + 3 * (size_t) vc);
+	hIndices.assign(&indices[0].value[0], &indices[0].value[0] + 3 * (size_t) ic);
 }
 
 Mesh::~Mesh()
@@ -30,21 +32,164 @@ Mesh::~Mesh()
 	}
 }
 
+void Mesh::setBoneWeights(const rgl_bone_weights_t* w, int32_t count)
+{
+	if (count != vertexCount) {
+		throw rgl::InvalidAPIArgument(rgl::format("Cannot set bone weights because vertex count do not match with bone weights count: "
+		                                          "vertexCount=%d, boneWeightsCount=%d",
+		                                          (int) vertexCount, (int) count));
+	}
+	RGL_CHECK_CUDA(cudaMemcpy(dBoneWeights.ensure(sizeof(rgl_bone_weights_t) * (size_t) count), w,
+	                          sizeof(rgl_bone_weights_t) * (size_t) count, cudaMemcpyHostToDevice));
+	boneWeightCount = count;
+}
+
+void Mesh::setRestposes(const rgl_mat3x4f* r, int32_t count)
+{
+	RGL_CHECK_CUDA(cudaMemcpy(dRestposes.ensure(sizeof(rgl_mat3x4f) * (size_t) count), r, sizeof(rgl_mat3x4f) * (size_t) count,
+	                          cudaMemcpyHostToDevice));
+	restposeCount = count;
+}
+
 void Mesh::ensureBlas(cudaStream_t s)
 {
 	if (blasBuilt) {
 		return;
 	}
-	rgl::buildBlas(dVertices.as<float>(), vertexCount, dIndices.as<int32_t>(), triangleCount, blas, s);
+	(void) s;
+	rgl::buildBlasHost(hVertices.data(), vertexCount, hIndices.data(), triangleCount, blas);
 	blasBuilt = true;
 }
 
 Entity::Entity(std::shared_ptr<Mesh> m, Scene* s) : mesh(std::move(m)), scene(s) {}
 
+Entity::~Entity()
+{
+	if (animBlas.nodes != nullptr) {
+		rgl::freeBlas(animBlas);
+	}
+}
+
+// First animation: the animated vertices start as the mesh's, the displacement as zero.
+void Entity::startAnimation()
+{
+	if (animated) {
+		return;
+	}
+	const size_t bytes = sizeof(float) * 3 * (size_t) mesh->vertexCount;
+	RGL_CHECK_CUDA(cudaMemcpy(dAnimVertices.ensure(bytes), mesh->dVertices.get(), bytes, cudaMemcpyDeviceToDevice));
+	RGL_CHECK_CUDA(cudaMemset(dAnimDisplacement.ensure(bytes), 0, bytes));
+	animated = true;
+}
+
+// dAnimDisplacement holds the new vertices: turn it into new - old, store new, rebuild the entity's
+// BLAS and record the animation time.
+void Entity::finishAnimation(cudaStream_t s)
+{
+	rgl::launchUpdateVertices(mesh->vertexCount, dAnimDisplacement.as<float>(), dAnimVertices.as<float>(), s);
+	rgl::buildBlas(dAnimVertices.as<float>(), mesh->vertexCount, mesh->dIndices.as<int32_t>(), mesh->triangleCount, animBlas, s);
+	RGL_CHECK_CUDA(cudaStreamSynchronize(s));
+	formerAnimTimed = animTimed;
+	formerAnimTimeNs = animTimeNs;
+	animTimed = scene->timeSet;
+	animTimeNs = scene->timeNs;
+	scene->markPosesDirty(); // the instance record points at the rebuilt BLAS
+}
+
+void Entity::applyExternalAnimation(const rgl_vec3f* vertices, int32_t count)
+{
+	if (skinned) {
+		throw rgl::InvalidAPIArgument("entity is animated by its skeleton; external animation cannot be applied");
+	}
+	if (count != mesh->vertexCount) {
+		throw rgl::InvalidAPIArgument(rgl::format(
+		    "Invalid argument: cannot apply external animation because vertex counts do not match: old=%d, new=%d", (int) mesh->vertexCount,
+		    (int) count));
+	}
+	startAnimation();
+	RGL_CHECK_CUDA(cudaMemcpy(dAnimDisplacement.get(), vertices, sizeof(float) * 3 * (size_t) count, cudaMemcpyHostToDevice));
+	finishAnimation(nullptr);
+}
+
+void Entity::setPoseAndAnimate(const rgl_mat3x4f* pose, int32_t bones)
+{
+	if (animated && !skinned) {
+		throw rgl::InvalidAPIArgument("entity is animated externally; skeleton animation cannot be applied");
+	}
+	if (mesh->boneWeightCount == 0) {
+		throw rgl::InvalidAPIArgument("Cannot create SkeletonAnimator because mesh has no bone weights defined.");
+	}
+	if (mesh->restposeCount == 0) {
+		throw rgl::InvalidAPIArgument("Cannot create SkeletonAnimator because mesh has no restposes defined.");
+	}
+	if (bones != mesh->restposeCount) {
+		throw rgl::InvalidAPIArgument(rgl::format(
+		    "Cannot perform skeleton animation because bones count do not match restposes count: bones=%d, restposes=%d", (int) bones,
+		    (int) mesh->restposeCount));
+	}
+	startAnimation();
+	skinned = true;
+	RGL_CHECK_CUDA(cudaMemcpy(dPose.ensure(sizeof(rgl_mat3x4f) * (size_t) bones), pose, sizeof(rgl_mat3x4f) * (size_t) bones,
+	                          cudaMemcpyHostToDevice));
+	rgl::launchSkin(mesh->vertexCount, mesh->dVertices.as<float>(), mesh->dBoneWeights.as<rgl::BoneWeights>(), dPose.as<Mat34>(),
+	                mesh->dRestposes.as<Mat34>(), bones, static_cast<Mat34*>(dBoneMatrices.ensure(sizeof(Mat34) * (size_t) bones)),
+	                dAnimDisplacement.as<float>(), skinError.device(), nullptr);
+	finishAnimation(nullptr);
+	rgl::refreshErrorSlots();
+	if (skinError.raised()) {
+		skinError.clear();
+		throw rgl::InvalidAPIArgument("bone weights reference a bone outside the pose");
+	}
+}
+
+const float* Entity::vertexDisplacementSincePrevFrame() const
+{
+	if (!animated || !formerAnimTimed || !scene->prevTimeSet || formerAnimTimeNs != scene->prevTimeNs) {
+		return nullptr;
+	}
+	return dAnimDisplacement.as<float>();
+}
+
 void Entity::setTransform(const Mat34& tf)
 {
+	formerTransform = transform;
+	formerTimed = transformTimed;
+	formerTimeNs = transformTimeNs;
 	transform = tf;
+	transformTimed = scene->timeSet;
+	transformTimeNs = scene->timeNs;
 	scene->markPosesDirty();
+}
+
+bool Entity::previousTransform(Mat34& out) const
+{
+	// Set only once: assume the same pose one step earlier (zero velocity), as for static objects.
+	if (transformTimed && !formerTimed) {
+		out = transform;
+		return true;
+	}
+	if (formerTimed && scene->prevTimeSet && formerTimeNs == scene->prevTimeNs) {
+		out = formerTransform;
+		return true;
+	}
+	return false;
+}
+
+void Scene::setTime(uint64_t ns)
+{
+	prevTimeNs = timeNs;
+	prevTimeSet = timeSet;
+	timeNs = ns;
+	timeSet = true;
+	markPosesDirty(); // previous poses in the instance records depend on the time step
+}
+
+float Scene::deltaTimeSeconds() const
+{
+	if (!timeSet || !prevTimeSet) {
+		return 0.0f;
+	}
+	return (float) ((double) ((int64_t) (timeNs - prevTimeNs)) * 1e-9);
 }
 
 void Entity::setId(int32_t newId)
@@ -97,6 +242,8 @@ void Scene::clear()
 	posesDirty = true;
 	timeSet = false;
 	timeNs = 0;
+	prevTimeSet = false;
+	prevTimeNs = 0;
 }
 
 void Scene::releaseDevice()
@@ -148,11 +295,15 @@ rgl::InstanceRec* Scene::fillInstanceRecords()
 		rgl::InstanceRec r{};
 		r.objectToWorld = e.transform;
 		r.worldToObject = rgl::inverse(e.transform);
-		r.nodes = e.mesh->blas.nodes;
-		r.tris = e.mesh->blas.tris;
+		const rgl::BlasBuild& bl = e.activeBlas();
+		r.nodes = bl.nodes;
+		r.tris = bl.tris;
+		r.vertexDisplacement = e.vertexDisplacementSincePrevFrame();
+		r.indices = e.mesh->dIndices.as<int32_t>();
 		r.entityId = e.id;
 		r.laserRetro = e.laserRetro;
-		const float* b = e.mesh->blas.bounds;
+		r.hasPrev = e.previousTransform(r.prevObjectToWorld) ? 1 : 0;
+		const float* b = bl.bounds;
 		float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
 		for (int c = 0; c < 8; ++c) {
 			rgl::Vec3 p = e.transform.point(rgl::v3((c & 1) ? b[3] : b[0], (c & 2) ? b[4] : b[1], (c & 4) ? b[5] : b[2]));
@@ -194,6 +345,10 @@ void Scene::prepare(cudaStream_t s)
 		return;
 	}
 	const int n = (int) entities.size();
+	if (n >= (1 << 24)) {
+		// The traversal packs the hit's instance index into 24 bits.
+		throw rgl::InvalidAPIArgument(rgl::format("a scene holds at most %d entities, got %d", (1 << 24) - 1, n));
+	}
 	for (auto& e : entities) {
 		e->mesh->ensureBlas(s);
 	}

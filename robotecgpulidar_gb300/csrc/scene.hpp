@@ -20,12 +20,21 @@ struct Mesh
 	~Mesh();
 	void ensureBlas(cudaStream_t s);
 
+	// Skinning data (reference src/scene/Mesh.cpp:44-66): one rgl_bone_weights_t per vertex, one
+	// restpose (inverse bind pose) per bone.
+	void setBoneWeights(const rgl_bone_weights_t* w, int32_t count);
+	void setRestposes(const rgl_mat3x4f* r, int32_t count);
+
 	int32_t vertexCount = 0;
 	int32_t triangleCount = 0;
 	rgl::DeviceBuffer dVertices{false};
 	rgl::DeviceBuffer dIndices{false};
+	std::vector<float> hVertices;   // host copies for the host BLAS build
+	std::vector<int32_t> hIndices;
 	rgl::BlasBuild blas;
 	bool blasBuilt = false;
+	rgl::DeviceBuffer dBoneWeights{false}, dRestposes{false};
+	int32_t boneWeightCount = 0, restposeCount = 0;
 };
 
 struct Entity
@@ -34,12 +43,41 @@ struct Entity
 	void setTransform(const rgl::Mat34& tf);
 	void setId(int32_t id);
 	void setLaserRetro(float retro);
+	~Entity();
+	// Mesh animation of this entity (reference src/scene/Entity.cpp:83-118, animator/*): new object-space
+	// vertices (given, or skinned from the mesh's bones); the entity then has its own BLAS over them.
+	void applyExternalAnimation(const rgl_vec3f* vertices, int32_t count);
+	void setPoseAndAnimate(const rgl_mat3x4f* pose, int32_t bones);
+	// Per-vertex displacement since the previous scene time step, or null (reference Entity.cpp:112-118).
+	const float* vertexDisplacementSincePrevFrame() const;
+	const rgl::BlasBuild& activeBlas() const { return animated ? animBlas : mesh->blas; }
+
+	// Pose of the scene's previous time step, if known (reference src/scene/Entity.cpp:62-81).
+	bool previousTransform(rgl::Mat34& out) const;
 
 	std::shared_ptr<Mesh> mesh;
 	Scene* scene;
 	rgl::Mat34 transform = rgl::Mat34::identity();
+	bool transformTimed = false;       // the transform was set while the scene had a time
+	uint64_t transformTimeNs = 0;
+	rgl::Mat34 formerTransform = rgl::Mat34::identity();
+	bool formerTimed = false;
+	uint64_t formerTimeNs = 0;
+	// Animation state: animated vertices, their displacement since the previous animation, bone
+	// matrices (skinning), the entity's BLAS over the animated vertices, animation times.
+	bool animated = false;
+	bool skinned = false;
+	rgl::DeviceBuffer dAnimVertices{false}, dAnimDisplacement{false}, dBoneMatrices{false}, dPose{false};
+	rgl::BlasBuild animBlas;
+	bool animTimed = false, formerAnimTimed = false;
+	uint64_t animTimeNs = 0, formerAnimTimeNs = 0;
+	rgl::ErrorSlot skinError;
 	int32_t id = RGL_DEFAULT_ENTITY_ID;
 	float laserRetro = 0.0f;
+
+private:
+	void startAnimation();
+	void finishAnimation(cudaStream_t s);
 };
 
 struct Texture
@@ -82,6 +120,12 @@ struct Scene
 
 	uint64_t timeNs = 0;
 	bool timeSet = false;
+	uint64_t prevTimeNs = 0;
+	bool prevTimeSet = false;
+	// rgl_scene_set_time: the current time becomes the previous one (reference src/scene/Scene.hpp:60-67).
+	void setTime(uint64_t ns);
+	// Seconds between the last two time steps, 0 when there is no previous one.
+	float deltaTimeSeconds() const;
 
 	// Statistics for the extension API.
 	uint64_t tlasBuilds = 0, tlasRefits = 0;

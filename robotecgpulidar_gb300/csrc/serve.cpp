@@ -36,6 +36,7 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t0));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t1));
+		RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
 		s->counter.ensure(sizeof(uint32_t));
 		slots.push_back(std::move(s));
 	}
@@ -53,11 +54,15 @@ Server::~Server()
 		worker.join();
 	}
 	cudaStreamSynchronize(stream);
+	for (auto& s : slots) {
+		cudaStreamSynchronize(s->stream);
+	}
 	cudaFreeHost(arena.host);
 	for (auto& s : slots) {
 		cudaEventDestroy(s->done);
 		cudaEventDestroy(s->t0);
 		cudaEventDestroy(s->t1);
+		cudaStreamDestroy(s->stream);
 	}
 	cudaStreamDestroy(stream);
 }
@@ -411,18 +416,18 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 
 	auto* dTileCounts = slot.tileCounts.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
 	auto* dTileOffsets = slot.tileOffsets.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
-	RGL_CHECK_CUDA(cudaEventRecord(slot.t0, stream));
-	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, stream));
-	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.t0, slot.stream));
+	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, slot.stream));
+	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, slot.stream));
 	rgl::launchTraceBatch(reinterpret_cast<const rgl::BatchJob*>(dBase), reinterpret_cast<const int32_t*>(dBase + offTask), n, 1, false,
-	                      sched, slot.counter.as<uint32_t>(), stream);
+	                      sched, slot.counter.as<uint32_t>(), slot.stream);
 	rgl::launchSegCompact(reinterpret_cast<const rgl::SegCompactJob*>(dBase + offSeg), reinterpret_cast<const int32_t*>(dBase + offTile), n,
-	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, stream);
+	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, slot.stream);
 	auto* hResults = static_cast<int32_t*>(slot.hResults.ensure(sizeof(int32_t) * 2 * n));
-	RGL_CHECK_CUDA(cudaMemcpyAsync(hResults, dResults, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, stream));
-	RGL_CHECK_CUDA(cudaEventRecord(slot.t1, stream));
-	RGL_CHECK_CUDA(cudaEventRecord(slot.done, stream));
-	RGL_CHECK_CUDA(cudaLaunchHostFunc(stream, &Server::batchDone, this));
+	RGL_CHECK_CUDA(cudaMemcpyAsync(hResults, dResults, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, slot.stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.t1, slot.stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.done, slot.stream));
+	RGL_CHECK_CUDA(cudaLaunchHostFunc(slot.stream, &Server::batchDone, this));
 }
 
 // Runs on a CUDA host thread once a batch's stream work is done: wakes the scheduler, which then
@@ -535,7 +540,7 @@ void Server::loop()
 					std::vector<Scene*> prepared;
 					for (auto* r : batch) {
 						if (std::find(prepared.begin(), prepared.end(), r->scene.get()) == prepared.end()) {
-							r->scene->prepare(stream);
+							r->scene->prepare(freeSlot->stream);
 							prepared.push_back(r->scene.get());
 						}
 

@@ -112,6 +112,7 @@ private:
 	struct Slot
 	{
 		std::vector<Request*> reqs;
+		cudaStream_t stream = nullptr; // slots run on their own streams: one batch's tail overlaps the next
 		cudaEvent_t done = nullptr;
 		cudaEvent_t t0 = nullptr, t1 = nullptr; // device time of the batch
 		rgl::DeviceBuffer tables{false}, tileCounts{false}, tileOffsets{false}, results{false}, counter{false};

@@ -407,6 +407,12 @@ const std::map<std::string, Player>& players()
 		     p.meshes[p.id(0)] = m;
 	     }},
 	    {"rgl_mesh_set_texture_coords", [](Playback& p) { rgl_mesh_set_texture_coords(p.mesh(0), p.ptr<rgl_vec2f>(1), p.i32(2)); }},
+	    {"rgl_mesh_set_bone_weights",
+	     [](Playback& p) { rgl_mesh_set_bone_weights(p.mesh(0), p.ptr<rgl_bone_weights_t>(1), p.i32(2)); }},
+	    {"rgl_mesh_set_restposes", [](Playback& p) { rgl_mesh_set_restposes(p.mesh(0), p.ptr<rgl_mat3x4f>(1), p.i32(2)); }},
+	    {"rgl_entity_set_pose_world", [](Playback& p) { rgl_entity_set_pose_world(p.entity(0), p.ptr<rgl_mat3x4f>(1), p.i32(2)); }},
+	    {"rgl_entity_apply_external_animation",
+	     [](Playback& p) { rgl_entity_apply_external_animation(p.entity(0), p.ptr<rgl_vec3f>(1), p.i32(2)); }},
 	    {"rgl_mesh_destroy",
 	     [](Playback& p) {
 		     rgl_mesh_destroy(p.mesh(0));

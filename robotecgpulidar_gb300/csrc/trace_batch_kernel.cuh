@@ -56,9 +56,10 @@ __device__ __forceinline__ void laneGroupTask(const BatchJob* __restrict__ job, 
 	for (int r = 0; r < ROUNDS; ++r) {
 		const int s = sub + r * G;
 		if (valid && s < nSamples) {
-			const Mat34 sr = (s == 0) ? ray : mul(ray, loadMat(job->samples + s));
+			const Mat34 traced = SHADING ? distortRay(job->p, beam, ray) : ray;
+			const Mat34 sr = (s == 0) ? traced : mul(traced, loadMat(job->samples + s));
 			sv[r] = traceSample<SHADING>(job->p.nearNonHitDistance, job->p.farNonHitDistance, job->p.defaultIntensity, sc, sr, minRange,
-			                             maxRange, st);
+			                             maxRange, st, s);
 		} else {
 			sv[r] = emptySample();
 		}
@@ -69,7 +70,7 @@ __device__ __forceinline__ void laneGroupTask(const BatchJob* __restrict__ job, 
 	red.init(job->p.farNonHitDistance);
 	reduceGroup<ROUNDS, SHADING>(sv, nSamples, G, groupLane0, leader, red);
 	if (leader) {
-		writeReturns(job->p, sc, beam, ray, red);
+		writeReturns<SHADING>(job->p, sc, job->samples, beam, ray, red);
 	}
 }
 
@@ -87,13 +88,14 @@ __device__ __forceinline__ void serialTask(const BatchJob* __restrict__ job, int
 	ReturnReducer red;
 	red.init(job->p.farNonHitDistance);
 	const int nSamples = job->p.nSamples;
+	const Mat34 traced = SHADING ? distortRay(job->p, beam, ray) : ray;
 	for (int s = 0; s < nSamples; ++s) {
-		const Mat34 sr = (s == 0) ? ray : mul(ray, loadMat(job->samples + s));
-		const SampleVal v =
-		    traceSample<SHADING>(job->p.nearNonHitDistance, job->p.farNonHitDistance, job->p.defaultIntensity, sc, sr, minRange, maxRange, st);
+		const Mat34 sr = (s == 0) ? traced : mul(traced, loadMat(job->samples + s));
+		const SampleVal v = traceSample<SHADING>(job->p.nearNonHitDistance, job->p.farNonHitDistance, job->p.defaultIntensity, sc, sr,
+		                                         minRange, maxRange, st, s);
 		red.add(s, v.hit, toSelected(v));
 	}
-	writeReturns(job->p, sc, beam, ray, red);
+	writeReturns<SHADING>(job->p, sc, job->samples, beam, ray, red);
 }
 
 // MODE 0: lane groups, one round; MODE 1: lane groups, two rounds (more than 32 samples); MODE 2: serial.

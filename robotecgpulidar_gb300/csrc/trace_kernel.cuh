@@ -97,8 +97,9 @@ struct SampleVal
 	uint32_t hit;
 	float dist;
 	float intensity;
-	int32_t inst; // instance index of a hit (its entity id and laser retro are read when written)
+	int32_t inst; // hit: instance index | sample index << 24 (entity id, laser retro, velocity read when written)
 	float nx, ny, nz, cosInc;
+	int32_t tri;  // SHADING: the hit's triangle record (velocity of animated meshes)
 };
 
 struct Selected
@@ -107,9 +108,10 @@ struct Selected
 	float intensity;
 	int32_t inst;
 	float nx, ny, nz, cosInc;
+	int32_t tri;
 };
 
-__device__ __forceinline__ SampleVal emptySample() { return SampleVal{0u, 0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f}; }
+__device__ __forceinline__ SampleVal emptySample() { return SampleVal{0u, 0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f, -1}; }
 
 __device__ __forceinline__ Mat34 loadMat(const Mat34* p)
 {
@@ -122,9 +124,12 @@ __device__ __forceinline__ Mat34 loadMat(const Mat34* p)
 // reference's FP64 norm of the object-space offset equals this within the stated tolerance), the
 // min-range rule turns a closer hit into the near non-hit without continuing, a miss gives the far
 // non-hit distance. With SHADING the world normal, |cos| of the incidence and intensity are added.
+constexpr int kSampleShift = 24; // instance indices stay below 1 << 24
+constexpr int32_t kInstMask = (1 << kSampleShift) - 1;
+
 template<bool SHADING>
 __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
-                                                   const HitRec& h, Vec3 d, float minRange)
+                                                   const HitRec& h, Vec3 d, float minRange, int sample)
 {
 	DevLoader ld;
 	SampleVal v = emptySample();
@@ -137,7 +142,7 @@ __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNo
 			const InstanceRec& inst = sc.instances[h.inst];
 			v.hit = 1;
 			v.dist = dist;
-			v.inst = h.inst;
+			v.inst = h.inst | (sample << kSampleShift);
 			if (SHADING) {
 				const TriRecord tr = ld.tri(inst.tris, h.tri);
 				const Vec3 wa = inst.objectToWorld.point(v3(tr.v0x, tr.v0y, tr.v0z));
@@ -150,6 +155,7 @@ __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNo
 				v.nz = n.z;
 				v.cosInc = c;
 				v.intensity = fmul(defaultIntensity, c);
+				v.tri = h.tri;
 			}
 		}
 	}
@@ -158,17 +164,17 @@ __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNo
 
 template<bool SHADING>
 __device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
-                                                 const Mat34& sr, float minRange, float maxRange, DevStack& st)
+                                                 const Mat34& sr, float minRange, float maxRange, DevStack& st, int sample)
 {
 	DevLoader ld;
 	const Vec3 d = sr.rayDir();
 	const HitRec h = traceClosest(sc, sr.rayOrigin(), d, maxRange, st, ld);
-	return sampleFromHit<SHADING>(nearNonHit, farNonHit, defaultIntensity, sc, h, d, minRange);
+	return sampleFromHit<SHADING>(nearNonHit, farNonHit, defaultIntensity, sc, h, d, minRange, sample);
 }
 
 __device__ __forceinline__ Selected toSelected(const SampleVal& v)
 {
-	return Selected{v.dist, v.intensity, v.inst, v.nx, v.ny, v.nz, v.cosInc};
+	return Selected{v.dist, v.intensity, v.inst, v.nx, v.ny, v.nz, v.cosInc, v.tri};
 }
 
 // In-order selection over a beam's samples; add() must see samples 0, 1, 2, ... in order.
@@ -182,7 +188,7 @@ struct ReturnReducer
 	{
 		haveFirst = false;
 		nonHitDist = farNonHit;
-		first = second = last = strongest = secondStrongest = Selected{0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+		first = second = last = strongest = secondStrongest = Selected{0.0f, 0.0f, 0, 0.0f, 0.0f, 0.0f, 0.0f, -1};
 	}
 	__device__ __forceinline__ void add(int s, uint32_t hit, const Selected& cur)
 	{
@@ -228,12 +234,83 @@ __device__ __forceinline__ float rayAzimuth(const Mat34& m)
 	return (v < 1.0f && v > -1.0f) ? atan2f(-m.m[2][0], m.m[2][2]) : 0.0f;
 }
 
-// Writes beam `beam`'s returns at points beam * returnCount + r. `ray` is the primary ray pose. Per
-// return point it also writes the beam's shared fields (reference optixPrograms.cu:288-326): ray
-// index, azimuth and elevation of the sensor-frame pose, ring id and time stamps (zero: this build
-// applies no velocity distortion).
-__device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneView& sc, uint32_t beam, const Mat34& ray,
-                                             const ReturnReducer& red)
+// The pose a beam is cast from: under velocity distortion the sensor-frame ray is moved by the sensor's
+// motion during the ray's time offset (reference optixPrograms.cu:60-70: translation offset * linear
+// velocity, rotation offset * angular velocity in degrees, both per millisecond), else the ray itself.
+// Kept out of line (like hitVelocities) so the traversal's register allocation does not pay for it.
+__device__ __noinline__ Mat34 distortRayOutOfLine(const TraceParams& p, uint32_t beam, const Mat34& ray)
+{
+	const float off = p.timeOffsetsMs[beam];
+	const float toDeg = (float) (180.0 / 3.14159265358979323846);
+	const Vec3 lv = p.sensorLinearVelocity, av = p.sensorAngularVelocity;
+	const Vec3 t = v3(fmul(fmul(off, lv.x), 0.001f), fmul(fmul(off, lv.y), 0.001f), fmul(fmul(off, lv.z), 0.001f));
+	const Vec3 r = v3(fmul(fmul(off, fmul(av.x, toDeg)), 0.001f), fmul(fmul(off, fmul(av.y, toDeg)), 0.001f),
+	                  fmul(fmul(off, fmul(av.z, toDeg)), 0.001f));
+	return mul(p.sensorToWorld, mul(translationRotationDeg(t, r), mul(p.worldToSensor, ray)));
+}
+
+__device__ __forceinline__ Mat34 distortRay(const TraceParams& p, uint32_t beam, const Mat34& ray)
+{
+	return (p.distortion && p.timeOffsetsMs != nullptr) ? distortRayOutOfLine(p, beam, ray) : ray;
+}
+
+// Velocities of a hit (reference optixPrograms.cu:169-212): the hit point of the selected sample
+// (sample pose `sr`, distance `dist`), its instance's pose one scene time step earlier, the sensor's
+// velocities. Absolute velocity is the displacement since the previous pose over the time step;
+// relative velocity is that velocity in the sensor frame minus the sensor's linear velocity and the
+// rotation of the hit point about the sensor; radial speed is its component along the sensor-to-hit
+// direction. NaN when the scene has no time step.
+__device__ __noinline__ void hitVelocities(const TraceParams& p, const InstanceRec& inst, const Mat34& sr, float dist, int32_t tri,
+                                            Vec3& absV, Vec3& relV, float& radial)
+{
+	const float nan = __int_as_float(0x7fc00000);
+	absV = relV = v3(nan, nan, nan);
+	radial = nan;
+	if (!(p.sceneDeltaTime > 0.0f)) {
+		return;
+	}
+	// The hit point in the instance's frame, and back in the world with the current pose, so an instance
+	// whose previous pose equals the current one moves by exactly zero.
+	const Vec3 d = sr.rayDir();
+	const Vec3 hitObject = inst.worldToObject.point(sr.rayOrigin() + d * (dist / length(d)));
+	const Vec3 hitWorld = inst.objectToWorld.point(hitObject);
+	Vec3 disp = v3(0.0f, 0.0f, 0.0f);
+	if (inst.hasPrev) {
+		disp = hitWorld - inst.prevObjectToWorld.point(hitObject);
+	}
+	if (inst.vertexDisplacement != nullptr && tri >= 0) {
+		// Animated mesh: the triangle's vertex displacements since the previous step, rotated into the
+		// world and interpolated at the hit's barycentric coordinates (reference optixPrograms.cu:185-195).
+		const TriRecord& tr = inst.tris[tri];
+		const Vec3 a = v3(tr.v0x, tr.v0y, tr.v0z), b = v3(tr.v1x, tr.v1y, tr.v1z), c = v3(tr.v2x, tr.v2y, tr.v2z);
+		const Vec3 n = cross(b - a, c - a);
+		const float nn = dot(n, n);
+		const float u = nn > 0.0f ? dot(cross(hitObject - a, c - a), n) / nn : 0.0f; // weight of b
+		const float w = nn > 0.0f ? dot(cross(b - a, hitObject - a), n) / nn : 0.0f; // weight of c
+		const int32_t* idx = inst.indices + 3 * tr.primId;
+		auto vdisp = [&](int k) {
+			const float* q = inst.vertexDisplacement + 3 * idx[k];
+			return inst.objectToWorld.vector(v3(q[0], q[1], q[2]));
+		};
+		disp = disp + vdisp(0) * fsub(fsub(1.0f, u), w) + vdisp(1) * u + vdisp(2) * w;
+	}
+	absV = v3(disp.x / p.sceneDeltaTime, disp.y / p.sceneDeltaTime, disp.z / p.sceneDeltaTime);
+	const Vec3 absInSensor = p.worldToSensorRotation.vector(absV);
+	const Vec3 hitInSensor = p.worldToSensor.point(hitWorld);
+	relV = (absInSensor - p.sensorLinearVelocity) + (v3(0.0f, 0.0f, 0.0f) - cross(p.sensorAngularVelocity, hitInSensor));
+	radial = dot(normalized(hitInSensor), relV);
+}
+
+// Writes beam `beam`'s returns at points beam * returnCount + r. `ray` is the primary ray pose as
+// given (XYZ and the beam fields use it; velocities use the pose the samples were cast from,
+// distortRay). Velocities, like shading, exist only in the SHADING variants of the kernel, which a
+// launch uses whenever one of those fields or velocity distortion is requested. Per return point it
+// also writes the beam's shared fields
+// (reference optixPrograms.cu:288-326): ray index, azimuth and elevation of the sensor-frame pose,
+// ring id and time stamps (the ray's time offset under velocity distortion, else 0).
+template<bool SHADING>
+__device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneView& sc, const Mat34* samples, uint32_t beam,
+                                             const Mat34& ray, const ReturnReducer& red)
 {
 	const TraceOutputs& out = p.out;
 	const int32_t returnMode = p.returnMode;
@@ -256,8 +333,9 @@ __device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneVi
 		if (out.azimuth) out.azimuth[pi] = azimuth;
 		if (out.elevation) out.elevation[pi] = elevation;
 		if (out.ringId) out.ringId[pi] = ring;
-		if (out.timeStampF64) out.timeStampF64[pi] = 0.0;
-		if (out.timeStampU32) out.timeStampU32[pi] = 0u;
+		const bool stamped = p.distortion && p.timeOffsetsMs;
+		if (out.timeStampF64) out.timeStampF64[pi] = stamped ? (double) fmul(p.timeOffsetsMs[beam], 1e-3f) : 0.0;
+		if (out.timeStampU32) out.timeStampU32[pi] = stamped ? (uint32_t) fmul(p.timeOffsetsMs[beam], 1e6f) : 0u;
 		if (!red.haveFirst) {
 			const float nonHitDist = red.nonHitDist;
 			Vec3 disp = dn * nonHitDist;
@@ -283,6 +361,13 @@ __device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneVi
 			}
 			if (out.incidentAngle) out.incidentAngle[pi] = __int_as_float(0x7fc00000);
 			if (out.laserRetro) out.laserRetro[pi] = 0.0f;
+			if (out.absVelocity) {
+				out.absVelocity[3 * pi] = out.absVelocity[3 * pi + 1] = out.absVelocity[3 * pi + 2] = __int_as_float(0x7fc00000);
+			}
+			if (out.relVelocity) {
+				out.relVelocity[3 * pi] = out.relVelocity[3 * pi + 1] = out.relVelocity[3 * pi + 2] = __int_as_float(0x7fc00000);
+			}
+			if (out.radialSpeed) out.radialSpeed[pi] = 0.0f;
 			continue;
 		}
 		Selected sel;
@@ -300,7 +385,7 @@ __device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneVi
 		}
 		if (out.distance) out.distance[pi] = sel.dist;
 		if (out.isHit) out.isHit[pi] = 1;
-		const InstanceRec& hitInst = sc.instances[sel.inst];
+		const InstanceRec& hitInst = sc.instances[sel.inst & kInstMask];
 		if (out.entityId) out.entityId[pi] = hitInst.entityId;
 		if (out.returnType) out.returnType[pi] = (uint8_t) type;
 		if (out.intensityF32) out.intensityF32[pi] = sel.intensity;
@@ -312,6 +397,25 @@ __device__ __forceinline__ void writeReturns(const TraceParams& p, const SceneVi
 		}
 		if (out.incidentAngle) out.incidentAngle[pi] = acosf(sel.cosInc);
 		if (out.laserRetro) out.laserRetro[pi] = hitInst.laserRetro;
+		if (SHADING && (out.absVelocity || out.relVelocity || out.radialSpeed)) {
+			const int sample = sel.inst >> kSampleShift;
+			const Mat34 traced = distortRay(p, beam, ray);
+			const Mat34 sr = sample == 0 ? traced : mul(traced, loadMat(samples + sample));
+			Vec3 absV, relV;
+			float radial;
+			hitVelocities(p, hitInst, sr, sel.dist, sel.tri, absV, relV, radial);
+			if (out.absVelocity) {
+				out.absVelocity[3 * pi] = absV.x;
+				out.absVelocity[3 * pi + 1] = absV.y;
+				out.absVelocity[3 * pi + 2] = absV.z;
+			}
+			if (out.relVelocity) {
+				out.relVelocity[3 * pi] = relV.x;
+				out.relVelocity[3 * pi + 1] = relV.y;
+				out.relVelocity[3 * pi + 2] = relV.z;
+			}
+			if (out.radialSpeed) out.radialSpeed[pi] = radial;
+		}
 	}
 }
 
@@ -332,13 +436,15 @@ __device__ __forceinline__ void reduceGroup(const SampleVal (&sv)[ROUNDS], int n
 		const float dist = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].dist : pick(r, sv[0].dist, sv[ROUNDS - 1].dist), src);
 		const int32_t ent = __shfl_sync(
 		    0xffffffffu, ROUNDS == 1 ? sv[0].inst : (int32_t) pickU(r, (uint32_t) sv[0].inst, (uint32_t) sv[ROUNDS - 1].inst), src);
-		Selected cur{dist, 0.0f, ent, 0.0f, 0.0f, 0.0f, 0.0f};
+		Selected cur{dist, 0.0f, ent, 0.0f, 0.0f, 0.0f, 0.0f, -1};
 		if (SHADING) {
 			cur.intensity = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].intensity : pick(r, sv[0].intensity, sv[ROUNDS - 1].intensity), src);
 			cur.nx = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].nx : pick(r, sv[0].nx, sv[ROUNDS - 1].nx), src);
 			cur.ny = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].ny : pick(r, sv[0].ny, sv[ROUNDS - 1].ny), src);
 			cur.nz = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].nz : pick(r, sv[0].nz, sv[ROUNDS - 1].nz), src);
 			cur.cosInc = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].cosInc : pick(r, sv[0].cosInc, sv[ROUNDS - 1].cosInc), src);
+			cur.tri = __shfl_sync(0xffffffffu, ROUNDS == 1 ? sv[0].tri : (int32_t) pickU(r, (uint32_t) sv[0].tri, (uint32_t) sv[ROUNDS - 1].tri),
+			                      src);
 		}
 		if (leader) {
 			red.add(s, hit, cur);

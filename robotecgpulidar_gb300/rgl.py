@@ -82,6 +82,8 @@ FIELD_DTYPE = {
     RGL_FIELD_TIME_STAMP_F64: (np.float64, 1), RGL_FIELD_TIME_STAMP_U32: (np.uint32, 1),
     RGL_FIELD_AZIMUTH_F32: (np.float32, 1), RGL_FIELD_ELEVATION_F32: (np.float32, 1),
     RGL_FIELD_RAY_POSE_MAT3x4_F32: (np.float32, 12),
+    RGL_FIELD_ABSOLUTE_VELOCITY_VEC3_F32: (np.float32, 3), RGL_FIELD_RELATIVE_VELOCITY_VEC3_F32: (np.float32, 3),
+    RGL_FIELD_RADIAL_SPEED_F32: (np.float32, 1),
 }
 
 # ---- return modes

@@ -7,7 +7,7 @@
 #include <vector>
 
 #include "bvh_core.hpp"
-#include "tlas_sah.hpp"
+#include "sah_build.hpp"
 #include "trace_core.hpp"
 
 using namespace rgl;
@@ -126,7 +126,7 @@ Blas buildWideHost(std::vector<float4> lo, std::vector<float4> hi, const float* 
 	return out;
 }
 
-// Wide TLAS from a host SAH topology (tlas_sah.hpp), collapsed like the device build.
+// Wide TLAS from a host SAH topology (sah_build.hpp), collapsed like the device build.
 Blas buildTlasSah(const std::vector<float4>& lo, const std::vector<float4>& hi)
 {
 	const int n = (int) lo.size();
@@ -155,7 +155,39 @@ Blas buildTlasSah(const std::vector<float4>& lo, const std::vector<float4>& hi)
 	return out;
 }
 
-int gTlasSah = 1; // the product builds the TLAS topology by SAH (tlas_sah.hpp)
+int gTlasSah = 1; // the product builds the TLAS topology by SAH (sah_build.hpp)
+
+// Wide BLAS from the product's binned SAH topology (sah_build.hpp), collapsed like the product.
+Blas buildBlasSah(const std::vector<float4>& lo, const std::vector<float4>& hi, const float* v, const int32_t* idx)
+{
+	const int n = (int) lo.size();
+	std::vector<Box> boxes(n);
+	for (int i = 0; i < n; ++i) {
+		boxes[i] = Box{lo[i].x, lo[i].y, lo[i].z, hi[i].x, hi[i].y, hi[i].z};
+	}
+	SahTree t = buildBinnedSahTree(boxes);
+	Blas out;
+	out.wide.resize(std::max(1, n));
+	out.tris.resize(n);
+	uint32_t wideCounter = 1, triCounter = 0;
+	std::vector<int2> qa(std::max(1, n)), qb(std::max(1, n));
+	uint32_t qaCount = 1, qbCount = 0;
+	qa[0] = make_int2(n == 1 ? ~0 : 0, 0);
+	CollapseInputs in{t.bin.data(), t.rangeFirst.data(), t.rangeLast.data(), t.sortedIds.data(), lo.data(), hi.data(), v, idx, kLeafMaxTris};
+	while (qaCount > 0) {
+		qbCount = 0;
+		CollapseOutputs o{out.wide.data(), out.tris.data(), &wideCounter, &triCounter, qb.data(), &qbCount, nullptr};
+		for (uint32_t i = 0; i < qaCount; ++i)
+			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
+		std::swap(qa, qb);
+		qaCount = qbCount;
+	}
+	out.wide.resize(wideCounter);
+	out.bounds = n == 1 ? boxes[0] : binBox(t.bin[0]);
+	return out;
+}
+
+int gBlasSah = 1; // the product builds mesh BLASes by binned SAH; 0: the device's Morton LBVH
 
 Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
 {
@@ -168,7 +200,7 @@ Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
 		lo[t] = make_float4(std::min({a[0], b[0], c[0]}), std::min({a[1], b[1], c[1]}), std::min({a[2], b[2], c[2]}), 0);
 		hi[t] = make_float4(std::max({a[0], b[0], c[0]}), std::max({a[1], b[1], c[1]}), std::max({a[2], b[2], c[2]}), 0);
 	}
-	return buildWideHost(lo, hi, v, idx, kLeafMaxTris);
+	return gBlasSah ? buildBlasSah(lo, hi, v, idx) : buildWideHost(lo, hi, v, idx, kLeafMaxTris);
 }
 
 struct HostStack
@@ -485,6 +517,8 @@ int gMaxStackDepth = 0;
 int harness_max_node_visits() { return gMaxNodeVisits; }
 // 1: build the TLAS topology with the host SAH builder instead of the Morton-ordered LBVH.
 void harness_set_tlas_sah(int on) { gTlasSah = on; }
+// 1: build mesh BLASes with the binned SAH (as the product does); 0: with the Morton LBVH.
+void harness_set_blas_sah(int on) { gBlasSah = on; }
 // Deepest traversal stack of a single ray in the last harness_cast call.
 int harness_max_stack_depth() { return gMaxStackDepth; }
 long harness_total_node_visits() { return gTotalNodeVisits; }
