@@ -352,7 +352,8 @@ RGL_API rgl_status_t rgl_mesh_set_texture_coords(rgl_mesh_t mesh, const rgl_vec2
 		CHECK_ARG(mesh != nullptr);
 		CHECK_ARG(uvs != nullptr);
 		CHECK_ARG(uv_count > 0);
-		notImplemented("rgl_mesh_set_texture_coords");
+		GraphRunCtx::synchronizeAll();
+		Meshes::get(mesh, "Mesh")->setTexCoords(uvs, uv_count);
 	});
 	RGL_TAPE_RECORD(T::handle(mesh), T::arr(uvs, uv_count), T::num(uv_count));
 	return status;
@@ -477,11 +478,14 @@ RGL_API rgl_status_t rgl_entity_set_id(rgl_entity_t entity, int32_t id)
 
 RGL_API rgl_status_t rgl_entity_set_intensity_texture(rgl_entity_t entity, rgl_texture_t texture)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(entity != nullptr);
 		CHECK_ARG(texture != nullptr);
-		notImplemented("rgl_entity_set_intensity_texture");
+		GraphRunCtx::synchronizeAll();
+		Entities::get(entity, "Entity")->setIntensityTexture(Textures::get(texture, "Texture"));
 	});
+	RGL_TAPE_RECORD(T::handle(entity), T::handle(texture));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_entity_set_laser_retro(rgl_entity_t entity, float retro)
@@ -523,29 +527,37 @@ RGL_API rgl_status_t rgl_entity_is_alive(rgl_entity_t entity, bool* out_alive)
 
 RGL_API rgl_status_t rgl_texture_create(rgl_texture_t* out_texture, const void* texels, int32_t width, int32_t height)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_texture != nullptr);
 		CHECK_ARG(texels != nullptr);
 		CHECK_ARG(width > 0);
 		CHECK_ARG(height > 0);
-		notImplemented("rgl_texture_create");
+		*out_texture = Textures::add(std::make_shared<Texture>(texels, width, height));
 	});
+	RGL_TAPE_RECORD(T::handle(out_texture ? *out_texture : nullptr), T::bin(texels, texels && width > 0 && height > 0 ? (size_t) width * height : 0),
+	                T::num(width), T::num(height));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_texture_destroy(rgl_texture_t texture)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(texture != nullptr);
+		GraphRunCtx::synchronizeAll();
 		Textures::release(texture, "Texture");
 	});
+	RGL_TAPE_RECORD(T::handle(texture));
+	return status;
 }
 
 RGL_API rgl_status_t rgl_texture_is_alive(rgl_texture_t texture, bool* out_alive)
 {
-	return safeCall([&]() {
+	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(out_alive != nullptr);
 		*out_alive = Textures::contains(texture);
 	});
+	RGL_TAPE_RECORD(T::handle(texture), T::flag(out_alive && *out_alive));
+	return status;
 }
 
 // ================================================================ scene
@@ -828,7 +840,11 @@ RGL_API rgl_status_t rgl_node_raytrace_configure_mask(rgl_node_t node, const int
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(rays_mask != nullptr);
 		CHECK_ARG(rays_count > 0);
-		notImplemented("rgl_node_raytrace_configure_mask");
+		auto n = getNodeAs<RaytraceNode>(node, "RaytraceNode");
+		if (n->ctx) {
+			n->ctx->synchronize();
+		}
+		n->setRayMask(rays_mask, (size_t) rays_count); // staged with the job at every run
 	});
 	RGL_TAPE_RECORD(T::handle(node), T::arr(rays_mask, rays_count), T::num(rays_count));
 	return status;
@@ -1003,7 +1019,10 @@ RGL_API rgl_status_t rgl_node_points_filter_ground(rgl_node_t* node, const rgl_v
 	const rgl_status_t status = safeCall([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(ground_angle_threshold >= 0);
-		notImplemented("rgl_node_points_filter_ground");
+		CHECK_ARG(sensor_up_vector != nullptr);
+		const rgl::Vec3 up = rgl::v3(sensor_up_vector->value[0], sensor_up_vector->value[1], sensor_up_vector->value[2]);
+		createOrUpdateNode<FilterGroundPointsNode>(node, "FilterGroundPointsNode",
+		                                           [&](FilterGroundPointsNode& n) { n.setParameters(up, ground_angle_threshold); });
 	});
 	RGL_TAPE_RECORD(T::handle(node ? *node : nullptr), T::arr(sensor_up_vector, 1), T::real(ground_angle_threshold));
 	return status;

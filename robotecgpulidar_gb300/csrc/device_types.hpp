@@ -81,7 +81,9 @@ struct alignas(16) InstanceRec
 	int32_t pad;
 	Mat34 prevObjectToWorld;   // 48 B, for hit-point velocities
 	const float* vertexDisplacement; // animated entity: per-vertex motion since the previous time step, or null
-	const int32_t* indices;          // the mesh's triangle vertex indices (with vertexDisplacement)
+	const int32_t* indices;          // the mesh's triangle vertex indices (with vertexDisplacement, texCoords)
+	uint64_t intensityTexture;       // cudaTextureObject_t of 8-bit texels, 0 without one
+	const float* texCoords;          // uv per vertex when intensityTexture is set
 };
 
 // Device view of a scene, read by the traversal kernel through one pointer so a captured CUDA graph
@@ -164,6 +166,7 @@ struct TraceParams
 	float sceneDeltaTime;       // seconds between the scene's last two time steps, 0 when unknown
 	Vec3 sensorLinearVelocity;  // rgl_node_raytrace_configure_velocity, sensor frame
 	Vec3 sensorAngularVelocity; // roll, pitch, yaw rates in rad/s
+	const int8_t* rayMask;      // per ray, 0: not cast (far non-hit), or null
 };
 
 // One sensor (or served request) of a batched traversal launch (trace_batch.cu): its raytrace

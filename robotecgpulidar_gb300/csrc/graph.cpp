@@ -231,6 +231,12 @@ void SetRangeRaysNode::validateImpl()
 	}
 }
 
+void RaytraceNode::setRayMask(const int8_t* mask, size_t n)
+{
+	RGL_CHECK_CUDA(cudaMemcpy(rayMask.ensure(n), mask, n, cudaMemcpyHostToDevice));
+	rayMaskCount = n;
+}
+
 void SetRingIdsRaysNode::setParameters(const int32_t* r, size_t n)
 {
 	RGL_CHECK_CUDA(cudaMemcpy(ids.ensure(sizeof(int32_t) * n), r, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
@@ -404,6 +410,9 @@ void RaytraceNode::validateImpl()
 	if (fields.count(RGL_FIELD_TIME_STAMP_F64) && !scene->timeSet) {
 		throw InvalidPipeline("requested for field TIME_STAMP_F64, but RaytraceNode cannot get time from scene");
 	}
+	if (rayMaskCount != 0 && rayMaskCount != rays->rayCount()) {
+		throw InvalidPipeline("Mask size does not match the number of rays");
+	}
 	if (distortion && rays->timeOffsetsDev() == nullptr) {
 		throw InvalidPipeline("requested for raytrace with velocity distortion, but RaytraceNode cannot get time offsets");
 	}
@@ -524,6 +533,7 @@ rgl::TraceParams RaytraceNode::traceParams()
 	p.sceneDeltaTime = scene->deltaTimeSeconds();
 	p.sensorLinearVelocity = sensorLinearVelocity;
 	p.sensorAngularVelocity = sensorAngularVelocity;
+	p.rayMask = rayMaskCount ? rayMask.as<int8_t>() : nullptr;
 	return p;
 }
 
@@ -881,6 +891,24 @@ const void* FromArrayPointsNode::fieldDev(rgl_field_t f)
 		throw InvalidPipeline(format("FromArrayPointsNode does not provide field %s", rgl::fieldName(f)));
 	}
 	return it->second.get();
+}
+
+// ---- FilterGroundPointsNode
+
+void FilterGroundPointsNode::prepareImpl(cudaStream_t)
+{
+	flags.ensure(std::max<size_t>(1, sizeof(int32_t) * input->capacity()));
+}
+
+void FilterGroundPointsNode::enqueueImpl(cudaStream_t s)
+{
+	rgl::launchGroundFlags(static_cast<const float*>(input->fieldDev(RGL_FIELD_NORMAL_VEC3_F32)), (int) input->capacity(),
+	                       input->deviceCount(), up, angle, flags.as<int32_t>(), s);
+}
+
+const void* FilterGroundPointsNode::fieldDev(rgl_field_t f)
+{
+	return f == RGL_FIELD_IS_GROUND_I32 ? flags.get() : input->fieldDev(f);
 }
 
 // ---- SpatialMergePointsNode

@@ -273,6 +273,9 @@ struct RaytraceNode : PointsNode
 		sensorAngularVelocity = angular;
 	}
 	void setDistortion(bool on) { distortion = on; }
+	// Rays whose mask entry is 0 are not cast: their beams return the far non-hit (reference
+	// optixPrograms.cu:55-58).
+	void setRayMask(const int8_t* mask, size_t count);
 	int sampleCount() const;
 	void checkErrors() override;
 	std::shared_ptr<Scene> sceneRef; // keeps a scene made by rgl_gb300_scene_create alive
@@ -301,6 +304,8 @@ private:
 	float defaultIntensity = 0.0f;
 	rgl::Vec3 sensorLinearVelocity{0.0f, 0.0f, 0.0f}, sensorAngularVelocity{0.0f, 0.0f, 0.0f};
 	bool distortion = false;
+	rgl::DeviceBuffer rayMask;
+	size_t rayMaskCount = 0;
 	rgl::ErrorSlot errorFlag;
 	// The node's traversal as a one-job persistent launch.
 	rgl::StagedParam<rgl::BatchJob> job;
@@ -446,6 +451,30 @@ struct FromArrayPointsNode : PointsNode
 private:
 	size_t count = 0;
 	std::map<rgl_field_t, rgl::DeviceBuffer> data;
+};
+
+// Ground classification by normals (reference src/graph/FilterGroundPointsNode.cpp:17-50): adds
+// IS_GROUND_I32, 1 where the normal is more than the threshold away from the sensor's up vector (the
+// reference's flag marks the points to keep when compacting by it).
+struct FilterGroundPointsNode : PointsNodeSingleInput
+{
+	const char* name() const override { return "FilterGroundPointsNode"; }
+	void setParameters(rgl::Vec3 upVector, float threshold)
+	{
+		up = upVector;
+		angle = threshold;
+	}
+	std::vector<rgl_field_t> requiredFields() const override { return {RGL_FIELD_XYZ_VEC3_F32, RGL_FIELD_NORMAL_VEC3_F32}; }
+	bool hasField(rgl_field_t f) const override { return f == RGL_FIELD_IS_GROUND_I32 || input->hasField(f); }
+	void prepareImpl(cudaStream_t s) override;
+	void enqueueImpl(cudaStream_t s) override;
+	const void* fieldDev(rgl_field_t f) override;
+	bool lastUpdateContentOnly() const override { return false; }
+
+private:
+	rgl::Vec3 up{0.0f, 0.0f, 1.0f};
+	float angle = 0.0f;
+	rgl::DeviceBuffer flags;
 };
 
 // Concatenation of >= 2 unorganised point clouds, inputs in the order they were linked (reference

@@ -191,6 +191,10 @@ void launchMergePoints(const void* dTable, int nInputs, int nFields, int maxCoun
 // *dAcc += (dAdd ? *dAdd : addStatic), one thread.
 void launchAddCount(int32_t* dAcc, const int32_t* dAdd, int32_t addStatic, cudaStream_t s);
 
+// IS_GROUND_I32 of the ground filter (reference nodeKernels.cu:322-332): out[i] = angle between the
+// normal and the sensor's up vector (unsigned) > threshold, i.e. 1 for points that are not ground.
+void launchGroundFlags(const float* normals, int cap, const int32_t* dCount, Vec3 up, float threshold, int32_t* out, cudaStream_t s);
+
 size_t compactScratchBytes(int cap);
 // Stable compaction of `cap` points (first *dInCount valid when dInCount != null) by int32 flags.
 // Writes the kept count to *dOutCount.

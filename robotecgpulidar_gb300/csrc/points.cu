@@ -406,6 +406,17 @@ __global__ void __launch_bounds__(kBlock) kMergePoints(const void* table, int nI
 
 __global__ void kAddCount(int32_t* acc, const int32_t* add, int32_t addStatic) { *acc += add ? *add : addStatic; }
 
+__global__ void kGroundFlags(const float* __restrict__ normals, int cap, const int32_t* dCount, Vec3 up, float threshold,
+                             int32_t* __restrict__ out)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= countOf(cap, dCount)) {
+		return;
+	}
+	const Vec3 n = loadXyz(normals, i);
+	out[i] = acosf(fabsf(dot(n, up))) > threshold ? 1 : 0;
+}
+
 } // namespace
 
 size_t mergeTableBytes(int nInputs, int nFields)
@@ -433,6 +444,14 @@ void launchMergePoints(const void* dTable, int nInputs, int nFields, int maxCoun
 	const dim3 grid((unsigned) std::max(1, blocks(maxCount, kMergeTile)), (unsigned) nInputs);
 	kMergePoints<<<grid, kBlock, 0, s>>>(dTable, nInputs, nFields, dBase, dOutCount);
 	countLaunch();
+}
+
+void launchGroundFlags(const float* normals, int cap, const int32_t* dCount, Vec3 up, float threshold, int32_t* out, cudaStream_t s)
+{
+	if (cap > 0) {
+		kGroundFlags<<<blocks(cap, kBlock), kBlock, 0, s>>>(normals, cap, dCount, up, threshold, out);
+		countLaunch();
+	}
 }
 
 void launchAddCount(int32_t* dAcc, const int32_t* dAdd, int32_t addStatic, cudaStream_t s)

@@ -51,6 +51,59 @@ void Mesh::setRestposes(const rgl_mat3x4f* r, int32_t count)
 	restposeCount = count;
 }
 
+void Mesh::setTexCoords(const rgl_vec2f* uvs, int32_t count)
+{
+	if (count != vertexCount) {
+		throw rgl::InvalidAPIArgument(rgl::format("Cannot set texture coordinates because vertex count do not match with texture "
+		                                          "coordinates count: vertexCount=%d, textureCoords=%d",
+		                                          (int) vertexCount, (int) count));
+	}
+	RGL_CHECK_CUDA(cudaMemcpy(dTexCoords.ensure(sizeof(rgl_vec2f) * (size_t) count), uvs, sizeof(rgl_vec2f) * (size_t) count,
+	                          cudaMemcpyHostToDevice));
+	hasTexCoords = true;
+}
+
+Texture::Texture(const void* texels, int32_t w, int32_t h) : width(w), height(h)
+{
+	const cudaChannelFormatDesc channel = cudaCreateChannelDesc<unsigned char>();
+	RGL_CHECK_CUDA(cudaMallocArray(&array, &channel, (size_t) w, (size_t) h));
+	const size_t pitch = (size_t) w;
+	cudaError_t e = cudaMemcpy2DToArray(array, 0, 0, texels, pitch, pitch, (size_t) h, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		cudaFreeArray(array);
+		RGL_CHECK_CUDA(e);
+	}
+	cudaResourceDesc res{};
+	res.resType = cudaResourceTypeArray;
+	res.res.array.array = array;
+	cudaTextureDesc tex{};
+	tex.addressMode[0] = cudaAddressModeWrap;
+	tex.addressMode[1] = cudaAddressModeWrap;
+	tex.filterMode = cudaFilterModePoint;
+	tex.readMode = cudaReadModeElementType;
+	tex.normalizedCoords = 1;
+	tex.maxAnisotropy = 1;
+	tex.maxMipmapLevelClamp = 99;
+	tex.minMipmapLevelClamp = 0;
+	tex.mipmapFilterMode = cudaFilterModePoint;
+	tex.borderColor[0] = 1.0f;
+	e = cudaCreateTextureObject(&object, &res, &tex, nullptr);
+	if (e != cudaSuccess) {
+		cudaFreeArray(array);
+		RGL_CHECK_CUDA(e);
+	}
+}
+
+Texture::~Texture()
+{
+	if (object) {
+		cudaDestroyTextureObject(object);
+	}
+	if (array) {
+		cudaFreeArray(array);
+	}
+}
+
 void Mesh::ensureBlas(cudaStream_t s)
 {
 	if (blasBuilt) {
@@ -203,6 +256,12 @@ void Entity::setId(int32_t newId)
 	scene->markPosesDirty();
 }
 
+void Entity::setIntensityTexture(std::shared_ptr<Texture> t)
+{
+	intensityTexture = std::move(t);
+	scene->markPosesDirty(); // the texture travels in the instance record
+}
+
 void Entity::setLaserRetro(float retro)
 {
 	laserRetro = retro;
@@ -300,6 +359,9 @@ rgl::InstanceRec* Scene::fillInstanceRecords()
 		r.tris = bl.tris;
 		r.vertexDisplacement = e.vertexDisplacementSincePrevFrame();
 		r.indices = e.mesh->dIndices.as<int32_t>();
+		const bool textured = e.intensityTexture && e.mesh->hasTexCoords;
+		r.intensityTexture = textured ? (uint64_t) e.intensityTexture->object : 0;
+		r.texCoords = textured ? e.mesh->dTexCoords.as<float>() : nullptr;
 		r.entityId = e.id;
 		r.laserRetro = e.laserRetro;
 		r.hasPrev = e.previousTransform(r.prevObjectToWorld) ? 1 : 0;

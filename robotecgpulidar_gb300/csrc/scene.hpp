@@ -35,6 +35,10 @@ struct Mesh
 	bool blasBuilt = false;
 	rgl::DeviceBuffer dBoneWeights{false}, dRestposes{false};
 	int32_t boneWeightCount = 0, restposeCount = 0;
+	// Texture coordinates, one per vertex (reference Mesh.cpp:24-37).
+	void setTexCoords(const rgl_vec2f* uvs, int32_t count);
+	rgl::DeviceBuffer dTexCoords{false};
+	bool hasTexCoords = false;
 };
 
 struct Entity
@@ -74,14 +78,24 @@ struct Entity
 	rgl::ErrorSlot skinError;
 	int32_t id = RGL_DEFAULT_ENTITY_ID;
 	float laserRetro = 0.0f;
+	std::shared_ptr<Texture> intensityTexture;
+	void setIntensityTexture(std::shared_ptr<Texture> t);
 
 private:
 	void startAnimation();
 	void finishAnimation(cudaStream_t s);
 };
 
+// Intensity texture (reference src/scene/Texture.cpp:22-67): 8-bit texels in a CUDA array behind a
+// texture object with the reference's sampling (point filter, wrap addressing, normalised coordinates,
+// element reads).
 struct Texture
 {
+	Texture(const void* texels, int32_t width, int32_t height);
+	~Texture();
+	cudaArray_t array = nullptr;
+	cudaTextureObject_t object = 0;
+	int32_t width = 0, height = 0;
 };
 
 struct Scene

@@ -413,6 +413,19 @@ const std::map<std::string, Player>& players()
 	    {"rgl_entity_set_pose_world", [](Playback& p) { rgl_entity_set_pose_world(p.entity(0), p.ptr<rgl_mat3x4f>(1), p.i32(2)); }},
 	    {"rgl_entity_apply_external_animation",
 	     [](Playback& p) { rgl_entity_apply_external_animation(p.entity(0), p.ptr<rgl_vec3f>(1), p.i32(2)); }},
+	    {"rgl_texture_create",
+	     [](Playback& p) {
+		     rgl_texture_t t = nullptr;
+		     rgl_texture_create(&t, p.ptr<void>(1), p.i32(2), p.i32(3));
+		     p.textures[p.id(0)] = t;
+	     }},
+	    {"rgl_texture_destroy",
+	     [](Playback& p) {
+		     rgl_texture_destroy(p.texture(0));
+		     p.textures.erase(p.id(0));
+	     }},
+	    {"rgl_texture_is_alive", [](Playback& p) { bool v = false; rgl_texture_is_alive(p.texture(0), &v); }},
+	    {"rgl_entity_set_intensity_texture", [](Playback& p) { rgl_entity_set_intensity_texture(p.entity(0), p.texture(1)); }},
 	    {"rgl_mesh_destroy",
 	     [](Playback& p) {
 		     rgl_mesh_destroy(p.mesh(0));

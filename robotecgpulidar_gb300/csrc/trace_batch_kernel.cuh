@@ -51,11 +51,16 @@ __device__ __forceinline__ void laneGroupTask(const BatchJob* __restrict__ job, 
 		beam = job->order ? __ldg(job->order + local) : (uint32_t) local;
 		loadRay(job, beam, ray, minRange, maxRange);
 	}
+	// A masked ray is not cast: all its samples are far non-hits (reference optixPrograms.cu:55-58).
+	const bool cast = valid && !(job->p.rayMask && job->p.rayMask[beam] == 0);
 	SampleVal sv[ROUNDS];
 #pragma unroll
 	for (int r = 0; r < ROUNDS; ++r) {
 		const int s = sub + r * G;
-		if (valid && s < nSamples) {
+		if (valid && !cast && s < nSamples) {
+			sv[r] = emptySample();
+			sv[r].dist = job->p.farNonHitDistance;
+		} else if (valid && s < nSamples) {
 			const Mat34 traced = SHADING ? distortRay(job->p, beam, ray) : ray;
 			const Mat34 sr = (s == 0) ? traced : mul(traced, loadMat(job->samples + s));
 			sv[r] = traceSample<SHADING>(job->p.nearNonHitDistance, job->p.farNonHitDistance, job->p.defaultIntensity, sc, sr, minRange,
@@ -89,10 +94,15 @@ __device__ __forceinline__ void serialTask(const BatchJob* __restrict__ job, int
 	red.init(job->p.farNonHitDistance);
 	const int nSamples = job->p.nSamples;
 	const Mat34 traced = SHADING ? distortRay(job->p, beam, ray) : ray;
+	const bool cast = !(job->p.rayMask && job->p.rayMask[beam] == 0);
 	for (int s = 0; s < nSamples; ++s) {
-		const Mat34 sr = (s == 0) ? traced : mul(traced, loadMat(job->samples + s));
-		const SampleVal v = traceSample<SHADING>(job->p.nearNonHitDistance, job->p.farNonHitDistance, job->p.defaultIntensity, sc, sr,
-		                                         minRange, maxRange, st, s);
+		SampleVal v = emptySample();
+		v.dist = job->p.farNonHitDistance;
+		if (cast) {
+			const Mat34 sr = (s == 0) ? traced : mul(traced, loadMat(job->samples + s));
+			v = traceSample<SHADING>(job->p.nearNonHitDistance, job->p.farNonHitDistance, job->p.defaultIntensity, sc, sr, minRange,
+			                         maxRange, st, s);
+		}
 		red.add(s, v.hit, toSelected(v));
 	}
 	writeReturns<SHADING>(job->p, sc, job->samples, beam, ray, red);

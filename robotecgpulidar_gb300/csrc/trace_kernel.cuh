@@ -127,9 +127,35 @@ __device__ __forceinline__ Mat34 loadMat(const Mat34* p)
 constexpr int kSampleShift = 24; // instance indices stay below 1 << 24
 constexpr int32_t kInstMask = (1 << kSampleShift) - 1;
 
+// Barycentric weights (of b and of c) of point p in triangle (a, b, c), from areas; 0 for a degenerate
+// triangle.
+__device__ __forceinline__ void barycentric(Vec3 p, Vec3 a, Vec3 b, Vec3 c, float& u, float& w)
+{
+	const Vec3 n = cross(b - a, c - a);
+	const float nn = dot(n, n);
+	u = nn > 0.0f ? dot(cross(p - a, c - a), n) / nn : 0.0f;
+	w = nn > 0.0f ? dot(cross(b - a, p - a), n) / nn : 0.0f;
+}
+
+// Intensity texel at a hit (reference optixPrograms.cu:151-166): the texture coordinates of the hit
+// triangle's vertices interpolated at the hit's barycentric coordinates, point-sampled with wrap.
+__device__ __noinline__ float texturedIntensity(const InstanceRec& inst, const TriRecord& tr, Vec3 hitObject)
+{
+	float u, w;
+	barycentric(hitObject, v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), u, w);
+	const int32_t* idx = inst.indices + 3 * tr.primId;
+	const float* ta = inst.texCoords + 2 * idx[0];
+	const float* tb = inst.texCoords + 2 * idx[1];
+	const float* tc = inst.texCoords + 2 * idx[2];
+	const float wa = fsub(fsub(1.0f, u), w);
+	const float tu = fadd(fadd(fmul(wa, ta[0]), fmul(u, tb[0])), fmul(w, tc[0]));
+	const float tv = fadd(fadd(fmul(wa, ta[1]), fmul(u, tb[1])), fmul(w, tc[1]));
+	return (float) tex2D<unsigned char>((cudaTextureObject_t) inst.intensityTexture, tu, tv);
+}
+
 template<bool SHADING>
 __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNonHit, float defaultIntensity, const SceneView& sc,
-                                                   const HitRec& h, Vec3 d, float minRange, int sample)
+                                                   const HitRec& h, Vec3 o, Vec3 d, float minRange, int sample)
 {
 	DevLoader ld;
 	SampleVal v = emptySample();
@@ -154,7 +180,11 @@ __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNo
 				v.ny = n.y;
 				v.nz = n.z;
 				v.cosInc = c;
-				v.intensity = fmul(defaultIntensity, c);
+				float base = defaultIntensity;
+				if (inst.intensityTexture != 0) {
+					base = texturedIntensity(inst, tr, inst.worldToObject.point(o + d * h.t));
+				}
+				v.intensity = fmul(base, c);
 				v.tri = h.tri;
 			}
 		}
@@ -169,7 +199,7 @@ __device__ __forceinline__ SampleVal traceSample(float nearNonHit, float farNonH
 	DevLoader ld;
 	const Vec3 d = sr.rayDir();
 	const HitRec h = traceClosest(sc, sr.rayOrigin(), d, maxRange, st, ld);
-	return sampleFromHit<SHADING>(nearNonHit, farNonHit, defaultIntensity, sc, h, d, minRange, sample);
+	return sampleFromHit<SHADING>(nearNonHit, farNonHit, defaultIntensity, sc, h, sr.rayOrigin(), d, minRange, sample);
 }
 
 __device__ __forceinline__ Selected toSelected(const SampleVal& v)
@@ -282,11 +312,8 @@ __device__ __noinline__ void hitVelocities(const TraceParams& p, const InstanceR
 		// Animated mesh: the triangle's vertex displacements since the previous step, rotated into the
 		// world and interpolated at the hit's barycentric coordinates (reference optixPrograms.cu:185-195).
 		const TriRecord& tr = inst.tris[tri];
-		const Vec3 a = v3(tr.v0x, tr.v0y, tr.v0z), b = v3(tr.v1x, tr.v1y, tr.v1z), c = v3(tr.v2x, tr.v2y, tr.v2z);
-		const Vec3 n = cross(b - a, c - a);
-		const float nn = dot(n, n);
-		const float u = nn > 0.0f ? dot(cross(hitObject - a, c - a), n) / nn : 0.0f; // weight of b
-		const float w = nn > 0.0f ? dot(cross(b - a, hitObject - a), n) / nn : 0.0f; // weight of c
+		float u, w; // weights of vertices 1 and 2
+		barycentric(hitObject, v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), u, w);
 		const int32_t* idx = inst.indices + 3 * tr.primId;
 		auto vdisp = [&](int k) {
 			const float* q = inst.vertexDisplacement + 3 * idx[k];

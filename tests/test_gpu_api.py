@@ -162,9 +162,9 @@ def test_entity_id_limit(rgl):
 
 
 def test_not_implemented_calls_are_recoverable(rgl):
-    n = rgl.node()
-    up = np.array([0, 0, 1], np.float32)
-    assert rgl.lib().rgl_node_points_filter_ground(C.byref(n), rgl.ptr(up), 0.3) == rgl.RGL_NOT_IMPLEMENTED
+    tex = C.c_void_p()
+    texels = np.zeros(4, np.float32)
+    assert rgl.lib().rgl_texture_create(C.byref(tex), rgl.ptr(texels), 2, 2) == rgl.RGL_NOT_IMPLEMENTED
     # the library keeps working afterwards
     rgl.raytrace(rgl.node())
 

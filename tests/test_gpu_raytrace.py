@@ -374,3 +374,102 @@ def test_laser_retro_of_hit_entity(rgl, oracle):
     sel = (rgl.result(n["out"], rgl.RGL_FIELD_ENTITY_ID_I32) == top) & hit
     assert sel.any() and np.all(got2[sel] == np.float32(0.9))
     assert np.array_equal(got2[hit & ~sel], got[hit & ~sel])
+
+
+def test_ray_mask_skips_masked_rays(rgl):
+    """Masked rays are not cast: their beams return the far non-hit (reference optixPrograms.cu:55-58);
+    the other beams are unchanged."""
+    scene = scenes.million_scene(seed=2, instances=8, spheres=2, cells=32, extent=60.0)
+    rgl.spawn_scene(scene)
+    rays = scenes.lidar_rays(16, 128)
+    fields = [rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_IS_HIT_I32, rgl.RGL_FIELD_XYZ_VEC3_F32]
+    n = _beam_field_graph(rgl, rays, scenes.translation(0, 0, 6.0), fields)
+    lib = rgl.lib()
+    rgl.check(lib.rgl_node_raytrace_configure_non_hits(n["trace"], 0.5, 77.0))
+    rgl.graph_run(n["rays"])
+    full = {f: rgl.result(n["out"], f) for f in fields}
+    mask = (np.arange(len(rays)) % 3 != 0).astype(np.int8)
+    rgl.check(lib.rgl_node_raytrace_configure_mask(n["trace"], rgl.ptr(mask), len(mask)))
+    rgl.graph_run(n["rays"])
+    got = {f: rgl.result(n["out"], f) for f in fields}
+    on = mask == 1
+    for f in fields:
+        assert np.array_equal(got[f][on], full[f][on])
+    assert not got[rgl.RGL_FIELD_IS_HIT_I32][~on].any()
+    assert np.all(got[rgl.RGL_FIELD_DISTANCE_F32][~on] == np.float32(77.0))
+    assert (full[rgl.RGL_FIELD_IS_HIT_I32][~on] == 1).any()
+    short = np.ones(len(rays) - 1, np.int8)
+    rgl.check(lib.rgl_node_raytrace_configure_mask(n["trace"], rgl.ptr(short), len(short)))
+    with pytest.raises(rgl.RGLError) as e:
+        rgl.graph_run(n["rays"])
+    assert e.value.status == rgl.RGL_INVALID_PIPELINE and "Mask size does not match the number of rays" in str(e.value)
+
+
+def test_ground_filter_flags_non_ground_points(rgl):
+    """IS_GROUND_I32 = angle(normal, up) > threshold (reference nodeKernels.cu:322-332); compacting by
+    it keeps the points off the ground: here the wall, not the floor."""
+    floor = scenes.Mesh(np.array([[-50, -50, 0], [50, -50, 0], [50, 50, 0], [-50, 50, 0]], np.float32),
+                        np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    wall = scenes.Mesh(np.array([[8, -50, -1], [8, 50, -1], [8, 50, 30], [8, -50, 30]], np.float32),
+                       np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    rgl.spawn_scene(scenes.Scene([floor, wall], [scenes.Entity(0, scenes.translation(0, 0, 0), 1),
+                                                 scenes.Entity(1, scenes.translation(0, 0, 0), 2)]))
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "ground", "cmp", "out", "all")}
+    rgl.rays_from_mat3x4f(n["rays"], scenes.lidar_rays(16, 180))
+    rgl.rays_transform(n["pose"], scenes.translation(0, 0, 2.0))
+    rgl.raytrace(n["trace"])
+    up = np.array([0, 0, 1], np.float32)
+    rgl.check(rgl.lib().rgl_node_points_filter_ground(C.byref(n["ground"]), rgl.ptr(up), 0.1))
+    rgl.points_compact_by_field(n["cmp"], rgl.RGL_FIELD_IS_GROUND_I32)
+    rgl.points_yield(n["out"], [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_ENTITY_ID_I32])
+    rgl.points_yield(n["all"], [rgl.RGL_FIELD_IS_GROUND_I32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32])
+    rgl.chain(n["rays"], n["pose"], n["trace"], n["ground"], n["cmp"], n["out"])
+    rgl.add_child(n["ground"], n["all"])
+    rgl.graph_run(n["rays"])
+    flags = rgl.result(n["all"], rgl.RGL_FIELD_IS_GROUND_I32)
+    ent = rgl.result(n["all"], rgl.RGL_FIELD_ENTITY_ID_I32)
+    hit = rgl.result(n["all"], rgl.RGL_FIELD_IS_HIT_I32) == 1
+    assert (hit & (ent == 1)).any() and (hit & (ent == 2)).any()
+    assert np.all(flags[hit & (ent == 1)] == 0) and np.all(flags[hit & (ent == 2)] == 1)
+    kept = rgl.result(n["out"], rgl.RGL_FIELD_ENTITY_ID_I32)
+    assert len(kept) == int(flags.sum()) and np.all(kept[kept != 0] == 2)
+
+
+def test_intensity_texture(rgl):
+    """Intensity = texel at the hit's interpolated texture coordinates (point sampling, wrap) times
+    |cos| of the incidence (reference optixPrograms.cu:151-167); entities without a texture keep the
+    default intensity."""
+    lib = rgl.lib()
+    quad = scenes.Mesh(np.array([[0, 0, 0], [4, 0, 0], [4, 4, 0], [0, 4, 0]], np.float32), np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    m = rgl.mesh_create(quad.vertices, quad.indices)
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    rgl.check(lib.rgl_mesh_set_texture_coords(m, rgl.ptr(uv), 4))
+    assert lib.rgl_mesh_set_texture_coords(m, rgl.ptr(uv), 3) == rgl.RGL_INVALID_ARGUMENT
+    texels = (np.arange(16, dtype=np.uint8) * 13 + 7).reshape(4, 4)  # row = v, column = u
+    tex = C.c_void_p()
+    rgl.check(lib.rgl_texture_create(C.byref(tex), rgl.ptr(np.ascontiguousarray(texels)), 4, 4))
+    textured, plain = rgl.entity_create(m), rgl.entity_create(m)
+    rgl.entity_set_transform(textured, scenes.translation(0, 0, 0))
+    rgl.entity_set_transform(plain, scenes.translation(10, 0, 0))
+    rgl.check(lib.rgl_entity_set_intensity_texture(textured, tex))
+    down = scenes.rotation_xyz(np.pi, 0, 0)
+    rays, expect = [], []
+    for j in range(4):
+        for i in range(4):
+            r = down.copy()
+            r[:, 3] = (i + 0.5, j + 0.5, 5.0)
+            rays.append(r)
+            expect.append(float(texels[j, i]))
+    r = down.copy()
+    r[:, 3] = (12.0, 2.0, 5.0)
+    rays.append(r)
+    expect.append(3.0)
+    n = {k: rgl.node() for k in ("rays", "trace", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], np.stack(rays))
+    rgl.raytrace(n["trace"])
+    rgl.check(lib.rgl_node_raytrace_configure_default_intensity(n["trace"], 3.0))
+    rgl.points_yield(n["out"], [rgl.RGL_FIELD_INTENSITY_F32, rgl.RGL_FIELD_IS_HIT_I32])
+    rgl.chain(n["rays"], n["trace"], n["out"])
+    rgl.graph_run(n["rays"])
+    assert (rgl.result(n["out"], rgl.RGL_FIELD_IS_HIT_I32) == 1).all()
+    assert np.array_equal(rgl.result(n["out"], rgl.RGL_FIELD_INTENSITY_F32), np.array(expect, np.float32))
