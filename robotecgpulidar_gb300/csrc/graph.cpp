@@ -27,7 +27,7 @@ uint64_t Node::nextParamVersion() { return gParamVersion.fetch_add(1, std::memor
 namespace {
 // Schedule of single-graph traversals (a batch of one job). The default is the fastest measured on
 // the 1M-triangle single-sensor scan: lane-group packing, one task per fetch, 80 registers.
-rgl::BatchSchedule gTraceSchedule{256, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 80};
+rgl::BatchSchedule gTraceSchedule{128, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 96};
 } // namespace
 rgl::BatchSchedule traceSchedule() { return gTraceSchedule; }
 void setTraceSchedule(const rgl::BatchSchedule& s) { gTraceSchedule = s; }
@@ -393,11 +393,12 @@ int RaytraceNode::sampleCount() const
 
 void RaytraceNode::validateImpl()
 {
+	// Fields the raytrace does not produce (IS_GROUND_I32 of a ground filter downstream, radar fields)
+	// are left to the nodes that produce them; a node that needs one from the raytrace itself fails its
+	// own validation ("requires ... to be present").
 	fields = findFieldsToCompute();
-	for (auto f : fields) {
-		if (!raytraceSupports(f)) {
-			throw rgl::NotImplemented(format("RaytraceNode cannot compute field %s in this implementation", rgl::fieldName(f)));
-		}
+	for (auto it = fields.begin(); it != fields.end();) {
+		it = raytraceSupports(*it) ? std::next(it) : fields.erase(it);
 	}
 	rays = exactlyOneInput<RaysNode>("IRaysNode");
 	if (scene == nullptr) {

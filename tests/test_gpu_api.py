@@ -162,9 +162,9 @@ def test_entity_id_limit(rgl):
 
 
 def test_not_implemented_calls_are_recoverable(rgl):
-    tex = C.c_void_p()
-    texels = np.zeros(4, np.float32)
-    assert rgl.lib().rgl_texture_create(C.byref(tex), rgl.ptr(texels), 2, 2) == rgl.RGL_NOT_IMPLEMENTED
+    n = rgl.node()
+    f = C.c_float(1.0)
+    assert rgl.lib().rgl_node_points_radar_track_objects(C.byref(n), f, f, f, f, f, f, f) == rgl.RGL_NOT_IMPLEMENTED
     # the library keeps working afterwards
     rgl.raytrace(rgl.node())
 

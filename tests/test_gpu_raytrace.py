@@ -269,7 +269,7 @@ def test_union_and_single_ray_traversals_agree(rgl, layers, vertices):
         rgl.check(lib.rgl_gb300_configure_trace_schedule(256, packing, 1, regs))
         rgl.graph_run(n["rays"])
         got[(packing, regs)] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
-    rgl.check(lib.rgl_gb300_configure_trace_schedule(256, 0, 1, 80))
+    rgl.check(lib.rgl_gb300_configure_trace_schedule(128, 0, 1, 96))  # back to the default
     ref = got[(1, 128)]
     for k, v in got.items():
         assert v == ref, f"schedule {k} differs from single-ray traversal"
