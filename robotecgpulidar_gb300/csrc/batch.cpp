@@ -108,12 +108,9 @@ void BatchRun::buildJobs()
 	beams = 0;
 	rays = 0;
 	for (size_t j = 0; j < n; ++j) {
-		const rgl::TraceParams p = members[j].trace->traceParams();
 		rgl::BatchJob& b = jobs[j];
-		b.p = p;
-		b.samples = members[j].trace->sampleTableDev();
-		b.order = nullptr;
-		b.groupSize = std::min(p.nSamples, 32);
+		members[j].trace->fillJob(b);
+		const rgl::TraceParams& p = b.p;
 		shading = shading || rgl::needsShadingKernel(p);
 		maxSamples = std::max(maxSamples, (int) p.nSamples);
 		beamBase[j] = beams;
@@ -215,8 +212,8 @@ void BatchRun::computeOrder(int order, cudaStream_t st)
 	auto* vals = static_cast<uint32_t*>(dOrder.ensure(sizeof(uint32_t) * beams));
 	for (size_t j = 0; j < members.size(); ++j) {
 		const Scene* sc = members[j].trace->scene;
-		rgl::launchBeamKeys(jobs[j].p.rays, jobs[j].p.nRays, (uint32_t) j, order, sc->worldLower(), sc->worldUpper(), keys + beamBase[j],
-		                    vals + beamBase[j], st);
+		rgl::launchBeamKeys(jobs[j].p.rays, jobs[j].hasRayTransform ? &jobs[j].rayTransform : nullptr, jobs[j].p.nRays, (uint32_t) j,
+		                    order, sc->worldLower(), sc->worldUpper(), keys + beamBase[j], vals + beamBase[j], st);
 	}
 	int jobBits = 0;
 	while ((size_t{1} << jobBits) < members.size()) {

@@ -194,6 +194,9 @@ void FromMat3x4fRaysNode::validateImpl()
 
 void TransformRaysNode::prepareImpl(cudaStream_t)
 {
+	if (folded) {
+		return; // the consuming raytrace applies the transform
+	}
 	out.ensure(sizeof(Mat34) * std::max<size_t>(1, rayCount()));
 	staged.host() = transform;
 	(void) staged.device();
@@ -201,6 +204,9 @@ void TransformRaysNode::prepareImpl(cudaStream_t)
 
 void TransformRaysNode::enqueueImpl(cudaStream_t s)
 {
+	if (folded) {
+		return;
+	}
 	rgl::launchTransformRays(input->raysDev(), out.as<Mat34>(), (int) rayCount(), staged.enqueue(s), s);
 }
 
@@ -404,6 +410,25 @@ void RaytraceNode::validateImpl()
 	if (scene == nullptr) {
 		scene = &Scene::defaultScene();
 	}
+	// Fold the sensor transform into the traversal prologue when this node is its only consumer
+	// (through nodes that pass rays through unchanged): one kernel and one pass over the rays less.
+	if (foldedTransform) {
+		foldedTransform->folded = false;
+		foldedTransform.reset();
+	}
+	{
+		Node* cur = this;
+		std::shared_ptr<RaysNode> up = rays;
+		while (up && up->outputs.size() == 1 && up->outputs[0].get() == cur && up->passesRaysThrough()) {
+			cur = up.get();
+			up = up->inputs.size() == 1 ? std::dynamic_pointer_cast<RaysNode>(up->inputs[0]) : nullptr;
+		}
+		auto tf = std::dynamic_pointer_cast<TransformRaysNode>(up);
+		if (tf && tf->outputs.size() == 1 && tf->outputs[0].get() == cur) {
+			tf->folded = true;
+			foldedTransform = tf;
+		}
+	}
 	// Reference src/graph/RaytraceNode.cpp:37-45.
 	if (fields.count(RGL_FIELD_RING_ID_U16) && rays->ringIdsDev() == nullptr) {
 		throw InvalidPipeline("requested for field RING_ID_U16, but RaytraceNode cannot get ring ids");
@@ -540,15 +565,25 @@ rgl::TraceParams RaytraceNode::traceParams()
 
 // The traversal is the persistent kernel of batched frames with this node as its only job: the job
 // record and the task count are staged every run (new ray contents need no re-capture).
-void RaytraceNode::stageJob()
+void RaytraceNode::fillJob(rgl::BatchJob& b)
 {
-	const rgl::TraceParams p = traceParams();
-	rgl::BatchJob& b = job.host();
 	b = rgl::BatchJob{};
-	b.p = p;
+	b.p = traceParams();
 	b.samples = sampleTable.as<Mat34>();
 	b.order = nullptr;
-	b.groupSize = std::min(p.nSamples, 32);
+	b.groupSize = std::min(b.p.nSamples, 32);
+	if (foldedTransform) {
+		b.p.rays = foldedTransform->sourceRaysDev();
+		b.hasRayTransform = 1;
+		b.rayTransform = foldedTransform->matrix();
+	}
+}
+
+void RaytraceNode::stageJob()
+{
+	rgl::BatchJob& b = job.host();
+	fillJob(b);
+	const rgl::TraceParams& p = b.p;
 	(void) job.device();
 	schedule = traceSchedule();
 	const int per = rgl::batchBeamsPerTask(schedule.packing, p.nSamples);

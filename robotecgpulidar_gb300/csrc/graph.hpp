@@ -79,6 +79,8 @@ struct RaysNode : virtual Node
 	virtual size_t ringIdsCount() const { return 0; }
 	virtual const float* timeOffsetsDev() const { return nullptr; }
 	virtual size_t timeOffsetsCount() const { return 0; }
+	// True for nodes that pass their input's ray poses through unchanged (ranges, ring ids, offsets).
+	virtual bool passesRaysThrough() const { return false; }
 };
 
 struct RaysNodeSingleInput : RaysNode
@@ -124,6 +126,12 @@ struct TransformRaysNode : RaysNodeSingleInput
 	rgl::Mat34 cumulativeRayTransform() const override { return rgl::mul(transform, input->cumulativeRayTransform()); }
 	bool lastUpdateContentOnly() const override { return true; } // the transform is staged every run
 
+	// Folded into the traversal of its only consumer: the raytrace reads this node's input rays and
+	// applies `transform` in its prologue with the same arithmetic, and this node launches nothing.
+	bool folded = false;
+	const rgl::Mat34* sourceRaysDev() const { return input->raysDev(); }
+	const rgl::Mat34& matrix() const { return transform; }
+
 private:
 	rgl::Mat34 transform = rgl::Mat34::identity();
 	rgl::StagedParam<rgl::Mat34> staged;
@@ -133,6 +141,7 @@ private:
 struct SetRangeRaysNode : RaysNodeSingleInput
 {
 	const char* name() const override { return "SetRangeRaysNode"; }
+	bool passesRaysThrough() const override { return true; }
 	void setParameters(const rgl_vec2f* ranges, size_t count);
 	void validateImpl() override;
 	void enqueueImpl(cudaStream_t) override {}
@@ -149,6 +158,7 @@ private:
 struct SetRingIdsRaysNode : RaysNodeSingleInput
 {
 	const char* name() const override { return "SetRingIdsRaysNode"; }
+	bool passesRaysThrough() const override { return true; }
 	void setParameters(const int32_t* ids, size_t n);
 	void validateImpl() override;
 	void enqueueImpl(cudaStream_t) override {}
@@ -165,6 +175,7 @@ private:
 struct SetTimeOffsetsRaysNode : RaysNodeSingleInput
 {
 	const char* name() const override { return "SetTimeOffsetsRaysNode"; }
+	bool passesRaysThrough() const override { return true; }
 	void setParameters(const float* offsets, size_t n);
 	void validateImpl() override;
 	void enqueueImpl(cudaStream_t) override {}
@@ -281,6 +292,9 @@ struct RaytraceNode : PointsNode
 	std::shared_ptr<Scene> sceneRef; // keeps a scene made by rgl_gb300_scene_create alive
 	// Launch parameters of the traversal for the current buffers (valid after prepareImpl).
 	rgl::TraceParams traceParams();
+	// The node's job of a traversal launch (parameters, sub-ray table, lane-group width, a folded
+	// sensor transform); order and task bases are the launcher's.
+	void fillJob(rgl::BatchJob& b);
 	void stageJob();
 	const rgl::Mat34* sampleTableDev() const { return sampleTable.as<rgl::Mat34>(); }
 	Scene* scene = nullptr;
@@ -291,6 +305,7 @@ struct RaytraceNode : PointsNode
 private:
 	std::set<rgl_field_t> findFieldsToCompute();
 	std::shared_ptr<RaysNode> rays;
+	std::shared_ptr<TransformRaysNode> foldedTransform; // see TransformRaysNode::folded
 	std::set<rgl_field_t> fields;
 	std::map<rgl_field_t, rgl::DeviceBuffer> outputs;
 	rgl::DeviceBuffer defaultRange;

@@ -131,7 +131,7 @@ void launchSegCompact(const SegCompactJob* dSegs, const int32_t* dTileBase, int 
                       uint32_t* dTileOffsets, int32_t* dCounts, cudaStream_t s);
 
 // Sort keys of one sensor's beams (job index in the top bits) and their local indices.
-void launchBeamKeys(const Mat34* rays, int n, uint32_t jobIndex, int order, const float* worldLo, const float* worldHi,
+void launchBeamKeys(const Mat34* rays, const Mat34* transform, int n, uint32_t jobIndex, int order, const float* worldLo, const float* worldHi,
                     uint32_t* keys, uint32_t* values, cudaStream_t stream);
 
 // ---- points.cu

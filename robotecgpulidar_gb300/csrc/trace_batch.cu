@@ -65,14 +65,17 @@ __device__ __forceinline__ uint32_t quant(float x, uint32_t levels)
 // Key = job index in bits 22..31, a 22-bit direction code below. Octahedral: the world direction
 // folded onto the octahedron, 11 bits per coordinate, interleaved. Morton: the point 5 % of the world
 // diagonal along the ray, 7 bits per axis over the world box, interleaved.
-__global__ void kBeamKeys(const Mat34* __restrict__ rays, int n, uint32_t jobIndex, int order, float3 lo, float3 inv, float probe,
-                          uint32_t* __restrict__ keys, uint32_t* __restrict__ values)
+__global__ void kBeamKeys(const Mat34* __restrict__ rays, Mat34 tf, int hasTf, int n, uint32_t jobIndex, int order, float3 lo, float3 inv,
+                          float probe, uint32_t* __restrict__ keys, uint32_t* __restrict__ values)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) {
 		return;
 	}
-	const Mat34 r = loadMat(rays + i);
+	Mat34 r = loadMat(rays + i);
+	if (hasTf) {
+		r = mul(tf, r); // a sensor transform folded into the traversal: key the world rays
+	}
 	const Vec3 o = r.rayOrigin();
 	const Vec3 d = normalized(r.rayDir());
 	uint32_t code = 0;
@@ -205,7 +208,7 @@ void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs
 	countLaunch();
 }
 
-void launchBeamKeys(const Mat34* rays, int n, uint32_t jobIndex, int order, const float* worldLo, const float* worldHi, uint32_t* keys,
+void launchBeamKeys(const Mat34* rays, const Mat34* transform, int n, uint32_t jobIndex, int order, const float* worldLo, const float* worldHi, uint32_t* keys,
                     uint32_t* values, cudaStream_t stream)
 {
 	if (n <= 0) {
@@ -219,7 +222,8 @@ void launchBeamKeys(const Mat34* rays, int n, uint32_t jobIndex, int order, cons
 	lo.y -= probe;
 	lo.z -= probe;
 	const float3 inv = make_float3(1.0f / (ex + 2 * probe), 1.0f / (ey + 2 * probe), 1.0f / (ez + 2 * probe));
-	kBeamKeys<<<(n + 255) / 256, 256, 0, stream>>>(rays, n, jobIndex, order, lo, inv, probe, keys, values);
+	const Mat34 tf = transform ? *transform : Mat34::identity();
+	kBeamKeys<<<(n + 255) / 256, 256, 0, stream>>>(rays, tf, transform ? 1 : 0, n, jobIndex, order, lo, inv, probe, keys, values);
 	countLaunch();
 }
 

@@ -98,3 +98,45 @@ def test_second_run_advances_noise_and_reset_reproduces(rgl):
     rgl.graph_run(n_rays)
     c = rgl.result(y, rgl.RGL_FIELD_DISTANCE_F32)
     assert not np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_folded_sensor_transform_equals_separate_kernel(rgl):
+    """A rays transform whose only consumer is the raytrace is applied in the traversal prologue (no
+    transform kernel); with a second consumer it runs as its own kernel. Both give the same bytes."""
+    scene = scenes.million_scene(seed=6, instances=10, spheres=2, cells=48, extent=90.0)
+    rgl.spawn_scene(scene)
+    rays = scenes.lidar_rays(32, 256)
+    pose = scenes.trs((3.0, -4.0, 5.0), (0.02, -0.03, 0.7))
+    fields = [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_AZIMUTH_F32]
+
+    def graph(extra_consumer):
+        n = {k: rgl.node() for k in ("rays", "pose", "range", "trace", "out")}
+        rgl.rays_from_mat3x4f(n["rays"], rays)
+        rgl.rays_transform(n["pose"], pose)
+        rgl.rays_set_range(n["range"], [[0.1, 80.0]])
+        rgl.raytrace(n["trace"])
+        rgl.points_yield(n["out"], fields)
+        rgl.chain(n["rays"], n["pose"], n["range"], n["trace"], n["out"])
+        if extra_consumer:
+            n["trace2"] = rgl.node()
+            rgl.raytrace(n["trace2"])
+            rgl.add_child(n["pose"], n["trace2"])
+        return n
+
+    a, b = graph(False), graph(True)
+    l0 = rgl.kernel_launch_count()
+    rgl.graph_run(a["rays"])
+    ra = {f: rgl.result_bytes(a["out"], f).tobytes() for f in fields}
+    l1 = rgl.kernel_launch_count()
+    rgl.graph_run(b["rays"])
+    rb = {f: rgl.result_bytes(b["out"], f).tobytes() for f in fields}
+    l2 = rgl.kernel_launch_count()
+    assert ra == rb
+    assert (l1 - l0) < (l2 - l1)  # the folded graph launches no transform kernel
+    # A new pose reaches the folded traversal without a new capture.
+    pose2 = scenes.trs((1.0, 2.0, 4.0), (0.0, 0.0, -0.4))
+    rgl.rays_transform(a["pose"], pose2)
+    rgl.rays_transform(b["pose"], pose2)
+    rgl.graph_run(a["rays"])
+    rgl.graph_run(b["rays"])
+    assert {f: rgl.result_bytes(a["out"], f).tobytes() for f in fields} == {f: rgl.result_bytes(b["out"], f).tobytes() for f in fields}
