@@ -715,6 +715,21 @@ void CompactByFieldPointsNode::validateImpl()
 		}
 	};
 	dfs(this);
+	// Transform and noise nodes that feed only this compaction (one consumer each, up the chain) run
+	// inside its pass, on the kept points only; nodes are validated in execution order, so each one
+	// has already reset its own flag this run.
+	chain.clear();
+	chainSource = input;
+	while (auto pw = std::dynamic_pointer_cast<PointwisePointsNode>(chainSource)) {
+		if (pw->outputs.size() != 1 || chain.size() == (size_t) rgl::kMaxPointOps) {
+			break;
+		}
+		chain.insert(chain.begin(), pw);
+		chainSource = pw->source();
+	}
+	for (auto& pw : chain) {
+		pw->absorbed = true;
+	}
 	if (count.get() == nullptr) {
 		count.ensure(sizeof(int32_t));
 		RGL_CHECK_CUDA(cudaMemset(count.get(), 0, sizeof(int32_t)));
@@ -744,18 +759,36 @@ void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cu
 {
 	const size_t cap = input->capacity();
 	rgl::FieldCopies fc{};
+	rgl::PointOps ops{};
+	ops.xyzField = -1;
+	ops.distField = -1;
+	const bool absorbs = !chain.empty();
 	for (auto f : which) {
 		if (fc.count == rgl::kMaxFieldCopies) {
 			throw rgl::InvalidAPIArgument(format("compaction of more than %d fields", rgl::kMaxFieldCopies));
 		}
 		rgl::FieldCopy c{};
 		c.size = (int32_t) rgl::fieldSize(f);
-		c.src = input->fieldDev(f);
+		if (absorbs && (f == RGL_FIELD_XYZ_VEC3_F32 || f == RGL_FIELD_DISTANCE_F32)) {
+			(f == RGL_FIELD_XYZ_VEC3_F32 ? ops.xyzField : ops.distField) = fc.count;
+			c.src = nullptr; // computed from the chain's source
+		} else {
+			c.src = input->fieldDev(f);
+		}
 		c.dst = outputs[f].get();
 		fc.f[fc.count++] = c;
 	}
-	rgl::launchCompact(static_cast<const int32_t*>(input->fieldDev(field)), (int) cap, input->deviceCount(), fc, count.as<int32_t>(),
-	                   scratch.get(), errorFlag.device(), s);
+	if (absorbs && (ops.xyzField >= 0 || ops.distField >= 0)) {
+		for (auto& pw : chain) {
+			pw->appendPointOp(ops, s);
+		}
+		ops.srcXyz = static_cast<const float*>(chainSource->fieldDev(RGL_FIELD_XYZ_VEC3_F32));
+		ops.srcDist = chainSource->hasField(RGL_FIELD_DISTANCE_F32) ? static_cast<const float*>(chainSource->fieldDev(RGL_FIELD_DISTANCE_F32))
+		                                                            : nullptr;
+	}
+	rgl::launchCompact(static_cast<const int32_t*>(input->fieldDev(field)), (int) cap, input->deviceCount(), fc,
+	                   ops.count > 0 || ops.xyzField >= 0 || ops.distField >= 0 ? &ops : nullptr, count.as<int32_t>(), scratch.get(),
+	                   errorFlag.device(), s);
 }
 
 void CompactByFieldPointsNode::enqueueImpl(cudaStream_t s)
@@ -789,25 +822,64 @@ void CompactByFieldPointsNode::checkErrors()
 	}
 }
 
+// ---- Pointwise nodes (transform, point noise)
+
+void PointwisePointsNode::computeOnDemand()
+{
+	if (computedOnDemand) {
+		return;
+	}
+	if (lastStream == nullptr) {
+		throw InvalidPipeline(format("Cannot get results from %s; it hasn't been run yet", name()));
+	}
+	allocateOutputs();
+	launchOwn(lastStream);
+	RGL_CHECK_CUDA(cudaStreamSynchronize(lastStream));
+	computedOnDemand = true;
+}
+
 // ---- TransformPointsNode
 
-void TransformPointsNode::prepareImpl(cudaStream_t)
+void TransformPointsNode::allocateOutputs() { out.ensure(std::max<size_t>(1, 12 * input->capacity())); }
+
+void TransformPointsNode::prepareImpl(cudaStream_t s)
 {
-	out.ensure(std::max<size_t>(1, 12 * input->capacity()));
+	beginRun(s);
+	if (!absorbed) {
+		allocateOutputs();
+	}
 	staged.host() = transform;
 	(void) staged.device();
 }
 
-void TransformPointsNode::enqueueImpl(cudaStream_t s)
+void TransformPointsNode::launchOwn(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
 	rgl::launchTransformPoints(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), out.as<float>(), (int) cap,
 	                           input->deviceCount(), staged.enqueue(s), s);
 }
 
+void TransformPointsNode::enqueueImpl(cudaStream_t s)
+{
+	if (!absorbed) {
+		launchOwn(s);
+	}
+}
+
+void TransformPointsNode::appendPointOp(rgl::PointOps& ops, cudaStream_t s)
+{
+	ops.op[ops.count++] = rgl::PointOp{rgl::kOpTransform, 0, staged.enqueue(s)};
+}
+
 const void* TransformPointsNode::fieldDev(rgl_field_t f)
 {
-	return f == RGL_FIELD_XYZ_VEC3_F32 ? out.get() : input->fieldDev(f);
+	if (f != RGL_FIELD_XYZ_VEC3_F32) {
+		return input->fieldDev(f);
+	}
+	if (absorbed) {
+		computeOnDemand();
+	}
+	return out.get();
 }
 
 // ---- Gaussian noise on points
@@ -819,33 +891,54 @@ void GaussianNoiseAngularHitpointNode::setParameters(float m, float sd, rgl_axis
 	axis = a;
 }
 
-void GaussianNoiseAngularHitpointNode::prepareImpl(cudaStream_t)
+void GaussianNoiseAngularHitpointNode::allocateOutputs()
 {
 	const size_t cap = input->capacity();
-	withDistance = input->hasField(RGL_FIELD_DISTANCE_F32);
 	outXyz.ensure(std::max<size_t>(1, 12 * cap));
 	if (withDistance) {
 		outDist.ensure(std::max<size_t>(1, 4 * cap));
 	}
+}
+
+void GaussianNoiseAngularHitpointNode::prepareImpl(cudaStream_t s)
+{
+	beginRun(s);
+	withDistance = input->hasField(RGL_FIELD_DISTANCE_F32);
+	if (!absorbed) {
+		allocateOutputs();
+	}
 	stageNoise(staged, seed, frame, 2, mean, stDev, 0.0f, axis, input->lookAtOriginTransform());
 }
 
-void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
+void GaussianNoiseAngularHitpointNode::launchOwn(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
 	rgl::launchNoiseAngularHitpoint(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)), outXyz.as<float>(),
 	                                withDistance ? outDist.as<float>() : nullptr, (int) cap, input->deviceCount(), staged.enqueue(s), s);
 }
 
+void GaussianNoiseAngularHitpointNode::enqueueImpl(cudaStream_t s)
+{
+	if (!absorbed) {
+		launchOwn(s);
+	}
+}
+
+void GaussianNoiseAngularHitpointNode::appendPointOp(rgl::PointOps& ops, cudaStream_t s)
+{
+	ops.op[ops.count++] = rgl::PointOp{rgl::kOpNoiseAngularHitpoint, withDistance ? 1 : 0, staged.enqueue(s)};
+}
+
 const void* GaussianNoiseAngularHitpointNode::fieldDev(rgl_field_t f)
 {
-	if (f == RGL_FIELD_XYZ_VEC3_F32) {
-		return outXyz.get();
+	const bool own = f == RGL_FIELD_XYZ_VEC3_F32 || (f == RGL_FIELD_DISTANCE_F32 && withDistance);
+	if (!own) {
+		return input->fieldDev(f);
 	}
-	if (f == RGL_FIELD_DISTANCE_F32 && withDistance) {
-		return outDist.get();
+	if (absorbed) {
+		computeOnDemand();
 	}
-	return input->fieldDev(f);
+	return f == RGL_FIELD_XYZ_VEC3_F32 ? outXyz.get() : outDist.get();
 }
 
 void GaussianNoiseDistanceNode::setParameters(float m, float b, float r)
@@ -855,15 +948,23 @@ void GaussianNoiseDistanceNode::setParameters(float m, float b, float r)
 	rise = r;
 }
 
-void GaussianNoiseDistanceNode::prepareImpl(cudaStream_t)
+void GaussianNoiseDistanceNode::allocateOutputs()
 {
 	const size_t cap = input->capacity();
 	outXyz.ensure(std::max<size_t>(1, 12 * cap));
 	outDist.ensure(std::max<size_t>(1, 4 * cap));
+}
+
+void GaussianNoiseDistanceNode::prepareImpl(cudaStream_t s)
+{
+	beginRun(s);
+	if (!absorbed) {
+		allocateOutputs();
+	}
 	stageNoise(staged, seed, frame, 3, mean, base, rise, 0, input->lookAtOriginTransform());
 }
 
-void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
+void GaussianNoiseDistanceNode::launchOwn(cudaStream_t s)
 {
 	const size_t cap = input->capacity();
 	rgl::launchNoiseDistance(static_cast<const float*>(input->fieldDev(RGL_FIELD_XYZ_VEC3_F32)),
@@ -871,15 +972,27 @@ void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
 	                         outDist.as<float>(), (int) cap, input->deviceCount(), staged.enqueue(s), s);
 }
 
+void GaussianNoiseDistanceNode::enqueueImpl(cudaStream_t s)
+{
+	if (!absorbed) {
+		launchOwn(s);
+	}
+}
+
+void GaussianNoiseDistanceNode::appendPointOp(rgl::PointOps& ops, cudaStream_t s)
+{
+	ops.op[ops.count++] = rgl::PointOp{rgl::kOpNoiseDistance, 1, staged.enqueue(s)};
+}
+
 const void* GaussianNoiseDistanceNode::fieldDev(rgl_field_t f)
 {
-	if (f == RGL_FIELD_XYZ_VEC3_F32) {
-		return outXyz.get();
+	if (f != RGL_FIELD_XYZ_VEC3_F32 && f != RGL_FIELD_DISTANCE_F32) {
+		return input->fieldDev(f);
 	}
-	if (f == RGL_FIELD_DISTANCE_F32) {
-		return outDist.get();
+	if (absorbed) {
+		computeOnDemand();
 	}
-	return input->fieldDev(f);
+	return f == RGL_FIELD_XYZ_VEC3_F32 ? outXyz.get() : outDist.get();
 }
 
 // ---- FromArrayPointsNode (reference src/graph/FromArrayPointsNode.cpp:18-46)

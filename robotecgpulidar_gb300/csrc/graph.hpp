@@ -247,6 +247,39 @@ protected:
 	std::shared_ptr<PointsNode> input;
 };
 
+// A node that maps XYZ (and distance) point by point: transform and point noise. When its only
+// consumer leads, through such nodes, to a compaction, the compaction applies it to the points it keeps
+// in its own pass (kCompact's point operations) and this node launches nothing; its fields are then
+// computed only if asked for directly after the run.
+struct PointwisePointsNode : PointsNodeSingleInput
+{
+	void validateImpl() override
+	{
+		PointsNodeSingleInput::validateImpl();
+		absorbed = false;
+	}
+	// Stages this node's parameters on `s` and appends its operation.
+	virtual void appendPointOp(rgl::PointOps& ops, cudaStream_t s) = 0;
+	std::shared_ptr<PointsNode> source() const { return input; }
+	bool absorbed = false;
+
+protected:
+	// Per-run bookkeeping of an absorbed node (call from prepareImpl).
+	void beginRun(cudaStream_t s)
+	{
+		lastStream = s;
+		computedOnDemand = false;
+	}
+	// Runs the node's own kernel on the run's stream and waits, once per run (absorbed nodes only).
+	void computeOnDemand();
+	virtual void allocateOutputs() = 0;
+	virtual void launchOwn(cudaStream_t s) = 0;
+
+private:
+	cudaStream_t lastStream = nullptr;
+	bool computedOnDemand = false;
+};
+
 struct RaytraceNode : PointsNode
 {
 	const char* name() const override { return "RaytraceNode"; }
@@ -371,12 +404,16 @@ struct CompactByFieldPointsNode : PointsNodeSingleInput
 	const int32_t* hostCount() const override { return static_cast<const int32_t*>(hCount.get()); }
 	const void* fieldDev(rgl_field_t f) override;
 	void checkErrors() override;
+	// Number of transform / noise nodes this compaction applies in its own pass (for tests).
+	size_t absorbedCount() const { return chain.size(); }
 
 private:
 	rgl_field_t field = RGL_FIELD_IS_HIT_I32;
 	std::set<rgl_field_t> eager;               // fields compacted during the run
 	std::map<rgl_field_t, rgl::DeviceBuffer> outputs;
 	std::set<rgl_field_t> lazyDone;            // fields compacted on demand after the run
+	std::vector<std::shared_ptr<PointwisePointsNode>> chain; // absorbed nodes, source side first
+	std::shared_ptr<PointsNode> chainSource;   // input of chain.front()
 	rgl::DeviceBuffer count;
 	rgl::PinnedBuffer hCount;
 	rgl::DeviceBuffer scratch;
@@ -386,7 +423,7 @@ private:
 	void compact(const std::vector<rgl_field_t>& which, cudaStream_t s);
 };
 
-struct TransformPointsNode : PointsNodeSingleInput
+struct TransformPointsNode : PointwisePointsNode
 {
 	const char* name() const override { return "TransformPointsNode"; }
 	void setParameters(const rgl::Mat34& tf) { transform = tf; }
@@ -399,6 +436,11 @@ struct TransformPointsNode : PointsNodeSingleInput
 	}
 	const void* fieldDev(rgl_field_t f) override;
 	bool lastUpdateContentOnly() const override { return true; } // the transform is staged every run
+	void appendPointOp(rgl::PointOps& ops, cudaStream_t s) override;
+
+protected:
+	void allocateOutputs() override;
+	void launchOwn(cudaStream_t s) override;
 
 private:
 	rgl::Mat34 transform = rgl::Mat34::identity();
@@ -406,7 +448,7 @@ private:
 	rgl::DeviceBuffer out;
 };
 
-struct GaussianNoiseAngularHitpointNode : PointsNodeSingleInput
+struct GaussianNoiseAngularHitpointNode : PointwisePointsNode
 {
 	const char* name() const override { return "GaussianNoiseAngularHitpointNode"; }
 	void setParameters(float mean, float stDev, rgl_axis_t axis);
@@ -420,6 +462,11 @@ struct GaussianNoiseAngularHitpointNode : PointsNodeSingleInput
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
 	bool lastUpdateContentOnly() const override { return true; } // parameters are staged every run
+	void appendPointOp(rgl::PointOps& ops, cudaStream_t s) override;
+
+protected:
+	void allocateOutputs() override;
+	void launchOwn(cudaStream_t s) override;
 
 private:
 	float mean = 0, stDev = 0;
@@ -430,7 +477,7 @@ private:
 	rgl::StagedParam<rgl::NoiseParams> staged;
 };
 
-struct GaussianNoiseDistanceNode : PointsNodeSingleInput
+struct GaussianNoiseDistanceNode : PointwisePointsNode
 {
 	const char* name() const override { return "GaussianNoiseDistanceNode"; }
 	void setParameters(float mean, float base, float rise);
@@ -444,6 +491,11 @@ struct GaussianNoiseDistanceNode : PointsNodeSingleInput
 	void enqueueImpl(cudaStream_t s) override;
 	const void* fieldDev(rgl_field_t f) override;
 	bool lastUpdateContentOnly() const override { return true; } // parameters are staged every run
+	void appendPointOp(rgl::PointOps& ops, cudaStream_t s) override;
+
+protected:
+	void allocateOutputs() override;
+	void launchOwn(cudaStream_t s) override;
 
 private:
 	float mean = 0, base = 0, rise = 0;

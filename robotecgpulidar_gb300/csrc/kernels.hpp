@@ -195,11 +195,39 @@ void launchAddCount(int32_t* dAcc, const int32_t* dAdd, int32_t addStatic, cudaS
 // normal and the sensor's up vector (unsigned) > threshold, i.e. 1 for points that are not ground.
 void launchGroundFlags(const float* normals, int cap, const int32_t* dCount, Vec3 up, float threshold, int32_t* out, cudaStream_t s);
 
+// Point operations a compaction applies to the XYZ (and distance) of the points it keeps: the chain of
+// transform and noise nodes between the compaction and its source, absorbed into its one pass. Each
+// operation uses the point's index before compaction, as its own kernel would.
+enum PointOpKind : int32_t
+{
+	kOpTransform = 0,           // params: Mat34 (TransformPointsNode)
+	kOpNoiseAngularHitpoint = 1, // params: NoiseParams; withDistance: the distance is recomputed
+	kOpNoiseDistance = 2,        // params: NoiseParams
+};
+constexpr int kMaxPointOps = 4;
+struct PointOp
+{
+	int32_t kind;
+	int32_t withDistance;
+	const void* params; // device copy, staged by the absorbed node
+};
+struct PointOps
+{
+	PointOp op[kMaxPointOps];
+	int32_t count;
+	int32_t xyzField;     // index of XYZ among the compaction's fields (written from the chain), or -1
+	int32_t distField;    // index of DISTANCE, or -1
+	int32_t pad;
+	const float* srcXyz;  // the chain source's XYZ
+	const float* srcDist; // the chain source's distance, or null
+};
+
 size_t compactScratchBytes(int cap);
 // Stable compaction of `cap` points (first *dInCount valid when dInCount != null) by int32 flags.
-// Writes the kept count to *dOutCount.
-void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, int32_t* dOutCount,
-                   void* scratch, int32_t* dError, cudaStream_t s);
+// Writes the kept count to *dOutCount. With `ops`, the fields at ops->xyzField / ops->distField are
+// computed from the chain's source instead of copied.
+void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, const PointOps* ops,
+                   int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s);
 // AoS packing: point i, field k -> out + i*pointSize + offset_k; padding fields (src == null) are zeroed.
 void launchFormat(const FieldCopies& fields, int pointSize, int cap, const int32_t* dCount, uint8_t* out, cudaStream_t s);
 // AoS -> SoA split for points given as an array (rgl_node_points_from_array).

@@ -100,6 +100,28 @@ __global__ void kNoiseAngularRay(const Mat34* __restrict__ in, Mat34* __restrict
 	}
 }
 
+// Per-point arithmetic of the point noise nodes, shared by their kernels and by the compaction that
+// absorbs them (the same expressions, so both paths give the same bits).
+__device__ __forceinline__ Vec3 angularHitpoint(const NoiseParams& np, int i, Vec3 p, float* distOut)
+{
+	float angle = np.mean + noiseNormal(np, i) * np.stDev;
+	Vec3 q = axisRotation(np.axis, angle).point(np.lookAt.point(p));
+	if (distOut) {
+		*distOut = length(q);
+	}
+	return np.lookAtInv.point(q);
+}
+
+__device__ __forceinline__ Vec3 distanceNoise(const NoiseParams& np, int i, Vec3 p, float& d)
+{
+	float sigma = d * np.stDevRise + np.stDev; // stDev holds the base deviation for distance noise
+	float e = np.mean + noiseNormal(np, i) * sigma;
+	Vec3 pl = np.lookAt.point(p);
+	Vec3 moved = pl + normalized(pl) * e;
+	d = d + e;
+	return np.lookAtInv.point(moved);
+}
+
 __global__ void kNoiseAngularHitpoint(const float* __restrict__ inXyz, float* __restrict__ outXyz, float* __restrict__ outDist,
                                       int cap, const int32_t* dCount, const NoiseParams* __restrict__ dNp)
 {
@@ -107,12 +129,7 @@ __global__ void kNoiseAngularHitpoint(const float* __restrict__ inXyz, float* __
 	loadNoise(np, dNp);
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < countOf(cap, dCount)) {
-		float angle = np.mean + noiseNormal(np, i) * np.stDev;
-		Vec3 q = axisRotation(np.axis, angle).point(np.lookAt.point(loadXyz(inXyz, i)));
-		if (outDist) {
-			outDist[i] = length(q);
-		}
-		storeXyz(outXyz, i, np.lookAtInv.point(q));
+		storeXyz(outXyz, i, angularHitpoint(np, i, loadXyz(inXyz, i), outDist ? outDist + i : nullptr));
 	}
 }
 
@@ -124,12 +141,8 @@ __global__ void kNoiseDistance(const float* __restrict__ inXyz, const float* __r
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < countOf(cap, dCount)) {
 		float d = inDist[i];
-		float sigma = d * np.stDevRise + np.stDev; // stDev holds the base deviation for distance noise
-		float e = np.mean + noiseNormal(np, i) * sigma;
-		Vec3 pl = np.lookAt.point(loadXyz(inXyz, i));
-		Vec3 moved = pl + normalized(pl) * e;
-		storeXyz(outXyz, i, np.lookAtInv.point(moved));
-		outDist[i] = d + e;
+		storeXyz(outXyz, i, distanceNoise(np, i, loadXyz(inXyz, i), d));
+		outDist[i] = d;
 	}
 }
 
@@ -166,15 +179,27 @@ __device__ __forceinline__ void copyElem(const uint8_t* src, uint8_t* dst, int s
 
 // One pass: per-tile flag counts, decoupled look-back for the tile offset, scatter of every field.
 // scratch: [0] tile ticket, [1..tiles] tile status words (zeroed before the launch).
+// Parameters of the absorbed point operations, copied into shared memory once per block.
+constexpr int kOpParamWords = (int) (sizeof(NoiseParams) / 4);
+static_assert(sizeof(NoiseParams) % 16 == 0 && sizeof(Mat34) <= sizeof(NoiseParams), "point-op parameter slot");
+
 __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ flags, int cap, const int32_t* dInCount,
-                                                   FieldCopies fc, int32_t* dOutCount, uint32_t* scratch, int32_t* errorFlag)
+                                                   FieldCopies fc, PointOps ops, int32_t* dOutCount, uint32_t* scratch,
+                                                   int32_t* errorFlag)
 {
 	__shared__ uint32_t warpSums[kBlock / 32];
 	__shared__ uint32_t tileBase;
 	__shared__ int tileShared;
+	__shared__ __align__(16) uint32_t opParams[kMaxPointOps][kOpParamWords];
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	if (tid == 0) {
 		tileShared = (int) atomicAdd(scratch, 1u);
+	}
+	for (int k = 0; k < ops.count; ++k) {
+		const int words = ops.op[k].kind == kOpTransform ? (int) (sizeof(Mat34) / 4) : kOpParamWords;
+		for (int w = tid; w < words; w += kBlock) {
+			opParams[k][w] = __ldg(static_cast<const uint32_t*>(ops.op[k].params) + w);
+		}
 	}
 	__syncthreads();
 	const int tile = tileShared;
@@ -246,9 +271,33 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 		if (keep[k]) {
 			const int i = first + k;
 			for (int f = 0; f < fc.count; ++f) {
+				if (f == ops.xyzField || f == ops.distField) {
+					continue;
+				}
 				const int sz = fc.f[f].size;
 				copyElem(static_cast<const uint8_t*>(fc.f[f].src) + (size_t) i * sz, static_cast<uint8_t*>(fc.f[f].dst) + (size_t) pos * sz,
 				         sz);
+			}
+			if (ops.xyzField >= 0 || ops.distField >= 0) {
+				// XYZ and distance of the chain's source, through the absorbed operations in order.
+				Vec3 p = ops.srcXyz ? loadXyz(ops.srcXyz, i) : v3(0.0f, 0.0f, 0.0f);
+				float d = ops.srcDist ? ops.srcDist[i] : 0.0f;
+				for (int o = 0; o < ops.count; ++o) {
+					const uint32_t* prm = opParams[o];
+					if (ops.op[o].kind == kOpTransform) {
+						p = reinterpret_cast<const Mat34*>(prm)->point(p);
+					} else if (ops.op[o].kind == kOpNoiseAngularHitpoint) {
+						p = angularHitpoint(*reinterpret_cast<const NoiseParams*>(prm), i, p, ops.op[o].withDistance ? &d : nullptr);
+					} else {
+						p = distanceNoise(*reinterpret_cast<const NoiseParams*>(prm), i, p, d);
+					}
+				}
+				if (ops.xyzField >= 0) {
+					storeXyz(static_cast<float*>(fc.f[ops.xyzField].dst), (int) pos, p);
+				}
+				if (ops.distField >= 0) {
+					static_cast<float*>(fc.f[ops.distField].dst)[pos] = d;
+				}
 			}
 			++pos;
 		}
@@ -504,16 +553,23 @@ void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz,
 
 size_t compactScratchBytes(int cap) { return sizeof(uint32_t) * (size_t) (1 + (cap + kCompactTile - 1) / kCompactTile); }
 
-void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, int32_t* dOutCount,
-                   void* scratch, int32_t* dError, cudaStream_t s)
+void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, const PointOps* ops,
+                   int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s)
 {
+	PointOps po{};
+	if (ops != nullptr) {
+		po = *ops;
+	} else {
+		po.xyzField = -1;
+		po.distField = -1;
+	}
 	if (cap <= 0) {
 		cudaMemsetAsync(dOutCount, 0, sizeof(int32_t), s);
 		return;
 	}
 	cudaMemsetAsync(scratch, 0, compactScratchBytes(cap), s);
 	int tiles = (cap + kCompactTile - 1) / kCompactTile;
-	kCompact<<<tiles, kBlock, 0, s>>>(flags, cap, dInCount, fields, dOutCount, static_cast<uint32_t*>(scratch), dError);
+	kCompact<<<tiles, kBlock, 0, s>>>(flags, cap, dInCount, fields, po, dOutCount, static_cast<uint32_t*>(scratch), dError);
 	countLaunch();
 }
 

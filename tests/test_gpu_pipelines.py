@@ -140,3 +140,49 @@ def test_folded_sensor_transform_equals_separate_kernel(rgl):
     rgl.graph_run(a["rays"])
     rgl.graph_run(b["rays"])
     assert {f: rgl.result_bytes(a["out"], f).tobytes() for f in fields} == {f: rgl.result_bytes(b["out"], f).tobytes() for f in fields}
+
+
+def test_point_chain_absorbed_by_compaction(rgl):
+    """Noise and transform nodes that feed only a compaction run inside its pass, on the kept points;
+    with a second consumer on the chain nothing is absorbed and each node runs its own kernel. Both give
+    the same bytes, and so do an absorbed node's own fields when asked for after the run."""
+    scene = scenes.million_scene(seed=6, instances=10, spheres=2, cells=48, extent=90.0)
+    rgl.spawn_scene(scene)
+    rays = scenes.lidar_rays(32, 256)
+    lib = rgl.lib()
+    XYZ, DIST = rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32
+    fields = [XYZ, DIST, rgl.RGL_FIELD_ENTITY_ID_I32]
+
+    def graph(extra_consumer):
+        n = {k: rgl.node() for k in ("rays", "range", "trace", "ang", "dist", "tf", "cmp", "out")}
+        rgl.rays_from_mat3x4f(n["rays"], rays)
+        rgl.rays_set_range(n["range"], [[0.1, 80.0]])
+        rgl.raytrace(n["trace"])
+        rgl.check(lib.rgl_node_gaussian_noise_angular_hitpoint(C.byref(n["ang"]), 0.0, SIGMA, rgl.RGL_AXIS_Z))
+        rgl.check(lib.rgl_node_gaussian_noise_distance(C.byref(n["dist"]), 0.0, 0.02, 0.001))
+        rgl.set_noise_seed(n["ang"], 77)
+        rgl.set_noise_seed(n["dist"], 78)
+        rgl.points_transform(n["tf"], scenes.trs((1.0, 2.0, 3.0), (0.1, 0.2, 0.3)))
+        rgl.points_compact_by_field(n["cmp"])
+        rgl.points_yield(n["out"], fields)
+        rgl.chain(n["rays"], n["range"], n["trace"], n["ang"], n["dist"], n["tf"], n["cmp"], n["out"])
+        if extra_consumer:
+            n["y2"] = rgl.node()
+            rgl.points_yield(n["y2"], [XYZ])
+            rgl.add_child(n["tf"], n["y2"])
+        return n
+
+    a, b = graph(False), graph(True)
+    l0 = rgl.kernel_launch_count()
+    rgl.graph_run(a["rays"])
+    ra = {f: rgl.result_bytes(a["out"], f).tobytes() for f in fields}
+    l1 = rgl.kernel_launch_count()
+    rgl.graph_run(b["rays"])
+    rb = {f: rgl.result_bytes(b["out"], f).tobytes() for f in fields}
+    l2 = rgl.kernel_launch_count()
+    assert ra == rb
+    assert (l2 - l1) - (l1 - l0) == 3  # the absorbed graph launches no noise or transform kernel
+    # An absorbed node's own output, computed on demand, equals the one its kernel wrote in the run.
+    for f in (XYZ, DIST):
+        assert rgl.result_bytes(a["dist"], f).tobytes() == rgl.result_bytes(b["dist"], f).tobytes()
+    assert rgl.result_bytes(a["tf"], XYZ).tobytes() == rgl.result_bytes(b["tf"], XYZ).tobytes()
