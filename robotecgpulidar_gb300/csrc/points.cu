@@ -188,8 +188,9 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
                                                    int32_t* errorFlag)
 {
 	__shared__ uint32_t warpSums[kBlock / 32];
-	__shared__ uint32_t tileBase;
+	__shared__ uint32_t tileBase, tileKept;
 	__shared__ int tileShared;
+	__shared__ uint16_t keptLocal[kCompactTile]; // tile-local indices of the kept points, in order
 	__shared__ __align__(16) uint32_t opParams[kMaxPointOps][kOpParamWords];
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	if (tid == 0) {
@@ -259,47 +260,54 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 			atomicExch(&status[tile], kFlagInc | (prefix + run));
 		}
 		tileBase = prefix;
+		tileKept = run;
 		const int tiles = (cap + kCompactTile - 1) / kCompactTile;
 		if (tile == tiles - 1) {
 			*dOutCount = (int32_t) (prefix + run);
 		}
 	}
 	__syncthreads();
-	uint32_t pos = tileBase + warpSums[warp] + (uint32_t) (incl - cnt);
+	// The tile's kept points in order, then one kept point per thread: consecutive threads write
+	// consecutive output positions, and the point operations run with every lane busy.
+	uint32_t local = warpSums[warp] + (uint32_t) (incl - cnt);
 #pragma unroll
 	for (int k = 0; k < kCompactItems; ++k) {
 		if (keep[k]) {
-			const int i = first + k;
-			for (int f = 0; f < fc.count; ++f) {
-				if (f == ops.xyzField || f == ops.distField) {
-					continue;
-				}
-				const int sz = fc.f[f].size;
-				copyElem(static_cast<const uint8_t*>(fc.f[f].src) + (size_t) i * sz, static_cast<uint8_t*>(fc.f[f].dst) + (size_t) pos * sz,
-				         sz);
+			keptLocal[local++] = (uint16_t) (tid * kCompactItems + k);
+		}
+	}
+	__syncthreads();
+	const uint32_t kept = tileKept;
+	for (uint32_t c = (uint32_t) tid; c < kept; c += kBlock) {
+		const int i = tile * kCompactTile + keptLocal[c];
+		const uint32_t pos = tileBase + c;
+		for (int f = 0; f < fc.count; ++f) {
+			if (f == ops.xyzField || f == ops.distField) {
+				continue;
 			}
-			if (ops.xyzField >= 0 || ops.distField >= 0) {
-				// XYZ and distance of the chain's source, through the absorbed operations in order.
-				Vec3 p = ops.srcXyz ? loadXyz(ops.srcXyz, i) : v3(0.0f, 0.0f, 0.0f);
-				float d = ops.srcDist ? ops.srcDist[i] : 0.0f;
-				for (int o = 0; o < ops.count; ++o) {
-					const uint32_t* prm = opParams[o];
-					if (ops.op[o].kind == kOpTransform) {
-						p = reinterpret_cast<const Mat34*>(prm)->point(p);
-					} else if (ops.op[o].kind == kOpNoiseAngularHitpoint) {
-						p = angularHitpoint(*reinterpret_cast<const NoiseParams*>(prm), i, p, ops.op[o].withDistance ? &d : nullptr);
-					} else {
-						p = distanceNoise(*reinterpret_cast<const NoiseParams*>(prm), i, p, d);
-					}
-				}
-				if (ops.xyzField >= 0) {
-					storeXyz(static_cast<float*>(fc.f[ops.xyzField].dst), (int) pos, p);
-				}
-				if (ops.distField >= 0) {
-					static_cast<float*>(fc.f[ops.distField].dst)[pos] = d;
+			const int sz = fc.f[f].size;
+			copyElem(static_cast<const uint8_t*>(fc.f[f].src) + (size_t) i * sz, static_cast<uint8_t*>(fc.f[f].dst) + (size_t) pos * sz, sz);
+		}
+		if (ops.xyzField >= 0 || ops.distField >= 0) {
+			// XYZ and distance of the chain's source, through the absorbed operations in order.
+			Vec3 p = ops.srcXyz ? loadXyz(ops.srcXyz, i) : v3(0.0f, 0.0f, 0.0f);
+			float d = ops.srcDist ? ops.srcDist[i] : 0.0f;
+			for (int o = 0; o < ops.count; ++o) {
+				const uint32_t* prm = opParams[o];
+				if (ops.op[o].kind == kOpTransform) {
+					p = reinterpret_cast<const Mat34*>(prm)->point(p);
+				} else if (ops.op[o].kind == kOpNoiseAngularHitpoint) {
+					p = angularHitpoint(*reinterpret_cast<const NoiseParams*>(prm), i, p, ops.op[o].withDistance ? &d : nullptr);
+				} else {
+					p = distanceNoise(*reinterpret_cast<const NoiseParams*>(prm), i, p, d);
 				}
 			}
-			++pos;
+			if (ops.xyzField >= 0) {
+				storeXyz(static_cast<float*>(fc.f[ops.xyzField].dst), (int) pos, p);
+			}
+			if (ops.distField >= 0) {
+				static_cast<float*>(fc.f[ops.distField].dst)[pos] = d;
+			}
 		}
 	}
 }
