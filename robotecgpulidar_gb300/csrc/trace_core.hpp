@@ -28,45 +28,50 @@ RGL_HD float minf_(float a, float b) { return a < b ? a : b; }
 RGL_HD float maxf_(float a, float b) { return a > b ? a : b; }
 RGL_HD float comp(Vec3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 
-// Per-ray constants of the watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013).
+// Per-ray constants of the watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013), held as
+// the rows of its shear: with the axes permuted so that kz is the direction's dominant one,
+// (x, y, z) -> (x_kx - Sx z_kz, x_ky - Sy z_kz, Sz z_kz). Rows with one unit, one -S and one zero
+// entry evaluate that map with FMAs and no per-triangle component selection.
 struct Watertight
 {
-	int kx, ky, kz;
-	float Sx, Sy, Sz;
+	Vec3 row0, row1, row2;
 };
 
 RGL_HD Watertight setupWatertight(Vec3 d)
 {
-	Watertight w;
 	float ax = absf_(d.x), ay = absf_(d.y), az = absf_(d.z);
-	w.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-	w.kx = w.kz == 2 ? 0 : w.kz + 1;
-	w.ky = w.kx == 2 ? 0 : w.kx + 1;
-	float dz = comp(d, w.kz);
+	int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+	int kx = kz == 2 ? 0 : kz + 1;
+	int ky = kx == 2 ? 0 : kx + 1;
+	float dz = comp(d, kz);
 	if (dz < 0.0f) {
-		int t = w.kx;
-		w.kx = w.ky;
-		w.ky = t;
+		int t = kx;
+		kx = ky;
+		ky = t;
 	}
-	w.Sx = comp(d, w.kx) / dz;
-	w.Sy = comp(d, w.ky) / dz;
-	w.Sz = 1.0f / dz;
+	const float Sx = comp(d, kx) / dz, Sy = comp(d, ky) / dz, Sz = 1.0f / dz;
+	auto unitAxis = [](int k, float v) { return Vec3{k == 0 ? v : 0.0f, k == 1 ? v : 0.0f, k == 2 ? v : 0.0f}; };
+	Watertight w;
+	w.row0 = unitAxis(kx, 1.0f) + unitAxis(kz, -Sx);
+	w.row1 = unitAxis(ky, 1.0f) + unitAxis(kz, -Sy);
+	w.row2 = unitAxis(kz, Sz);
 	return w;
 }
 
+// One sheared coordinate: row . v with FMAs. The zero and unit entries contribute exact terms, so the
+// result is x_k - S z_kz rounded at most twice, by the same steps for a vertex in every triangle.
+RGL_HD float shear(Vec3 row, Vec3 v) { return fmaf(row.x, v.x, fmaf(row.y, v.y, row.z * v.z)); }
+
 // Watertight test of triangle (a, b, c) against a ray with origin o. On a hit with
-// 0 < t <= tBest returns true and the new t. Edge functions are evaluated without FMA so a shared edge
-// yields exactly opposite values in both triangles; exact zeros are re-evaluated in double.
+// 0 < t <= tBest returns true and the new t. Each vertex is sheared by the same arithmetic in every
+// triangle that holds it; edge functions are evaluated without FMA so a shared edge yields exactly
+// opposite values in both triangles; exact zeros are re-evaluated in double.
 RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& w, float tBest, float& tOut)
 {
 	Vec3 A = a - o, B = b - o, C = c - o;
-	float Akz = comp(A, w.kz), Bkz = comp(B, w.kz), Ckz = comp(C, w.kz);
-	float Ax = fsub(comp(A, w.kx), fmul(w.Sx, Akz));
-	float Ay = fsub(comp(A, w.ky), fmul(w.Sy, Akz));
-	float Bx = fsub(comp(B, w.kx), fmul(w.Sx, Bkz));
-	float By = fsub(comp(B, w.ky), fmul(w.Sy, Bkz));
-	float Cx = fsub(comp(C, w.kx), fmul(w.Sx, Ckz));
-	float Cy = fsub(comp(C, w.ky), fmul(w.Sy, Ckz));
+	float Ax = shear(w.row0, A), Ay = shear(w.row1, A);
+	float Bx = shear(w.row0, B), By = shear(w.row1, B);
+	float Cx = shear(w.row0, C), Cy = shear(w.row1, C);
 	float U = fsub(fmul(Cx, By), fmul(Cy, Bx));
 	float V = fsub(fmul(Ax, Cy), fmul(Ay, Cx));
 	float W = fsub(fmul(Bx, Ay), fmul(By, Ax));
@@ -85,7 +90,7 @@ RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& 
 	if (det == 0.0f) {
 		return false;
 	}
-	float Az = w.Sz * Akz, Bz = w.Sz * Bkz, Cz = w.Sz * Ckz;
+	float Az = shear(w.row2, A), Bz = shear(w.row2, B), Cz = shear(w.row2, C);
 	float T = fadd(fadd(fmul(U, Az), fmul(V, Bz)), fmul(W, Cz));
 	float t = T / det;
 	if (!(t > 0.0f) || !(t <= tBest)) {
