@@ -8,6 +8,14 @@
 
 using rgl::format;
 
+namespace {
+
+// Grows buf to hold `bytes`, at least doubling its capacity: a run of growing batches reallocates
+// (and so waits for the device) only a few times.
+void* grow(rgl::DeviceBuffer& buf, size_t bytes) { return buf.ensure(bytes <= buf.capacity() ? bytes : std::max(bytes, 2 * buf.capacity())); }
+
+} // namespace
+
 Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmBudgetBytes), maxInFlight(std::max(1, maxInFlightBatches))
 {
 	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -39,6 +47,15 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 		RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
 		s->counter.ensure(sizeof(uint32_t));
 		slots.push_back(std::move(s));
+	}
+	// Per-batch device buffers sized up front for the largest batch (two returns per beam), within
+	// this slot's share of the budget: a batch never allocates, so it never waits for the other
+	// slot's work on the device.
+	const int64_t points = std::min<int64_t>(2 * maxBatchBeams, budget / (kRawBytesPerPoint * maxInFlight));
+	if (points > 0) {
+		for (auto& sl : slots) {
+			reserveRaw(*sl, points, points / rgl::kSegTile + 4096);
+		}
 	}
 	worker = std::thread([this] { loop(); });
 }
@@ -331,7 +348,18 @@ Server::Stats Server::stats()
 	return s;
 }
 
-// Builds and enqueues one batch from slot.reqs (already admitted, outputs allocated).
+void Server::reserveRaw(Slot& slot, int64_t points, int64_t tiles)
+{
+	points = std::max<int64_t>(points, 1);
+	tiles = std::max<int64_t>(tiles, 1);
+	grow(slot.rawFlags, sizeof(int32_t) * (size_t) points);
+	grow(slot.rawXyz, sizeof(float) * 3 * (size_t) points);
+	grow(slot.rawDist, sizeof(float) * (size_t) points);
+	grow(slot.rawEnt, sizeof(int32_t) * (size_t) points);
+	grow(slot.tileCounts, sizeof(uint32_t) * (size_t) tiles);
+	grow(slot.tileOffsets, sizeof(uint32_t) * (size_t) tiles);
+}
+
 void Server::configure(const rgl::BatchSchedule& s, int64_t maxBeams)
 {
 	std::lock_guard<std::mutex> g(m);
@@ -339,6 +367,7 @@ void Server::configure(const rgl::BatchSchedule& s, int64_t maxBeams)
 	maxBatchBeams = maxBeams;
 }
 
+// Builds and enqueues one batch from slot.reqs (already admitted, outputs allocated).
 void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 {
 	const int n = (int) slot.reqs.size();
@@ -346,10 +375,15 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 	for (auto* r : slot.reqs) {
 		points += r->points;
 	}
-	auto* flags = static_cast<int32_t*>(slot.rawFlags.ensure(sizeof(int32_t) * std::max<int64_t>(points, 1)));
-	auto* xyz = static_cast<float*>(slot.rawXyz.ensure(sizeof(float) * 3 * std::max<int64_t>(points, 1)));
-	auto* dist = static_cast<float*>(slot.rawDist.ensure(sizeof(float) * std::max<int64_t>(points, 1)));
-	auto* ent = static_cast<int32_t*>(slot.rawEnt.ensure(sizeof(int32_t) * std::max<int64_t>(points, 1)));
+	int64_t maxTiles = 0;
+	for (auto* r : slot.reqs) {
+		maxTiles += (r->points + rgl::kSegTile - 1) / rgl::kSegTile;
+	}
+	reserveRaw(slot, points, maxTiles);
+	auto* flags = slot.rawFlags.as<int32_t>();
+	auto* xyz = slot.rawXyz.as<float>();
+	auto* dist = slot.rawDist.as<float>();
+	auto* ent = slot.rawEnt.as<int32_t>();
 
 	// Table layout (16-byte aligned parts): jobs[n] | task bases[n+1] | segments[n] | tile bases[n+1].
 	auto align = [](size_t x) { return (x + 15) & ~size_t{15}; };
@@ -358,13 +392,13 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 	const size_t offTile = offSeg + align(sizeof(rgl::SegCompactJob) * n);
 	const size_t tableBytes = offTile + align(sizeof(int32_t) * (n + 1));
 	auto* hBase = static_cast<uint8_t*>(slot.hTables.ensure(tableBytes));
-	auto* dBase = static_cast<uint8_t*>(slot.tables.ensure(tableBytes));
+	auto* dBase = static_cast<uint8_t*>(grow(slot.tables, tableBytes));
 	auto* jobs = reinterpret_cast<rgl::BatchJob*>(hBase);
 	auto* taskBase = reinterpret_cast<int32_t*>(hBase + offTask);
 	auto* segs = reinterpret_cast<rgl::SegCompactJob*>(hBase + offSeg);
 	auto* tileBase = reinterpret_cast<int32_t*>(hBase + offTile);
 	// Results: counts[n], then one traversal error flag per request.
-	auto* dResults = static_cast<int32_t*>(slot.results.ensure(sizeof(int32_t) * 2 * n));
+	auto* dResults = static_cast<int32_t*>(grow(slot.results, sizeof(int32_t) * 2 * n));
 	int64_t pointBase = 0, tasks = 0, tiles = 0;
 	for (int j = 0; j < n; ++j) {
 		Request& r = *slot.reqs[j];
@@ -414,8 +448,8 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 	taskBase[n] = (int32_t) tasks;
 	tileBase[n] = (int32_t) tiles;
 
-	auto* dTileCounts = slot.tileCounts.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
-	auto* dTileOffsets = slot.tileOffsets.ensure(sizeof(uint32_t) * std::max<int64_t>(tiles, 1));
+	auto* dTileCounts = slot.tileCounts.get();
+	auto* dTileOffsets = slot.tileOffsets.get();
 	RGL_CHECK_CUDA(cudaEventRecord(slot.t0, slot.stream));
 	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, slot.stream));
 	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, slot.stream));

@@ -122,6 +122,8 @@ private:
 	};
 
 	static constexpr int64_t kRawBytesPerPoint = 4 + 12 + 4 + 4; // flags, xyz, distance, entity id
+	// Grows a slot's raw point and compaction-tile buffers (never shrinks them).
+	void reserveRaw(Slot& slot, int64_t points, int64_t tiles);
 	static constexpr int64_t kOutBytesPerPoint = 12 + 4 + 4;
 
 	// Result arena: one pinned, device-mapped host allocation made with the server, handed out by a
