@@ -1359,22 +1359,34 @@ void GraphRunCtx::run()
 	for (auto& n : order) {
 		n->prepareImpl(stream_);
 	}
-	if (timingEnabled()) {
-		RGL_CHECK_CUDA(cudaEventRecord(runStart, stream_));
-	}
+	// Run timing covers the device work of the run: in a captured run the two events are the first
+	// and last nodes of the CUDA graph, so the host's launch call is not inside the interval.
+	const bool timed = timingEnabled();
 	if (!cudaGraphsEnabled()) {
 		releaseGraph();
+		if (timed) {
+			recordEvent(runStart, stream_);
+		}
 		for (auto& n : order) {
 			n->enqueueImpl(stream_);
 		}
+		if (timed) {
+			recordEvent(runStop, stream_);
+		}
 	} else {
-		if (version > execVersion || exec == nullptr || execEpoch != rgl::allocationEpoch()) {
+		if (version > execVersion || exec == nullptr || execEpoch != rgl::allocationEpoch() || execTimed != timed) {
 			releaseGraph();
 			const uint64_t launches0 = rgl::launchCount();
 			RGL_CHECK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
 			try {
+				if (timed) {
+					recordEvent(runStart, stream_);
+				}
 				for (auto& n : order) {
 					n->enqueueImpl(stream_);
+				}
+				if (timed) {
+					recordEvent(runStop, stream_);
 				}
 			}
 			catch (...) {
@@ -1393,15 +1405,13 @@ void GraphRunCtx::run()
 			execKernels = rgl::launchCount() - launches0;
 			execEpoch = rgl::allocationEpoch();
 			execVersion = version;
+			execTimed = timed;
 			++captures;
 		} else {
 			++replays;
 			rgl::countLaunch(execKernels);
 		}
 		RGL_CHECK_CUDA(cudaGraphLaunch(exec, stream_));
-	}
-	if (timingEnabled()) {
-		RGL_CHECK_CUDA(cudaEventRecord(runStop, stream_));
 	}
 	RGL_CHECK_CUDA(cudaEventRecord(done, stream_));
 }

@@ -643,6 +643,7 @@ private:
 	cudaGraphExec_t exec = nullptr;
 	uint64_t execEpoch = 0;
 	uint64_t execVersion = 0;
+	bool execTimed = false; // the capture holds the run-timing events
 	uint64_t execKernels = 0;
 };
 

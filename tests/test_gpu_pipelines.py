@@ -186,3 +186,32 @@ def test_point_chain_absorbed_by_compaction(rgl):
     for f in (XYZ, DIST):
         assert rgl.result_bytes(a["dist"], f).tobytes() == rgl.result_bytes(b["dist"], f).tobytes()
     assert rgl.result_bytes(a["tf"], XYZ).tobytes() == rgl.result_bytes(b["tf"], XYZ).tobytes()
+
+
+def test_run_timing_covers_the_captured_run(rgl):
+    """With timing on, a graph run reports the device time of the whole run and of its traversal: both
+    positive, the traversal within the run, for captured runs (events recorded inside the CUDA graph)
+    and for eager ones; turning timing on after a capture re-captures the run."""
+    scene = scenes.million_scene(seed=6, instances=10, spheres=2, cells=48, extent=90.0)
+    rgl.spawn_scene(scene)
+    lib = rgl.lib()
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "cmp", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], scenes.lidar_rays(32, 512))
+    rgl.rays_transform(n["pose"], scenes.translation(0, 0, 3.0))
+    rgl.raytrace(n["trace"])
+    rgl.points_compact_by_field(n["cmp"])
+    rgl.points_yield(n["out"], [rgl.RGL_FIELD_XYZ_VEC3_F32])
+    rgl.chain(n["rays"], n["pose"], n["trace"], n["cmp"], n["out"])
+    run_ms, trace_ms = C.c_float(), C.c_float()
+    try:
+        rgl.graph_run(n["rays"])  # captured without timing
+        rgl.check(lib.rgl_gb300_configure_timing(True))
+        for graphs in (True, False):
+            rgl.check(lib.rgl_gb300_configure_cuda_graphs(graphs))
+            for _ in range(3):
+                rgl.graph_run(n["rays"])
+                rgl.check(lib.rgl_gb300_graph_get_timing(n["rays"], C.byref(run_ms), C.byref(trace_ms)))
+                assert 0.0 < trace_ms.value <= run_ms.value < 50.0
+    finally:
+        rgl.check(lib.rgl_gb300_configure_timing(False))
+        rgl.check(lib.rgl_gb300_configure_cuda_graphs(True))
