@@ -184,7 +184,8 @@ constexpr int kOpParamWords = (int) (sizeof(NoiseParams) / 4);
 static_assert(sizeof(NoiseParams) % 16 == 0 && sizeof(Mat34) <= sizeof(NoiseParams), "point-op parameter slot");
 
 __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ flags, int cap, const int32_t* dInCount,
-                                                   FieldCopies fc, PointOps ops, int32_t* dOutCount, uint32_t* scratch,
+                                                   const __grid_constant__ FieldCopies fc, const __grid_constant__ PointOps ops,
+                                                   int32_t* dOutCount, uint32_t* scratch,
                                                    int32_t* errorFlag)
 {
 	__shared__ uint32_t warpSums[kBlock / 32];
@@ -321,14 +322,17 @@ struct WordMap
 };
 
 // Word-aligned layouts: one thread per output 32-bit word, coalesced stores.
-__global__ void kFormatWords(FieldCopies fc, WordMap wm, int pointWords, int cap, const int32_t* dCount, uint32_t* __restrict__ out)
+// The point of word w is w / pointWords; `magic` = ceil(2^32 / pointWords) turns that into one
+// multiply-high, exact for w < 2^26 (pointWords <= 64), and is 0 for larger launches.
+__global__ void kFormatWords(const __grid_constant__ FieldCopies fc, const __grid_constant__ WordMap wm, int pointWords, uint32_t magic,
+                             int cap, const int32_t* dCount, uint32_t* __restrict__ out)
 {
 	long w = (long) blockIdx.x * blockDim.x + threadIdx.x;
 	long n = countOf(cap, dCount);
 	if (w >= n * pointWords) {
 		return;
 	}
-	int i = (int) (w / pointWords);
+	int i = magic != 0 ? (int) __umulhi((uint32_t) w, magic) : (int) (w / pointWords);
 	int k = (int) (w - (long) i * pointWords);
 	int f = wm.field[k];
 	uint32_t v = 0;
@@ -340,7 +344,7 @@ __global__ void kFormatWords(FieldCopies fc, WordMap wm, int pointWords, int cap
 }
 
 // Any layout: one thread per point, byte copies (padding bytes zeroed).
-__global__ void kFormatBytes(FieldCopies fc, int pointSize, int cap, const int32_t* dCount, uint8_t* __restrict__ out)
+__global__ void kFormatBytes(const __grid_constant__ FieldCopies fc, int pointSize, int cap, const int32_t* dCount, uint8_t* __restrict__ out)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= countOf(cap, dCount)) {
@@ -356,7 +360,7 @@ __global__ void kFormatBytes(FieldCopies fc, int pointSize, int cap, const int32
 	}
 }
 
-__global__ void kAosToSoa(const uint8_t* __restrict__ in, int pointSize, int n, FieldCopies fc)
+__global__ void kAosToSoa(const uint8_t* __restrict__ in, int pointSize, int n, const __grid_constant__ FieldCopies fc)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) {
@@ -607,7 +611,8 @@ void launchFormat(const FieldCopies& fields, int pointSize, int cap, const int32
 		}
 		int pw = pointSize / 4;
 		long total = (long) cap * pw;
-		kFormatWords<<<blocks(total, kBlock), kBlock, 0, s>>>(fields, wm, pw, cap, dCount, reinterpret_cast<uint32_t*>(out));
+		const uint32_t magic = total < (1l << 26) ? (uint32_t) (((1ull << 32) + (uint64_t) pw - 1) / (uint64_t) pw) : 0u;
+		kFormatWords<<<blocks(total, kBlock), kBlock, 0, s>>>(fields, wm, pw, magic, cap, dCount, reinterpret_cast<uint32_t*>(out));
 	} else {
 		kFormatBytes<<<blocks(cap, kBlock), kBlock, 0, s>>>(fields, pointSize, cap, dCount, out);
 	}
