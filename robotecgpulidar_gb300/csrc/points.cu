@@ -228,43 +228,69 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 		warpSums[warp] = (uint32_t) incl;
 	}
 	__syncthreads();
-	if (tid == 0) {
+	if (warp == 0) {
+		// Tile total and per-warp offsets (lane 0), the tile's status word, then a look-back by the
+		// whole warp: 32 predecessors' status words per step, summed up to the nearest inclusive prefix.
 		uint32_t run = 0;
-		for (int w = 0; w < kBlock / 32; ++w) {
-			uint32_t v = warpSums[w];
-			warpSums[w] = run;
-			run += v;
+		if (lane == 0) {
+			for (int w = 0; w < kBlock / 32; ++w) {
+				uint32_t v = warpSums[w];
+				warpSums[w] = run;
+				run += v;
+			}
 		}
+		run = __shfl_sync(0xffffffffu, run, 0);
 		uint32_t* status = scratch + 1;
+		if (lane == 0) {
+			atomicExch(&status[tile], (tile == 0 ? kFlagInc : kFlagAgg) | run);
+		}
 		uint32_t prefix = 0;
-		if (tile == 0) {
-			atomicExch(&status[0], kFlagInc | run);
-		} else {
-			atomicExch(&status[tile], kFlagAgg | run);
-			int k = tile - 1, spins = 0;
-			while (k >= 0) {
-				uint32_t s = *((volatile uint32_t*) &status[k]);
-				uint32_t fl = s & ~kValueMask;
-				if (fl == 0u) {
-					if (++spins > kSpinLimit) {
-						atomicExch(errorFlag, 1);
-						break;
-					}
-					continue;
-				}
-				prefix += s & kValueMask;
-				if (fl == kFlagInc) {
+		int spins = 0;
+		for (int k = tile - 1; tile > 0;) {
+			const int idx = k - lane;
+			// Before tile 0 counts as an inclusive prefix of 0, so every window ends there.
+			uint32_t st = kFlagInc | 0u;
+			if (idx >= 0) {
+				st = *((volatile uint32_t*) &status[idx]);
+			}
+			while (__any_sync(0xffffffffu, (st & ~kValueMask) == 0u)) {
+				if (++spins > kSpinLimit) {
 					break;
 				}
-				--k;
+				if ((st & ~kValueMask) == 0u) {
+					st = *((volatile uint32_t*) &status[idx]);
+				}
 			}
-			atomicExch(&status[tile], kFlagInc | (prefix + run));
+			if (spins > kSpinLimit) {
+				if (lane == 0) {
+					atomicExch(errorFlag, 1);
+				}
+				break;
+			}
+			const unsigned inc = __ballot_sync(0xffffffffu, (st & ~kValueMask) == kFlagInc);
+			// Lanes up to the nearest inclusive prefix (lowest such lane) contribute.
+			const int stop = inc ? __ffs((int) inc) - 1 : 31;
+			uint32_t v = lane <= stop ? (st & kValueMask) : 0u;
+#pragma unroll
+			for (int off = 16; off > 0; off >>= 1) {
+				v += __shfl_xor_sync(0xffffffffu, v, off);
+			}
+			prefix += v;
+			if (inc) {
+				break;
+			}
+			k -= 32;
 		}
-		tileBase = prefix;
-		tileKept = run;
-		const int tiles = (cap + kCompactTile - 1) / kCompactTile;
-		if (tile == tiles - 1) {
-			*dOutCount = (int32_t) (prefix + run);
+		if (lane == 0) {
+			if (tile > 0) {
+				atomicExch(&status[tile], kFlagInc | (prefix + run));
+			}
+			tileBase = prefix;
+			tileKept = run;
+			const int tiles = (cap + kCompactTile - 1) / kCompactTile;
+			if (tile == tiles - 1) {
+				*dOutCount = (int32_t) (prefix + run);
+			}
 		}
 	}
 	__syncthreads();
