@@ -34,7 +34,7 @@ BatchRun::BatchRun(std::vector<Node::Ptr> a) : anchors(std::move(a)), dKeys(fals
 	RGL_CHECK_CUDA(cudaEventCreate(&traceStart));
 	RGL_CHECK_CUDA(cudaEventCreate(&traceStop));
 	// Allocated here: the first use may be inside a stream capture, where allocation is not allowed.
-	RGL_CHECK_CUDA(cudaMemset(dCounter.ensure(sizeof(uint32_t)), 0, sizeof(uint32_t)));
+	RGL_CHECK_CUDA(cudaMemset(dCounter.ensure(rgl::kTraceCounterBytes), 0, rgl::kTraceCounterBytes));
 	RGL_CHECK_CUDA(cudaMemset(dError.ensure(sizeof(int32_t)), 0, sizeof(int32_t)));
 }
 

@@ -581,31 +581,31 @@ void RaytraceNode::fillJob(rgl::BatchJob& b)
 
 void RaytraceNode::stageJob()
 {
-	rgl::BatchJob& b = job.host();
+	rgl::BatchJob& b = job.host().job;
 	fillJob(b);
 	const rgl::TraceParams& p = b.p;
 	(void) job.device();
 	schedule = traceSchedule();
 	const int per = rgl::batchBeamsPerTask(schedule.packing, p.nSamples);
-	rgl::TaskRange& tr = tasks.host();
+	rgl::TaskRange& tr = job.host().tasks;
 	tr.base[0] = 0;
 	tr.base[1] = (p.nRays + per - 1) / per;
-	(void) tasks.device();
 	shading = rgl::needsShadingKernel(p);
 	if (counter.get() == nullptr) {
-		RGL_CHECK_CUDA(cudaMemset(counter.ensure(sizeof(uint32_t)), 0, sizeof(uint32_t)));
+		RGL_CHECK_CUDA(cudaMemset(counter.ensure(rgl::kTraceCounterBytes), 0, rgl::kTraceCounterBytes));
 	}
 	rgl::prepareTraceBatch(1, p.nSamples, shading, schedule);
 }
 
 void RaytraceNode::enqueueImpl(cudaStream_t s)
 {
-	const rgl::BatchJob* dJob = job.enqueue(s);
-	const rgl::TaskRange* dTasks = tasks.enqueue(s);
+	const StagedTrace* staged = job.enqueue(s);
+	const rgl::BatchJob* dJob = &staged->job;
+	const rgl::TaskRange* dTasks = &staged->tasks;
 	if (timingEnabled() && evStart) {
 		recordEvent(evStart, s);
 	}
-	rgl::launchTraceBatch(dJob, dTasks->base, 1, job.host().p.nSamples, shading, schedule, counter.as<uint32_t>(), s);
+	rgl::launchTraceBatch(dJob, dTasks->base, 1, job.host().job.p.nSamples, shading, schedule, counter.as<uint32_t>(), s);
 	RGL_CHECK_CUDA(cudaGetLastError());
 	if (timingEnabled() && evStart) {
 		recordEvent(evStop, s);
@@ -743,7 +743,12 @@ void CompactByFieldPointsNode::sizeBuffers(const std::vector<rgl_field_t>& which
 	for (auto f : which) {
 		outputs[f].ensure(std::max<size_t>(1, rgl::fieldSize(f) * cap));
 	}
-	scratch.ensure(rgl::compactScratchBytes((int) cap));
+	// The compaction kernel leaves its scratch zeroed; a new allocation is zeroed once here.
+	const void* old = scratch.get();
+	const size_t bytes = rgl::compactScratchBytes((int) cap);
+	if (scratch.ensure(bytes) != old) {
+		RGL_CHECK_CUDA(cudaMemset(scratch.get(), 0, scratch.capacity()));
+	}
 }
 
 // Per-run host state lives here, not in enqueueImpl: a replayed capture does not call enqueueImpl.

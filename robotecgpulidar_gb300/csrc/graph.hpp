@@ -356,8 +356,13 @@ private:
 	size_t rayMaskCount = 0;
 	rgl::ErrorSlot errorFlag;
 	// The node's traversal as a one-job persistent launch.
-	rgl::StagedParam<rgl::BatchJob> job;
-	rgl::StagedParam<rgl::TaskRange> tasks;
+	// The job and its task bases, uploaded by one copy per run.
+	struct StagedTrace
+	{
+		rgl::BatchJob job;
+		rgl::TaskRange tasks;
+	};
+	rgl::StagedParam<StagedTrace> job;
 	rgl::DeviceBuffer counter;
 	rgl::BatchSchedule schedule{};
 	bool shading = false;

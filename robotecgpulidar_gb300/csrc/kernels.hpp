@@ -107,8 +107,11 @@ int batchBeamsPerTask(int packing, int nSamples);
 // Resolves and caches the launch configuration (occupancy, shared-memory opt-in) of a schedule;
 // call it outside stream capture before the first captured launch of that schedule.
 void prepareTraceBatch(int nJobs, int maxSamples, bool shading, const BatchSchedule& s);
-// Persistent launch over `nJobs` sensors; dTaskBase holds nJobs + 1 prefix sums of tasks per sensor.
-// Resets *dCounter on the stream first.
+// The traversal's counter block: task ticket and finished blocks, zeroed once when allocated; every
+// launch leaves it zero again.
+constexpr size_t kTraceCounterBytes = 2 * sizeof(uint32_t);
+// Persistent launch over `nJobs` sensors; dTaskBase holds nJobs + 1 prefix sums of tasks per sensor;
+// dCounter is a kTraceCounterBytes counter block (launches that share one must be stream-ordered).
 void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs, int maxSamples, bool shading,
                       const BatchSchedule& s, uint32_t* dCounter, cudaStream_t stream);
 // ---- segcompact.cu: compaction of many requests' points in three launches
@@ -224,7 +227,8 @@ struct PointOps
 
 size_t compactScratchBytes(int cap);
 // Stable compaction of `cap` points (first *dInCount valid when dInCount != null) by int32 flags.
-// Writes the kept count to *dOutCount. With `ops`, the fields at ops->xyzField / ops->distField are
+// Writes the kept count to *dOutCount. `scratch` (compactScratchBytes) is zero before the first launch
+// and each launch leaves it zero. With `ops`, the fields at ops->xyzField / ops->distField are
 // computed from the chain's source instead of copied.
 void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, const PointOps* ops,
                    int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s);

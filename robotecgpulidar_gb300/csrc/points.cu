@@ -178,7 +178,8 @@ __device__ __forceinline__ void copyElem(const uint8_t* src, uint8_t* dst, int s
 }
 
 // One pass: per-tile flag counts, decoupled look-back for the tile offset, scatter of every field.
-// scratch: [0] tile ticket, [1..tiles] tile status words (zeroed before the launch).
+// scratch: [0] tile ticket, [1..tiles] tile status words, [tiles + 1] finished tiles; zero before the
+// first launch, and the last tile to finish zeroes it again for the next one.
 // Parameters of the absorbed point operations, copied into shared memory once per block.
 constexpr int kOpParamWords = (int) (sizeof(NoiseParams) / 4);
 static_assert(sizeof(NoiseParams) % 16 == 0 && sizeof(Mat34) <= sizeof(NoiseParams), "point-op parameter slot");
@@ -335,6 +336,20 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 			if (ops.distField >= 0) {
 				static_cast<float*>(fc.f[ops.distField].dst)[pos] = d;
 			}
+		}
+	}
+	// Re-arm the scratch for the next launch once every tile has finished its look-back.
+	__shared__ bool lastTile;
+	__syncthreads();
+	const int tiles = (cap + kCompactTile - 1) / kCompactTile;
+	if (tid == 0) {
+		__threadfence();
+		lastTile = atomicAdd(&scratch[1 + tiles], 1u) == (uint32_t) (tiles - 1);
+	}
+	__syncthreads();
+	if (lastTile) {
+		for (int k = tid; k < tiles + 2; k += kBlock) {
+			scratch[k] = 0u;
 		}
 	}
 }
@@ -589,7 +604,7 @@ void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz,
 	}
 }
 
-size_t compactScratchBytes(int cap) { return sizeof(uint32_t) * (size_t) (1 + (cap + kCompactTile - 1) / kCompactTile); }
+size_t compactScratchBytes(int cap) { return sizeof(uint32_t) * (size_t) (2 + (cap + kCompactTile - 1) / kCompactTile); }
 
 void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, const PointOps* ops,
                    int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s)
@@ -605,7 +620,6 @@ void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const
 		cudaMemsetAsync(dOutCount, 0, sizeof(int32_t), s);
 		return;
 	}
-	cudaMemsetAsync(scratch, 0, compactScratchBytes(cap), s);
 	int tiles = (cap + kCompactTile - 1) / kCompactTile;
 	kCompact<<<tiles, kBlock, 0, s>>>(flags, cap, dInCount, fields, po, dOutCount, static_cast<uint32_t*>(scratch), dError);
 	countLaunch();

@@ -45,7 +45,7 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t0));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t1));
 		RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-		s->counter.ensure(sizeof(uint32_t));
+		RGL_CHECK_CUDA(cudaMemset(s->counter.ensure(rgl::kTraceCounterBytes), 0, rgl::kTraceCounterBytes));
 		slots.push_back(std::move(s));
 	}
 	// Per-batch device buffers sized up front for the largest batch (two returns per beam), within

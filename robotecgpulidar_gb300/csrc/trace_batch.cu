@@ -202,7 +202,6 @@ void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs
 	}
 	const LaunchShape ls = batchLaunchShape(nJobs, maxSamples, shading, s);
 	int chunk = s.chunk < 1 ? 1 : s.chunk;
-	RGL_BATCH_CUDA_OK(cudaMemsetAsync(dCounter, 0, sizeof(uint32_t), stream));
 	void* args[] = {(void*) &dJobs, (void*) &dTaskBase, (void*) &nJobs, (void*) &dCounter, (void*) &chunk};
 	RGL_BATCH_CUDA_OK(cudaLaunchKernel(ls.fn, dim3(ls.grid), dim3(s.block), args, ls.smem, stream));
 	countLaunch();

@@ -168,6 +168,16 @@ __global__ void __maxnreg__(REGS) kTraceBatch(const BatchJob* __restrict__ jobs,
 			}
 		}
 	}
+	// The last block to finish re-arms both counters for the next launch, so no launch needs a memset
+	// first: every block has left the task loop when it counts itself finished.
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		__threadfence();
+		if (atomicAdd(counter + 1, 1u) == gridDim.x - 1) {
+			atomicExch(counter, 0u);
+			atomicExch(counter + 1, 0u);
+		}
+	}
 }
 
 } // namespace
