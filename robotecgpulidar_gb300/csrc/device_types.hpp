@@ -17,7 +17,7 @@
 namespace rgl {
 
 // Maximum triangles referenced by one leaf child of a wide node (3-bit count, 5-bit offset in meta).
-constexpr int kLeafMaxTris = 3;
+constexpr int kLeafMaxTris = 2;
 constexpr int kWideArity = 8;
 
 // 80-byte wide node = five 16-byte words, loaded with five 128-bit loads.
