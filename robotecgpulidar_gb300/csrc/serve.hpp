@@ -149,7 +149,7 @@ private:
 
 	int64_t budget;
 	int maxInFlight;
-	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 80}; // guarded by m
+	rgl::BatchSchedule schedule{128, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 96}; // guarded by m
 	int64_t maxBatchBeams = 32 << 20;                                                     // guarded by m
 	cudaStream_t stream = nullptr;
 	std::vector<std::unique_ptr<Pattern>> patterns;
