@@ -155,12 +155,8 @@ RGL_HD void quantizeAxis(float p, float scale, float clo, float chi, uint8_t& ql
 	while (hi < 255 && fadd(p, (float) hi * scale) < chi) {
 		++hi;
 	}
-	// Widen by one grid step. The traversal evaluates planes as fma(q, scale * inv, (p - o) * inv),
-	// whose error is at most 4u|t| + 3u * 255 * scale * |inv| (u = 2^-24); the extra step moves every
-	// plane outward by scale, which exceeds the second term, and the traversal's relative slack on
-	// the exit distance covers the first. No hit inside the exact child box is lost.
-	lo = lo > 0 ? lo - 1 : 0;
-	hi = hi < 255 ? hi + 1 : 255;
+	// No widening: the traversal moves every near plane earlier and every far plane later by a slack
+	// that covers its plane-distance error (trace_core.hpp kPlaneSlack).
 	qlo = (uint8_t) lo;
 	qhi = (uint8_t) hi;
 }

@@ -143,13 +143,21 @@ RGL_HD int popc8(uint32_t x)
 // Entries pushed inside an instance sit above its leave entry, so each group is popped in the frame
 // it was pushed in. `Stack` provides push(a, b), pop(a&, b&), size().
 
-// Slab test of a dequantised child box in the FMA form t = q * (s * inv) + (p - o) * inv. The computed
-// t differs from the exact plane distance by at most 4u|t| + 3u * 255 * s * |inv| (u = 2^-24), plus
-// the rounding of the folded offset described in traverseBlas. The builder widens every child box by
-// one grid step s (bvh_core.hpp quantizeAxis), which moves each plane outward by s * |inv| in t and
-// covers the absolute terms; entry <= exit * (1 + 5e-7) covers the relative ones.
-// Axis-parallel rays (inv = +-1e30 after safeInv) stay exact: their slab only yields +-huge values.
-constexpr float kSlabRelSlack = 1.0000005f;
+// Slab test of a dequantised child box. Per axis a plane distance is evaluated as
+// fma(1 + q 2^-15, S, D -+ e) with S = 2^15 A, A = s * inv (one grid step in t, exact: s is a power of
+// two), C = (p - o) * inv and D = C - S (see the node loop). Against the exact distance of the ray
+// with direction 1/inv it errs by at most
+//  * relative: inv, the FMA and the |t| share of the C terms, 6u|t| (u = 2^-24); entry and exit
+//    together 12u, covered by entry <= exit * (1 + 2e-6) (34u);
+//  * absolute: C rounds twice and D and D -+ e once each, 4u|C| + 2^-8 |A| with |C| <= |t| + 255 |A|,
+//    i.e. (2^-8 + 1020u) |A| < 0.0041 |A| beyond the relative part; near planes are moved earlier and
+//    far planes later by e = 0.01 |A| (kPlaneSlack).
+// Child boxes are the builder's verified enclosures (bvh_core.hpp quantizeAxis), so no hit inside the
+// exact child box is lost. Axis-parallel rays (inv = +-1e30 after safeInv) only yield +-huge plane
+// distances on that axis: the slab there is all or nothing, as it must be.
+constexpr float kSlabRelSlack = 1.000002f;
+// Absolute slack of a plane distance: 0.01 grid steps, as a fraction of |S| = 2^15 |A|.
+constexpr float kPlaneSlack = 0.01f / 32768.0f;
 
 RGL_HD uint32_t lowestBit(uint32_t x)
 {
@@ -297,12 +305,14 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 		const uint32_t childBase = w1.x, triBase = w1.y;
 		const float Ax = sx * r.inv.x, Ay = sy * r.inv.y, Az = sz * r.inv.z;
 		const float Cx = (asFloat(w0.x) - r.o.x) * r.inv.x, Cy = (asFloat(w0.y) - r.o.y) * r.inv.y, Cz = (asFloat(w0.z) - r.o.z) * r.inv.z;
-		// Plane distance q * A + C evaluated as fma(1 + q * 2^-15, 2^15 * A, C - 2^15 * A): 2^15 * A is
-		// exact and the product term is exact, so the only extra rounding is that of C - 2^15 * A,
-		// at most u|C| + 2^-9 |A|. With |C| <= |t| + 255 |A|, the relative slack (5u of 8.4u used) and
-		// the one-grid-step widening |A| (2^-9 + 1020u of 1 used) still cover every error.
+		// Plane distance q * A + C evaluated as fma(1 + q * 2^-15, 2^15 * A, C - 2^15 * A): 2^15 * A and
+		// the product term are exact; the error bound and the slacks that cover it are derived above
+		// kSlabRelSlack.
 		const float Sx = 32768.0f * Ax, Sy = 32768.0f * Ay, Sz = 32768.0f * Az;
 		const float Dx = Cx - Sx, Dy = Cy - Sy, Dz = Cz - Sz;
+		// Near planes earlier, far planes later, by kPlaneSlack grid steps.
+		const float ex = kPlaneSlack * absf_(Sx), ey = kPlaneSlack * absf_(Sy), ez = kPlaneSlack * absf_(Sz);
+		const float Dnx = Dx - ex, Dny = Dy - ey, Dnz = Dz - ez, Dfx = Dx + ex, Dfy = Dy + ey, Dfz = Dz + ez;
 		// near/far quantised planes per axis (packed bytes), swapped for negative directions
 		const bool negx = (r.oct & 1u) != 0, negy = (r.oct & 2u) != 0, negz = (r.oct & 4u) != 0;
 		const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y, fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
@@ -315,9 +325,9 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 		for (int s = 0; s < kWideArity; ++s) {
 			const int k = s & 3;
 			const bool hiw = s >= 4;
-			const float tnx = fmaf(byteMantissa(hiw ? nx1 : nx0, k), Sx, Dx), tfx = fmaf(byteMantissa(hiw ? fx1 : fx0, k), Sx, Dx);
-			const float tny = fmaf(byteMantissa(hiw ? ny1 : ny0, k), Sy, Dy), tfy = fmaf(byteMantissa(hiw ? fy1 : fy0, k), Sy, Dy);
-			const float tnz = fmaf(byteMantissa(hiw ? nz1 : nz0, k), Sz, Dz), tfz = fmaf(byteMantissa(hiw ? fz1 : fz0, k), Sz, Dz);
+			const float tnx = fmaf(byteMantissa(hiw ? nx1 : nx0, k), Sx, Dnx), tfx = fmaf(byteMantissa(hiw ? fx1 : fx0, k), Sx, Dfx);
+			const float tny = fmaf(byteMantissa(hiw ? ny1 : ny0, k), Sy, Dny), tfy = fmaf(byteMantissa(hiw ? fy1 : fy0, k), Sy, Dfy);
+			const float tnz = fmaf(byteMantissa(hiw ? nz1 : nz0, k), Sz, Dnz), tfz = fmaf(byteMantissa(hiw ? fz1 : fz0, k), Sz, Dfz);
 			const float tEntry = max4(tnx, tny, tnz, 0.0f);
 			const float tExit = min4(tfx, tfy, tfz, best.t);
 			hitSlots |= (tEntry <= tExit * kSlabRelSlack) ? (1u << s) : 0u;

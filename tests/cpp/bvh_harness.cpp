@@ -369,8 +369,10 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 				const float bnz = byteMantissa(hiw ? nz1 : nz0, k), bfz = byteMantissa(hiw ? fz1 : fz0, k);
 				uint32_t h = 0u; // no short circuit: every ray's test is straight-line code
 				for (int r = 0; r < P; ++r) {
-					const float tEntry = max4(fmaf(bnx, Sx[r], Dx[r]), fmaf(bny, Sy[r], Dy[r]), fmaf(bnz, Sz[r], Dz[r]), 0.0f);
-					const float tExit = min4(fmaf(bfx, Sx[r], Dx[r]), fmaf(bfy, Sy[r], Dy[r]), fmaf(bfz, Sz[r], Dz[r]), best[r].t);
+					// The traversal's plane slack: near planes earlier, far planes later.
+					const float ex = kPlaneSlack * absf_(Sx[r]), ey = kPlaneSlack * absf_(Sy[r]), ez = kPlaneSlack * absf_(Sz[r]);
+					const float tEntry = max4(fmaf(bnx, Sx[r], Dx[r] - ex), fmaf(bny, Sy[r], Dy[r] - ey), fmaf(bnz, Sz[r], Dz[r] - ez), 0.0f);
+					const float tExit = min4(fmaf(bfx, Sx[r], Dx[r] + ex), fmaf(bfy, Sy[r], Dy[r] + ey), fmaf(bfz, Sz[r], Dz[r] + ez), best[r].t);
 					h |= (tEntry <= tExit * kSlabRelSlack) ? 1u : 0u;
 				}
 				hitSlots |= h << s;
@@ -388,8 +390,9 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 					const float ax = fmaf(lx, Sx[r], Dx[r]), bx = fmaf(hx, Sx[r], Dx[r]);
 					const float ay = fmaf(ly, Sy[r], Dy[r]), by = fmaf(hy, Sy[r], Dy[r]);
 					const float az = fmaf(lz, Sz[r], Dz[r]), bz = fmaf(hz, Sz[r], Dz[r]);
-					const float tEntry = max4(minf_(ax, bx), minf_(ay, by), minf_(az, bz), 0.0f);
-					const float tExit = min4(maxf_(ax, bx), maxf_(ay, by), maxf_(az, bz), best[r].t);
+					const float ex = kPlaneSlack * absf_(Sx[r]), ey = kPlaneSlack * absf_(Sy[r]), ez = kPlaneSlack * absf_(Sz[r]);
+					const float tEntry = max4(minf_(ax, bx) - ex, minf_(ay, by) - ey, minf_(az, bz) - ez, 0.0f);
+					const float tExit = min4(maxf_(ax, bx) + ex, maxf_(ay, by) + ey, maxf_(az, bz) + ez, best[r].t);
 					h |= (tEntry <= tExit * kSlabRelSlack) ? 1u : 0u;
 				}
 				hitSlots |= h << s;
