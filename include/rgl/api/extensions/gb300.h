@@ -44,7 +44,7 @@ RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t*
  * Traversal schedule of graph runs (rgl_graph_run). Every raytrace runs on the persistent traversal
  * kernel of batched frames as a one-job launch; this sets its block size (64, 128, 256), packing
  * (0: a beam's sub-rays on adjacent lanes, walking the scene together; 1: one lane per beam), tasks
- * per fetch (1..64) and register budget (64, 80, 96, 128). The default is 128, 0, 1, 96. Changes speed
+ * per fetch (1..64) and register budget (64, 80, 96, 128). The default is 128, 0, 1, 128. Changes speed
  * only, never results.
  */
 RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs);

@@ -27,7 +27,7 @@ uint64_t Node::nextParamVersion() { return gParamVersion.fetch_add(1, std::memor
 namespace {
 // Schedule of single-graph traversals (a batch of one job). The default is the fastest measured on
 // the 1M-triangle single-sensor scan: lane-group packing, one task per fetch, 80 registers.
-rgl::BatchSchedule gTraceSchedule{128, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 96};
+rgl::BatchSchedule gTraceSchedule{128, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 128};
 } // namespace
 rgl::BatchSchedule traceSchedule() { return gTraceSchedule; }
 void setTraceSchedule(const rgl::BatchSchedule& s) { gTraceSchedule = s; }
