@@ -236,12 +236,14 @@ def run_ours(args):
 
     lib = rgl.lib()
     rgl.check(lib.rgl_configure_logging(rgl.RGL_LOG_LEVEL_OFF, None, False))
+    rgl.check(lib.rgl_gb300_configure_blas_builder(BLAS_BUILDERS[args.blas_builder]))
     scene = scenes.million_scene()
     rays = scenes.lidar_rays(CHANNELS, AZIMUTHS)
     n_beams = rays.shape[0]
     rays_per_step = n_beams * SUBRAYS
     nodes = build_pipeline(rgl, scene, rays)
     rgl.check(lib.rgl_gb300_configure_timing(True))
+    builds0 = blas_build_stats(rgl)
 
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -261,6 +263,7 @@ def run_ours(args):
         rgl.graph_run(nodes["rays"])
         rgl.check(lib.rgl_gb300_graph_sync(nodes["rays"]))
         k += 1
+    builds1 = blas_build_stats(rgl)
 
     # ---- device-resident timed region
     if dist:
@@ -353,6 +356,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
+            "scene_build": {"blas_builder": args.blas_builder, "meshes": builds1[0] - builds0[0],
+                            "triangles": int(T), "blas_ms": builds1[1] - builds0[1]},
             "beams_per_s": world * n_beams * args.steps / (total_ms / 1e3),
             "wall_s_timed_region": wall,
         }
@@ -861,6 +866,17 @@ def run_serving(args):
     return 0
 
 
+BLAS_BUILDERS = {"device_sah": 0, "host_sah": 1, "device_lbvh": 2}
+
+
+def blas_build_stats(rgl):
+    import ctypes as C
+
+    n, ms = C.c_int64(), C.c_double()
+    rgl.check(rgl.lib().rgl_gb300_get_blas_build_stats(C.byref(n), C.byref(ms)))
+    return n.value, ms.value
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -876,6 +892,8 @@ def main():
     ap.add_argument("--trace-seconds", type=float, default=30.0, help="serving: length of each arrival trace")
     ap.add_argument("--max-lag", type=float, default=5.0, help="serving: stop a trace once the loop lags arrivals by this much (s)")
     ap.add_argument("--capacity-requests", type=int, default=2000, help="serving: requests of the all-at-once capacity run")
+    ap.add_argument("--blas-builder", choices=list(BLAS_BUILDERS), default="device_sah",
+                    help="mesh BLAS builder: binned SAH on the device (default), the same tree built on the host, or the device LBVH")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -61,6 +61,23 @@ RGL_API rgl_status_t rgl_gb300_get_kernel_launch_count(uint64_t* out_count);
  */
 RGL_API rgl_status_t rgl_gb300_scene_get_stats(int64_t* out_node_bytes, int64_t* out_triangle_bytes, int32_t* out_instances);
 
+/*
+ * Builder of mesh BLASes (acceleration structures over a mesh's triangles), for meshes whose BLAS is
+ * built after the call. No counterpart in the reference, whose OptiX GAS build
+ * (src/scene/GASBuilder.hpp:31-100) has no choice of builder.
+ *   RGL_GB300_BLAS_DEVICE_SAH   (default) binned SAH topology built on the device, then the 8-wide collapse
+ *   RGL_GB300_BLAS_HOST_SAH     the same binned SAH tree built on the host and uploaded
+ *   RGL_GB300_BLAS_DEVICE_LBVH  Morton codes, onesweep radix sort and LBVH on the device (as for animated entities)
+ */
+#define RGL_GB300_BLAS_DEVICE_SAH 0
+#define RGL_GB300_BLAS_HOST_SAH 1
+#define RGL_GB300_BLAS_DEVICE_LBVH 2
+RGL_API rgl_status_t rgl_gb300_configure_blas_builder(int32_t builder);
+
+/* Number of mesh BLAS builds since the library was loaded and their total wall time (ms, host clock,
+ * the build's device work waited for). */
+RGL_API rgl_status_t rgl_gb300_get_blas_build_stats(int64_t* out_builds, double* out_total_ms);
+
 /* SM count and compute capability (major * 10 + minor) of the device in use. */
 RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_compute_capability);
 
@@ -78,6 +95,9 @@ RGL_API rgl_status_t rgl_gb300_device_info(int32_t* out_sm_count, int32_t* out_c
  * Limits: count <= 16,777,216 (larger counts return RGL_INVALID_ARGUMENT), element_size 1..256 bytes.
  * The fixed array (65,548 bytes) stays resident on every device that loads the library until exit.
  * The first call on a device looks up the array's device address, so make it before any stream capture.
+ * Under CUDA's lazy module loading (the default) that first call also makes the driver load the
+ * library's device code and the array on the device, which the driver allocates; callers that must
+ * allocate nothing at run time make one warm-up call at initialisation. Later calls allocate nothing.
  * All calls share the array and clear what they use when they start; calls whose GPU work overlaps
  * (other streams or host threads) race on it and must be serialised by the caller.
  */

@@ -1244,6 +1244,29 @@ RGL_API rgl_status_t rgl_gb300_scene_get_stats(int64_t* out_node_bytes, int64_t*
 	});
 }
 
+RGL_API rgl_status_t rgl_gb300_configure_blas_builder(int32_t builder)
+{
+	return safeCall([&]() {
+		CHECK_ARG(builder == RGL_GB300_BLAS_DEVICE_SAH || builder == RGL_GB300_BLAS_HOST_SAH || builder == RGL_GB300_BLAS_DEVICE_LBVH);
+		setBlasBuilder(builder);
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_get_blas_build_stats(int64_t* out_builds, double* out_total_ms)
+{
+	return safeCall([&]() {
+		int64_t builds = 0;
+		double ms = 0.0;
+		blasBuildStats(builds, ms);
+		if (out_builds) {
+			*out_builds = builds;
+		}
+		if (out_total_ms) {
+			*out_total_ms = ms;
+		}
+	});
+}
+
 // Allocation-free compaction (include/rgl/api/extensions/gb300.h). Status handling as safeCall() but
 // without its first-call CUDA initialisation, which calls cudaFree(nullptr): this entry point uses the
 // caller's current device and context as they are.

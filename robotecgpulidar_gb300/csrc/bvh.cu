@@ -198,7 +198,7 @@ struct WideBuildResult
 // nodes. Leaf records are triangles (dV/dI given) or primitive indices (dV null). Frees lo, hi, cb and
 // its temporaries and synchronises s (a one-off build).
 WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const float* dV, const int32_t* dI, int leafMax,
-                          WideNode* outNodes, TriRecord* outLeaves, Box* outBoxes, cudaStream_t s)
+                          WideNode* outNodes, TriRecord* outLeaves, Box* outBoxes, cudaStream_t s, bool sah)
 {
 	uint32_t* codes = mallocAsync<uint32_t>(n, s);
 	uint32_t* ids = mallocAsync<uint32_t>(n, s);
@@ -217,14 +217,18 @@ WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const flo
 	RGL_CUDA_OK(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * 8, s));
 	int32_t* err = reinterpret_cast<int32_t*>(ctr + 4);
 
-	kMorton<<<blocks(n, 256), 256, 0, s>>>(lo, hi, n, cb, codes, ids);
-	countLaunch();
-	sortPairs(codes, ids, n, 30, sortScratch, err, s);
-	if (n > 1) {
-		kLbvh<<<blocks(n - 1, 256), 256, 0, s>>>(codes, n, bin, rf, rl, pi, pl);
+	if (sah) {
+		buildSahTopologyDevice(lo, hi, n, bin, rf, rl, ids, s);
+	} else {
+		kMorton<<<blocks(n, 256), 256, 0, s>>>(lo, hi, n, cb, codes, ids);
 		countLaunch();
-		kBottomUp<<<blocks(n, 256), 256, 0, s>>>(n, ids, lo, hi, bin, pi, pl, visits);
-		countLaunch();
+		sortPairs(codes, ids, n, 30, sortScratch, err, s);
+		if (n > 1) {
+			kLbvh<<<blocks(n - 1, 256), 256, 0, s>>>(codes, n, bin, rf, rl, pi, pl);
+			countLaunch();
+			kBottomUp<<<blocks(n, 256), 256, 0, s>>>(n, ids, lo, hi, bin, pi, pl, visits);
+			countLaunch();
+		}
 	}
 	int2 root = make_int2(n == 1 ? ~0 : 0, 0);
 	uint32_t one[2] = {1u, 0u};
@@ -236,20 +240,29 @@ WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const flo
 	int2* qb = q1;
 	uint32_t* ca = ctr + 2;
 	uint32_t* cbn = ctr + 3;
-	// A wide level descends at least one binary level; binary depth is below 64 for 30-bit keys with
-	// index tie-break, so 64 launches always drain the queue (empty launches exit immediately).
+	// A wide level descends at least one binary level. The LBVH's binary depth is below 64 (30-bit keys
+	// with index tie-break); an SAH tree may be deeper, so the queue is checked after every 16 levels
+	// (empty launches exit immediately).
 	const int grid = 152 * 4;
-	for (int level = 0; level < 64; ++level) {
-		RGL_CUDA_OK(cudaMemsetAsync(cbn, 0, sizeof(uint32_t), s));
-		CollapseOutputs co{outNodes, outLeaves, ctr, ctr + 1, qb, cbn, outBoxes};
-		kCollapse<<<grid, 128, 0, s>>>(qa, ca, ci, co);
-		countLaunch();
-		int2* tq = qa;
-		qa = qb;
-		qb = tq;
-		uint32_t* tc = ca;
-		ca = cbn;
-		cbn = tc;
+	uint32_t pending = 1;
+	for (int round = 0; pending != 0; ++round) {
+		for (int level = 0; level < 16; ++level) {
+			RGL_CUDA_OK(cudaMemsetAsync(cbn, 0, sizeof(uint32_t), s));
+			CollapseOutputs co{outNodes, outLeaves, ctr, ctr + 1, qb, cbn, outBoxes};
+			kCollapse<<<grid, 128, 0, s>>>(qa, ca, ci, co);
+			countLaunch();
+			int2* tq = qa;
+			qa = qb;
+			qb = tq;
+			uint32_t* tc = ca;
+			ca = cbn;
+			cbn = tc;
+		}
+		RGL_CUDA_OK(cudaMemcpyAsync(&pending, ca, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+		RGL_CUDA_OK(cudaStreamSynchronize(s));
+		if (round > (n >> 4) + 4) {
+			throw std::runtime_error("BVH build: wide collapse does not terminate");
+		}
 	}
 	uint32_t hostCtr[8];
 	RGL_CUDA_OK(cudaMemcpyAsync(hostCtr, ctr, sizeof(hostCtr), cudaMemcpyDeviceToHost, s));
@@ -282,7 +295,7 @@ WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const flo
 
 } // namespace
 
-void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, int nTris, BlasBuild& out, cudaStream_t s)
+void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, int nTris, BlasBuild& out, cudaStream_t s, bool sah)
 {
 	(void) nVertices;
 	if (nTris <= 0) {
@@ -306,7 +319,7 @@ void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, i
 	RGL_CUDA_OK(cudaMemcpyAsync(cb, cbInit, sizeof(cbInit), cudaMemcpyHostToDevice, s));
 	kTriBounds<<<blocks(T, 256), 256, 0, s>>>(dVertices, dIndices, T, lo, hi, cb);
 	countLaunch();
-	const WideBuildResult r = buildWide(lo, hi, cb, T, dVertices, dIndices, kLeafMaxTris, out.nodes, out.tris, nullptr, s);
+	const WideBuildResult r = buildWide(lo, hi, cb, T, dVertices, dIndices, kLeafMaxTris, out.nodes, out.tris, nullptr, s, sah);
 	out.nodeCount = r.nodeCount;
 	out.bounds[0] = r.bounds.lox;
 	out.bounds[1] = r.bounds.loy;

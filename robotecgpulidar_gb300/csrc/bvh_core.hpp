@@ -26,10 +26,12 @@ RGL_HD Box unite(const Box& a, const Box& b)
 	return Box{a.lox < b.lox ? a.lox : b.lox, a.loy < b.loy ? a.loy : b.loy, a.loz < b.loz ? a.loz : b.loz,
 	           a.hix > b.hix ? a.hix : b.hix, a.hiy > b.hiy ? a.hiy : b.hiy, a.hiz > b.hiz ? a.hiz : b.hiz};
 }
+// Half the surface area, evaluated in the same order without FMA contraction on host and device, so
+// the device builders choose exactly what the host builder chooses.
 RGL_HD float halfArea(const Box& b)
 {
-	float dx = b.hix - b.lox, dy = b.hiy - b.loy, dz = b.hiz - b.loz;
-	return dx * dy + dy * dz + dz * dx;
+	const float dx = fsub(b.hix, b.lox), dy = fsub(b.hiy, b.loy), dz = fsub(b.hiz, b.loz);
+	return fadd(fadd(fmul(dx, dy), fmul(dy, dz)), fmul(dz, dx));
 }
 RGL_HD Box binBox(const BinNode& n) { return Box{n.lox, n.loy, n.loz, n.hix, n.hiy, n.hiz}; }
 
@@ -116,9 +118,10 @@ RGL_HD void lbvhInternal(int i, const uint32_t* codes, int n, int32_t& left, int
 	last = hi;
 }
 
-// Quantisation grid of a wide node: origin p = lo - 2^(e-127) and 2^(e-127) * kQuantSpan >= extent,
-// leaving one spare grid step below and above every child so each child box can be widened by one
-// step on each side (see quantizeAxis).
+// Quantisation grid of a wide node: origin p = lo - 2^(e-127) (rounded down to a float) and
+// 2^(e-127) * kQuantSpan >= extent, so the node box spans grid steps 1 .. 253 at most. Child bounds
+// are rounded outward to whole steps (quantizeAxis) and never widened further; the spare steps at
+// both ends keep the outward-rounded bounds inside 0 .. 255 whatever the rounding of p.
 constexpr double kQuantSpan = 252.0;
 
 // Smallest power of two 2^(e-127) with kQuantSpan * 2^(e-127) >= ext, as the biased exponent byte e.
@@ -174,7 +177,7 @@ RGL_HD uint32_t atomicAddU32(uint32_t* p, uint32_t v)
 }
 
 // Quantisation frame of a wide node over its box nb: per-axis exponents and an origin one grid step
-// below the box (rounded down), so child boxes can be widened downward by a step.
+// below the box (rounded down to a float), see kQuantSpan.
 RGL_HD void setWideFrame(WideNode& w, const Box& nb)
 {
 	w.ex = quantExponent(nb.hix - nb.lox);
@@ -200,7 +203,7 @@ RGL_HD void clearChild(WideNode& w, int k)
 	w.qhix[k] = w.qhiy[k] = w.qhiz[k] = 0;
 }
 
-// Conservative 8-bit box of child slot k in the node's frame (verified and widened, quantizeAxis).
+// Conservative 8-bit box of child slot k in the node's frame (rounded outward and verified, quantizeAxis).
 RGL_HD void quantizeChild(WideNode& w, int k, const Box& b)
 {
 	const float sx = exp2Byte(w.ex), sy = exp2Byte(w.ey), sz = exp2Byte(w.ez);

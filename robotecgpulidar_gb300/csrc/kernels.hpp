@@ -29,9 +29,16 @@ struct BlasBuild
 	int32_t triCount = 0;
 	float bounds[6] = {0, 0, 0, 0, 0, 0}; // object-space box lo.xyz, hi.xyz (host copy)
 };
-// Builds a BLAS on the device from device vertices/indices (Morton LBVH + wide collapse); synchronises
-// `stream` at the end. Used for animated entities, whose BLAS is rebuilt at every animation.
-void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, int nTris, BlasBuild& out, cudaStream_t stream);
+// Builds a BLAS on the device from device vertices/indices and synchronises `stream` at the end:
+// triangle boxes, the binary topology (binned SAH, sah.cu, when `sah`; else Morton codes, onesweep
+// sort and LBVH), then the wide collapse. Mesh BLASes use the SAH topology; animated entities, whose
+// BLAS is rebuilt at every animation, the LBVH.
+void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, int nTris, BlasBuild& out, cudaStream_t stream,
+               bool sah);
+// ---- sah.cu: binary binned-SAH topology of n primitive boxes (device lo/hi), the host builder's tree
+// (sah_build.hpp buildBinnedSahTree) computed on the device; output in the collapse's input format.
+void buildSahTopologyDevice(const float4* lo, const float4* hi, int n, BinNode* bin, int32_t* rangeFirst, int32_t* rangeLast,
+                            uint32_t* sortedIds, cudaStream_t stream);
 // Builds the BLAS of a mesh on the host from host vertices/indices (binned SAH topology, the same wide
 // collapse) and uploads it; storage of `out` is reused when large enough.
 void buildBlasHost(const float* hVertices, int nVertices, const int32_t* hIndices, int nTris, BlasBuild& out);

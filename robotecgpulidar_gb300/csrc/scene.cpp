@@ -1,6 +1,10 @@
 #include "scene.hpp"
 
+#include <rgl/api/extensions/gb300.h>
+
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <set>
@@ -104,13 +108,41 @@ Texture::~Texture()
 	}
 }
 
+namespace {
+std::atomic<int32_t> gBlasBuilder{RGL_GB300_BLAS_DEVICE_SAH};
+std::atomic<int64_t> gBlasBuilds{0};
+std::atomic<int64_t> gBlasBuildNs{0};
+} // namespace
+
+void setBlasBuilder(int32_t builder) { gBlasBuilder = builder; }
+void blasBuildStats(int64_t& builds, double& ms)
+{
+	builds = gBlasBuilds.load();
+	ms = (double) gBlasBuildNs.load() * 1e-6;
+}
+
+// The mesh's BLAS, built by the configured builder (rgl_gb300_configure_blas_builder) on first use:
+// by default on the device (binned SAH topology, sah.cu, then the wide collapse); the host build of
+// the same tree and the device LBVH stay selectable.
 void Mesh::ensureBlas(cudaStream_t s)
 {
 	if (blasBuilt) {
 		return;
 	}
-	(void) s;
-	rgl::buildBlasHost(hVertices.data(), vertexCount, hIndices.data(), triangleCount, blas);
+	const auto t0 = std::chrono::steady_clock::now();
+	switch (gBlasBuilder.load()) {
+		case RGL_GB300_BLAS_HOST_SAH:
+			rgl::buildBlasHost(hVertices.data(), vertexCount, hIndices.data(), triangleCount, blas);
+			break;
+		case RGL_GB300_BLAS_DEVICE_LBVH:
+			rgl::buildBlas(dVertices.as<float>(), vertexCount, dIndices.as<int32_t>(), triangleCount, blas, s, false);
+			break;
+		default:
+			rgl::buildBlas(dVertices.as<float>(), vertexCount, dIndices.as<int32_t>(), triangleCount, blas, s, true);
+			break;
+	}
+	gBlasBuildNs += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+	++gBlasBuilds;
 	blasBuilt = true;
 }
 
@@ -140,7 +172,7 @@ void Entity::startAnimation()
 void Entity::finishAnimation(cudaStream_t s)
 {
 	rgl::launchUpdateVertices(mesh->vertexCount, dAnimDisplacement.as<float>(), dAnimVertices.as<float>(), s);
-	rgl::buildBlas(dAnimVertices.as<float>(), mesh->vertexCount, mesh->dIndices.as<int32_t>(), mesh->triangleCount, animBlas, s);
+	rgl::buildBlas(dAnimVertices.as<float>(), mesh->vertexCount, mesh->dIndices.as<int32_t>(), mesh->triangleCount, animBlas, s, false);
 	RGL_CHECK_CUDA(cudaStreamSynchronize(s));
 	formerAnimTimed = animTimed;
 	formerAnimTimeNs = animTimeNs;
@@ -345,6 +377,7 @@ void Scene::checkDeviceErrors()
 // Instance records (world boxes padded outward) in pinned host memory, and the world bounds.
 rgl::InstanceRec* Scene::fillInstanceRecords()
 {
+	static const Mat34 identityPose = Mat34::identity();
 	const int n = (int) entities.size();
 	worldLo[0] = worldLo[1] = worldLo[2] = INFINITY;
 	worldHi[0] = worldHi[1] = worldHi[2] = -INFINITY;
@@ -354,6 +387,7 @@ rgl::InstanceRec* Scene::fillInstanceRecords()
 		rgl::InstanceRec r{};
 		r.objectToWorld = e.transform;
 		r.worldToObject = rgl::inverse(e.transform);
+		r.flags = std::memcmp(&e.transform, &identityPose, sizeof(Mat34)) == 0 ? rgl::kInstanceIdentity : 0;
 		const rgl::BlasBuild& bl = e.activeBlas();
 		r.nodes = bl.nodes;
 		r.tris = bl.tris;

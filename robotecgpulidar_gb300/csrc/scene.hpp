@@ -14,6 +14,10 @@
 
 struct Scene;
 
+// Builder of mesh BLASes built from now on (RGL_GB300_BLAS_*), and the count and wall time of builds.
+void setBlasBuilder(int32_t builder);
+void blasBuildStats(int64_t& builds, double& ms);
+
 struct Mesh
 {
 	Mesh(const rgl_vec3f* vertices, int32_t vertexCount, const rgl_vec3i* indices, int32_t indexCount);
@@ -29,7 +33,7 @@ struct Mesh
 	int32_t triangleCount = 0;
 	rgl::DeviceBuffer dVertices{false};
 	rgl::DeviceBuffer dIndices{false};
-	std::vector<float> hVertices;   // host copies for the host BLAS build
+	std::vector<float> hVertices;   // host copies for the host BLAS build (RGL_GB300_BLAS_HOST_SAH)
 	std::vector<int32_t> hIndices;
 	rgl::BlasBuild blas;
 	bool blasBuilt = false;

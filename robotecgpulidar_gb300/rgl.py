@@ -189,6 +189,8 @@ def _proto(l):
         "rgl_gb300_graph_sync": [vp],
         "rgl_gb300_device_info": [P(i32), P(i32)],
         "rgl_gb300_scene_get_stats": [P(C.c_int64), P(C.c_int64), P(i32)],
+        "rgl_gb300_configure_blas_builder": [i32],
+        "rgl_gb300_get_blas_build_stats": [P(C.c_int64), P(C.c_double)],
         "rgl_gb300_compact_by_flags_noalloc": [vp, vp, i32, i32, vp, P(i32), vp],
         "rgl_gb300_configure_cuda_graphs": [C.c_bool],
         "rgl_gb300_graph_get_capture_stats": [vp, P(C.c_int64), P(C.c_int64)],

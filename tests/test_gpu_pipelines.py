@@ -100,6 +100,18 @@ def test_second_run_advances_noise_and_reset_reproduces(rgl):
     assert not np.array_equal(a, b) and np.array_equal(a, c)
 
 
+def build_scene_now(rgl):
+    """Runs a one-ray raytrace so the scene's acceleration structures (built on the device, with their
+    own kernel launches) exist before launch counts are compared."""
+    n_rays, n_rt = rgl.node(), rgl.node()
+    rgl.rays_from_mat3x4f(n_rays, [scenes.translation(0, 0, 0)])
+    rgl.raytrace(n_rt)
+    rgl.chain(n_rays, n_rt)
+    rgl.graph_run(n_rays)
+    rgl.check(rgl.lib().rgl_gb300_graph_sync(n_rays))
+    rgl.check(rgl.lib().rgl_graph_destroy(n_rays))
+
+
 def test_folded_sensor_transform_equals_separate_kernel(rgl):
     """A rays transform whose only consumer is the raytrace is applied in the traversal prologue (no
     transform kernel); with a second consumer it runs as its own kernel. Both give the same bytes."""
@@ -123,6 +135,7 @@ def test_folded_sensor_transform_equals_separate_kernel(rgl):
             rgl.add_child(n["pose"], n["trace2"])
         return n
 
+    build_scene_now(rgl)
     a, b = graph(False), graph(True)
     l0 = rgl.kernel_launch_count()
     rgl.graph_run(a["rays"])
@@ -172,6 +185,7 @@ def test_point_chain_absorbed_by_compaction(rgl):
             rgl.add_child(n["tf"], n["y2"])
         return n
 
+    build_scene_now(rgl)
     a, b = graph(False), graph(True)
     l0 = rgl.kernel_launch_count()
     rgl.graph_run(a["rays"])
