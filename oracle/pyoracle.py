@@ -41,7 +41,8 @@ def lib():
         l.orc_beam_samples.argtypes = [C.c_float, C.c_float, C.c_int, C.c_int, C.c_void_p]
         l.orc_raytrace.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int32,
                                    C.c_float, C.c_float, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
-                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p]
         l.orc_transform_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         l.orc_transform_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         l.orc_philox4x32_10.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -117,15 +118,19 @@ class OracleScene:
         rtype = np.zeros(npts, np.uint8)
         inten = np.zeros(npts, np.float32)
         amb = np.zeros(npts, np.uint8)
+        normal = np.zeros((npts, 3), np.float32)
+        incident = np.zeros(npts, np.float32)
+        tri_tie = np.zeros(npts, np.uint8)
         tf = None if ray_transform is None else np.ascontiguousarray(ray_transform, dtype=np.float32).reshape(12)
         rg = None if ranges is None else np.ascontiguousarray(ranges, dtype=np.float32).reshape(-1, 2)
         threads = threads or os.cpu_count() or 1
         ns = self._l.orc_raytrace(self.h, _p(rays), n, _p(tf), _p(rg), 0 if rg is None else rg.shape[0],
                                   int(np.int32(np.uint32(return_mode & 0xFFFFFFFF))), h_div, v_div, layers, vertices,
                                   near, far, default_intensity, threads, _p(xyz), _p(dist), _p(ent), _p(hit),
-                                  _p(rtype), _p(inten), _p(amb))
+                                  _p(rtype), _p(inten), _p(amb), _p(normal), _p(incident), _p(tri_tie))
         return {"xyz": xyz, "distance": dist, "entity_id": ent, "is_hit": hit, "return_type": rtype,
-                "intensity": inten, "ambiguous": amb, "samples": ns}
+                "intensity": inten, "ambiguous": amb, "normal": normal, "incident_angle": incident,
+                "triangle_tie": tri_tie, "samples": ns}
 
 
 def beam_samples(h_div, v_div, layers, vertices):

@@ -350,8 +350,9 @@ struct Hit
 	int tri = -1;
 	bool nearEdge = false;
 	double nearMissT = std::numeric_limits<double>::infinity();
-	double secondT = std::numeric_limits<double>::infinity(); // closest hit of another entity
-	int secondEntity = -1;
+	int entity = -1;
+	double secondT = std::numeric_limits<double>::infinity(); // closest hit of an entity other than `entity`
+	double sinGraze = 1.0; // sine of the angle between the ray and the hit triangle's plane
 };
 
 inline bool slab(const Node& n, D3 o, D3 inv, double tmax)
@@ -414,18 +415,25 @@ void testTri(const Tri& tr, int triIdx, D3 o, D3 d, int kx, int ky, int kz, doub
 		h.nearMissT = std::min(h.nearMissT, t);
 		return;
 	}
-	(void) dlen;
 	if (t < h.t) {
-		if (h.tri >= 0) {
-			h.secondT = std::min(h.secondT, h.t);
+		// A new closest hit of another entity makes the previous closest (nearer than every other hit
+		// seen) the closest hit of an entity other than the new one; within one entity it stays.
+		if (h.tri >= 0 && h.entity != tr.entityId) {
+			h.secondT = h.t;
 		}
 		h.t = t;
 		h.tri = triIdx;
+		h.entity = tr.entityId;
 		h.nearEdge = dmin < eps;
-	} else {
+		h.sinGraze = std::fabs(dot(cross(e01, tr.v2 - tr.v0), d)) / (area2 * dlen);
+	} else if (tr.entityId != h.entity) {
 		h.secondT = std::min(h.secondT, t);
 	}
 }
+
+// Relative band within which two entities' surfaces are at the same depth for FP32: the watertight t
+// errs by about 4e-7 / sin(grazing angle) of the distance, and distances carry the 1e-5 tolerance.
+inline double depthBand(double sinGraze) { return std::max(1e-5, 4e-7 / std::max(sinGraze, 1e-6)); }
 
 Hit castRay(const Scene& s, D3 o, D3 d, double tmax)
 {
@@ -450,7 +458,8 @@ Hit castRay(const Scene& s, D3 o, D3 d, double tmax)
 	stack[sp++] = 0;
 	while (sp > 0) {
 		const Node& n = s.nodes[stack[--sp]];
-		double tlim = std::min(tmax, h.t) * (1.0 + 1e-6);
+		// hits of other entities within the depth band behind the closest one are still collected
+		double tlim = std::min(tmax * (1.0 + 1e-6), h.t * (1.0 + depthBand(h.sinGraze)));
 		if (!slab(n, o, inv, tlim)) {
 			continue;
 		}
@@ -467,6 +476,9 @@ Hit castRay(const Scene& s, D3 o, D3 d, double tmax)
 }
 
 // ---------------------------------------------------------------- return selection
+
+// Relative distance tolerance of the GPU path against this oracle (the parity bound).
+constexpr double kDistanceTolerance = 1e-5;
 
 inline int returnCount(int32_t mode) { return (int) (((uint32_t) mode) >> 24); }
 inline int returnType(int32_t mode, int r) { return (int) ((((uint32_t) mode) >> (8 * r)) & 0xffu); }
@@ -487,7 +499,10 @@ struct Sample
 	float dist;
 	float intensity;
 	int entity;
+	int tri;        // the hit triangle (scene triangle index), -1 for non-hits
 	bool ambiguous;
+	D3 normal;      // unit world normal of the hit triangle (edge v0v1 x edge v0v2)
+	double cosInc;  // |normal . direction| with the sample's unnormalised direction
 };
 
 } // namespace
@@ -554,10 +569,17 @@ int orc_beam_samples(float hDivergence, float vDivergence, int layers, int verti
 //   ranges: nRanges x 2 floats (nRanges == 1 or nRays; NULL -> {0, FLT_MAX}).
 //   Outputs are sized returnCount * nRays; any output pointer may be NULL.
 //   ambiguous: 1 byte per output point.
+//   normal (3 floats per point) and incident angle (radians): reference optixPrograms.cu:138-150, the
+//   world normal of the hit triangle and acos(|normal . ray direction|); NaN for non-hits
+//   (nodeKernels.cu:196-201).
+//   triTie: 1 byte per output point, 1 when two hit samples of the beam that hit different triangles
+//   have distances within the unresolved band (twice the distance tolerance): the selected sample,
+//   and with it the fields taken from its triangle (normal, incident angle, intensity), may then
+//   differ from the FP32 path's although the distance and entity agree.
 int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, const float* ranges, int nRanges, int32_t returnMode,
                  float hDiv, float vDiv, int layers, int vertices, float nearDist, float farDist, float defaultIntensity,
                  int nThreads, float* outXyz, float* outDist, int32_t* outEntity, int32_t* outIsHit, uint8_t* outReturnType,
-                 float* outIntensity, uint8_t* outAmbiguous)
+                 float* outIntensity, uint8_t* outAmbiguous, float* outNormal, float* outIncident, uint8_t* outTriTie)
 {
 	const Scene& s = *static_cast<Scene*>(h);
 	const int R = returnCount(returnMode);
@@ -591,6 +613,7 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 					Hit hit = castRay(s, o, d, (double) maxR);
 					Sample& S = smp[si];
 					S.ambiguous = false;
+					S.tri = -1;
 					if (hit.tri < 0) {
 						S.hit = false;
 						S.dist = farDist;
@@ -605,11 +628,14 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 					if (hit.nearEdge || hit.nearMissT <= hit.t * (1.0 + 1e-6)) {
 						S.ambiguous = true;
 					}
-					if (hit.secondT <= hit.t * (1.0 + 1e-6)) {
-						S.ambiguous = true; // two surfaces at the same depth
+					// Decisions that compare a distance are ambiguous within what FP32 resolves: another
+					// entity's surface at nearly the same depth (depthBand: FP32 picks the closer one by its
+					// watertight t), and a hit at a range bound (the 1e-5 distance tolerance).
+					if (hit.secondT <= hit.t * (1.0 + depthBand(hit.sinGraze))) {
+						S.ambiguous = true;
 					}
-					if (std::fabs(hit.t - (double) maxR) <= 1e-6 * (double) maxR ||
-					    std::fabs(dist - (double) minR) <= 1e-6 * std::max((double) minR, 1e-30)) {
+					if (std::fabs(hit.t - (double) maxR) <= kDistanceTolerance * (double) maxR ||
+					    std::fabs(dist - (double) minR) <= kDistanceTolerance * std::max((double) minR, dist)) {
 						S.ambiguous = true;
 					}
 					if (dist < (double) minR) {
@@ -622,9 +648,13 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 					S.hit = true;
 					S.dist = (float) dist;
 					S.entity = tr.entityId;
+					S.tri = hit.tri;
 					D3 n = cross(tr.v1 - tr.v0, tr.v2 - tr.v0);
-					double cosI = std::fabs(dot(n * (1.0 / len(n)), d));
+					n = n * (1.0 / len(n));
+					double cosI = std::fabs(dot(n, d));
 					S.intensity = (float) ((double) defaultIntensity * cosI);
+					S.normal = n;
+					S.cosInc = cosI;
 				}
 				// Return selection, in sample order (reference nodeKernels.cu:334-399).
 				int first = -1, second = -1, last = -1, strongest = -1, secondStrongest = -1;
@@ -638,6 +668,7 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 				for (int a = 0; a < nSamples; ++a) {
 					beamAmb = beamAmb || smp[a].ambiguous;
 				}
+				bool triTie = false;
 				if (first >= 0) {
 					for (i = i + 1; i < nSamples; ++i) {
 						if (!smp[i].hit)
@@ -669,9 +700,15 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 							if (!smp[c].hit)
 								continue;
 							float da = smp[a].dist, dc = smp[c].dist;
-							if (da != dc && std::fabs(da - dc) <= 2e-6f * std::max(da, dc)) {
-								beamAmb = true;
-								break;
+							// Within twice the distance tolerance the order of two samples is not resolved.
+							// It only changes the output's entity when they hit different entities; on one
+							// entity a swap moves the point by less than the distance tolerance.
+							if (std::fabs(da - dc) <= (float) (2.0 * kDistanceTolerance) * std::max(da, dc)) {
+								if (smp[a].entity != smp[c].entity) {
+									beamAmb = true;
+									break;
+								}
+								triTie = triTie || smp[a].tri != smp[c].tri;
 							}
 						}
 					}
@@ -684,6 +721,8 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 					int type = returnType(returnMode, r);
 					if (outAmbiguous)
 						outAmbiguous[p] = beamAmb ? 1 : 0;
+					if (outTriTie)
+						outTriTie[p] = triTie ? 1 : 0;
 					if (first < 0) {
 						float nh = smp[0].dist;
 						F3 disp = {nd.x * nh, nd.y * nh, nd.z * nh};
@@ -708,6 +747,10 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 							outReturnType[p] = (uint8_t) type;
 						if (outIntensity)
 							outIntensity[p] = 0.0f;
+						if (outNormal)
+							outNormal[3 * p] = outNormal[3 * p + 1] = outNormal[3 * p + 2] = std::numeric_limits<float>::quiet_NaN();
+						if (outIncident)
+							outIncident[p] = std::numeric_limits<float>::quiet_NaN();
 						continue;
 					}
 					int sel = -1;
@@ -739,6 +782,13 @@ int orc_raytrace(void* h, const float* rays, int nRays, const float* rayTf, cons
 						outReturnType[p] = (uint8_t) type;
 					if (outIntensity)
 						outIntensity[p] = smp[sel].intensity;
+					if (outNormal) {
+						outNormal[3 * p] = (float) smp[sel].normal.x;
+						outNormal[3 * p + 1] = (float) smp[sel].normal.y;
+						outNormal[3 * p + 2] = (float) smp[sel].normal.z;
+					}
+					if (outIncident)
+						outIncident[p] = (float) std::acos(std::min(smp[sel].cosInc, 1.0));
 				}
 			}
 		}

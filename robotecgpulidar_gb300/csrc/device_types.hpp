@@ -78,13 +78,21 @@ struct alignas(16) InstanceRec
 	int32_t hasPrev;           // prevObjectToWorld holds the pose of the scene's previous time step
 	float lox, loy, loz, hix, hiy, hiz; // world-space box (TLAS leaf bounds)
 	float laserRetro;          // rgl_entity_set_laser_retro
-	int32_t pad;
+	int32_t flags;             // kInstanceIdentity: objectToWorld is the identity
 	Mat34 prevObjectToWorld;   // 48 B, for hit-point velocities
 	const float* vertexDisplacement; // animated entity: per-vertex motion since the previous time step, or null
 	const int32_t* indices;          // the mesh's triangle vertex indices (with vertexDisplacement, texCoords)
 	uint64_t intensityTexture;       // cudaTextureObject_t of 8-bit texels, 0 without one
 	const float* texCoords;          // uv per vertex when intensityTexture is set
 };
+
+constexpr int32_t kInstanceIdentity = 1;
+
+// A world point in the instance's object frame, as worldToObject applied to the offset from the
+// instance origin: the subtraction is exact (or nearly) for points near the instance, so the result
+// keeps the precision of the offset instead of losing the instance origin's magnitude (an instance
+// 400 m from the world origin would otherwise shift ray origins by ~3e-5 m).
+RGL_HD Vec3 worldToInstance(const InstanceRec& ir, Vec3 pW) { return ir.worldToObject.vector(pW - ir.objectToWorld.translation()); }
 
 // Device view of a scene, read by the traversal kernel through one pointer so a captured CUDA graph
 // stays valid when the acceleration structure is rebuilt.

@@ -15,6 +15,7 @@ struct HitRec
 	float t;       // ray parameter (units of the unnormalised direction)
 	int32_t inst;  // instance index, -1 when nothing was hit
 	int32_t tri;   // index into the instance BLAS triangle records
+	int32_t prim;  // the triangle's index in its mesh (breaks ties in t)
 };
 
 #if defined(__CUDA_ARCH__)
@@ -250,15 +251,17 @@ RGL_HD uint32_t highestBit(uint32_t x)
 #endif
 }
 
-// Closest-hit order: smaller t first; equal t goes to the smaller (instance, triangle) pair. The order
-// does not depend on the traversal order, so every traversal that tests all triangles at the minimal
-// t (every correct one does: their boxes are never culled) returns the same hit.
-RGL_HD bool closerHit(float t, int32_t inst, int32_t tri, const HitRec& best)
+// Closest-hit order: smaller t first; equal t goes to the smaller (instance, mesh triangle index) pair.
+// The order depends neither on the traversal order nor on the order of the BLAS's triangle records
+// (which a device build allocates with atomics), so every traversal that tests all triangles at the
+// minimal t (every correct one does: their boxes are never culled) returns the same hit from every
+// build of the same mesh.
+RGL_HD bool closerHit(float t, int32_t inst, int32_t prim, const HitRec& best)
 {
 	if (t != best.t) {
 		return t < best.t;
 	}
-	return (uint32_t) inst != (uint32_t) best.inst ? (uint32_t) inst < (uint32_t) best.inst : (uint32_t) tri < (uint32_t) best.tri;
+	return (uint32_t) inst != (uint32_t) best.inst ? (uint32_t) inst < (uint32_t) best.inst : (uint32_t) prim < (uint32_t) best.prim;
 }
 
 // A ray in the frame being traversed: origin, direction, inverse direction and its octant.
@@ -278,6 +281,130 @@ RGL_HD FrameRay frameRay(Vec3 o, Vec3 d)
 	return r;
 }
 
+// Error-free transformations (Knuth's TwoSum, the FMA form of TwoProduct) and the compensated dot
+// product built from them (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 2005, Dot2): the result is as accurate as if computed in twice the working precision.
+RGL_HD void twoSum(float a, float b, float& s, float& e)
+{
+	s = fadd(a, b);
+	const float bb = fsub(s, a);
+	e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
+}
+RGL_HD void twoProd(float a, float b, float& p, float& e)
+{
+	p = fmul(a, b);
+	e = fmaf(a, b, -p);
+}
+// a . (bh + bl), bl a small correction of bh.
+RGL_HD float dotCompensated(Vec3 a, Vec3 bh, Vec3 bl)
+{
+	float p0, e0, p1, e1, p2, e2, s1, f1, s2, f2;
+	twoProd(a.x, bh.x, p0, e0);
+	twoProd(a.y, bh.y, p1, e1);
+	twoProd(a.z, bh.z, p2, e2);
+	twoSum(p0, p1, s1, f1);
+	twoSum(s1, p2, s2, f2);
+	const float err = fadd(fadd(fadd(e0, e1), fadd(e2, f1)), fadd(f2, fadd(fadd(fmul(a.x, bl.x), fmul(a.y, bl.y)), fmul(a.z, bl.z))));
+	return fadd(s2, err);
+}
+
+// Ray parameter of the hit with triangle (a, b, c), normal n = (b - a) x (c - a), from its plane:
+// t = n.(a - o) / n.d, with a - o exact (TwoSum) and both dot products compensated. The watertight
+// test decides hit or miss exactly, but its t comes from barycentric weights of the sheared, projected
+// triangle, whose relative error grows as 1 / sin(grazing angle): at 0.9 degrees over terrain 50 m
+// away it reached 2.5e-5 of the distance. In the plane form a grazing angle only divides the normal's
+// rounding, which is weighted by the hit's offset from the vertex (the triangle's size), not by the
+// distance. Returns `t` when the plane form is undefined (ray in the plane).
+RGL_HD float planeHitT(Vec3 a, Vec3 n, Vec3 o, Vec3 d, float t)
+{
+	Vec3 eh, el;
+	twoSum(a.x, -o.x, eh.x, el.x);
+	twoSum(a.y, -o.y, eh.y, el.y);
+	twoSum(a.z, -o.z, eh.z, el.z);
+	const float num = dotCompensated(n, eh, el);
+	const float den = dotCompensated(n, d, v3(0.0f, 0.0f, 0.0f));
+	const float tp = num / den;
+	return (tp > 0.0f && tp < 3.0e38f) ? tp : t;
+}
+
+// m * v + translation with every product and sum error-free: hi + lo is m * v to about u^2 relative.
+RGL_HD void compensatedPoint(const Mat34& m, Vec3 v, Vec3& hi, Vec3& lo)
+{
+	float r[3], q[3];
+	for (int i = 0; i < 3; ++i) {
+		float p0, e0, p1, e1, p2, e2, s1, f1, s2, f2, s3, f3;
+		twoProd(m.m[i][0], v.x, p0, e0);
+		twoProd(m.m[i][1], v.y, p1, e1);
+		twoProd(m.m[i][2], v.z, p2, e2);
+		twoSum(p0, p1, s1, f1);
+		twoSum(s1, p2, s2, f2);
+		twoSum(s2, m.m[i][3], s3, f3);
+		r[i] = s3;
+		q[i] = fadd(fadd(fadd(e0, e1), fadd(e2, f1)), fadd(f2, f3));
+	}
+	hi = v3(r[0], r[1], r[2]);
+	lo = v3(q[0], q[1], q[2]);
+}
+
+// Sine of the angle between ray and triangle plane below which the closest hit's t is finished from
+// the plane (refineClosest); at or above it the watertight t stands (its error, about 4e-7 / sine of
+// the distance, stays below 4e-6), unless the hit is close on a transformed instance (below).
+constexpr float kRefineSine = 0.1f;
+
+// The closest hit's t finished from the hit triangle's plane when the ray grazes it. On an instance
+// with the identity transform (a scene-sized mesh) the instance frame is the world frame and planeHitT
+// is exact up to the rounding of the normal. A transformed instance rounds the ray into its frame by
+// about u |o - instance origin|, and a grazing angle divides that offset along the ray (0.08 degrees:
+// 4e-5 of the distance; a sensor inside a sphere 0.4 m from its wall at 1.2 degrees: 3e-5); there the
+// plane is evaluated in the world frame: the vertex moved to the world by compensatedPoint, the normal
+// by the transposed inverse, so the only remaining rounding is the normal's, weighted by the hit's
+// offset from the vertex.
+template<class NodeLoader>
+RGL_HD HitRec refineClosest(const SceneView& sc, Vec3 oW, Vec3 dW, HitRec best, const NodeLoader& load)
+{
+	if (best.inst < 0) {
+		return best;
+	}
+	const InstanceRec& ir = load.instance(sc.instances, best.inst);
+	const bool identity = (ir.flags & kInstanceIdentity) != 0;
+	const TriRecord tr = load.tri(ir.tris, best.tri);
+	const Vec3 a = v3(tr.v0x, tr.v0y, tr.v0z);
+	const Vec3 n = cross(v3(tr.v1x, tr.v1y, tr.v1z) - a, v3(tr.v2x, tr.v2y, tr.v2z) - a);
+	const Vec3 d = identity ? dW : ir.worldToObject.vector(dW);
+	const float nd = dot(n, d), nn = dot(n, n), dd = dot(d, d);
+	const float s2 = fmul(nd, nd), q = fmul(nn, dd); // sin^2 = s2 / q
+	const bool grazing = s2 < kRefineSine * kRefineSine * q;
+	// On a transformed instance the ray's rounding into the instance frame, about u |o - instance
+	// origin|, also weighs against a hit closer than half that offset (a sensor inside a large instance).
+	const Vec3 off = oW - ir.objectToWorld.translation();
+	const bool close = !identity && fmul(fmul(best.t, best.t), dot(dW, dW)) < 0.25f * dot(off, off);
+	if (!grazing && !close) {
+		return best;
+	}
+	if (identity) {
+		best.t = planeHitT(a, n, oW, dW, best.t);
+		return best;
+	}
+	Vec3 ah, al;
+	compensatedPoint(ir.objectToWorld, a, ah, al);
+	const Mat34& w = ir.worldToObject;
+	const Vec3 nW = v3(fadd(fadd(fmul(w.m[0][0], n.x), fmul(w.m[1][0], n.y)), fmul(w.m[2][0], n.z)),
+	                   fadd(fadd(fmul(w.m[0][1], n.x), fmul(w.m[1][1], n.y)), fmul(w.m[2][1], n.z)),
+	                   fadd(fadd(fmul(w.m[0][2], n.x), fmul(w.m[1][2], n.y)), fmul(w.m[2][2], n.z)));
+	Vec3 eh, el;
+	twoSum(ah.x, -oW.x, eh.x, el.x);
+	twoSum(ah.y, -oW.y, eh.y, el.y);
+	twoSum(ah.z, -oW.z, eh.z, el.z);
+	el = v3(fadd(el.x, al.x), fadd(el.y, al.y), fadd(el.z, al.z));
+	const float num = dotCompensated(nW, eh, el);
+	const float den = dotCompensated(nW, dW, v3(0.0f, 0.0f, 0.0f));
+	const float tp = num / den;
+	if (tp > 0.0f && tp < 3.0e38f) {
+		best.t = tp;
+	}
+	return best;
+}
+
 // Closest hit over all instances for a world-space ray o + t d, t in (0, tmax].
 template<class Stack, class NodeLoader>
 RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, Stack& st, const NodeLoader& load)
@@ -286,6 +413,7 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 	best.t = tmax; // hits with t == tmax are accepted
 	best.inst = -1;
 	best.tri = -1;
+	best.prim = -1;
 	if (sc.nInstances <= 0) {
 		return best;
 	}
@@ -358,10 +486,11 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 					float t;
 					if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), r.o, wt,
 					                      best.t, t) &&
-					    closerHit(t, inst, first + k, best)) {
+					    closerHit(t, inst, tr.primId, best)) {
 						best.t = t;
 						best.inst = inst;
 						best.tri = first + k;
+						best.prim = tr.primId;
 					}
 				}
 			}
@@ -370,7 +499,7 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 		bool enterRoot = false;
 		while (hits == 0) {
 			if (st.size() == base) {
-				return best;
+				return refineClosest(sc, oW, dW, best, load);
 			}
 			uint32_t a, b;
 			st.pop(a, b);
@@ -383,7 +512,7 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 				const InstanceRec& ir = load.instance(sc.instances, (int32_t) a);
 				st.push(0u, kLeaveInstance);
 				const Vec3 od = ir.worldToObject.vector(dW);
-				r = frameRay(ir.worldToObject.point(oW), od);
+				r = frameRay(worldToInstance(ir, oW), od);
 				wt = setupWatertight(od);
 				nodes = ir.nodes;
 				leaves = ir.tris;

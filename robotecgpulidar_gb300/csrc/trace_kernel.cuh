@@ -182,7 +182,7 @@ __device__ __forceinline__ SampleVal sampleFromHit(float nearNonHit, float farNo
 				v.cosInc = c;
 				float base = defaultIntensity;
 				if (inst.intensityTexture != 0) {
-					base = texturedIntensity(inst, tr, inst.worldToObject.point(o + d * h.t));
+					base = texturedIntensity(inst, tr, worldToInstance(inst, o + d * h.t));
 				}
 				v.intensity = fmul(base, c);
 				v.tri = h.tri;
@@ -302,7 +302,7 @@ __device__ __noinline__ void hitVelocities(const TraceParams& p, const InstanceR
 	// The hit point in the instance's frame, and back in the world with the current pose, so an instance
 	// whose previous pose equals the current one moves by exactly zero.
 	const Vec3 d = sr.rayDir();
-	const Vec3 hitObject = inst.worldToObject.point(sr.rayOrigin() + d * (dist / length(d)));
+	const Vec3 hitObject = worldToInstance(inst, sr.rayOrigin() + d * (dist / length(d)));
 	const Vec3 hitWorld = inst.objectToWorld.point(hitObject);
 	Vec3 disp = v3(0.0f, 0.0f, 0.0f);
 	if (inst.hasPrev) {

@@ -325,6 +325,7 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 		best[r].t = r < n ? tmax : -1.0f; // an inactive ray culls every box and triangle
 		best[r].inst = -1;
 		best[r].tri = -1;
+		best[r].prim = -1;
 	}
 	if (sc.nInstances <= 0) {
 		return;
@@ -422,10 +423,11 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 					const Vec3 a = v3(tr.v0x, tr.v0y, tr.v0z), b = v3(tr.v1x, tr.v1y, tr.v1z), c = v3(tr.v2x, tr.v2y, tr.v2z);
 					for (int r = 0; r < P; ++r) {
 						float t;
-						if (r < n && intersectTriangle(a, b, c, f.o, sp.wt(r), best[r].t, t) && closerHit(t, inst, first + k, best[r])) {
+						if (r < n && intersectTriangle(a, b, c, f.o, sp.wt(r), best[r].t, t) && closerHit(t, inst, tr.primId, best[r])) {
 							best[r].t = t;
 							best[r].inst = inst;
 							best[r].tri = first + k;
+							best[r].prim = tr.primId;
 						}
 					}
 				}
@@ -447,7 +449,7 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 			} else if (b == kEnterInstance) {
 				const InstanceRec& ir = load.instance(sc.instances, (int32_t) a);
 				st.push(0u, kLeaveInstance);
-				setPacketFrame<P>(f, ir.worldToObject.point(oW), &ir.worldToObject, sp, grp);
+				setPacketFrame<P>(f, worldToInstance(ir, oW), &ir.worldToObject, sp, grp);
 				nodes = ir.nodes;
 				leaves = ir.tris;
 				inst = (int32_t) a;
@@ -503,7 +505,8 @@ bool castPackets(const SceneView& sv, int nRays, int group, const float* rays, H
 			return false;
 		}
 		for (int r = 0; r < n; ++r) {
-			out[g0 + r] = h[r];
+			// the closest hit's distance from its plane, as the single-ray traversal finishes
+			out[g0 + r] = refineClosest(sv, v3(p0[0], p0[1], p0[2]), sp.dir(r), h[r], ld);
 		}
 	}
 	return true;
@@ -561,13 +564,17 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 		inst[i].nodes = blas[instMesh[i]].wide.data();
 		inst[i].tris = blas[instMesh[i]].tris.data();
 		inst[i].entityId = instId[i];
+		{
+			const Mat34 id = Mat34::identity();
+			inst[i].flags = std::memcmp(&tf, &id, sizeof(Mat34)) == 0 ? kInstanceIdentity : 0;
+		}
 		Box b = blas[instMesh[i]].bounds;
 		Box w = emptyBox();
 		for (int c = 0; c < 8; ++c) {
 			Vec3 p = tf.point(v3((c & 1) ? b.hix : b.lox, (c & 2) ? b.hiy : b.loy, (c & 4) ? b.hiz : b.loz));
 			w = unite(w, Box{p.x, p.y, p.z, p.x, p.y, p.z});
 		}
-		float pad = 1e-6f * (std::max({std::fabs(w.lox), std::fabs(w.hix), std::fabs(w.loy), std::fabs(w.hiy),
+		float pad = 4e-6f * (std::max({std::fabs(w.lox), std::fabs(w.hix), std::fabs(w.loy), std::fabs(w.hiy),
 		                               std::fabs(w.loz), std::fabs(w.hiz)}) + 1.0f);
 		w = Box{w.lox - pad, w.loy - pad, w.loz - pad, w.hix + pad, w.hiy + pad, w.hiz + pad};
 		inst[i].lox = w.lox;

@@ -217,3 +217,104 @@ def test_distance_noise_statistics_match_reference_test(rgl):
 
     z = (d - (3.0 + g["mean"])) / (3.0 * g["st_dev_per_meter"] + g["st_dev"])
     assert stats.kstest(z, "norm").pvalue > 1e-4
+
+
+def test_angular_ray_noise_matches_oracle_and_is_reproducible(rgl, oracle):
+    """rgl_node_gaussian_noise_angular_ray (reference gaussianNoiseKernels.cu:20-29): every ray is
+    rotated about the axis of the sensor frame L = (cumulative ray transform)^-1 by mean + sigma * n,
+    out = L^-1 R L ray. The oracle applies its FP64 Philox restatement to the same rays and casts
+    them; the GPU result must agree within the parity bounds (a wrong draw moves a hit by metres, far
+    beyond them) and reproduce bit for bit for the same seed and frame."""
+    import accuracy
+
+    scene = scenes.plain_scene()
+    rgl.spawn_scene(scene)
+    rays = scenes.lidar_rays(32, 512)
+    pose = scenes.trs((3.0, -4.0, 1.8), (0.0, 0.0, 0.6))
+    mean, sigma = 0.01, math.radians(2.0)
+    n = {k: rgl.node() for k in ("rays", "pose", "noise", "range", "trace", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], rays)
+    rgl.rays_transform(n["pose"], pose)
+    rgl.check(rgl.lib().rgl_node_gaussian_noise_angular_ray(C.byref(n["noise"]), mean, sigma, rgl.RGL_AXIS_Z))
+    rgl.set_noise_seed(n["noise"], 1234)
+    rgl.rays_set_range(n["range"], [[0.1, 100.0]])
+    rgl.raytrace(n["trace"])
+    fields = [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32,
+              rgl.RGL_FIELD_RETURN_TYPE_U8]
+    rgl.points_yield(n["out"], fields)
+    rgl.chain(n["rays"], n["pose"], n["noise"], n["range"], n["trace"], n["out"])
+    rgl.graph_run(n["rays"])
+    got = {f: rgl.result(n["out"], f) for f in fields}
+    world = oracle.transform_rays(pose, rays)
+    noisy = oracle.noise_angular_ray(oracle.inv34(pose), mean, sigma, rgl.RGL_AXIS_Z, 1234, 0, world)
+    exp = oracle.OracleScene(scene).raytrace(noisy, ranges=[[0.1, 100.0]])
+    stats, _ = accuracy.evaluate(rgl, got, exp)
+    assert stats["mismatches_outside_ambiguity_band"] == 0, stats.get("mismatch_examples")
+    assert stats["nonhit_distances_exact"]
+    # The draw is computed in FP32 here and in FP64 by the oracle, so each cast ray differs from the
+    # oracle's by about 1e-7 rad; a hit at grazing angle g moves along the ray by that times 1/sin(g).
+    # Distances must agree within 1e-5 plus 1e-6 / sin(g), sin(g) = cos(incident angle).
+    both = (got[rgl.RGL_FIELD_IS_HIT_I32] == 1) & (exp["is_hit"] == 1) & (exp["ambiguous"] == 0)
+    de = exp["distance"][both].astype(np.float64)
+    rel = np.abs(got[rgl.RGL_FIELD_DISTANCE_F32][both] - de) / de
+    graze = np.maximum(np.cos(exp["incident_angle"][both].astype(np.float64)), 1e-3)
+    assert (rel <= 1e-5 + 1e-6 / graze).all(), f"max rel {rel.max()}"
+    assert np.median(rel) < 1e-6
+    assert got[rgl.RGL_FIELD_IS_HIT_I32].sum() > 5000
+    # The draw differs from the noiseless scan, advances with the frame and repeats for the same seed.
+    clean = oracle.OracleScene(scene).raytrace(world, ranges=[[0.1, 100.0]])
+    assert np.abs(got[rgl.RGL_FIELD_DISTANCE_F32] - clean["distance"])[(clean["is_hit"] == 1) & (exp["is_hit"] == 1)].max() > 0.1
+    rgl.graph_run(n["rays"])
+    second = rgl.result(n["out"], rgl.RGL_FIELD_XYZ_VEC3_F32)
+    assert not np.array_equal(second, got[rgl.RGL_FIELD_XYZ_VEC3_F32])
+    rgl.set_noise_seed(n["noise"], 1234, 0)
+    rgl.graph_run(n["rays"])
+    assert np.array_equal(rgl.result(n["out"], rgl.RGL_FIELD_XYZ_VEC3_F32), got[rgl.RGL_FIELD_XYZ_VEC3_F32])
+
+
+@pytest.mark.parametrize("kind", ["angular_ray", "angular_hitpoint"])
+def test_angular_noise_statistics_match_reference_stress_test(rgl, kind):
+    """Restates reference test/src/graph/gaussianStressTest.cpp:97-148: 100,000 identical rays from
+    (0, 0, 1) along +Z at a cube whose face is 3 m ahead, angular noise (mean 0.1 rad, sigma 0.01 rad
+    about Y) on the rays before the raytrace or on the hit points after it, points taken back into the
+    lidar frame. The angle atan2(z, x) of each point is pi/2 - (rotation), so its mean and sigma must
+    match within 0.002 (the reference's epsilon), the distance field must equal |xyz| within 2e-6
+    relative per metre, and a KS test must accept the normal shape. Four runs (frames) instead of
+    256."""
+    from scipy import stats
+
+    cube = scenes.cube_mesh(1.0)
+    e = rgl.entity_create(rgl.mesh_create(cube.vertices, cube.indices))
+    rgl.entity_set_transform(e, scenes.translation(0, 0, 5))
+    lidar = scenes.translation(0, 0, 1)
+    mean, sigma = 0.1, 0.01
+    lib = rgl.lib()
+    n = {k: rgl.node() for k in ("rays", "pose", "noise", "trace", "back", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], np.tile(scenes.translation(0, 0, 0), (100000, 1, 1)))
+    rgl.rays_transform(n["pose"], lidar)
+    rgl.raytrace(n["trace"])
+    rgl.points_transform(n["back"], oracle_free_inverse(lidar))
+    rgl.points_yield(n["out"], [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32])
+    if kind == "angular_ray":
+        rgl.check(lib.rgl_node_gaussian_noise_angular_ray(C.byref(n["noise"]), mean, sigma, rgl.RGL_AXIS_Y))
+        rgl.chain(n["rays"], n["pose"], n["noise"], n["trace"], n["back"], n["out"])
+    else:
+        rgl.check(lib.rgl_node_gaussian_noise_angular_hitpoint(C.byref(n["noise"]), mean, sigma, rgl.RGL_AXIS_Y))
+        rgl.chain(n["rays"], n["pose"], n["trace"], n["noise"], n["back"], n["out"])
+    rgl.set_noise_seed(n["noise"], 2024)
+    expected_mean = math.atan2(3.0 * math.cos(mean), 3.0 * math.sin(mean))
+    for _ in range(4):
+        rgl.graph_run(n["rays"])
+        xyz = rgl.result(n["out"], rgl.RGL_FIELD_XYZ_VEC3_F32).astype(np.float64)
+        d = rgl.result(n["out"], rgl.RGL_FIELD_DISTANCE_F32).astype(np.float64)
+        assert np.all(np.abs(np.linalg.norm(xyz, axis=1) - d) <= 2e-6 * np.maximum(d, 1.0))
+        ang = np.arctan2(xyz[:, 2], xyz[:, 0])
+        assert abs(ang.mean() - expected_mean) < 0.002
+        assert abs(ang.std() - sigma) < 0.002
+        assert stats.kstest((ang - expected_mean) / sigma, "norm").pvalue > 1e-4
+
+
+def oracle_free_inverse(m34):
+    """Inverse of a rigid 3x4 pose, in float64 then float32 (test helper, no oracle involved)."""
+    m = np.vstack([np.asarray(m34, np.float64), [0, 0, 0, 1]])
+    return np.ascontiguousarray(np.linalg.inv(m)[:3].astype(np.float32))

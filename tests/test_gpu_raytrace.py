@@ -376,6 +376,52 @@ def test_laser_retro_of_hit_entity(rgl, oracle):
     assert np.array_equal(got2[hit & ~sel], got[hit & ~sel])
 
 
+def test_normal_and_incident_angle_match_oracle(rgl, oracle):
+    """Hit normal and incident angle of the selected sample (reference optixPrograms.cu:138-150: the
+    normalised cross product of the world-space edges AB and AC, acos(|normal . ray direction|); NaN for
+    non-hits, nodeKernels.cu:196-201) against the oracle's FP64 values, on rotated, scaled and one
+    mirrored instance with FIRST_LAST over 5 sub-rays. The GPU forms the world vertices and the cross
+    product in FP32 as the reference does; with vertex coordinates up to 60 m and edges down to 3 cm
+    that is about 4e-6 m of rounding per coordinate, 1.3e-4 relative to an edge, so components and
+    cosines are held to 1e-3."""
+    scene = scenes.million_scene(seed=4, instances=10, spheres=2, cells=32, extent=60.0)
+    scene.entities.append(scenes.Entity(1, scenes.trs((10.0, 5.0, 5.0), (0.3, -0.2, 0.5), (-2.0, 2.0, 2.0)), 99))
+    rgl.spawn_scene(scene)
+    rays = scenes.lidar_rays(32, 256)
+    pose = scenes.translation(20.0, 0.0, 7.0)
+    fields = [rgl.RGL_FIELD_NORMAL_VEC3_F32, rgl.RGL_FIELD_INCIDENT_ANGLE_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32,
+              rgl.RGL_FIELD_DISTANCE_F32]
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], rays)
+    rgl.rays_transform(n["pose"], pose)
+    rgl.raytrace(n["trace"])
+    lib = rgl.lib()
+    rgl.check(lib.rgl_node_raytrace_configure_return_mode(n["trace"], rgl.RGL_RETURN_FIRST_LAST))
+    rgl.check(lib.rgl_node_raytrace_configure_beam_divergence(n["trace"], math.radians(0.3), math.radians(0.3)))
+    rgl.configure_beam_samples(n["trace"], 1, 4)
+    rgl.points_yield(n["out"], fields)
+    rgl.chain(n["rays"], n["pose"], n["trace"], n["out"])
+    rgl.graph_run(n["rays"])
+    got = {f: rgl.result(n["out"], f) for f in fields}
+    exp = oracle.OracleScene(scene).raytrace(rays, ray_transform=pose, return_mode=rgl.RGL_RETURN_FIRST_LAST,
+                                             h_div=math.radians(0.3), v_div=math.radians(0.3), layers=1, vertices=4)
+    hit = got[rgl.RGL_FIELD_IS_HIT_I32] == 1
+    # Beams whose hit samples on different triangles tie in distance within the unresolved band may
+    # select another triangle of the same entity (same distance and entity, another normal).
+    ok = hit & (exp["is_hit"] == 1) & (exp["ambiguous"] == 0) & (exp["triangle_tie"] == 0)
+    ok &= got[rgl.RGL_FIELD_ENTITY_ID_I32] == exp["entity_id"]
+    assert ok.sum() > 3000 and (got[rgl.RGL_FIELD_ENTITY_ID_I32][ok] == 99).sum() > 100
+    gn, en = got[rgl.RGL_FIELD_NORMAL_VEC3_F32][ok], exp["normal"][ok]
+    assert np.abs(np.linalg.norm(gn, axis=1) - 1.0).max() <= 1e-5
+    assert np.abs(gn - en).max() <= 1e-3
+    ga, ea = got[rgl.RGL_FIELD_INCIDENT_ANGLE_F32][ok], exp["incident_angle"][ok]
+    assert np.abs(np.cos(ga.astype(np.float64)) - np.cos(ea.astype(np.float64))).max() <= 1e-3
+    assert np.all((ga >= 0.0) & (ga <= np.float32(math.pi / 2) + 1e-6))
+    # Non-hits carry NaN normals and angles, as the reference writes them.
+    assert np.isnan(got[rgl.RGL_FIELD_NORMAL_VEC3_F32][~hit]).all()
+    assert np.isnan(got[rgl.RGL_FIELD_INCIDENT_ANGLE_F32][~hit]).all()
+
+
 def test_ray_mask_skips_masked_rays(rgl):
     """Masked rays are not cast: their beams return the far non-hit (reference optixPrograms.cu:55-58);
     the other beams are unchanged."""
