@@ -15,9 +15,11 @@
  *    a node, otherwise the existing node is re-parameterised;
  *  - results are read into caller buffers sized with rgl_graph_get_result_size.
  *
- * Calls outside the lidar ray-casting path (radar, textures, skeletal
- * animation, velocity/distortion, ring ids, time offsets, ray masks, merges,
- * ground filter, tape) are exported with these signatures and return
+ * Beside the ray-casting path this library implements ring ids, time offsets,
+ * ray masks, velocities and velocity distortion, external and skeleton mesh
+ * animation, intensity textures, laser retro, spatial and temporal merges,
+ * points from arrays, the ground filter and tape record/playback. The radar
+ * nodes are exported with the reference's signatures and return
  * RGL_NOT_IMPLEMENTED.
  */
 #pragma once

@@ -26,7 +26,8 @@ uint64_t Node::nextParamVersion() { return gParamVersion.fetch_add(1, std::memor
 
 namespace {
 // Schedule of single-graph traversals (a batch of one job). The default is the fastest measured on
-// the 1M-triangle single-sensor scan: lane-group packing, one task per fetch, 80 registers.
+// the 1M-triangle single-sensor scan: lane-group packing, 128-thread blocks, one task per fetch, 128
+// registers per thread (0.287 ms against 0.294 ms at 96 registers for the traversal of that scan).
 rgl::BatchSchedule gTraceSchedule{128, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 128};
 } // namespace
 rgl::BatchSchedule traceSchedule() { return gTraceSchedule; }

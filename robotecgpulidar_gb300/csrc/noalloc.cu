@@ -15,6 +15,9 @@
 //    until the process exits;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress, with that
 //    device current); make that first call before starting any stream capture on that device;
+//  * under CUDA's lazy module loading (the default) the first call on a device also makes the driver
+//    load this module, allocating device memory for its code and the array; callers that must not
+//    allocate at run time make one warm-up call at initialisation, after which calls allocate nothing;
 //  * all calls share the array and clear the words they use at the start of each call; calls whose
 //    work overlaps on the GPU (other streams, other host threads) race on it, so serialise them;
 //  * the call waits for its own work on the given stream before it returns.

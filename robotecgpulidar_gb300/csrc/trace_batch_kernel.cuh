@@ -1,6 +1,6 @@
-// Device side of the persistent batch traversal: task functions and the kernel template shared by
-// trace_batch.cu (lane-group and serial packings) and trace_packet.cu (packet packing). Included
-// by those two files only; each instantiates its own kernels.
+// Device side of the persistent batch traversal: the task functions of the two packings (a beam's
+// sub-rays on adjacent lanes, or one lane per beam) and the kernel template. Included by
+// trace_batch.cu, which instantiates the kernels.
 #pragma once
 
 #include "trace_kernel.cuh"
