@@ -195,8 +195,11 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 	__shared__ uint16_t keptLocal[kCompactTile]; // tile-local indices of the kept points, in order
 	__shared__ __align__(16) uint32_t opParams[kMaxPointOps][kOpParamWords];
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	__shared__ uint32_t lbBallot[kBlock / 32], lbSum[kBlock / 32];
+	__shared__ int lbFail;
 	if (tid == 0) {
 		tileShared = (int) atomicAdd(scratch, 1u);
+		lbFail = 0;
 	}
 	for (int k = 0; k < ops.count; ++k) {
 		const int words = ops.op[k].kind == kOpTransform ? (int) (sizeof(Mat34) / 4) : kOpParamWords;
@@ -210,11 +213,21 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 	const int first = tile * kCompactTile + tid * kCompactItems;
 	int keep[kCompactItems];
 	int cnt = 0;
+	if (first + kCompactItems <= n && (reinterpret_cast<uintptr_t>(flags + first) & 15u) == 0) {
+		// one 16-byte load of the thread's four flags
+		const int4 f4 = __ldg(reinterpret_cast<const int4*>(flags + first));
+		keep[0] = f4.x != 0;
+		keep[1] = f4.y != 0;
+		keep[2] = f4.z != 0;
+		keep[3] = f4.w != 0;
+		cnt = keep[0] + keep[1] + keep[2] + keep[3];
+	} else {
 #pragma unroll
-	for (int k = 0; k < kCompactItems; ++k) {
-		int i = first + k;
-		keep[k] = (i < n) && flags[i] != 0;
-		cnt += keep[k];
+		for (int k = 0; k < kCompactItems; ++k) {
+			int i = first + k;
+			keep[k] = (i < n) && flags[i] != 0;
+			cnt += keep[k];
+		}
 	}
 	// block exclusive scan of cnt
 	int incl = cnt;
@@ -229,69 +242,79 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 		warpSums[warp] = (uint32_t) incl;
 	}
 	__syncthreads();
-	if (warp == 0) {
-		// Tile total and per-warp offsets (lane 0), the tile's status word, then a look-back by the
-		// whole warp: 32 predecessors' status words per step, summed up to the nearest inclusive prefix.
+	if (tid == 0) {
+		// Per-warp offsets and the tile total, then the tile's status word: its aggregate (tile 0: its
+		// inclusive prefix), published before the look-back so successors never wait on a look-back.
 		uint32_t run = 0;
-		if (lane == 0) {
-			for (int w = 0; w < kBlock / 32; ++w) {
-				uint32_t v = warpSums[w];
-				warpSums[w] = run;
-				run += v;
+		for (int w = 0; w < kBlock / 32; ++w) {
+			const uint32_t v = warpSums[w];
+			warpSums[w] = run;
+			run += v;
+		}
+		atomicExch(&scratch[1 + tile], (tile == 0 ? kFlagInc : kFlagAgg) | run);
+		tileKept = run;
+	}
+	// Decoupled look-back by the whole block: each step reads the status words of the kBlock
+	// predecessors before the window's end (one per thread, spinning until it is published) and sums
+	// them up to the nearest inclusive prefix. With every tile of a one-wave grid resident at once,
+	// a window reaches back kBlock tiles per L2 round trip instead of 32.
+	uint32_t prefix = 0;
+	for (int k = tile - 1; tile > 0; k -= kBlock) {
+		const int idx = k - tid;
+		uint32_t st = kFlagInc; // before tile 0: an inclusive prefix of 0
+		if (idx >= 0) {
+			const volatile uint32_t* p = scratch + 1 + idx;
+			int spins = 0;
+			st = *p;
+			while ((st & ~kValueMask) == 0u && ++spins < kSpinLimit) {
+				st = *p;
+			}
+			if ((st & ~kValueMask) == 0u) {
+				lbFail = 1; // never expected: the predecessor holds an earlier ticket and is running
+				st = kFlagInc;
 			}
 		}
-		run = __shfl_sync(0xffffffffu, run, 0);
-		uint32_t* status = scratch + 1;
+		const unsigned inc = __ballot_sync(0xffffffffu, (st & ~kValueMask) == kFlagInc);
 		if (lane == 0) {
-			atomicExch(&status[tile], (tile == 0 ? kFlagInc : kFlagAgg) | run);
+			lbBallot[warp] = inc;
 		}
-		uint32_t prefix = 0;
-		int spins = 0;
-		for (int k = tile - 1; tile > 0;) {
-			const int idx = k - lane;
-			// Before tile 0 counts as an inclusive prefix of 0, so every window ends there.
-			uint32_t st = kFlagInc | 0u;
-			if (idx >= 0) {
-				st = *((volatile uint32_t*) &status[idx]);
-			}
-			while (__any_sync(0xffffffffu, (st & ~kValueMask) == 0u)) {
-				if (++spins > kSpinLimit) {
-					break;
-				}
-				if ((st & ~kValueMask) == 0u) {
-					st = *((volatile uint32_t*) &status[idx]);
-				}
-			}
-			if (spins > kSpinLimit) {
-				if (lane == 0) {
-					atomicExch(errorFlag, 1);
-				}
-				break;
-			}
-			const unsigned inc = __ballot_sync(0xffffffffu, (st & ~kValueMask) == kFlagInc);
-			// Lanes up to the nearest inclusive prefix (lowest such lane) contribute.
-			const int stop = inc ? __ffs((int) inc) - 1 : 31;
-			uint32_t v = lane <= stop ? (st & kValueMask) : 0u;
+		__syncthreads();
+		int stop = kBlock - 1; // lowest thread holding an inclusive prefix, if any
+		bool found = false;
+		for (int w = kBlock / 32 - 1; w >= 0; --w) {
+			const unsigned bw = lbBallot[w];
+			stop = bw ? w * 32 + __ffs((int) bw) - 1 : stop;
+			found = found || bw != 0u;
+		}
+		uint32_t v = tid <= stop ? (st & kValueMask) : 0u;
 #pragma unroll
-			for (int off = 16; off > 0; off >>= 1) {
-				v += __shfl_xor_sync(0xffffffffu, v, off);
-			}
-			prefix += v;
-			if (inc) {
-				break;
-			}
-			k -= 32;
+		for (int off = 16; off > 0; off >>= 1) {
+			v += __shfl_xor_sync(0xffffffffu, v, off);
 		}
 		if (lane == 0) {
-			if (tile > 0) {
-				atomicExch(&status[tile], kFlagInc | (prefix + run));
-			}
-			tileBase = prefix;
-			tileKept = run;
-			const int tiles = (cap + kCompactTile - 1) / kCompactTile;
-			if (tile == tiles - 1) {
-				*dOutCount = (int32_t) (prefix + run);
-			}
+			lbSum[warp] = v;
+		}
+		__syncthreads();
+		for (int w = 0; w < kBlock / 32; ++w) {
+			prefix += lbSum[w];
+		}
+		__syncthreads(); // lbBallot and lbSum are rewritten by the next step
+		if (found) {
+			break;
+		}
+	}
+	if (tid == 0) {
+		if (lbFail) {
+			atomicExch(errorFlag, 1);
+		}
+		const uint32_t run = tileKept;
+		if (tile > 0) {
+			atomicExch(&scratch[1 + tile], kFlagInc | (prefix + run));
+		}
+		tileBase = prefix;
+		const int tiles = (cap + kCompactTile - 1) / kCompactTile;
+		if (tile == tiles - 1) {
+			*dOutCount = (int32_t) (prefix + run);
 		}
 	}
 	__syncthreads();

@@ -126,8 +126,10 @@ __global__ void __maxnreg__(REGS) kTraceBatch(const BatchJob* __restrict__ jobs,
 	const int total = sBase[nJobs];
 	const int lane = threadIdx.x & 31;
 
+	uint2 spill[kLocalStack];
 	DevStack st;
 	st.sm = dyn + threadIdx.x;
+	st.spill = spill;
 	st.stride = blockDim.x;
 	st.sp = 0;
 	st.overflow = false;

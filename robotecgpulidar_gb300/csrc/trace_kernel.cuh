@@ -23,14 +23,17 @@ constexpr int kSmemStack = 24;  // entries per thread in shared memory
 constexpr int kLocalStack = 40; // overflow entries per thread in local memory
 
 // Traversal stack: the first kSmemStack entries in this thread's shared-memory column (stride =
-// threads per block), the rest in local memory. Overflow past both is flagged, never written.
+// threads per block), the rest in a local-memory array the kernel declares. Overflow past both is
+// flagged, never written. The struct holds only scalars and pointers, so its fields live in
+// registers; an array member indexed at run time would put the whole struct, the stack pointer
+// included, in local memory.
 struct DevStack
 {
 	uint2* sm;
+	uint2* spill; // kLocalStack entries
 	int stride;
 	int sp;
 	bool overflow;
-	uint2 local[kLocalStack];
 
 	__device__ __forceinline__ void push(uint32_t a, uint32_t b)
 	{
@@ -38,7 +41,7 @@ struct DevStack
 		if (sp < kSmemStack) {
 			sm[sp * stride] = e;
 		} else if (sp < kSmemStack + kLocalStack) {
-			local[sp - kSmemStack] = e;
+			spill[sp - kSmemStack] = e;
 		} else {
 			overflow = true;
 			return;
@@ -48,7 +51,7 @@ struct DevStack
 	__device__ __forceinline__ void pop(uint32_t& a, uint32_t& b)
 	{
 		--sp;
-		const uint2 e = sp < kSmemStack ? sm[sp * stride] : local[sp - kSmemStack];
+		const uint2 e = sp < kSmemStack ? sm[sp * stride] : spill[sp - kSmemStack];
 		a = e.x;
 		b = e.y;
 	}
@@ -79,7 +82,7 @@ struct DevLoader
 		t.v1x = b.x;
 		t.v1y = b.y;
 		t.v1z = b.z;
-		t.pad1 = 0;
+		t.invNormalLen = b.w;
 		t.v2x = c.x;
 		t.v2y = c.y;
 		t.v2z = c.z;

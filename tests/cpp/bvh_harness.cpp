@@ -203,6 +203,10 @@ Blas buildBlas(const float* v, int nv, const int32_t* idx, int nt)
 	return gBlasSah ? buildBlasSah(lo, hi, v, idx) : buildWideHost(lo, hi, v, idx, kLeafMaxTris);
 }
 
+// Stack entries the device keeps on chip (shared memory); pushes and pops past them are counted.
+int gStackOnChip = 24;
+long gDeepPushes = 0, gDeepPops = 0;
+
 struct HostStack
 {
 	uint32_t a[512], b[512];
@@ -215,6 +219,7 @@ struct HostStack
 			overflow = true;
 			return;
 		}
+		gDeepPushes += sp >= gStackOnChip ? 1 : 0;
 		a[sp] = x;
 		b[sp] = y;
 		++sp;
@@ -223,6 +228,7 @@ struct HostStack
 	void pop(uint32_t& x, uint32_t& y)
 	{
 		--sp;
+		gDeepPops += sp >= gStackOnChip ? 1 : 0;
 		x = a[sp];
 		y = b[sp];
 	}
@@ -326,6 +332,7 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 		best[r].inst = -1;
 		best[r].tri = -1;
 		best[r].prim = -1;
+		best[r].refine = 0;
 	}
 	if (sc.nInstances <= 0) {
 		return;
@@ -528,6 +535,14 @@ void harness_set_blas_sah(int on) { gBlasSah = on; }
 // Deepest traversal stack of a single ray in the last harness_cast call.
 int harness_max_stack_depth() { return gMaxStackDepth; }
 long harness_total_node_visits() { return gTotalNodeVisits; }
+// Stack entries held on chip (the rest would live in local memory on the device), and the pushes and
+// pops of the last harness_cast call that went past them.
+void harness_set_stack_on_chip(int entries) { gStackOnChip = entries; }
+void harness_deep_stack_ops(long* out)
+{
+	out[0] = gDeepPushes;
+	out[1] = gDeepPops;
+}
 // Totals of the last harness_cast call: triangle tests, TLAS leaf reads, instance entries, TLAS
 // node visits.
 void harness_work_counters(long* out)
@@ -602,6 +617,7 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	gTotalNodeVisits = 0;
 	gTriTests = gBinLoads = gInstLoads = gTlasVisits = 0;
 	gMaxStackDepth = 0;
+	gDeepPushes = gDeepPops = 0;
 	if (gPacketGroup > 0) {
 		gNodeVisits = 0;
 		std::vector<HitRec> hits(nRays);
