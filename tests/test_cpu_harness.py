@@ -16,8 +16,8 @@ SRC = os.path.join(ROOT, "tests", "cpp", "bvh_harness.cpp")
 OUT = os.path.join(ROOT, "tests", "cpp", "_build", "libbvh_harness.so")
 
 
-@pytest.fixture(scope="module")
-def harness():
+def load_harness():
+    """Builds tests/cpp/bvh_harness.cpp (when older than its sources) and loads it."""
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(
         os.path.getmtime(p) for p in [SRC] + [os.path.join(ROOT, "robotecgpulidar_gb300", "csrc", f)
@@ -28,6 +28,11 @@ def harness():
                         "-I", os.path.join(ROOT, "robotecgpulidar_gb300", "csrc"), "-I", os.path.join(cuda, "include"),
                         "-o", OUT, SRC], check=True)
     return C.CDLL(OUT)
+
+
+@pytest.fixture(scope="module")
+def harness():
+    return load_harness()
 
 
 def cast(h, scene, rays, tmax):
