@@ -194,11 +194,15 @@ struct WideBuildResult
 };
 
 // Wide BVH over n primitive boxes lo/hi (device) whose centroid bounds are in cb (6 ordered uints),
-// all written on stream s: Morton codes, onesweep sort, LBVH, bottom-up bounds, collapse into 8-wide
-// nodes. Leaf records are triangles (dV/dI given) or primitive indices (dV null). Frees lo, hi, cb and
-// its temporaries and synchronises s (a one-off build).
+// all written on stream s: the binary topology (binned SAH when `sah`, else Morton codes, onesweep
+// sort, LBVH and bottom-up bounds), then the collapse into 8-wide nodes, one launch per depth. Leaf
+// records are triangles (dV/dI given) or primitive indices (dV null). With levelStarts, it receives the
+// first node index of every depth and the node count (the collapse allocates the nodes of depth L + 1
+// while it writes depth L, so the counter before each launch starts the next depth). Frees lo, hi, cb
+// and its temporaries and synchronises s (a one-off build).
 WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const float* dV, const int32_t* dI, int leafMax,
-                          WideNode* outNodes, TriRecord* outLeaves, Box* outBoxes, cudaStream_t s, bool sah)
+                          WideNode* outNodes, TriRecord* outLeaves, Box* outBoxes, cudaStream_t s, bool sah,
+                          std::vector<int32_t>* levelStarts = nullptr)
 {
 	uint32_t* codes = mallocAsync<uint32_t>(n, s);
 	uint32_t* ids = mallocAsync<uint32_t>(n, s);
@@ -245,8 +249,16 @@ WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const flo
 	// (empty launches exit immediately).
 	const int grid = 152 * 4;
 	uint32_t pending = 1;
+	uint32_t* snap = levelStarts ? mallocAsync<uint32_t>(16, s) : nullptr; // node counter before each launch of a round
+	uint32_t hostSnap[16];
+	if (levelStarts) {
+		levelStarts->assign(1, 0);
+	}
 	for (int round = 0; pending != 0; ++round) {
 		for (int level = 0; level < 16; ++level) {
+			if (snap) {
+				RGL_CUDA_OK(cudaMemcpyAsync(snap + level, ctr, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+			}
 			RGL_CUDA_OK(cudaMemsetAsync(cbn, 0, sizeof(uint32_t), s));
 			CollapseOutputs co{outNodes, outLeaves, ctr, ctr + 1, qb, cbn, outBoxes};
 			kCollapse<<<grid, 128, 0, s>>>(qa, ca, ci, co);
@@ -259,7 +271,13 @@ WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const flo
 			cbn = tc;
 		}
 		RGL_CUDA_OK(cudaMemcpyAsync(&pending, ca, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+		if (snap) {
+			RGL_CUDA_OK(cudaMemcpyAsync(hostSnap, snap, sizeof(hostSnap), cudaMemcpyDeviceToHost, s));
+		}
 		RGL_CUDA_OK(cudaStreamSynchronize(s));
+		if (levelStarts) {
+			levelStarts->insert(levelStarts->end(), hostSnap, hostSnap + 16);
+		}
 		if (round > (n >> 4) + 4) {
 			throw std::runtime_error("BVH build: wide collapse does not terminate");
 		}
@@ -277,6 +295,9 @@ WideBuildResult buildWide(float4* lo, float4* hi, uint32_t* cb, int n, const flo
 	void* temps[] = {lo, hi, cb, codes, ids, sortScratch, bin, rf, rl, pi, pl, visits, q0, q1, ctr};
 	for (void* p : temps) {
 		RGL_CUDA_OK(cudaFreeAsync(p, s));
+	}
+	if (snap) {
+		RGL_CUDA_OK(cudaFreeAsync(snap, s));
 	}
 	RGL_CUDA_OK(cudaStreamSynchronize(s));
 	if (hostCtr[4] != 0) {
@@ -445,10 +466,10 @@ __global__ void __launch_bounds__(256) kRefitTlas(WideNode* nodes, const TriReco
 
 } // namespace
 
-// The TLAS is a wide BVH over the instances' world boxes, one instance per leaf child. Its topology is
-// built on the host by a full sweep SAH over the (few) instance boxes and collapsed with the BLAS
-// collapse (sah_build.hpp); node depths (contiguous per depth: the collapse allocates nodes level by
-// level) drive the refit kernel, which keeps the topology on pose changes.
+// The TLAS is a wide BVH over the instances' world boxes, one instance per leaf child, built on the
+// device like a mesh BLAS (binned SAH topology, then the wide collapse with one instance per leaf).
+// The node range of every depth (contiguous: the collapse allocates nodes depth by depth) drives the
+// refit kernel, which keeps the topology on pose changes.
 void buildTlas(const InstanceRec* hInst, int n, TlasBuild& t, cudaStream_t s)
 {
 	t.nInstances = n;
@@ -458,81 +479,49 @@ void buildTlas(const InstanceRec* hInst, int n, TlasBuild& t, cudaStream_t s)
 		return;
 	}
 	if (n > t.capacity) {
-		freeTlas(t);
+		cudaFree(t.nodes);
+		cudaFree(t.leaves);
+		cudaFree(t.boxes);
+		t.nodes = nullptr;
+		t.leaves = nullptr;
+		t.boxes = nullptr;
 		t.capacity = n;
 		RGL_CUDA_OK(cudaMalloc(&t.nodes, sizeof(WideNode) * (size_t) n));
 		RGL_CUDA_OK(cudaMalloc(&t.leaves, sizeof(TriRecord) * (size_t) n));
 		RGL_CUDA_OK(cudaMalloc(&t.boxes, sizeof(Box) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.levelStarts, sizeof(int32_t) * 66));
-		t.nInstances = n;
 	}
-	std::vector<Box> boxes(n);
-	std::vector<float4> lo(n), hi(n);
+	std::vector<float4> hLo(n), hHi(n);
 	for (int i = 0; i < n; ++i) {
 		const InstanceRec& r = hInst[i];
-		boxes[i] = Box{r.lox, r.loy, r.loz, r.hix, r.hiy, r.hiz};
-		lo[i] = make_float4(r.lox, r.loy, r.loz, 0.0f);
-		hi[i] = make_float4(r.hix, r.hiy, r.hiz, 0.0f);
+		hLo[i] = make_float4(r.lox, r.loy, r.loz, 0.0f);
+		hHi[i] = make_float4(r.hix, r.hiy, r.hiz, 0.0f);
 	}
-	SahTree tree = buildSahTree(boxes);
-	std::vector<WideNode> wide(n);
-	std::vector<TriRecord> leaves(n);
-	std::vector<Box> wideBoxes(n);
-	uint32_t wideCounter = 1, leafCounter = 0;
-	std::vector<int2> qa(n), qb(n);
-	uint32_t qaCount = 1, qbCount = 0;
-	qa[0] = make_int2(n == 1 ? ~0 : 0, 0);
-	CollapseInputs in{tree.bin.data(), tree.rangeFirst.data(), tree.rangeLast.data(), tree.sortedIds.data(), lo.data(), hi.data(),
-	                  nullptr, nullptr, 1};
-	while (qaCount > 0) {
-		qbCount = 0;
-		CollapseOutputs o{wide.data(), leaves.data(), &wideCounter, &leafCounter, qb.data(), &qbCount, wideBoxes.data()};
-		for (uint32_t i = 0; i < qaCount; ++i) {
-			collapseItem(qa[i].x, (uint32_t) qa[i].y, in, o);
-		}
-		std::swap(qa, qb);
-		qaCount = qbCount;
-	}
-	if (leafCounter != (uint32_t) n || wideCounter > (uint32_t) n) {
-		throw std::runtime_error("TLAS build: collapse produced an inconsistent tree");
-	}
-	t.nodeCount = wideCounter;
-	// Depth of every node, then the first index per depth.
-	std::vector<int> depth(wideCounter, 0);
-	int maxDepth = 0;
-	for (uint32_t i = 0; i < wideCounter; ++i) {
-		uint32_t rank = 0;
-		for (int k = 0; k < kWideArity; ++k) {
-			if ((wide[i].imask >> k) & 1u) {
-				depth[wide[i].childBase + rank] = depth[i] + 1;
-				maxDepth = std::max(maxDepth, depth[i] + 1);
-				++rank;
-			}
-		}
-	}
-	for (uint32_t i = 1; i < wideCounter; ++i) {
-		if (depth[i] < depth[i - 1]) {
-			throw std::runtime_error("TLAS build: node depths are not contiguous");
-		}
-	}
-	if (maxDepth + 2 > 66) {
-		throw std::runtime_error("TLAS build: tree deeper than 64 levels");
-	}
-	std::vector<int32_t> starts(maxDepth + 2, (int32_t) wideCounter);
-	for (int L = maxDepth; L >= 0; --L) {
-		for (uint32_t i = 0; i < wideCounter; ++i) {
-			if (depth[i] == L) {
-				starts[L] = (int32_t) i;
-				break;
-			}
-		}
-	}
-	t.nLevels = maxDepth + 1;
+	float4* lo = mallocAsync<float4>(n, s);
+	float4* hi = mallocAsync<float4>(n, s);
+	uint32_t* cb = mallocAsync<uint32_t>(8, s); // centroid bounds: read by the Morton path only
 	// Pageable sources: each copy is staged before the call returns.
-	RGL_CUDA_OK(cudaMemcpyAsync(t.nodes, wide.data(), sizeof(WideNode) * wideCounter, cudaMemcpyHostToDevice, s));
-	RGL_CUDA_OK(cudaMemcpyAsync(t.leaves, leaves.data(), sizeof(TriRecord) * (size_t) n, cudaMemcpyHostToDevice, s));
-	RGL_CUDA_OK(cudaMemcpyAsync(t.boxes, wideBoxes.data(), sizeof(Box) * wideCounter, cudaMemcpyHostToDevice, s));
-	RGL_CUDA_OK(cudaMemcpyAsync(t.levelStarts, starts.data(), sizeof(int32_t) * starts.size(), cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(lo, hLo.data(), sizeof(float4) * (size_t) n, cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(hi, hHi.data(), sizeof(float4) * (size_t) n, cudaMemcpyHostToDevice, s));
+	std::vector<int32_t> starts;
+	const WideBuildResult r = buildWide(lo, hi, cb, n, nullptr, nullptr, 1, t.nodes, t.leaves, reinterpret_cast<Box*>(t.boxes), s,
+	                                    true, &starts);
+	t.nodeCount = r.nodeCount;
+	// Depths past the deepest node hold no nodes (their starts equal the node count): dropped.
+	int levels = (int) starts.size() - 1;
+	while (levels > 1 && starts[(size_t) levels - 1] == (int32_t) r.nodeCount) {
+		--levels;
+	}
+	if (starts.back() != (int32_t) r.nodeCount || starts[(size_t) levels] != (int32_t) r.nodeCount) {
+		throw std::runtime_error("TLAS build: depth ranges do not cover the nodes");
+	}
+	if (levels + 1 > t.levelCapacity) {
+		cudaFree(t.levelStarts);
+		t.levelStarts = nullptr;
+		t.levelCapacity = levels + 1;
+		RGL_CUDA_OK(cudaMalloc(&t.levelStarts, sizeof(int32_t) * (size_t) t.levelCapacity));
+	}
+	t.nLevels = levels;
+	RGL_CUDA_OK(cudaMemcpyAsync(t.levelStarts, starts.data(), sizeof(int32_t) * (size_t) (levels + 1), cudaMemcpyHostToDevice, s));
 }
 
 void refitTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)

@@ -203,17 +203,6 @@ RGL_HD void clearChild(WideNode& w, int k)
 	w.qhix[k] = w.qhiy[k] = w.qhiz[k] = 0;
 }
 
-// 1 / |(b - a) x (c - a)| without contraction (the same on host and device), 0 when degenerate.
-RGL_HD float inverseNormalLength(const float* a, const float* b, const float* c)
-{
-	const float e1x = fsub(b[0], a[0]), e1y = fsub(b[1], a[1]), e1z = fsub(b[2], a[2]);
-	const float e2x = fsub(c[0], a[0]), e2y = fsub(c[1], a[1]), e2z = fsub(c[2], a[2]);
-	const float nx = fsub(fmul(e1y, e2z), fmul(e1z, e2y)), ny = fsub(fmul(e1z, e2x), fmul(e1x, e2z)),
-	            nz = fsub(fmul(e1x, e2y), fmul(e1y, e2x));
-	const float nn = fadd(fadd(fmul(nx, nx), fmul(ny, ny)), fmul(nz, nz));
-	return nn > 0.0f ? 1.0f / sqrtf(nn) : 0.0f;
-}
-
 // Conservative 8-bit box of child slot k in the node's frame (rounded outward and verified, quantizeAxis).
 RGL_HD void quantizeChild(WideNode& w, int k, const Box& b)
 {
@@ -396,7 +385,7 @@ RGL_HD void collapseItem(int32_t binRoot, uint32_t wideIdx, const CollapseInputs
 				tr.v1x = b[0];
 				tr.v1y = b[1];
 				tr.v1z = b[2];
-				tr.invNormalLen = inverseNormalLength(a, b, cc);
+				tr.pad1 = 0;
 				tr.v2x = cc[0];
 				tr.v2y = cc[1];
 				tr.v2z = cc[2];

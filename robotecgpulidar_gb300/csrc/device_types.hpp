@@ -44,15 +44,13 @@ struct alignas(16) WideNode
 };
 static_assert(sizeof(WideNode) == 80, "wide node is 80 bytes");
 
-// Triangle in leaf order: three 16-byte words (v0.xyz, original triangle index), (v1.xyz, 1 / |normal|),
-// (v2.xyz, -). invNormalLen is 1 / |(v1 - v0) x (v2 - v0)| (0 for a degenerate triangle); with the
-// watertight test's determinant it gives the sine of a hit's grazing angle for free.
+// Triangle in leaf order: three 16-byte words (v0.xyz, original triangle index), (v1.xyz, -), (v2.xyz, -).
 struct alignas(16) TriRecord
 {
 	float v0x, v0y, v0z;
 	int32_t primId;
 	float v1x, v1y, v1z;
-	float invNormalLen;
+	int32_t pad1;
 	float v2x, v2y, v2z;
 	int32_t pad2;
 };

@@ -51,12 +51,14 @@ struct TlasBuild
 	float* boxes = nullptr;          // float box (6 floats) of every wide node, kept for the refit
 	int32_t* levelStarts = nullptr;  // first node index of each depth, nLevels + 1 entries
 	int32_t nLevels = 0;
+	int32_t levelCapacity = 0;       // entries allocated for levelStarts
 	int32_t capacity = 0;
 	int32_t nInstances = 0;
 	uint32_t nodeCount = 0;
 };
-// (Re)builds the TLAS over `nInstances` instance records given in HOST memory: SAH topology on the host,
-// then the device copies of nodes, leaf records, node boxes and depth ranges on `stream`.
+// (Re)builds the TLAS over `nInstances` instance records given in HOST memory, on the device: their world
+// boxes are uploaded, then the binned SAH topology and the wide collapse run on `stream`, which is
+// synchronised at the end (a build happens only when the set of entities changes).
 void buildTlas(const InstanceRec* hInstances, int nInstances, TlasBuild& t, cudaStream_t stream);
 // Refits the TLAS after instance boxes changed (same instance set): one single-block launch.
 void refitTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);

@@ -329,32 +329,73 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 	}
 	__syncthreads();
 	const uint32_t kept = tileKept;
-	for (uint32_t c = (uint32_t) tid; c < kept; c += kBlock) {
-		const int i = tile * kCompactTile + keptLocal[c];
-		const uint32_t pos = tileBase + c;
-		for (int f = 0; f < fc.count; ++f) {
-			if (f == ops.xyzField || f == ops.distField) {
+	// Kept points c = tid + j * kBlock (at most kCompactItems per thread). Each field's source values of
+	// all the thread's points are loaded before the first store: the compiler cannot move a load past a
+	// store to a pointer that may alias it, so a point-at-a-time loop would serialise the loads.
+	int src[kCompactItems];
+#pragma unroll
+	for (int j = 0; j < kCompactItems; ++j) {
+		const uint32_t c = (uint32_t) (tid + j * kBlock);
+		src[j] = c < kept ? tile * kCompactTile + keptLocal[c] : -1;
+	}
+	for (int f = 0; f < fc.count; ++f) {
+		if (f == ops.xyzField || f == ops.distField) {
+			continue;
+		}
+		const int sz = fc.f[f].size;
+		const uint8_t* s = static_cast<const uint8_t*>(fc.f[f].src);
+		uint8_t* d = static_cast<uint8_t*>(fc.f[f].dst);
+		if (sz == 4) {
+			uint32_t v[kCompactItems];
+#pragma unroll
+			for (int j = 0; j < kCompactItems; ++j) {
+				v[j] = src[j] >= 0 ? reinterpret_cast<const uint32_t*>(s)[src[j]] : 0u;
+			}
+#pragma unroll
+			for (int j = 0; j < kCompactItems; ++j) {
+				if (src[j] >= 0) {
+					reinterpret_cast<uint32_t*>(d)[tileBase + tid + j * kBlock] = v[j];
+				}
+			}
+		} else {
+#pragma unroll
+			for (int j = 0; j < kCompactItems; ++j) {
+				if (src[j] >= 0) {
+					copyElem(s + (size_t) src[j] * sz, d + (size_t) (tileBase + tid + j * kBlock) * sz, sz);
+				}
+			}
+		}
+	}
+	if (ops.xyzField >= 0 || ops.distField >= 0) {
+		// XYZ and distance of the chain's source, through the absorbed operations in order.
+		Vec3 p[kCompactItems];
+		float dd[kCompactItems];
+#pragma unroll
+		for (int j = 0; j < kCompactItems; ++j) {
+			p[j] = (src[j] >= 0 && ops.srcXyz) ? loadXyz(ops.srcXyz, src[j]) : v3(0.0f, 0.0f, 0.0f);
+			dd[j] = (src[j] >= 0 && ops.srcDist) ? ops.srcDist[src[j]] : 0.0f;
+		}
+#pragma unroll
+		for (int j = 0; j < kCompactItems; ++j) {
+			if (src[j] < 0) {
 				continue;
 			}
-			const int sz = fc.f[f].size;
-			copyElem(static_cast<const uint8_t*>(fc.f[f].src) + (size_t) i * sz, static_cast<uint8_t*>(fc.f[f].dst) + (size_t) pos * sz, sz);
-		}
-		if (ops.xyzField >= 0 || ops.distField >= 0) {
-			// XYZ and distance of the chain's source, through the absorbed operations in order.
-			Vec3 p = ops.srcXyz ? loadXyz(ops.srcXyz, i) : v3(0.0f, 0.0f, 0.0f);
-			float d = ops.srcDist ? ops.srcDist[i] : 0.0f;
+			const int i = src[j];
+			const uint32_t pos = tileBase + (uint32_t) (tid + j * kBlock);
+			Vec3 q = p[j];
+			float d = dd[j];
 			for (int o = 0; o < ops.count; ++o) {
 				const uint32_t* prm = opParams[o];
 				if (ops.op[o].kind == kOpTransform) {
-					p = reinterpret_cast<const Mat34*>(prm)->point(p);
+					q = reinterpret_cast<const Mat34*>(prm)->point(q);
 				} else if (ops.op[o].kind == kOpNoiseAngularHitpoint) {
-					p = angularHitpoint(*reinterpret_cast<const NoiseParams*>(prm), i, p, ops.op[o].withDistance ? &d : nullptr);
+					q = angularHitpoint(*reinterpret_cast<const NoiseParams*>(prm), i, q, ops.op[o].withDistance ? &d : nullptr);
 				} else {
-					p = distanceNoise(*reinterpret_cast<const NoiseParams*>(prm), i, p, d);
+					q = distanceNoise(*reinterpret_cast<const NoiseParams*>(prm), i, q, d);
 				}
 			}
 			if (ops.xyzField >= 0) {
-				storeXyz(static_cast<float*>(fc.f[ops.xyzField].dst), (int) pos, p);
+				storeXyz(static_cast<float*>(fc.f[ops.xyzField].dst), (int) pos, q);
 			}
 			if (ops.distField >= 0) {
 				static_cast<float*>(fc.f[ops.distField].dst)[pos] = d;

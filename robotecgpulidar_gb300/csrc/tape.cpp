@@ -5,7 +5,9 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <cctype>
 #include <cerrno>
+#include <cmath>
 #include <chrono>
 #include <cinttypes>
 #include <cstdio>
@@ -124,17 +126,41 @@ void recordFailed(const char* fn, const char* why)
 std::string handle(const void* h) { return std::to_string((uint64_t) (uintptr_t) h); }
 std::string num(int64_t v) { return std::to_string(v); }
 std::string unum(uint64_t v) { return std::to_string(v); }
-std::string real(float v)
+// Floats as yaml-cpp's emitter writes them (the reference recorder's): shortest-round-trip digits
+// (9 significant for float, 17 for double) in %g form, and the YAML spellings .inf, -.inf, .nan.
+std::string real(float v) { return real((double) v, 9); }
+std::string real(double v) { return real(v, 17); }
+std::string real(double v, int digits)
 {
-	char b[32];
-	std::snprintf(b, sizeof(b), "%.9g", (double) v);
+	if (std::isnan(v)) {
+		return ".nan";
+	}
+	if (std::isinf(v)) {
+		return v > 0 ? ".inf" : "-.inf";
+	}
+	char b[40];
+	std::snprintf(b, sizeof(b), "%.*g", digits, v);
 	return b;
 }
-std::string real(double v)
+
+// A float argument: plain decimal, or a YAML special (.inf, -.inf, +.inf, .nan in any of the YAML
+// core schema's capitalisations), as a tape from either recorder holds it.
+float parseFloat(const std::string& s)
 {
-	char b[40];
-	std::snprintf(b, sizeof(b), "%.17g", v);
-	return b;
+	std::string t = s;
+	for (auto& ch : t) {
+		ch = (char) std::tolower((unsigned char) ch);
+	}
+	if (t == ".inf" || t == "+.inf") {
+		return INFINITY;
+	}
+	if (t == "-.inf") {
+		return -INFINITY;
+	}
+	if (t == ".nan") {
+		return NAN;
+	}
+	return std::strtof(s.c_str(), nullptr);
 }
 std::string flag(bool v) { return v ? "true" : "false"; }
 std::string text(const char* s)
@@ -344,7 +370,7 @@ struct Playback
 	uint64_t id(size_t i) const { return std::strtoull(a(i).c_str(), nullptr, 10); }
 	int64_t i64(size_t i) const { return std::strtoll(a(i).c_str(), nullptr, 10); }
 	int32_t i32(size_t i) const { return (int32_t) i64(i); }
-	float f32(size_t i) const { return std::strtof(a(i).c_str(), nullptr); }
+	float f32(size_t i) const { return parseFloat(a(i)); }
 	bool b(size_t i) const { return a(i) == "true" || a(i) == "True" || a(i) == "1"; }
 	template<class T>
 	const T* ptr(size_t i) const

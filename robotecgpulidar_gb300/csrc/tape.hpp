@@ -46,6 +46,8 @@ std::string num(int64_t v);
 std::string unum(uint64_t v);
 std::string real(float v);
 std::string real(double v);
+std::string real(double v, int significantDigits);
+float parseFloat(const std::string& s);
 std::string flag(bool v);
 std::string text(const char* s);
 std::string bin(const void* data, size_t bytes);

@@ -16,7 +16,6 @@ struct HitRec
 	int32_t inst;  // instance index, -1 when nothing was hit
 	int32_t tri;   // index into the instance BLAS triangle records
 	int32_t prim;  // the triangle's index in its mesh (breaks ties in t)
-	int32_t refine; // the hit grazes its triangle or lies close on a transformed instance (refineClosest)
 };
 
 #if defined(__CUDA_ARCH__)
@@ -68,7 +67,7 @@ RGL_HD float shear(Vec3 row, Vec3 v) { return fmaf(row.x, v.x, fmaf(row.y, v.y, 
 // 0 < t <= tBest returns true and the new t. Each vertex is sheared by the same arithmetic in every
 // triangle that holds it; edge functions are evaluated without FMA so a shared edge yields exactly
 // opposite values in both triangles; exact zeros are re-evaluated in double.
-RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& w, float tBest, float& tOut, float& detOut)
+RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& w, float tBest, float& tOut)
 {
 	Vec3 A = a - o, B = b - o, C = c - o;
 	float Ax = shear(w.row0, A), Ay = shear(w.row1, A);
@@ -99,13 +98,7 @@ RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& 
 		return false;
 	}
 	tOut = t;
-	detOut = det;
 	return true;
-}
-RGL_HD bool intersectTriangle(Vec3 a, Vec3 b, Vec3 c, Vec3 o, const Watertight& w, float tBest, float& tOut)
-{
-	float det;
-	return intersectTriangle(a, b, c, o, w, tBest, tOut, det);
 }
 
 RGL_HD float safeInv(float d)
@@ -358,36 +351,6 @@ RGL_HD void compensatedPoint(const Mat34& m, Vec3 v, Vec3& hi, Vec3& lo)
 // the distance, stays below 4e-6), unless the hit is close on a transformed instance (below).
 constexpr float kRefineSine = 0.1f;
 
-// Grazing and closeness, decided where a closest-hit candidate is accepted, from values the
-// traversal already holds. The watertight determinant is n . d / d_kz (n the triangle's unnormalised
-// normal, d_kz the direction's dominant component), so sin(grazing angle) = |det| * K / |n| with the
-// per-frame constant K = |d_kz| / |d| and the triangle record's 1 / |n|. A hit on a transformed
-// instance is close when t^2 < closeT2 = (|o - instance origin| / 2)^2 / |d|^2 (set on entering the
-// instance; -1 on identity instances). Rays flagged here go through refineClosest, which decides
-// again from the triangle itself.
-struct RefineFrame
-{
-	float K;       // |d_kz| / |d| in the current instance frame
-	float closeT2; // see above
-};
-RGL_HD RefineFrame refineFrame(const InstanceRec& ir, Vec3 oW, Vec3 dW, Vec3 od)
-{
-	RefineFrame f;
-	const float m = maxf_(maxf_(absf_(od.x), absf_(od.y)), absf_(od.z));
-	f.K = m / sqrtf(dot(od, od));
-	if ((ir.flags & kInstanceIdentity) != 0) {
-		f.closeT2 = -1.0f;
-	} else {
-		const Vec3 off = oW - ir.objectToWorld.translation();
-		f.closeT2 = fmul(0.25f, dot(off, off)) / dot(dW, dW);
-	}
-	return f;
-}
-RGL_HD int32_t needsRefine(const RefineFrame& f, float det, float invNormalLen, float t)
-{
-	return (fmul(fmul(absf_(det), f.K), invNormalLen) < kRefineSine || fmul(t, t) < f.closeT2) ? 1 : 0;
-}
-
 // The closest hit's t finished from the hit triangle's plane when the ray grazes it. On an instance
 // with the identity transform (a scene-sized mesh) the instance frame is the world frame and planeHitT
 // is exact up to the rounding of the normal. A transformed instance rounds the ray into its frame by
@@ -451,14 +414,12 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 	best.inst = -1;
 	best.tri = -1;
 	best.prim = -1;
-	best.refine = 0;
 	if (sc.nInstances <= 0) {
 		return best;
 	}
 	const int base = st.size();
 	FrameRay r = frameRay(oW, dW);
 	Watertight wt = setupWatertight(dW); // valid inside an instance
-	RefineFrame rf{0.0f, -1.0f};         // valid inside an instance
 	const WideNode* nodes = sc.tlas;
 	const TriRecord* leaves = sc.tlasLeaves;
 	int32_t inst = -1; // -1: the TLAS (world frame)
@@ -522,15 +483,14 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 				const int cnt = (int) (meta >> 5);
 				for (int k = 0; k < cnt; ++k) {
 					TriRecord tr = load.tri(leaves, first + k);
-					float t, det;
+					float t;
 					if (intersectTriangle(v3(tr.v0x, tr.v0y, tr.v0z), v3(tr.v1x, tr.v1y, tr.v1z), v3(tr.v2x, tr.v2y, tr.v2z), r.o, wt,
-					                      best.t, t, det) &&
+					                      best.t, t) &&
 					    closerHit(t, inst, tr.primId, best)) {
 						best.t = t;
 						best.inst = inst;
 						best.tri = first + k;
 						best.prim = tr.primId;
-						best.refine = needsRefine(rf, det, tr.invNormalLen, t);
 					}
 				}
 			}
@@ -539,7 +499,7 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 		bool enterRoot = false;
 		while (hits == 0) {
 			if (st.size() == base) {
-				return best.refine ? refineClosest(sc, oW, dW, best, load) : best;
+				return refineClosest(sc, oW, dW, best, load);
 			}
 			uint32_t a, b;
 			st.pop(a, b);
@@ -554,7 +514,6 @@ RGL_HD HitRec traceClosest(const SceneView& sc, Vec3 oW, Vec3 dW, float tmax, St
 				const Vec3 od = ir.worldToObject.vector(dW);
 				r = frameRay(worldToInstance(ir, oW), od);
 				wt = setupWatertight(od);
-				rf = refineFrame(ir, oW, dW, od);
 				nodes = ir.nodes;
 				leaves = ir.tris;
 				inst = (int32_t) a;

@@ -82,7 +82,7 @@ struct DevLoader
 		t.v1x = b.x;
 		t.v1y = b.y;
 		t.v1z = b.z;
-		t.invNormalLen = b.w;
+		t.pad1 = 0;
 		t.v2x = c.x;
 		t.v2y = c.y;
 		t.v2z = c.z;

@@ -332,7 +332,6 @@ RGL_HD void traceClosestPacket(const SceneView& sc, Vec3 oW, int n, float tmax, 
 		best[r].inst = -1;
 		best[r].tri = -1;
 		best[r].prim = -1;
-		best[r].refine = 0;
 	}
 	if (sc.nInstances <= 0) {
 		return;

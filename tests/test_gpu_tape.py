@@ -3,7 +3,10 @@ error cases of test/src/TapeTest.cpp:55-163): calls go to <path>.yaml (one `- fn
 item per call, the library version first) and <path>.bin (arrays at 16-byte aligned offsets), and
 playing the tape back rebuilds the recorded scene."""
 import ctypes as C
+import json
+import os
 import re
+import sys
 
 import numpy as np
 import pytest
@@ -11,6 +14,8 @@ import pytest
 from robotecgpulidar_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
+
+RGL_LOG_LEVEL_WARN = 3
 
 
 def write(path, text):
@@ -139,3 +144,46 @@ def test_record_and_play_back(rgl, tmp_path):
     assert probe_hits(rgl)[0] == [0, 0]  # empty scene after cleanup
     rgl.check(rgl.lib().rgl_tape_play(str(base).encode()))
     assert probe_hits(rgl) == before
+
+
+GOLDEN_TAPE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_tape")
+
+
+def test_plays_tape_in_the_reference_recorders_form(rgl, tmp_path):
+    """A tape written in the reference recorder's exact form (tests/golden/make_reference_tape.py:
+    yaml-cpp's block sequence of flow maps, recorded addresses as handles, enums as integers, floats
+    with 9 digits and .inf, arrays at 16-byte aligned offsets of the binary file) plays back: every
+    call succeeds (nothing logged at warning level or above, so the three recorded result sizes equal
+    the played graph's), the scene is rebuilt with the recorded poses, ids and laser retro, and the
+    same graph built by direct calls yields the recorded hit count (the oracle's) and entity mix."""
+    exp = json.load(open(GOLDEN_TAPE + ".json"))
+    lib = rgl.lib()
+    log = tmp_path / "play.log"
+    rgl.check(lib.rgl_cleanup())
+    rgl.check(lib.rgl_configure_logging(RGL_LOG_LEVEL_WARN, str(log).encode(), False))
+    try:
+        rgl.check(lib.rgl_tape_play(GOLDEN_TAPE.encode()))
+        assert probe_hits(rgl) == ([11, 22], [4.0, 5.0], [0.0, 0.5])
+    finally:
+        rgl.check(lib.rgl_configure_logging(rgl.RGL_LOG_LEVEL_OFF, None, False))
+    text = open(log).read() if log.exists() else ""
+    assert text.strip() == "", text
+
+    sys.path.insert(0, os.path.dirname(GOLDEN_TAPE))
+    import make_reference_tape as mk
+
+    _, rays, sensor, _ = mk.session()
+    n = {k: rgl.node() for k in ("rays", "pose", "range", "trace", "noise", "cmp", "out")}
+    rgl.rays_from_mat3x4f(n["rays"], rays)
+    rgl.rays_transform(n["pose"], sensor)
+    rgl.rays_set_range(n["range"], [[0.1, 60.0]])
+    rgl.raytrace(n["trace"])
+    rgl.check(lib.rgl_node_raytrace_configure_return_mode(n["trace"], rgl.RGL_RETURN_FIRST))
+    rgl.check(lib.rgl_node_gaussian_noise_distance(C.byref(n["noise"]), 0.0, 0.02, 0.001))
+    rgl.points_compact_by_field(n["cmp"])
+    rgl.points_yield(n["out"], [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_DISTANCE_F32])
+    rgl.chain(*n.values())
+    rgl.graph_run(n["rays"])
+    ent = rgl.result(n["out"], rgl.RGL_FIELD_ENTITY_ID_I32)
+    assert len(ent) == exp["hit_points"]
+    assert {int(k): v for k, v in exp["hits_per_entity"].items()} == {e: int((ent == e).sum()) for e in (11, 22, 33)}
