@@ -3,7 +3,12 @@
 // three launches for the whole batch:
 //   kSegCount    one block per 1024-point tile: number of kept points in the tile;
 //   kSegScan     one block per segment: exclusive scan of its tile counts, and the segment's total;
-//   kSegScatter  one block per tile: in-tile ranks from warp ballots, then the field copies.
+//   kSegScatter  one block per tile: in-tile ranks from warp ballots gather the kept points into shared
+//                memory, then the block writes the tile's contiguous output ranges word by word.
+// The outputs are usually pinned host memory mapped for the device (the server's result arena), which
+// the GPU writes across the host link: there, stores from consecutive lanes to consecutive words (full
+// 128-byte lines) run several times faster than each kept point storing its own 12- and 4-byte
+// pieces at scattered offsets.
 // Order is preserved, so each segment's output equals a compaction of that segment alone (reference
 // CompactByFieldPointsNode semantics, src/graph/CompactByFieldPointsNode.cpp:33-105: keep points
 // whose flag is non-zero, in order). HBM-bound: flags are read twice, fields once, kept points
@@ -134,13 +139,17 @@ __global__ void __launch_bounds__(kThreads) kSegScatter(const SegCompactJob* __r
 {
 	extern __shared__ int32_t sBase[];
 	__shared__ uint32_t warpCounts[kThreads / 32];
+	__shared__ float sXyz[3 * kSegTile];
+	__shared__ float sDist[kSegTile];
+	__shared__ int32_t sEnt[kSegTile];
 	stageBases(sBase, tileBase, nSeg);
 	const int t = blockIdx.x;
 	const int j = findSegment(sBase, nSeg, t);
 	const SegCompactJob& sg = segs[j];
 	const int start = (t - sBase[j]) * kSegTile;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint32_t base = tileOffsets[t];
+	// The tile's kept points, in order, into shared memory.
+	uint32_t kept = 0;
 	for (int k = 0; k < kItems; ++k) {
 		const int p = start + k * kThreads + threadIdx.x;
 		const bool keep = p < sg.nPoints && __ldg(sg.flags + p) != 0;
@@ -156,15 +165,27 @@ __global__ void __launch_bounds__(kThreads) kSegScatter(const SegCompactJob* __r
 			total += cw;
 		}
 		if (keep) {
-			const uint32_t dst = base + before + __popc(ballot & ((1u << lane) - 1u));
-			sg.outXyz[3 * dst] = __ldg(sg.xyz + 3 * p);
-			sg.outXyz[3 * dst + 1] = __ldg(sg.xyz + 3 * p + 1);
-			sg.outXyz[3 * dst + 2] = __ldg(sg.xyz + 3 * p + 2);
-			sg.outDist[dst] = __ldg(sg.dist + p);
-			sg.outEnt[dst] = __ldg(sg.ent + p);
+			const uint32_t r = kept + before + __popc(ballot & ((1u << lane) - 1u));
+			sXyz[3 * r] = __ldg(sg.xyz + 3 * p);
+			sXyz[3 * r + 1] = __ldg(sg.xyz + 3 * p + 1);
+			sXyz[3 * r + 2] = __ldg(sg.xyz + 3 * p + 2);
+			sDist[r] = __ldg(sg.dist + p);
+			sEnt[r] = __ldg(sg.ent + p);
 		}
-		base += total;
+		kept += total;
 		__syncthreads();
+	}
+	// Contiguous output ranges of the tile, one word per thread and step.
+	const uint32_t base = tileOffsets[t];
+	float* ox = sg.outXyz + 3 * (size_t) base;
+	for (uint32_t w = threadIdx.x; w < 3 * kept; w += kThreads) {
+		ox[w] = sXyz[w];
+	}
+	float* od = sg.outDist + base;
+	int32_t* oe = sg.outEnt + base;
+	for (uint32_t w = threadIdx.x; w < kept; w += kThreads) {
+		od[w] = sDist[w];
+		oe[w] = sEnt[w];
 	}
 }
 

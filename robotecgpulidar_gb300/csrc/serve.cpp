@@ -14,6 +14,22 @@ namespace {
 // (and so waits for the device) only a few times.
 void* grow(rgl::DeviceBuffer& buf, size_t bytes) { return buf.ensure(bytes <= buf.capacity() ? bytes : std::max(bytes, 2 * buf.capacity())); }
 
+// Layout of a batch's upload (16-byte aligned parts): jobs[n] | task bases[n+1] | segments[n] | tile bases[n+1].
+struct TableLayout
+{
+	size_t offTask, offSeg, offTile, bytes;
+};
+TableLayout tableLayout(int n)
+{
+	auto align = [](size_t x) { return (x + 15) & ~size_t{15}; };
+	TableLayout t;
+	t.offTask = align(sizeof(rgl::BatchJob) * n);
+	t.offSeg = t.offTask + align(sizeof(int32_t) * (n + 1));
+	t.offTile = t.offSeg + align(sizeof(rgl::SegCompactJob) * n);
+	t.bytes = t.offTile + align(sizeof(int32_t) * (n + 1));
+	return t;
+}
+
 } // namespace
 
 Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmBudgetBytes), maxInFlight(std::max(1, maxInFlightBatches))
@@ -42,20 +58,26 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 	for (int i = 0; i < maxInFlight; ++i) {
 		auto s = std::make_unique<Slot>();
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->counted, cudaEventDisableTiming));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t0));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t1));
 		RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
 		RGL_CHECK_CUDA(cudaMemset(s->counter.ensure(rgl::kTraceCounterBytes), 0, rgl::kTraceCounterBytes));
 		slots.push_back(std::move(s));
 	}
-	// Per-batch device buffers sized up front for the largest batch (two returns per beam), within
-	// this slot's share of the budget: a batch never allocates, so it never waits for the other
-	// slot's work on the device.
+	// Per-batch buffers sized up front for the largest batch (two returns per beam, kMaxBatchJobs
+	// requests), within this slot's share of the budget: a batch never allocates or frees, which would
+	// wait for the other slots' work on the device.
 	const int64_t points = std::min<int64_t>(2 * maxBatchBeams, budget / (kRawBytesPerPoint * maxInFlight));
-	if (points > 0) {
-		for (auto& sl : slots) {
+	const TableLayout most = tableLayout(rgl::kMaxBatchJobs);
+	for (auto& sl : slots) {
+		if (points > 0) {
 			reserveRaw(*sl, points, points / rgl::kSegTile + 4096);
 		}
+		sl->hTables.ensure(most.bytes);
+		sl->tables.ensure(most.bytes);
+		sl->hResults.ensure(sizeof(int32_t) * 2 * rgl::kMaxBatchJobs);
+		sl->results.ensure(sizeof(int32_t) * 2 * rgl::kMaxBatchJobs);
 	}
 	worker = std::thread([this] { loop(); });
 }
@@ -77,6 +99,7 @@ Server::~Server()
 	cudaFreeHost(arena.host);
 	for (auto& s : slots) {
 		cudaEventDestroy(s->done);
+		cudaEventDestroy(s->counted);
 		cudaEventDestroy(s->t0);
 		cudaEventDestroy(s->t1);
 		cudaStreamDestroy(s->stream);
@@ -356,6 +379,9 @@ void Server::reserveRaw(Slot& slot, int64_t points, int64_t tiles)
 	grow(slot.rawXyz, sizeof(float) * 3 * (size_t) points);
 	grow(slot.rawDist, sizeof(float) * (size_t) points);
 	grow(slot.rawEnt, sizeof(int32_t) * (size_t) points);
+	grow(slot.outXyz, sizeof(float) * 3 * (size_t) points);
+	grow(slot.outDist, sizeof(float) * (size_t) points);
+	grow(slot.outEnt, sizeof(int32_t) * (size_t) points);
 	grow(slot.tileCounts, sizeof(uint32_t) * (size_t) tiles);
 	grow(slot.tileOffsets, sizeof(uint32_t) * (size_t) tiles);
 }
@@ -367,8 +393,12 @@ void Server::configure(const rgl::BatchSchedule& s, int64_t maxBeams)
 	maxBatchBeams = maxBeams;
 }
 
-// Builds and enqueues one batch from slot.reqs (already admitted, outputs allocated).
-void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
+// Builds and enqueues one batch from slot.reqs (already admitted, outputs allocated). Its traversal
+// starts on the device once the batch launched before it (on slot `after`) has traced and compacted:
+// batches trace one after another at the full speed of the GPU, while each batch's result copies
+// (copy engine) overlap the next batch's traversal. Two traversals sharing the GPU would both finish
+// late and then leave it idle during their copies.
+void Server::launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after)
 {
 	const int n = (int) slot.reqs.size();
 	int64_t points = 0;
@@ -384,13 +414,13 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 	auto* xyz = slot.rawXyz.as<float>();
 	auto* dist = slot.rawDist.as<float>();
 	auto* ent = slot.rawEnt.as<int32_t>();
+	auto* outXyz = slot.outXyz.as<float>();
+	auto* outDist = slot.outDist.as<float>();
+	auto* outEnt = slot.outEnt.as<int32_t>();
+	slot.pointBase.assign((size_t) n, 0);
 
-	// Table layout (16-byte aligned parts): jobs[n] | task bases[n+1] | segments[n] | tile bases[n+1].
-	auto align = [](size_t x) { return (x + 15) & ~size_t{15}; };
-	const size_t offTask = align(sizeof(rgl::BatchJob) * n);
-	const size_t offSeg = offTask + align(sizeof(int32_t) * (n + 1));
-	const size_t offTile = offSeg + align(sizeof(rgl::SegCompactJob) * n);
-	const size_t tableBytes = offTile + align(sizeof(int32_t) * (n + 1));
+	const TableLayout lay = tableLayout(n);
+	const size_t offTask = lay.offTask, offSeg = lay.offSeg, offTile = lay.offTile, tableBytes = lay.bytes;
 	auto* hBase = static_cast<uint8_t*>(slot.hTables.ensure(tableBytes));
 	auto* dBase = static_cast<uint8_t*>(grow(slot.tables, tableBytes));
 	auto* jobs = reinterpret_cast<rgl::BatchJob*>(hBase);
@@ -436,11 +466,12 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 		sg.xyz = xyz + 3 * pointBase;
 		sg.dist = dist + pointBase;
 		sg.ent = ent + pointBase;
-		sg.outXyz = r.devOut;
-		sg.outDist = r.devOut + 3 * r.points;
-		sg.outEnt = reinterpret_cast<int32_t*>(r.devOut + 4 * r.points);
+		sg.outXyz = outXyz + 3 * pointBase;
+		sg.outDist = outDist + pointBase;
+		sg.outEnt = outEnt + pointBase;
 		sg.nPoints = (int32_t) r.points;
 		segs[j] = sg;
+		slot.pointBase[(size_t) j] = pointBase;
 		tileBase[j] = (int32_t) tiles;
 		tiles += (r.points + rgl::kSegTile - 1) / rgl::kSegTile;
 		pointBase += r.points;
@@ -450,17 +481,49 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched)
 
 	auto* dTileCounts = slot.tileCounts.get();
 	auto* dTileOffsets = slot.tileOffsets.get();
-	RGL_CHECK_CUDA(cudaEventRecord(slot.t0, slot.stream));
 	RGL_CHECK_CUDA(cudaMemcpyAsync(dBase, hBase, tableBytes, cudaMemcpyHostToDevice, slot.stream));
 	RGL_CHECK_CUDA(cudaMemsetAsync(dResults + n, 0, sizeof(int32_t) * n, slot.stream));
+	if (after != nullptr && after != &slot) {
+		RGL_CHECK_CUDA(cudaStreamWaitEvent(slot.stream, after->counted, 0));
+	}
+	RGL_CHECK_CUDA(cudaEventRecord(slot.t0, slot.stream));
 	rgl::launchTraceBatch(reinterpret_cast<const rgl::BatchJob*>(dBase), reinterpret_cast<const int32_t*>(dBase + offTask), n, 1, false,
 	                      sched, slot.counter.as<uint32_t>(), slot.stream);
 	rgl::launchSegCompact(reinterpret_cast<const rgl::SegCompactJob*>(dBase + offSeg), reinterpret_cast<const int32_t*>(dBase + offTile), n,
 	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, slot.stream);
 	auto* hResults = static_cast<int32_t*>(slot.hResults.ensure(sizeof(int32_t) * 2 * n));
 	RGL_CHECK_CUDA(cudaMemcpyAsync(hResults, dResults, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, slot.stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.counted, slot.stream));
+	slot.phase = Phase::Tracing;
+	RGL_CHECK_CUDA(cudaLaunchHostFunc(slot.stream, &Server::batchDone, this));
+}
+
+// Once a batch's kept counts are in host memory: the copies of exactly the kept points of every
+// request from the slot's staging buffers into the request's block of the result arena, on the
+// slot's stream (copy engine), then the batch's completion.
+void Server::copyOut(Slot& slot)
+{
+	const auto* hCounts = static_cast<const int32_t*>(slot.hResults.get());
+	const size_t n = slot.reqs.size();
+	const auto* outXyz = slot.outXyz.as<float>();
+	const auto* outDist = slot.outDist.as<float>();
+	const auto* outEnt = slot.outEnt.as<int32_t>();
+	for (size_t j = 0; j < n; ++j) {
+		const Request& r = *slot.reqs[j];
+		const int64_t kept = hCounts[j];
+		if (hCounts[n + j] != 0 || kept <= 0 || kept > r.points) {
+			continue; // failed (retire reports it) or nothing kept
+		}
+		const int64_t b = slot.pointBase[j];
+		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut, outXyz + 3 * b, sizeof(float) * 3 * (size_t) kept, cudaMemcpyDeviceToHost, slot.stream));
+		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut + 3 * r.points, outDist + b, sizeof(float) * (size_t) kept, cudaMemcpyDeviceToHost,
+		                               slot.stream));
+		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut + 4 * r.points, outEnt + b, sizeof(int32_t) * (size_t) kept, cudaMemcpyDeviceToHost,
+		                               slot.stream));
+	}
 	RGL_CHECK_CUDA(cudaEventRecord(slot.t1, slot.stream));
 	RGL_CHECK_CUDA(cudaEventRecord(slot.done, slot.stream));
+	slot.phase = Phase::Copying;
 	RGL_CHECK_CUDA(cudaLaunchHostFunc(slot.stream, &Server::batchDone, this));
 }
 
@@ -492,7 +555,7 @@ void Server::retire(Slot& slot)
 		r.count = hCounts[j];
 		r.state = failed ? State::Failed : State::Done;
 		if (failed) {
-			r.error = "traversal stack overflow on the device";
+			r.error = hCounts[n + j] == 2 ? "the result copies could not be enqueued" : "traversal stack overflow on the device";
 			++st.failed;
 		}
 		r.completed = now;
@@ -519,7 +582,27 @@ void Server::loop()
 	std::unique_lock<std::mutex> lk(m);
 	for (;;) {
 		const uint64_t seen = wakeups;
-		while (!inFlight.empty() && cudaEventQuery(inFlight.front()->done) == cudaSuccess) {
+		// Batches whose counts arrived get their result copies; finished batches retire in order.
+		const std::vector<Slot*> running(inFlight.begin(), inFlight.end());
+		for (Slot* s : running) {
+			if (s->phase == Phase::Tracing && cudaEventQuery(s->counted) == cudaSuccess) {
+				lk.unlock();
+				try {
+					copyOut(*s);
+				}
+				catch (std::exception& e) {
+					// The copies could not be enqueued: the batch's requests fail when it retires.
+					auto* hCounts = static_cast<int32_t*>(s->hResults.get());
+					for (size_t j = 0; j < s->reqs.size(); ++j) {
+						hCounts[s->reqs.size() + j] = 2;
+					}
+					cudaEventRecord(s->done, s->stream);
+					s->phase = Phase::Copying;
+				}
+				lk.lock();
+			}
+		}
+		while (!inFlight.empty() && inFlight.front()->phase == Phase::Copying && cudaEventQuery(inFlight.front()->done) == cudaSuccess) {
 			Slot* s = inFlight.front();
 			lk.unlock();
 			retire(*s);
@@ -548,7 +631,6 @@ void Server::loop()
 					break; // the result arena is full until clients release results
 				}
 				r->hostOut = reinterpret_cast<float*>(arena.host + r->outOffset);
-				r->devOut = reinterpret_cast<float*>(arena.dev + r->outOffset);
 				pending.pop_front();
 				reserved += r->reservedBytes;
 				st.peakReserved = std::max(st.peakReserved, reserved);
@@ -564,6 +646,8 @@ void Server::loop()
 				freeSlot->busy = true;
 				freeSlot->reqs = batch;
 				inFlight.push_back(freeSlot);
+				Slot* after = lastLaunched;
+				lastLaunched = freeSlot;
 				++st.batches;
 				st.jobsInBatches += (int64_t) batch.size();
 				const rgl::BatchSchedule sched = schedule;
@@ -579,7 +663,7 @@ void Server::loop()
 						}
 
 					}
-					launch(*freeSlot, sched);
+					launch(*freeSlot, sched, after);
 				}
 				catch (std::exception& e) {
 					ok = false;

@@ -13,9 +13,12 @@
 //
 // Each request's result is XYZ, distance and entity id of its hit points, in point order, equal to
 // what the graph rays_from_mat3x4f(pattern) -> rays_transform(pose) -> rays_set_range ->
-// raytrace(scene, mode) -> compact_by_field(IS_HIT) -> yield writes. The compaction writes it straight
-// into pinned host memory (mapped for the device), so a completed request's result is already in
-// host memory; release() returns the block to the server's pool.
+// raytrace(scene, mode) -> compact_by_field(IS_HIT) -> yield writes. The compaction writes every
+// request's result into the batch slot's device staging buffers and the kept counts to pinned host
+// memory; once the counts arrive, the scheduler enqueues copy-engine copies of exactly the kept bytes
+// into each request's block of the pinned host result arena (the copies run while the other slot's
+// batch traverses, and take no SM time). A completed request's result is in host memory; release()
+// returns its block to the arena.
 //
 // While a server runs, the scenes it traces must not be modified (drain() first).
 #pragma once
@@ -89,10 +92,9 @@ private:
 		float minRange, maxRange;
 		int64_t beams, points;
 		int64_t reservedBytes;
-		// Result block in the pinned arena, mapped for the device: xyz | distance | entity id, `points`
-		// capacity each. The compaction writes it directly; no copy follows.
+		// Result block in the pinned arena: xyz | distance | entity id, `points` capacity each, filled
+		// by the batch's result copies.
 		float* hostOut = nullptr;
-		float* devOut = nullptr; // the device address of hostOut
 		size_t outOffset = 0;
 		int outOrder = -1;
 		int32_t count = 0;
@@ -108,20 +110,32 @@ private:
 	};
 	// One in-flight batch slot: device and pinned buffers reused by every batch launched from it.
 	// The job table, task bases, compaction segments and tile bases travel in one upload; the
-	// per-request counts and the traversal's error flag come back in one download.
+	// per-request counts and the traversal's error flag come back in one download. A batch is
+	// Tracing until its counts arrive (event `counted`), then Copying until its result copies are
+	// done (event `done`).
+	enum class Phase
+	{
+		Tracing,
+		Copying
+	};
 	struct Slot
 	{
 		std::vector<Request*> reqs;
-		cudaStream_t stream = nullptr; // slots run on their own streams: one batch's tail overlaps the next
-		cudaEvent_t done = nullptr;
+		std::vector<int64_t> pointBase; // first point of each request in the slot's buffers
+		cudaStream_t stream = nullptr;  // slots run on their own streams: one batch's tail overlaps the next
+		cudaEvent_t counted = nullptr, done = nullptr;
 		cudaEvent_t t0 = nullptr, t1 = nullptr; // device time of the batch
 		rgl::DeviceBuffer tables{false}, tileCounts{false}, tileOffsets{false}, results{false}, counter{false};
 		rgl::DeviceBuffer rawFlags{false}, rawXyz{false}, rawDist{false}, rawEnt{false};
+		rgl::DeviceBuffer outXyz{false}, outDist{false}, outEnt{false}; // compacted results before the copies
 		rgl::PinnedBuffer hTables, hResults;
+		Phase phase = Phase::Tracing;
 		bool busy = false;
 	};
 
-	static constexpr int64_t kRawBytesPerPoint = 4 + 12 + 4 + 4; // flags, xyz, distance, entity id
+	// Device bytes of a point while its batch is on the GPU: flags, xyz, distance and entity id as
+	// traced, then xyz, distance and entity id compacted.
+	static constexpr int64_t kRawBytesPerPoint = 4 + 12 + 4 + 4 + 12 + 4 + 4;
 	// Grows a slot's raw point and compaction-tile buffers (never shrinks them).
 	void reserveRaw(Slot& slot, int64_t points, int64_t tiles);
 	static constexpr int64_t kOutBytesPerPoint = 12 + 4 + 4;
@@ -142,19 +156,21 @@ private:
 	Arena arena;
 
 	void loop();
-	void launch(Slot& slot, const rgl::BatchSchedule& sched);
+	void launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after);
+	void copyOut(Slot& slot);
 	void retire(Slot& slot);
 	Request& get(int64_t id);
 	static void CUDART_CB batchDone(void* self);
 
 	int64_t budget;
 	int maxInFlight;
-	rgl::BatchSchedule schedule{128, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 96}; // guarded by m
-	int64_t maxBatchBeams = 32 << 20;                                                     // guarded by m
+	rgl::BatchSchedule schedule{128, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 128}; // guarded by m
+	int64_t maxBatchBeams = 8 << 20;                                                       // guarded by m
 	cudaStream_t stream = nullptr;
 	std::vector<std::unique_ptr<Pattern>> patterns;
 	std::vector<std::unique_ptr<Slot>> slots;
 	std::deque<Slot*> inFlight;
+	Slot* lastLaunched = nullptr; // slot of the most recent batch (guarded by m)
 
 	std::mutex m;
 	std::condition_variable cvWork, cvDone;
