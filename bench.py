@@ -887,7 +887,7 @@ def main():
     ap.add_argument("--workload", choices=["single_sensor", "multi_sensor", "serving", "config0", "config1"], default="single_sensor",
                     help="single_sensor: the 1M-tri scan (the headline line); multi_sensor: 64 sensors, batched vs plain loop; "
                          "serving: Poisson scan requests, served vs plain loop")
-    ap.add_argument("--rates", type=lambda v: [float(x) for x in v.split(",")], default=[100, 200, 500, 1000, 2000, 5000],
+    ap.add_argument("--rates", type=lambda v: [float(x) for x in v.split(",")], default=[100, 200, 500, 1000, 2000, 5000, 10000, 15000],
                     help="serving: request rates (per second) to sweep")
     ap.add_argument("--trace-seconds", type=float, default=30.0, help="serving: length of each arrival trace")
     ap.add_argument("--max-lag", type=float, default=5.0, help="serving: stop a trace once the loop lags arrivals by this much (s)")

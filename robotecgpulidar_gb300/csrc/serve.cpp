@@ -35,9 +35,10 @@ TableLayout tableLayout(int n)
 Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmBudgetBytes), maxInFlight(std::max(1, maxInFlightBatches))
 {
 	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-	// Result arena: a quarter of the budget, between 64 MB and 8 GB, rounded down to a power of two
-	// of the minimum block.
-	const size_t want = (size_t) std::min<int64_t>(std::max<int64_t>(budget / 4, 64ll << 20), 8ll << 30);
+	// Result arena: a quarter of the budget, between 64 MB and 32 GB, rounded down to a power of two
+	// of the minimum block. Requests wait for arena space when clients hold results, so the arena
+	// bounds how far a burst of requests runs ahead of the client's reads.
+	const size_t want = (size_t) std::min<int64_t>(std::max<int64_t>(budget / 4, 64ll << 20), 32ll << 30);
 	int order = 0;
 	while ((Arena::kMinBlock << (order + 1)) <= want) {
 		++order;
