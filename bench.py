@@ -452,6 +452,7 @@ def run_multi_sensor(args):
         d2h.append(read_results())
         e2e_b.append(time.perf_counter() - t0)
     sched = rgl.batch_schedule(batch)
+    tuning = [dict(s, ms=round(ms, 4)) for s, ms in rgl.batch_tuning(batch)]
     st = rgl.batch_stats(batch)
     rgl.batch_destroy(batch)
 
@@ -510,7 +511,7 @@ def run_multi_sensor(args):
         "batched": {"device_mrays_s": rays_per_frame * args.steps / (sum(dev_ms) / 1e3) / 1e6, "wall_mrays_s": mrays(wall_b),
                     "frame_ms_p50": pct(wall_b, 0.5), "frame_ms_p99": pct(wall_b, 0.99), "device_frame_ms": statistics.mean(dev_ms),
                     "trace_ms": trace_mean, "e2e_mrays_s": mrays(e2e_b), "e2e_frame_ms_p50": pct(e2e_b, 0.5),
-                    "e2e_frame_ms_p99": pct(e2e_b, 0.99), "schedule": sched, "first_frame_s_incl_tuning": first_frame_s,
+                    "e2e_frame_ms_p99": pct(e2e_b, 0.99), "schedule": sched, "tuning": tuning, "first_frame_s_incl_tuning": first_frame_s,
                     "captures": st["captures"], "replays": st["replays"], "tunings": st["tunings"]},
         "plain_loop": {"wall_mrays_s": mrays(wall_p), "frame_ms_p50": pct(wall_p, 0.5), "frame_ms_p99": pct(wall_p, 0.99),
                        "e2e_mrays_s": mrays(e2e_p), "e2e_frame_ms_p50": pct(e2e_p, 0.5), "e2e_frame_ms_p99": pct(e2e_p, 0.99)},

@@ -141,6 +141,15 @@ RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32
                                                   int32_t* out_order, int32_t* out_chunk, int32_t* out_regs);
 
 /*
+ * The candidates timed by the batch's last tuning, in the order tried: five int32 per candidate
+ * (block, packing, order, chunk, regs) into out_schedules and its traversal time (ms, best of its
+ * repetitions) into out_ms, at most `capacity` candidates; out_count receives the number tried
+ * (0 before any tuning). No counterpart in the reference, which has no batched traversal.
+ */
+RGL_API rgl_status_t rgl_gb300_batch_get_tuning(rgl_gb300_batch_t batch, int32_t capacity, int32_t* out_schedules, float* out_ms,
+                                                int32_t* out_count);
+
+/*
  * Statistics of a batch: device time of the last completed frame and of its traversal launch (ms),
  * beams and traced rays (beams x sub-rays) of the last frame, and the number of captures, replays and
  * tunings so far. Waits for the last frame.

@@ -1386,6 +1386,32 @@ RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32
 	});
 }
 
+RGL_API rgl_status_t rgl_gb300_batch_get_tuning(rgl_gb300_batch_t batch, int32_t capacity, int32_t* out_schedules, float* out_ms,
+                                                int32_t* out_count)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		CHECK_ARG(capacity >= 0);
+		CHECK_ARG(capacity == 0 || (out_schedules != nullptr && out_ms != nullptr));
+		auto b = Batches::get(batch, "Batch");
+		b->synchronize();
+		const auto& t = b->lastTuning;
+		for (size_t i = 0; i < t.size() && (int32_t) i < capacity; ++i) {
+			const rgl::BatchSchedule& s = t[i].s;
+			int32_t* o = out_schedules + 5 * i;
+			o[0] = s.block;
+			o[1] = s.packing;
+			o[2] = s.order;
+			o[3] = s.chunk;
+			o[4] = s.regs;
+			out_ms[i] = t[i].ms;
+		}
+		if (out_count) {
+			*out_count = (int32_t) t.size();
+		}
+	});
+}
+
 RGL_API rgl_status_t rgl_gb300_batch_get_stats(rgl_gb300_batch_t batch, float* out_frame_ms, float* out_trace_ms, int64_t* out_beams,
                                                int64_t* out_rays, int64_t* out_captures, int64_t* out_replays, int64_t* out_tunings)
 {

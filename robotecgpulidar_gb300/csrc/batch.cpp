@@ -249,8 +249,9 @@ float BatchRun::timeTrace(const rgl::BatchSchedule& s, int reps)
 	return best;
 }
 
-// Staged search: packing x beam order first, then the register budget (64, 80, 96, 128), the block
-// size (64, 128, 256) and the chunk (1, 2, 4), each stage keeping the best so far. Every candidate runs the real
+// Staged search: packing x beam order first (128 threads, 128 registers: the setting at which both
+// packings run without spills), then the register budget (64, 80, 96, 128), the block size (64, 128,
+// 256) and the chunk (1, 2, 4), each stage keeping the best so far. Every candidate runs the real
 // traversal of this frame's rays over the current scene; its outputs are overwritten by the frame.
 void BatchRun::tune()
 {
@@ -268,7 +269,7 @@ void BatchRun::tune()
 	for (int order : {rgl::kOrderNatural, rgl::kOrderOctahedral, rgl::kOrderMorton}) {
 		computeOrder(order, stream);
 		for (int packing : {rgl::kPackLaneGroup, rgl::kPackSerial}) {
-			rgl::BatchSchedule s{256, packing, order, 1, packing == rgl::kPackSerial ? 128 : 80};
+			rgl::BatchSchedule s{128, packing, order, 1, 128};
 			const float ms = measure(s);
 			if (ms < bestMs) {
 				bestMs = ms;

@@ -426,8 +426,9 @@ namespace {
 // re-quantises its children in a new frame with the builder's arithmetic. Topology and slots stay.
 __global__ void __launch_bounds__(256) kRefitTlas(WideNode* nodes, const TriRecord* __restrict__ leaves, Box* boxes,
                                                   const InstanceRec* __restrict__ inst, const int32_t* __restrict__ levelStarts,
-                                                  int nLevels)
+                                                  const int32_t* __restrict__ nLevelsWord)
 {
+	const int nLevels = *nLevelsWord;
 	for (int L = nLevels - 1; L >= 0; --L) {
 		const int a = levelStarts[L], b = levelStarts[L + 1];
 		for (int i = a + (int) threadIdx.x; i < b; i += blockDim.x) {
@@ -464,31 +465,125 @@ __global__ void __launch_bounds__(256) kRefitTlas(WideNode* nodes, const TriReco
 	}
 }
 
+// World boxes of the instances (their records' padded boxes) as the builder's primitive boxes.
+__global__ void kTlasBoxes(const InstanceRec* __restrict__ inst, int n, float4* lo, float4* hi)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		const InstanceRec& r = inst[i];
+		lo[i] = make_float4(r.lox, r.loy, r.loz, 0.0f);
+		hi[i] = make_float4(r.hix, r.hiy, r.hiz, 0.0f);
+	}
+}
+
+// The wide collapse of a small binary tree by one block, depth by depth until its queue is empty,
+// recording the first node of every depth and the number of depths (the collapse allocates depth
+// L + 1 while it writes depth L). counters: [0] wide nodes, [1] leaf records, [2], [3] queue counts.
+__global__ void __launch_bounds__(256) kCollapseSmall(int2* qa, int2* qb, uint32_t* counters, CollapseInputs in, WideNode* wide,
+                                                      TriRecord* leaves, Box* boxes, int32_t* levelStarts, int32_t* nLevels, int n)
+{
+	if (threadIdx.x == 0) {
+		counters[0] = 1u;
+		counters[1] = 0u;
+		counters[2] = 1u;
+		qa[0] = make_int2(n == 1 ? ~0 : 0, 0);
+		levelStarts[0] = 0;
+	}
+	uint32_t* ca = counters + 2;
+	uint32_t* cb = counters + 3;
+	int level = 0;
+	for (;; ++level) {
+		__syncthreads();
+		const uint32_t cnt = *(volatile uint32_t*) ca;
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			levelStarts[level + 1] = (int32_t) *(volatile uint32_t*) counters;
+			*cb = 0u;
+		}
+		__syncthreads();
+		if (cnt == 0u || level > n + 1) {
+			break;
+		}
+		const CollapseOutputs out{wide, leaves, counters, counters + 1, qb, cb, boxes};
+		for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+			const int2 it = qa[i];
+			collapseItem(it.x, (uint32_t) it.y, in, out);
+		}
+		int2* tq = qa;
+		qa = qb;
+		qb = tq;
+		uint32_t* tc = ca;
+		ca = cb;
+		cb = tc;
+	}
+	if (threadIdx.x == 0) {
+		*nLevels = level;
+	}
+}
+
 } // namespace
 
 // The TLAS is a wide BVH over the instances' world boxes, one instance per leaf child, built on the
 // device like a mesh BLAS (binned SAH topology, then the wide collapse with one instance per leaf).
 // The node range of every depth (contiguous: the collapse allocates nodes depth by depth) drives the
-// refit kernel, which keeps the topology on pose changes.
-void buildTlas(const InstanceRec* hInst, int n, TlasBuild& t, cudaStream_t s)
+// refit kernel.
+namespace {
+
+void allocTlas(TlasBuild& t, int n)
 {
+	if (n <= t.capacity) {
+		return;
+	}
+	freeTlas(t);
+	t.capacity = n;
+	RGL_CUDA_OK(cudaMalloc(&t.nodes, sizeof(WideNode) * (size_t) n));
+	RGL_CUDA_OK(cudaMalloc(&t.leaves, sizeof(TriRecord) * (size_t) n));
+	RGL_CUDA_OK(cudaMalloc(&t.boxes, sizeof(Box) * (size_t) n));
+	t.levelCapacity = n + 2;
+	RGL_CUDA_OK(cudaMalloc(&t.levelStarts, sizeof(int32_t) * (size_t) t.levelCapacity));
+	RGL_CUDA_OK(cudaMalloc(&t.nLevels, sizeof(int32_t)));
+	if (n <= kSahSmallMax) {
+		RGL_CUDA_OK(cudaMalloc(&t.lo, sizeof(float4) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.hi, sizeof(float4) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.sahScratch, sahSmallScratchBytes(n)));
+		RGL_CUDA_OK(cudaMalloc(&t.bin, sizeof(BinNode) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.rangeFirst, sizeof(int32_t) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.rangeLast, sizeof(int32_t) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.sortedIds, sizeof(uint32_t) * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.queue, sizeof(int2) * 2 * (size_t) n));
+		RGL_CUDA_OK(cudaMalloc(&t.counters, sizeof(uint32_t) * 4));
+	}
+}
+
+// The rebuild of up to kSahSmallMax instances from their device records: four launches, no host
+// interaction, so a captured frame can hold it.
+void rebuildTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
+{
+	const int n = t.nInstances;
+	kTlasBoxes<<<blocks(n, 128), 128, 0, s>>>(dInst, n, t.lo, t.hi);
+	countLaunch();
+	enqueueSahTopologySmall(t.lo, t.hi, n, t.sahScratch, t.bin, t.rangeFirst, t.rangeLast, t.sortedIds, s);
+	const CollapseInputs ci{t.bin, t.rangeFirst, t.rangeLast, reinterpret_cast<const int32_t*>(t.sortedIds), t.lo, t.hi, nullptr, nullptr, 1};
+	kCollapseSmall<<<1, 256, 0, s>>>(t.queue, t.queue + n, t.counters, ci, t.nodes, t.leaves, reinterpret_cast<Box*>(t.boxes),
+	                                 t.levelStarts, t.nLevels, n);
+	countLaunch();
+}
+
+} // namespace
+
+void buildTlas(const InstanceRec* hInst, const InstanceRec* dInst, int n, TlasBuild& t, cudaStream_t s)
+{
+	if (n > 0) {
+		allocTlas(t, n);
+	}
 	t.nInstances = n;
 	t.nodeCount = 0;
-	t.nLevels = 0;
 	if (n <= 0) {
 		return;
 	}
-	if (n > t.capacity) {
-		cudaFree(t.nodes);
-		cudaFree(t.leaves);
-		cudaFree(t.boxes);
-		t.nodes = nullptr;
-		t.leaves = nullptr;
-		t.boxes = nullptr;
-		t.capacity = n;
-		RGL_CUDA_OK(cudaMalloc(&t.nodes, sizeof(WideNode) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.leaves, sizeof(TriRecord) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.boxes, sizeof(Box) * (size_t) n));
+	if (n <= kSahSmallMax) {
+		rebuildTlas(dInst, t, s);
+		return;
 	}
 	std::vector<float4> hLo(n), hHi(n);
 	for (int i = 0; i < n; ++i) {
@@ -511,22 +606,29 @@ void buildTlas(const InstanceRec* hInst, int n, TlasBuild& t, cudaStream_t s)
 	while (levels > 1 && starts[(size_t) levels - 1] == (int32_t) r.nodeCount) {
 		--levels;
 	}
-	if (starts.back() != (int32_t) r.nodeCount || starts[(size_t) levels] != (int32_t) r.nodeCount) {
+	if (starts.back() != (int32_t) r.nodeCount || starts[(size_t) levels] != (int32_t) r.nodeCount || levels + 1 > t.levelCapacity) {
 		throw std::runtime_error("TLAS build: depth ranges do not cover the nodes");
 	}
-	if (levels + 1 > t.levelCapacity) {
-		cudaFree(t.levelStarts);
-		t.levelStarts = nullptr;
-		t.levelCapacity = levels + 1;
-		RGL_CUDA_OK(cudaMalloc(&t.levelStarts, sizeof(int32_t) * (size_t) t.levelCapacity));
-	}
-	t.nLevels = levels;
 	RGL_CUDA_OK(cudaMemcpyAsync(t.levelStarts, starts.data(), sizeof(int32_t) * (size_t) (levels + 1), cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaMemcpyAsync(t.nLevels, &levels, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+	RGL_CUDA_OK(cudaStreamSynchronize(s));
+}
+
+void updateTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
+{
+	if (t.nInstances <= 0) {
+		return;
+	}
+	if (t.nInstances <= kSahSmallMax) {
+		rebuildTlas(dInst, t, s);
+	} else {
+		refitTlas(dInst, t, s);
+	}
 }
 
 void refitTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
 {
-	if (t.nInstances <= 0 || t.nLevels <= 0) {
+	if (t.nInstances <= 0) {
 		return;
 	}
 	kRefitTlas<<<1, 256, 0, s>>>(t.nodes, t.leaves, reinterpret_cast<Box*>(t.boxes), dInst, t.levelStarts, t.nLevels);
@@ -535,10 +637,11 @@ void refitTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
 
 void freeTlas(TlasBuild& t)
 {
-	cudaFree(t.nodes);
-	cudaFree(t.leaves);
-	cudaFree(t.boxes);
-	cudaFree(t.levelStarts);
+	void* ptrs[] = {t.nodes, t.leaves, t.boxes, t.levelStarts, t.nLevels, t.lo, t.hi, t.sahScratch, t.bin, t.rangeFirst,
+	                t.rangeLast, t.sortedIds, t.queue, t.counters};
+	for (void* p : ptrs) {
+		cudaFree(p);
+	}
 	t = TlasBuild{};
 }
 

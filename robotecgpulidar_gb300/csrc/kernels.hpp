@@ -39,6 +39,12 @@ void buildBlas(const float* dVertices, int nVertices, const int32_t* dIndices, i
 // (sah_build.hpp buildBinnedSahTree) computed on the device; output in the collapse's input format.
 void buildSahTopologyDevice(const float4* lo, const float4* hi, int n, BinNode* bin, int32_t* rangeFirst, int32_t* rangeLast,
                             uint32_t* sortedIds, cudaStream_t stream);
+// The same topology for 1..kSahSmallMax boxes, built by one block with no host interaction (so it can
+// be captured in a CUDA graph); `scratch` holds sahSmallScratchBytes(n) bytes.
+constexpr int kSahSmallMax = 2048;
+size_t sahSmallScratchBytes(int n);
+void enqueueSahTopologySmall(const float4* lo, const float4* hi, int n, void* scratch, BinNode* bin, int32_t* rangeFirst,
+                             int32_t* rangeLast, uint32_t* sortedIds, cudaStream_t stream);
 // Builds the BLAS of a mesh on the host from host vertices/indices (binned SAH topology, the same wide
 // collapse) and uploads it; storage of `out` is reused when large enough.
 void buildBlasHost(const float* hVertices, int nVertices, const int32_t* hIndices, int nTris, BlasBuild& out);
@@ -49,17 +55,33 @@ struct TlasBuild
 	WideNode* nodes = nullptr;       // wide nodes over the instances (at most nInstances)
 	TriRecord* leaves = nullptr;     // one record per instance; primId = instance index
 	float* boxes = nullptr;          // float box (6 floats) of every wide node, kept for the refit
-	int32_t* levelStarts = nullptr;  // first node index of each depth, nLevels + 1 entries
-	int32_t nLevels = 0;
+	int32_t* levelStarts = nullptr;  // first node index of each depth, nLevels + 1 entries (device)
+	int32_t* nLevels = nullptr;      // number of depths (device word, read by the refit)
 	int32_t levelCapacity = 0;       // entries allocated for levelStarts
 	int32_t capacity = 0;
 	int32_t nInstances = 0;
-	uint32_t nodeCount = 0;
+	uint32_t nodeCount = 0;          // node count of the last host-synchronous build (statistics)
+	// Scratch of the graph-capturable rebuild (instances up to kSahSmallMax), sized with `capacity`.
+	float4* lo = nullptr;
+	float4* hi = nullptr;
+	void* sahScratch = nullptr;
+	BinNode* bin = nullptr;
+	int32_t* rangeFirst = nullptr;
+	int32_t* rangeLast = nullptr;
+	uint32_t* sortedIds = nullptr;
+	int2* queue = nullptr;           // two collapse queues of `capacity` items each
+	uint32_t* counters = nullptr;    // wide nodes, leaf records, queue counts
 };
-// (Re)builds the TLAS over `nInstances` instance records given in HOST memory, on the device: their world
-// boxes are uploaded, then the binned SAH topology and the wide collapse run on `stream`, which is
-// synchronised at the end (a build happens only when the set of entities changes).
-void buildTlas(const InstanceRec* hInstances, int nInstances, TlasBuild& t, cudaStream_t stream);
+// Builds the TLAS over `nInstances` instance records (host copy hInstances, device copy dInstances,
+// current on `stream`). Up to kSahSmallMax instances it enqueues the graph-capturable rebuild
+// (rebuildTlas); beyond, the multi-block device build, which synchronises `stream`.
+void buildTlas(const InstanceRec* hInstances, const InstanceRec* dInstances, int nInstances, TlasBuild& t, cudaStream_t stream);
+// After instance poses changed (same instance set): a full rebuild of the topology over the new
+// world boxes when it can be enqueued without host interaction (up to kSahSmallMax instances: the
+// instance boxes, one-block binned SAH, one-block wide collapse), otherwise a refit that keeps the
+// topology. A refit only is cheaper but degrades as entities move across the scene: after a few
+// frames of random re-poses the old topology's boxes cover most of the scene.
+void updateTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);
 // Refits the TLAS after instance boxes changed (same instance set): one single-block launch.
 void refitTlas(const InstanceRec* dInstances, TlasBuild& t, cudaStream_t stream);
 void freeTlas(TlasBuild& t);

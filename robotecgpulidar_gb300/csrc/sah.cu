@@ -1034,4 +1034,64 @@ void buildSahTopologyDevice(const float4* lo, const float4* hi, int n, BinNode* 
 	}
 }
 
+namespace {
+static_assert(kBigTask == kSahSmallMax, "one block builds ranges up to kSahSmallMax primitives");
+
+// Root task and control words of a one-block build.
+__global__ void kSahSmallRoot(SahTask* task, uint32_t* ctr, int n)
+{
+	if (threadIdx.x < kCtrWords) {
+		ctr[threadIdx.x] = (threadIdx.x == kCtrNodes || threadIdx.x == kCtrBlock) ? 1u : 0u;
+	}
+	if (threadIdx.x == 0) {
+		task[0] = SahTask{0, n, 0, 0};
+	}
+}
+
+struct SmallScratch
+{
+	float4* cen;
+	uint32_t* ids;
+	SahTask* task;
+	uint32_t* ctr;
+};
+SmallScratch carveSmall(void* scratch, int n)
+{
+	uint8_t* p = static_cast<uint8_t*>(scratch);
+	auto take = [&](size_t bytes) {
+		uint8_t* q = p;
+		p += (bytes + 255) & ~size_t{255};
+		return q;
+	};
+	SmallScratch s;
+	s.cen = reinterpret_cast<float4*>(take(sizeof(float4) * (size_t) n));
+	s.ids = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t) n));
+	s.task = reinterpret_cast<SahTask*>(take(sizeof(SahTask)));
+	s.ctr = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * kCtrWords));
+	return s;
+}
+} // namespace
+
+size_t sahSmallScratchBytes(int n)
+{
+	auto up = [](size_t b) { return (b + 255) & ~size_t{255}; };
+	return up(sizeof(float4) * (size_t) n) + up(sizeof(uint32_t) * (size_t) n) + up(sizeof(SahTask)) + up(sizeof(uint32_t) * kCtrWords);
+}
+
+void enqueueSahTopologySmall(const float4* lo, const float4* hi, int n, void* scratch, BinNode* bin, int32_t* rangeFirst,
+                             int32_t* rangeLast, uint32_t* sortedIds, cudaStream_t s)
+{
+	if (n <= 0 || n > kSahSmallMax) {
+		throw std::runtime_error("SAH build: one-block topology takes 1.." + std::to_string(kSahSmallMax) + " primitives");
+	}
+	const SmallScratch sc = carveSmall(scratch, n);
+	kSahInit<<<blocksFor(n, 256), 256, 0, s>>>(lo, hi, n, sc.cen, sc.ids, sortedIds);
+	countLaunch();
+	if (n >= 2) {
+		kSahSmallRoot<<<1, 32, 0, s>>>(sc.task, sc.ctr, n);
+		kSahBlock<<<1, kThreads, 0, s>>>(sc.task, lo, hi, sc.cen, sortedIds, bin, rangeFirst, rangeLast, sc.ctr);
+		countLaunch(2);
+	}
+}
+
 } // namespace rgl

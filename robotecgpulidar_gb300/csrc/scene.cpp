@@ -454,10 +454,10 @@ void Scene::prepare(cudaStream_t s)
 		RGL_CHECK_CUDA(cudaMemcpyAsync(dInst, rec, sizeof(rgl::InstanceRec) * n, cudaMemcpyHostToDevice, s));
 	}
 	if (topologyDirty || tlas.nInstances != n) {
-		rgl::buildTlas(rec, n, tlas, s);
+		rgl::buildTlas(rec, dInst, n, tlas, s);
 		++tlasBuilds;
 	} else {
-		rgl::refitTlas(dInst, tlas, s);
+		rgl::updateTlas(dInst, tlas, s);
 		++tlasRefits;
 	}
 	auto* v = static_cast<rgl::SceneView*>(hView.ensure(sizeof(rgl::SceneView)));
@@ -492,7 +492,7 @@ void Scene::enqueueRefit(cudaStream_t s)
 		return;
 	}
 	RGL_CHECK_CUDA(cudaMemcpyAsync(dInstances.get(), hInstances.get(), sizeof(rgl::InstanceRec) * n, cudaMemcpyHostToDevice, s));
-	rgl::refitTlas(dInstances.as<rgl::InstanceRec>(), tlas, s);
+	rgl::updateTlas(dInstances.as<rgl::InstanceRec>(), tlas, s);
 }
 
 void Scene::recordReady(cudaStream_t s)

@@ -200,6 +200,7 @@ def _proto(l):
         "rgl_gb300_batch_configure_schedule": [vp, C.c_bool, i32, i32, i32, i32, i32],
         "rgl_gb300_batch_get_schedule": [vp, P(i32), P(i32), P(i32), P(i32), P(i32)],
         "rgl_gb300_batch_get_stats": [vp, P(f), P(f), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)],
+        "rgl_gb300_batch_get_tuning": [vp, i32, P(i32), P(f), P(i32)],
         "rgl_gb300_configure_trace_schedule": [i32, i32, i32, i32],
         "rgl_gb300_scene_create": [P(vp)],
         "rgl_gb300_scene_destroy": [vp],
@@ -462,6 +463,17 @@ def batch_schedule(b) -> dict:
     v = [C.c_int32() for _ in range(5)]
     check(lib().rgl_gb300_batch_get_schedule(b, *[C.byref(x) for x in v]))
     return dict(zip(["block", "packing", "order", "chunk", "regs"], [x.value for x in v]))
+
+
+def batch_tuning(b) -> list:
+    """The last tuning's candidates: [(schedule dict, ms), ...] in the order tried."""
+    n = C.c_int32()
+    check(lib().rgl_gb300_batch_get_tuning(b, 0, None, None, C.byref(n)))
+    sch = (C.c_int32 * (5 * max(1, n.value)))()
+    ms = (C.c_float * max(1, n.value))()
+    check(lib().rgl_gb300_batch_get_tuning(b, n.value, sch, ms, C.byref(n)))
+    keys = ["block", "packing", "order", "chunk", "regs"]
+    return [(dict(zip(keys, sch[5 * i:5 * i + 5])), ms[i]) for i in range(n.value)]
 
 
 def batch_stats(b) -> dict:

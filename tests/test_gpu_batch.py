@@ -140,9 +140,15 @@ def test_batched_frame_equals_solo_runs(rgl, sched):
     st = rgl.batch_stats(batch)
     assert st["beams"] == sum(pattern_rays(c["rays"]).shape[0] for c in SENSORS)
     assert st["frame_ms"] > 0 and st["trace_ms"] > 0
+    tuning = rgl.batch_tuning(batch)
     if sched["autotune"]:
         assert st["tunings"] == 1
+        # Every stage is recorded; the kept schedule is the fastest candidate tried.
+        assert len(tuning) >= 12 and all(ms > 0 for _, ms in tuning)
+        assert {(s["packing"], s["order"]) for s, _ in tuning[:6]} == {(p, o) for p in (0, 1) for o in (0, 1, 2)}
+        assert rgl.batch_schedule(batch) == min(tuning, key=lambda c: c[1])[0]
     else:
+        assert tuning == []
         assert rgl.batch_schedule(batch) == {k: v for k, v in sched.items() if k != "autotune"}
     assert_same(rgl, batched, solo_results(rgl, graphs))
     rgl.batch_destroy(batch)
