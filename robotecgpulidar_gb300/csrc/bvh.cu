@@ -476,19 +476,68 @@ __global__ void kTlasBoxes(const InstanceRec* __restrict__ inst, int n, float4* 
 	}
 }
 
-// The wide collapse of a small binary tree by one block, depth by depth until its queue is empty,
-// recording the first node of every depth and the number of depths (the collapse allocates depth
-// L + 1 while it writes depth L). counters: [0] wide nodes, [1] leaf records, [2], [3] queue counts.
-__global__ void __launch_bounds__(256) kCollapseSmall(int2* qa, int2* qb, uint32_t* counters, CollapseInputs in, WideNode* wide,
-                                                      TriRecord* leaves, Box* boxes, int32_t* levelStarts, int32_t* nLevels, int n)
+// Shared-memory layout of the one-block collapse over n primitives (16-byte aligned parts): primitive
+// boxes lo[n] | hi[n] | binary nodes[n - 1] | two queues[n] | sorted ids[n] | ranges first[n - 1],
+// last[n - 1] | counters[4].
+struct SmallCollapseLayout
 {
+	size_t lo, hi, bin, q0, q1, ids, rf, rl, ctr, bytes;
+};
+__host__ __device__ SmallCollapseLayout smallCollapseLayout(int n)
+{
+	auto up = [](size_t b) { return (b + 15) & ~size_t{15}; };
+	const size_t m = (size_t) (n > 1 ? n - 1 : 1);
+	SmallCollapseLayout L;
+	L.lo = 0;
+	L.hi = L.lo + up(sizeof(float4) * (size_t) n);
+	L.bin = L.hi + up(sizeof(float4) * (size_t) n);
+	L.q0 = L.bin + up(sizeof(BinNode) * m);
+	L.q1 = L.q0 + up(sizeof(int2) * (size_t) n);
+	L.ids = L.q1 + up(sizeof(int2) * (size_t) n);
+	L.rf = L.ids + up(sizeof(int32_t) * (size_t) n);
+	L.rl = L.rf + up(sizeof(int32_t) * m);
+	L.ctr = L.rl + up(sizeof(int32_t) * m);
+	L.bytes = L.ctr + 16;
+	return L;
+}
+
+// The wide collapse of a small binary tree by one block, depth by depth until its queue is empty. The
+// tree, the primitive boxes, the queues and the counters live in shared memory, so each depth costs
+// shared-memory latency, not a chain of global loads. Records the first node of every depth and the
+// number of depths (the collapse allocates depth L + 1 while it writes depth L).
+__global__ void __launch_bounds__(256) kCollapseSmall(CollapseInputs gin, WideNode* wide, TriRecord* leaves, Box* boxes,
+                                                      int32_t* levelStarts, int32_t* nLevels, int n)
+{
+	extern __shared__ __align__(16) uint8_t smem[];
+	const SmallCollapseLayout L = smallCollapseLayout(n);
+	float4* lo = reinterpret_cast<float4*>(smem + L.lo);
+	float4* hi = reinterpret_cast<float4*>(smem + L.hi);
+	BinNode* bin = reinterpret_cast<BinNode*>(smem + L.bin);
+	int2* qa = reinterpret_cast<int2*>(smem + L.q0);
+	int2* qb = reinterpret_cast<int2*>(smem + L.q1);
+	int32_t* ids = reinterpret_cast<int32_t*>(smem + L.ids);
+	int32_t* rf = reinterpret_cast<int32_t*>(smem + L.rf);
+	int32_t* rl = reinterpret_cast<int32_t*>(smem + L.rl);
+	uint32_t* counters = reinterpret_cast<uint32_t*>(smem + L.ctr);
+	for (int i = threadIdx.x; i < n; i += blockDim.x) {
+		lo[i] = gin.triLo[i];
+		hi[i] = gin.triHi[i];
+		ids[i] = gin.sortedIds[i];
+	}
+	for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+		bin[i] = gin.bin[i];
+		rf[i] = gin.rangeFirst[i];
+		rl[i] = gin.rangeLast[i];
+	}
 	if (threadIdx.x == 0) {
-		counters[0] = 1u;
-		counters[1] = 0u;
-		counters[2] = 1u;
+		counters[0] = 1u; // wide nodes (the root)
+		counters[1] = 0u; // leaf records
+		counters[2] = 1u; // items in qa
+		counters[3] = 0u;
 		qa[0] = make_int2(n == 1 ? ~0 : 0, 0);
 		levelStarts[0] = 0;
 	}
+	const CollapseInputs in{bin, rf, rl, ids, lo, hi, nullptr, nullptr, gin.leafMax};
 	uint32_t* ca = counters + 2;
 	uint32_t* cb = counters + 3;
 	int level = 0;
@@ -550,8 +599,8 @@ void allocTlas(TlasBuild& t, int n)
 		RGL_CUDA_OK(cudaMalloc(&t.rangeFirst, sizeof(int32_t) * (size_t) n));
 		RGL_CUDA_OK(cudaMalloc(&t.rangeLast, sizeof(int32_t) * (size_t) n));
 		RGL_CUDA_OK(cudaMalloc(&t.sortedIds, sizeof(uint32_t) * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.queue, sizeof(int2) * 2 * (size_t) n));
-		RGL_CUDA_OK(cudaMalloc(&t.counters, sizeof(uint32_t) * 4));
+		// Shared memory of the one-block collapse for up to n instances (set outside any capture).
+		RGL_CUDA_OK(cudaFuncSetAttribute(kCollapseSmall, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smallCollapseLayout(n).bytes));
 	}
 }
 
@@ -564,8 +613,8 @@ void rebuildTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
 	countLaunch();
 	enqueueSahTopologySmall(t.lo, t.hi, n, t.sahScratch, t.bin, t.rangeFirst, t.rangeLast, t.sortedIds, s);
 	const CollapseInputs ci{t.bin, t.rangeFirst, t.rangeLast, reinterpret_cast<const int32_t*>(t.sortedIds), t.lo, t.hi, nullptr, nullptr, 1};
-	kCollapseSmall<<<1, 256, 0, s>>>(t.queue, t.queue + n, t.counters, ci, t.nodes, t.leaves, reinterpret_cast<Box*>(t.boxes),
-	                                 t.levelStarts, t.nLevels, n);
+	kCollapseSmall<<<1, 256, smallCollapseLayout(n).bytes, s>>>(ci, t.nodes, t.leaves, reinterpret_cast<Box*>(t.boxes), t.levelStarts,
+	                                                            t.nLevels, n);
 	countLaunch();
 }
 
@@ -638,7 +687,7 @@ void refitTlas(const InstanceRec* dInst, TlasBuild& t, cudaStream_t s)
 void freeTlas(TlasBuild& t)
 {
 	void* ptrs[] = {t.nodes, t.leaves, t.boxes, t.levelStarts, t.nLevels, t.lo, t.hi, t.sahScratch, t.bin, t.rangeFirst,
-	                t.rangeLast, t.sortedIds, t.queue, t.counters};
+	                t.rangeLast, t.sortedIds};
 	for (void* p : ptrs) {
 		cudaFree(p);
 	}

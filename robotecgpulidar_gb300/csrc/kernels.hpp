@@ -69,8 +69,6 @@ struct TlasBuild
 	int32_t* rangeFirst = nullptr;
 	int32_t* rangeLast = nullptr;
 	uint32_t* sortedIds = nullptr;
-	int2* queue = nullptr;           // two collapse queues of `capacity` items each
-	uint32_t* counters = nullptr;    // wide nodes, leaf records, queue counts
 };
 // Builds the TLAS over `nInstances` instance records (host copy hInstances, device copy dInstances,
 // current on `stream`). Up to kSahSmallMax instances it enqueues the graph-capturable rebuild
