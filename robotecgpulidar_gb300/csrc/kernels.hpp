@@ -155,10 +155,15 @@ struct SegCompactJob
 	float* outDist;
 	int32_t* outEnt;
 	int32_t nPoints;
-	int32_t pad;
+	int32_t packed; // 1: the segment's output is one block, xyz | distance | entity id of its kept points
+	                // back to back from outXyz (distance at outXyz + 3 * kept, entity id at + 4 * kept);
+	                // outDist and outEnt are not read
 };
 // dTileBase: nSeg + 1 prefix sums of ceil(nPoints / kSegTile) per segment; dCounts receives the
 // kept count of every segment.
+// Copies n words from device memory into pinned host memory through the device's mapping (a kernel,
+// not the copy engine, so it never waits behind other streams' copies).
+void launchPublishWords(const int32_t* src, int32_t* dstMappedHost, int n, cudaStream_t stream);
 void launchSegCompact(const SegCompactJob* dSegs, const int32_t* dTileBase, int nSeg, int totalTiles, uint32_t* dTileCounts,
                       uint32_t* dTileOffsets, int32_t* dCounts, cudaStream_t s);
 

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(1024) kSegScan(const int32_t* __restrict__ til
 }
 
 __global__ void __launch_bounds__(kThreads) kSegScatter(const SegCompactJob* __restrict__ segs, const int32_t* __restrict__ tileBase,
-                                                        int nSeg, const uint32_t* __restrict__ tileOffsets)
+                                                        int nSeg, const uint32_t* __restrict__ tileOffsets, const int32_t* __restrict__ counts)
 {
 	extern __shared__ int32_t sBase[];
 	__shared__ uint32_t warpCounts[kThreads / 32];
@@ -181,11 +181,18 @@ __global__ void __launch_bounds__(kThreads) kSegScatter(const SegCompactJob* __r
 	for (uint32_t w = threadIdx.x; w < 3 * kept; w += kThreads) {
 		ox[w] = sXyz[w];
 	}
-	float* od = sg.outDist + base;
-	int32_t* oe = sg.outEnt + base;
+	float* od = (sg.packed ? sg.outXyz + 3 * (size_t) counts[j] : sg.outDist) + base;
+	int32_t* oe = (sg.packed ? reinterpret_cast<int32_t*>(sg.outXyz + 4 * (size_t) counts[j]) : sg.outEnt) + base;
 	for (uint32_t w = threadIdx.x; w < kept; w += kThreads) {
 		od[w] = sDist[w];
 		oe[w] = sEnt[w];
+	}
+}
+
+__global__ void kPublishWords(const int32_t* __restrict__ src, volatile int32_t* dst, int n)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		dst[i] = src[i];
 	}
 }
 
@@ -197,6 +204,16 @@ void check(cudaError_t e, const char* what)
 }
 
 } // namespace
+
+void launchPublishWords(const int32_t* src, int32_t* dstMappedHost, int n, cudaStream_t s)
+{
+	if (n <= 0) {
+		return;
+	}
+	kPublishWords<<<1, 256, 0, s>>>(src, dstMappedHost, n);
+	countLaunch();
+	check(cudaGetLastError(), "publish");
+}
 
 void launchSegCompact(const SegCompactJob* dSegs, const int32_t* dTileBase, int nSeg, int totalTiles, uint32_t* dTileCounts,
                       uint32_t* dTileOffsets, int32_t* dCounts, cudaStream_t s)
@@ -212,7 +229,7 @@ void launchSegCompact(const SegCompactJob* dSegs, const int32_t* dTileBase, int 
 	kSegScan<<<nSeg, 1024, 0, s>>>(dTileBase, dTileCounts, dTileOffsets, dCounts);
 	countLaunch();
 	if (totalTiles > 0) {
-		kSegScatter<<<totalTiles, kThreads, smem, s>>>(dSegs, dTileBase, nSeg, dTileOffsets);
+		kSegScatter<<<totalTiles, kThreads, smem, s>>>(dSegs, dTileBase, nSeg, dTileOffsets, dCounts);
 		countLaunch();
 	}
 	check(cudaGetLastError(), "launch");

@@ -47,15 +47,19 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 	arena.freeByOrder.assign(order + 1, {});
 	arena.freeByOrder[order].insert(0);
 	void* h = nullptr;
-	RGL_CHECK_CUDA(cudaHostAlloc(&h, Arena::kMinBlock << order, cudaHostAllocMapped | cudaHostAllocPortable));
-	void* d = nullptr;
-	RGL_CHECK_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+	RGL_CHECK_CUDA(cudaHostAlloc(&h, Arena::kMinBlock << order, cudaHostAllocPortable));
 	arena.host = static_cast<uint8_t*>(h);
-	arena.dev = static_cast<uint8_t*>(d);
-	// The device writes every page of the arena once now, so the first batches that land in a page
-	// do not pay the device's first access to it.
-	RGL_CHECK_CUDA(cudaMemsetAsync(d, 0, Arena::kMinBlock << order, stream));
-	RGL_CHECK_CUDA(cudaStreamSynchronize(stream));
+	// The copy engine writes every page of the arena once now (the path the result copies take), so
+	// the first batches that land in a page do not pay the first access to it.
+	{
+		const size_t total = Arena::kMinBlock << order, piece = std::min<size_t>(total, 64u << 20);
+		rgl::DeviceBuffer zeros{false};
+		RGL_CHECK_CUDA(cudaMemsetAsync(zeros.ensure(piece), 0, piece, stream));
+		for (size_t off = 0; off < total; off += piece) {
+			RGL_CHECK_CUDA(cudaMemcpyAsync(arena.host + off, zeros.get(), std::min(piece, total - off), cudaMemcpyDeviceToHost, stream));
+		}
+		RGL_CHECK_CUDA(cudaStreamSynchronize(stream));
+	}
 	for (int i = 0; i < maxInFlight; ++i) {
 		auto s = std::make_unique<Slot>();
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
@@ -77,7 +81,10 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 		}
 		sl->hTables.ensure(most.bytes);
 		sl->tables.ensure(most.bytes);
-		sl->hResults.ensure(sizeof(int32_t) * 2 * rgl::kMaxBatchJobs);
+		void* hr = sl->hResults.ensure(sizeof(int32_t) * 2 * rgl::kMaxBatchJobs);
+		void* hrDev = nullptr;
+		RGL_CHECK_CUDA(cudaHostGetDevicePointer(&hrDev, hr, 0));
+		sl->hResultsDev = static_cast<int32_t*>(hrDev);
 		sl->results.ensure(sizeof(int32_t) * 2 * rgl::kMaxBatchJobs);
 	}
 	worker = std::thread([this] { loop(); });
@@ -313,7 +320,7 @@ const void* Server::resultHost(int64_t id, rgl_field_t field, int32_t& count)
 	if (field == RGL_FIELD_XYZ_VEC3_F32) {
 		return base;
 	}
-	return field == RGL_FIELD_DISTANCE_F32 ? base + 3 * r.points : base + 4 * r.points;
+	return field == RGL_FIELD_DISTANCE_F32 ? base + 3 * (size_t) r.count : base + 4 * (size_t) r.count;
 }
 
 void Server::resultData(int64_t id, rgl_field_t field, void* dst)
@@ -380,9 +387,7 @@ void Server::reserveRaw(Slot& slot, int64_t points, int64_t tiles)
 	grow(slot.rawXyz, sizeof(float) * 3 * (size_t) points);
 	grow(slot.rawDist, sizeof(float) * (size_t) points);
 	grow(slot.rawEnt, sizeof(int32_t) * (size_t) points);
-	grow(slot.outXyz, sizeof(float) * 3 * (size_t) points);
-	grow(slot.outDist, sizeof(float) * (size_t) points);
-	grow(slot.outEnt, sizeof(int32_t) * (size_t) points);
+	grow(slot.staged, sizeof(float) * 5 * (size_t) points);
 	grow(slot.tileCounts, sizeof(uint32_t) * (size_t) tiles);
 	grow(slot.tileOffsets, sizeof(uint32_t) * (size_t) tiles);
 }
@@ -415,9 +420,7 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after)
 	auto* xyz = slot.rawXyz.as<float>();
 	auto* dist = slot.rawDist.as<float>();
 	auto* ent = slot.rawEnt.as<int32_t>();
-	auto* outXyz = slot.outXyz.as<float>();
-	auto* outDist = slot.outDist.as<float>();
-	auto* outEnt = slot.outEnt.as<int32_t>();
+	auto* staged = slot.staged.as<float>();
 	slot.pointBase.assign((size_t) n, 0);
 
 	const TableLayout lay = tableLayout(n);
@@ -467,10 +470,11 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after)
 		sg.xyz = xyz + 3 * pointBase;
 		sg.dist = dist + pointBase;
 		sg.ent = ent + pointBase;
-		sg.outXyz = outXyz + 3 * pointBase;
-		sg.outDist = outDist + pointBase;
-		sg.outEnt = outEnt + pointBase;
+		sg.outXyz = staged + 5 * pointBase; // the request's block: room for 5 words per point
+		sg.outDist = nullptr;
+		sg.outEnt = nullptr;
 		sg.nPoints = (int32_t) r.points;
+		sg.packed = 1;
 		segs[j] = sg;
 		slot.pointBase[(size_t) j] = pointBase;
 		tileBase[j] = (int32_t) tiles;
@@ -492,34 +496,29 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after)
 	                      sched, slot.counter.as<uint32_t>(), slot.stream);
 	rgl::launchSegCompact(reinterpret_cast<const rgl::SegCompactJob*>(dBase + offSeg), reinterpret_cast<const int32_t*>(dBase + offTile), n,
 	                      (int) tiles, static_cast<uint32_t*>(dTileCounts), static_cast<uint32_t*>(dTileOffsets), dResults, slot.stream);
-	auto* hResults = static_cast<int32_t*>(slot.hResults.ensure(sizeof(int32_t) * 2 * n));
-	RGL_CHECK_CUDA(cudaMemcpyAsync(hResults, dResults, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, slot.stream));
+	// Counts and error flags reach pinned host memory by a kernel's stores: a copy would queue behind
+	// the other slot's result copies on the copy engine, and this batch's successor waits for it.
+	rgl::launchPublishWords(dResults, slot.hResultsDev, 2 * n, slot.stream);
 	RGL_CHECK_CUDA(cudaEventRecord(slot.counted, slot.stream));
 	slot.phase = Phase::Tracing;
 	RGL_CHECK_CUDA(cudaLaunchHostFunc(slot.stream, &Server::batchDone, this));
 }
 
-// Once a batch's kept counts are in host memory: the copies of exactly the kept points of every
-// request from the slot's staging buffers into the request's block of the result arena, on the
-// slot's stream (copy engine), then the batch's completion.
+// Once a batch's kept counts are in host memory: one copy per request of exactly its kept points'
+// block (xyz, distances, entity ids back to back) from the slot's staging buffer into the request's
+// block of the result arena, on the slot's stream (copy engine), then the batch's completion.
 void Server::copyOut(Slot& slot)
 {
-	const auto* hCounts = static_cast<const int32_t*>(slot.hResults.get());
+	const auto* hCounts = static_cast<const volatile int32_t*>(slot.hResults.get());
 	const size_t n = slot.reqs.size();
-	const auto* outXyz = slot.outXyz.as<float>();
-	const auto* outDist = slot.outDist.as<float>();
-	const auto* outEnt = slot.outEnt.as<int32_t>();
+	const auto* staged = slot.staged.as<float>();
 	for (size_t j = 0; j < n; ++j) {
 		const Request& r = *slot.reqs[j];
 		const int64_t kept = hCounts[j];
 		if (hCounts[n + j] != 0 || kept <= 0 || kept > r.points) {
 			continue; // failed (retire reports it) or nothing kept
 		}
-		const int64_t b = slot.pointBase[j];
-		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut, outXyz + 3 * b, sizeof(float) * 3 * (size_t) kept, cudaMemcpyDeviceToHost, slot.stream));
-		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut + 3 * r.points, outDist + b, sizeof(float) * (size_t) kept, cudaMemcpyDeviceToHost,
-		                               slot.stream));
-		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut + 4 * r.points, outEnt + b, sizeof(int32_t) * (size_t) kept, cudaMemcpyDeviceToHost,
+		RGL_CHECK_CUDA(cudaMemcpyAsync(r.hostOut, staged + 5 * slot.pointBase[j], sizeof(float) * 5 * (size_t) kept, cudaMemcpyDeviceToHost,
 		                               slot.stream));
 	}
 	RGL_CHECK_CUDA(cudaEventRecord(slot.t1, slot.stream));

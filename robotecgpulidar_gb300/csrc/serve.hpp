@@ -92,8 +92,8 @@ private:
 		float minRange, maxRange;
 		int64_t beams, points;
 		int64_t reservedBytes;
-		// Result block in the pinned arena: xyz | distance | entity id, `points` capacity each, filled
-		// by the batch's result copies.
+		// Result block in the pinned arena (room for `points` points), filled by one copy: xyz of the
+		// kept points, then their distances, then their entity ids, back to back.
 		float* hostOut = nullptr;
 		size_t outOffset = 0;
 		int outOrder = -1;
@@ -127,8 +127,9 @@ private:
 		cudaEvent_t t0 = nullptr, t1 = nullptr; // device time of the batch
 		rgl::DeviceBuffer tables{false}, tileCounts{false}, tileOffsets{false}, results{false}, counter{false};
 		rgl::DeviceBuffer rawFlags{false}, rawXyz{false}, rawDist{false}, rawEnt{false};
-		rgl::DeviceBuffer outXyz{false}, outDist{false}, outEnt{false}; // compacted results before the copies
+		rgl::DeviceBuffer staged{false}; // compacted results: per request one block, xyz | distance | entity id
 		rgl::PinnedBuffer hTables, hResults;
+		int32_t* hResultsDev = nullptr; // device address of hResults (written by a kernel, not a copy)
 		Phase phase = Phase::Tracing;
 		bool busy = false;
 	};
@@ -145,7 +146,6 @@ private:
 	struct Arena
 	{
 		uint8_t* host = nullptr;
-		uint8_t* dev = nullptr;
 		int maxOrder = 0;
 		std::vector<std::set<size_t>> freeByOrder; // block offsets
 		static constexpr size_t kMinBlock = 64 << 10;
