@@ -756,12 +756,16 @@ void CompactByFieldPointsNode::sizeBuffers(const std::vector<rgl_field_t>& which
 void CompactByFieldPointsNode::prepareImpl(cudaStream_t s)
 {
 	sizeBuffers(std::vector<rgl_field_t>(eager.begin(), eager.end()));
-	hCount.ensure(sizeof(int32_t));
+	if (hCountDev == nullptr) {
+		void* d = nullptr;
+		RGL_CHECK_CUDA(cudaHostGetDevicePointer(&d, hCount.ensure(sizeof(int32_t)), 0));
+		hCountDev = static_cast<int32_t*>(d);
+	}
 	lastStream = s;
 	lazyDone.clear();
 }
 
-void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cudaStream_t s)
+void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cudaStream_t s, int32_t* hostCount)
 {
 	const size_t cap = input->capacity();
 	rgl::FieldCopies fc{};
@@ -794,14 +798,14 @@ void CompactByFieldPointsNode::compact(const std::vector<rgl_field_t>& which, cu
 	}
 	rgl::launchCompact(static_cast<const int32_t*>(input->fieldDev(field)), (int) cap, input->deviceCount(), fc,
 	                   ops.count > 0 || ops.xyzField >= 0 || ops.distField >= 0 ? &ops : nullptr, count.as<int32_t>(), scratch.get(),
-	                   errorFlag.device(), s);
+	                   errorFlag.device(), s, hostCount);
 }
 
 void CompactByFieldPointsNode::enqueueImpl(cudaStream_t s)
 {
-	compact(std::vector<rgl_field_t>(eager.begin(), eager.end()), s);
-	// The count reaches the host with the run: reading results needs no extra blocking copy.
-	RGL_CHECK_CUDA(cudaMemcpyAsync(hCount.get(), count.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+	// The count reaches the host with the run, stored by the kernel into the mapped pinned word:
+	// reading results needs no blocking copy, and the run has no copy node waiting on the copy engine.
+	compact(std::vector<rgl_field_t>(eager.begin(), eager.end()), s, hCountDev);
 }
 
 const void* CompactByFieldPointsNode::fieldDev(rgl_field_t f)

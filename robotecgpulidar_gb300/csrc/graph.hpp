@@ -421,11 +421,12 @@ private:
 	std::shared_ptr<PointsNode> chainSource;   // input of chain.front()
 	rgl::DeviceBuffer count;
 	rgl::PinnedBuffer hCount;
+	int32_t* hCountDev = nullptr; // device address of hCount (the kernel stores the count there)
 	rgl::DeviceBuffer scratch;
 	rgl::ErrorSlot errorFlag;
 	cudaStream_t lastStream = nullptr;
 	void sizeBuffers(const std::vector<rgl_field_t>& which);
-	void compact(const std::vector<rgl_field_t>& which, cudaStream_t s);
+	void compact(const std::vector<rgl_field_t>& which, cudaStream_t s, int32_t* hostCount = nullptr);
 };
 
 struct TransformPointsNode : PointwisePointsNode

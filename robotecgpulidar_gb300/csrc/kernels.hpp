@@ -264,8 +264,10 @@ size_t compactScratchBytes(int cap);
 // Writes the kept count to *dOutCount. `scratch` (compactScratchBytes) is zero before the first launch
 // and each launch leaves it zero. With `ops`, the fields at ops->xyzField / ops->distField are
 // computed from the chain's source instead of copied.
+// hostCount (optional): pinned host memory mapped for the device that also receives the kept count,
+// written by the kernel (no copy node after it).
 void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, const PointOps* ops,
-                   int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s);
+                   int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s, int32_t* hostCount = nullptr);
 // AoS packing: point i, field k -> out + i*pointSize + offset_k; padding fields (src == null) are zeroed.
 void launchFormat(const FieldCopies& fields, int pointSize, int cap, const int32_t* dCount, uint8_t* out, cudaStream_t s);
 // AoS -> SoA split for points given as an array (rgl_node_points_from_array).

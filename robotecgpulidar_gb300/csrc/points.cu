@@ -187,7 +187,7 @@ static_assert(sizeof(NoiseParams) % 16 == 0 && sizeof(Mat34) <= sizeof(NoisePara
 __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ flags, int cap, const int32_t* dInCount,
                                                    const __grid_constant__ FieldCopies fc, const __grid_constant__ PointOps ops,
                                                    int32_t* dOutCount, uint32_t* scratch,
-                                                   int32_t* errorFlag)
+                                                   int32_t* errorFlag, int32_t* hostCount)
 {
 	__shared__ uint32_t warpSums[kBlock / 32];
 	__shared__ uint32_t tileBase, tileKept;
@@ -315,6 +315,9 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 		const int tiles = (cap + kCompactTile - 1) / kCompactTile;
 		if (tile == tiles - 1) {
 			*dOutCount = (int32_t) (prefix + run);
+			if (hostCount) {
+				*(volatile int32_t*) hostCount = (int32_t) (prefix + run);
+			}
 		}
 	}
 	__syncthreads();
@@ -671,7 +674,7 @@ void launchNoiseDistance(const float* inXyz, const float* inDist, float* outXyz,
 size_t compactScratchBytes(int cap) { return sizeof(uint32_t) * (size_t) (2 + (cap + kCompactTile - 1) / kCompactTile); }
 
 void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const FieldCopies& fields, const PointOps* ops,
-                   int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s)
+                   int32_t* dOutCount, void* scratch, int32_t* dError, cudaStream_t s, int32_t* hostCount)
 {
 	PointOps po{};
 	if (ops != nullptr) {
@@ -682,10 +685,13 @@ void launchCompact(const int32_t* flags, int cap, const int32_t* dInCount, const
 	}
 	if (cap <= 0) {
 		cudaMemsetAsync(dOutCount, 0, sizeof(int32_t), s);
+		if (hostCount) {
+			cudaMemsetAsync(hostCount, 0, sizeof(int32_t), s);
+		}
 		return;
 	}
 	int tiles = (cap + kCompactTile - 1) / kCompactTile;
-	kCompact<<<tiles, kBlock, 0, s>>>(flags, cap, dInCount, fields, po, dOutCount, static_cast<uint32_t*>(scratch), dError);
+	kCompact<<<tiles, kBlock, 0, s>>>(flags, cap, dInCount, fields, po, dOutCount, static_cast<uint32_t*>(scratch), dError, hostCount);
 	countLaunch();
 }
 
