@@ -375,9 +375,10 @@ REPOSE_FRACTION = 0.2
 
 def run_multi_sensor(args):
     """64 uneven sensors on the 1M-triangle scene, 20 % of the entities re-posed every frame. Times
-    the batched frame (rgl_gb300_batch_run: one CUDA graph with the refit, every sensor's nodes and one
-    persistent traversal launch) against the plain loop of one rgl_graph_run per sensor graph, both
-    over the same graphs and poses."""
+    the batched frame (rgl_gb300_batch_run: the refit, then per wave of sensors one CUDA graph with
+    their nodes and one persistent traversal launch) against the plain loop of one rgl_graph_run per
+    sensor graph, both over the same graphs and poses. Besides the device-only frame, both are timed
+    end to end: run, then read every graph's XYZ, distance and entity id into pinned host buffers."""
     from robotecgpulidar_gb300 import build as b
 
     b.build()
@@ -424,6 +425,7 @@ def run_multi_sensor(args):
     clocks.start()
     # ---- batched frames
     batch = rgl.batch_create([g["rays"] for g in graphs])
+    rgl.batch_configure_waves(batch, args.waves)
     t0 = time.perf_counter()
     repose()
     rgl.batch_run(batch)
@@ -434,11 +436,13 @@ def run_multi_sensor(args):
         rgl.batch_run(batch)
     rgl.batch_stats(batch)
     launches0 = rgl.kernel_launch_count()
-    dev_ms, trace_ms, wall_b = [], [], []
+    dev_ms, trace_ms, wall_b, call_b = [], [], [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         repose()
+        t1 = time.perf_counter()
         rgl.batch_run(batch)
+        call_b.append(time.perf_counter() - t1)
         st = rgl.batch_stats(batch)  # waits for the frame
         wall_b.append(time.perf_counter() - t0)
         dev_ms.append(st["frame_ms"])
@@ -452,6 +456,7 @@ def run_multi_sensor(args):
         d2h.append(read_results())
         e2e_b.append(time.perf_counter() - t0)
     sched = rgl.batch_schedule(batch)
+    waves = rgl.batch_waves(batch)
     tuning = [dict(s, ms=round(ms, 4)) for s, ms in rgl.batch_tuning(batch)]
     st = rgl.batch_stats(batch)
     rgl.batch_destroy(batch)
@@ -462,12 +467,14 @@ def run_multi_sensor(args):
         for g in graphs:
             rgl.graph_run(g["rays"])
         sync_all()
-    wall_p, e2e_p = [], []
+    wall_p, e2e_p, call_p = [], [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         repose()
+        t1 = time.perf_counter()
         for g in graphs:
             rgl.graph_run(g["rays"])
+        call_p.append(time.perf_counter() - t1)
         sync_all()
         wall_p.append(time.perf_counter() - t0)
     for _ in range(args.steps):
@@ -512,14 +519,16 @@ def run_multi_sensor(args):
                     "frame_ms_p50": pct(wall_b, 0.5), "frame_ms_p99": pct(wall_b, 0.99), "device_frame_ms": statistics.mean(dev_ms),
                     "trace_ms": trace_mean, "e2e_mrays_s": mrays(e2e_b), "e2e_frame_ms_p50": pct(e2e_b, 0.5),
                     "e2e_frame_ms_p99": pct(e2e_b, 0.99), "schedule": sched, "tuning": tuning, "first_frame_s_incl_tuning": first_frame_s,
-                    "captures": st["captures"], "replays": st["replays"], "tunings": st["tunings"]},
+                    "host_run_call_ms_p50": pct(call_b, 0.5), "waves": waves, "captures": st["captures"], "replays": st["replays"], "tunings": st["tunings"]},
         "plain_loop": {"wall_mrays_s": mrays(wall_p), "frame_ms_p50": pct(wall_p, 0.5), "frame_ms_p99": pct(wall_p, 0.99),
+                       "host_run_calls_ms_p50": pct(call_p, 0.5),
                        "e2e_mrays_s": mrays(e2e_p), "e2e_frame_ms_p50": pct(e2e_p, 0.5), "e2e_frame_ms_p99": pct(e2e_p, 0.99)},
         "speedup_wall": mrays(wall_b) / mrays(wall_p),
         "speedup_e2e": mrays(e2e_b) / mrays(e2e_p),
         "e2e": {"value": mrays(e2e_b), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(statistics.mean(d2h))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "kernel": "kTraceBatch", "algorithmic_bytes_per_launch": int(algo_bytes), "kernel_ms": trace_mean},
+                     "kernel": "kTraceBatch", "algorithmic_bytes_per_frame": int(algo_bytes), "launches_per_frame": waves,
+                     "kernel_ms": trace_mean},
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -890,6 +899,7 @@ def main():
                          "serving: Poisson scan requests, served vs plain loop")
     ap.add_argument("--rates", type=lambda v: [float(x) for x in v.split(",")], default=[100, 200, 500, 1000, 2000, 5000, 10000, 15000],
                     help="serving: request rates (per second) to sweep")
+    ap.add_argument("--waves", type=int, default=0, help="multi_sensor: waves per batched frame (0: automatic)")
     ap.add_argument("--trace-seconds", type=float, default=30.0, help="serving: length of each arrival trace")
     ap.add_argument("--max-lag", type=float, default=5.0, help="serving: stop a trace once the loop lags arrivals by this much (s)")
     ap.add_argument("--capacity-requests", type=int, default=2000, help="serving: requests of the all-at-once capacity run")

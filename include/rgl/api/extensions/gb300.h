@@ -110,10 +110,10 @@ RGL_API rgl_status_t rgl_gb300_compact_by_flags_noalloc(const int32_t* flags, co
  *
  * A batch is a list of ordinary graphs, given by any one node of each; each graph must hold exactly
  * one raytrace node (the graphs may trace different scenes). rgl_gb300_batch_run runs one frame:
- * every graph is validated and prepared as by rgl_graph_run, then one CUDA graph holds the frame's
+ * every graph is validated and prepared as by rgl_graph_run, then CUDA graphs hold the frame's
  * device work (instance upload and TLAS refit after rgl_entity_set_transform, every graph's nodes,
- * and ONE persistent traversal launch over all sensors). It is captured on the first frame and
- * replayed while nothing structural changes. Results are read per graph with
+ * and one persistent traversal launch per wave of sensors, see rgl_gb300_batch_configure_waves).
+ * They are captured on the first frame and replayed while nothing structural changes. Results are read per graph with
  * rgl_graph_get_result_size/_data and equal what rgl_graph_run of that graph alone writes.
  * At most 1024 graphs per batch. Destroy a batch before destroying its graphs.
  */
@@ -139,6 +139,18 @@ RGL_API rgl_status_t rgl_gb300_batch_configure_schedule(rgl_gb300_batch_t batch,
                                                         int32_t order, int32_t chunk, int32_t regs);
 RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32_t* out_block, int32_t* out_packing,
                                                   int32_t* out_order, int32_t* out_chunk, int32_t* out_regs);
+
+/*
+ * Waves of a batch frame. The frame's graphs are cut, in batch order, into `waves` contiguous runs of
+ * about equal traced rays, each traced by its own persistent launch (which starts while the previous
+ * one drains) and followed by its graphs' later nodes; a graph's results are ready, and
+ * rgl_graph_get_result_* returns, once its wave's later nodes end, so reads of the first graphs
+ * overlap the device work of the rest. 0 (the default) picks one wave per 4 Mi traced rays, at most
+ * 8; the count never exceeds the number of graphs. get_waves gives the count of the last frame (0
+ * before the first). Changes speed and result latency only, never results.
+ */
+RGL_API rgl_status_t rgl_gb300_batch_configure_waves(rgl_gb300_batch_t batch, int32_t waves);
+RGL_API rgl_status_t rgl_gb300_batch_get_waves(rgl_gb300_batch_t batch, int32_t* out_waves);
 
 /*
  * The candidates timed by the batch's last tuning, in the order tried: five int32 per candidate

@@ -1386,6 +1386,27 @@ RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32
 	});
 }
 
+RGL_API rgl_status_t rgl_gb300_batch_configure_waves(rgl_gb300_batch_t batch, int32_t waves)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		CHECK_ARG(waves >= 0 && waves <= rgl::kMaxBatchJobs);
+		auto b = Batches::get(batch, "Batch");
+		b->synchronize();
+		b->wavesWanted = waves;
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_batch_get_waves(rgl_gb300_batch_t batch, int32_t* out_waves)
+{
+	return safeCall([&]() {
+		CHECK_ARG(batch != nullptr);
+		CHECK_ARG(out_waves != nullptr);
+		auto b = Batches::get(batch, "Batch");
+		*out_waves = std::max(0, b->waveCount());
+	});
+}
+
 RGL_API rgl_status_t rgl_gb300_batch_get_tuning(rgl_gb300_batch_t batch, int32_t capacity, int32_t* out_schedules, float* out_ms,
                                                 int32_t* out_count)
 {

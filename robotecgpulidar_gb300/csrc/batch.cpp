@@ -11,31 +11,61 @@ using rgl::format;
 using rgl::InvalidPipeline;
 
 namespace {
-constexpr int kBranches = 4;
+constexpr int kBranches = 4;     // forked streams at creation; grown to the largest wave
+constexpr int kMaxBranches = 32;
 
 bool sameSchedule(const rgl::BatchSchedule& a, const rgl::BatchSchedule& b)
 {
 	return a.block == b.block && a.packing == b.packing && a.order == b.order && a.chunk == b.chunk && a.regs == b.regs;
 }
+
+// Gives every kernel node of a captured frame except the traversal launches the greatest priority:
+// a wave's later nodes, ready when its traversal completes, then take the SM slots that free up
+// before the blocks of the next traversal launch waiting for them.
+cudaError_t prioritizeNodeKernels(cudaGraph_t graph, int priority)
+{
+	size_t n = 0;
+	cudaError_t e = cudaGraphGetNodes(graph, nullptr, &n);
+	std::vector<cudaGraphNode_t> nodes(n);
+	if (e == cudaSuccess && n > 0) {
+		e = cudaGraphGetNodes(graph, nodes.data(), &n);
+	}
+	for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+		cudaGraphNodeType type;
+		e = cudaGraphNodeGetType(nodes[i], &type);
+		if (e != cudaSuccess || type != cudaGraphNodeTypeKernel) {
+			continue;
+		}
+		cudaKernelNodeParams params = {};
+		e = cudaGraphKernelNodeGetParams(nodes[i], &params);
+		if (e != cudaSuccess || rgl::isTraceBatchKernel(params.func)) {
+			continue;
+		}
+		cudaLaunchAttributeValue v = {};
+		v.priority = priority;
+		e = cudaGraphKernelNodeSetAttribute(nodes[i], cudaLaunchAttributePriority, &v);
+	}
+	return e;
+}
 } // namespace
 
 BatchRun::BatchRun(std::vector<Node::Ptr> a) : anchors(std::move(a)), dKeys(false), dOrder(false), dSortScratch(false), dError(false)
 {
+	int least = 0;
+	RGL_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &priorityHigh));
 	RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-	branches.resize(kBranches);
-	joinEv.resize(kBranches);
 	for (int b = 0; b < kBranches; ++b) {
-		RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&branches[b], cudaStreamNonBlocking));
-		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&joinEv[b], cudaEventDisableTiming));
+		addBranch();
 	}
 	RGL_CHECK_CUDA(cudaEventCreateWithFlags(&forkEv, cudaEventDisableTiming));
+	RGL_CHECK_CUDA(cudaStreamCreateWithPriority(&postStream, cudaStreamNonBlocking, priorityHigh));
+	RGL_CHECK_CUDA(cudaEventCreateWithFlags(&postJoin, cudaEventDisableTiming));
 	RGL_CHECK_CUDA(cudaEventCreate(&frameStart));
 	RGL_CHECK_CUDA(cudaEventCreate(&frameStop));
 	RGL_CHECK_CUDA(cudaEventCreate(&traceStart));
 	RGL_CHECK_CUDA(cudaEventCreate(&traceStop));
 	// Allocated here: the first use may be inside a stream capture, where allocation is not allowed.
-	RGL_CHECK_CUDA(cudaMemset(dCounter.ensure(rgl::kTraceCounterBytes), 0, rgl::kTraceCounterBytes));
-	RGL_CHECK_CUDA(cudaMemset(dError.ensure(sizeof(int32_t)), 0, sizeof(int32_t)));
+	RGL_CHECK_CUDA(cudaMemsetAsync(dError.ensure(sizeof(int32_t)), 0, sizeof(int32_t), stream));
 }
 
 BatchRun::~BatchRun()
@@ -44,7 +74,7 @@ BatchRun::~BatchRun()
 		cudaEventSynchronize(frameStop);
 	}
 	releaseExec();
-	for (int b = 0; b < kBranches; ++b) {
+	for (size_t b = 0; b < branches.size(); ++b) {
 		cudaEventDestroy(joinEv[b]);
 		cudaStreamDestroy(branches[b]);
 	}
@@ -53,6 +83,11 @@ BatchRun::~BatchRun()
 	cudaEventDestroy(frameStop);
 	cudaEventDestroy(traceStart);
 	cudaEventDestroy(traceStop);
+	cudaEventDestroy(postJoin);
+	for (cudaEvent_t e : waveTraced) {
+		cudaEventDestroy(e);
+	}
+	cudaStreamDestroy(postStream);
 	cudaStreamDestroy(stream);
 }
 
@@ -124,6 +159,65 @@ void BatchRun::buildJobs()
 		throw rgl::InvalidAPIArgument(format("a batch casts at most %d beams per frame, got %lld", std::numeric_limits<int32_t>::max() / 2,
 		                                     (long long) beams));
 	}
+	splitWaves();
+	shape.push_back(waveCount());
+}
+
+// Cuts the members, in batch order, into waves of about equal traced rays: wave w ends at the first
+// member whose running ray total reaches (w + 1) / W of the frame's. No wave is empty.
+void BatchRun::splitWaves()
+{
+	const int n = (int) members.size();
+	int W = wavesWanted > 0 ? wavesWanted : (int) std::min<int64_t>(kAutoWaves, std::max<int64_t>(1, rays / kRaysPerWave));
+	W = std::max(1, std::min(W, n));
+	waveFirst.assign(1, 0);
+	int64_t acc = 0;
+	for (int j = 0; j < n; ++j) {
+		acc += (int64_t) jobs[j].p.nRays * jobs[j].p.nSamples;
+		const int w = waveCount();
+		const bool last = w == W - 1;
+		// Close wave w after member j if it reached its share, leaving a member for each later wave.
+		if (!last && j + 1 < n && n - (j + 1) >= W - (w + 1) && (acc * W >= rays * (w + 1) || n - (j + 1) == W - (w + 1))) {
+			waveFirst.push_back(j + 1);
+		}
+	}
+	waveFirst.push_back(n);
+}
+
+// A forked stream at the greatest priority, so that the graphs' node kernels on it start before
+// pending traversal blocks.
+void BatchRun::addBranch()
+{
+	cudaStream_t st = nullptr;
+	cudaEvent_t ev = nullptr;
+	RGL_CHECK_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, priorityHigh));
+	branches.push_back(st);
+	RGL_CHECK_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+	joinEv.push_back(ev);
+}
+
+// One counter block and one completion event per wave, and a forked stream per graph of the largest
+// wave (up to kMaxBranches), so a wave's later nodes all start together; made outside any capture.
+void BatchRun::ensureWaveResources()
+{
+	int widest = 0;
+	for (int w = 0; w < waveCount(); ++w) {
+		widest = std::max(widest, waveFirst[w + 1] - waveFirst[w]);
+	}
+	while ((int) branches.size() < std::min(widest, kMaxBranches)) {
+		addBranch();
+	}
+	while ((int) waveTraced.size() < waveCount()) {
+		cudaEvent_t e = nullptr;
+		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+		waveTraced.push_back(e);
+	}
+	const size_t bytes = rgl::kTraceCounterBytes * waveCount();
+	if (bytes > counterBytesZeroed) {
+		RGL_CHECK_CUDA(cudaStreamSynchronize(stream)); // the old counter blocks may still be in use
+		RGL_CHECK_CUDA(cudaMemsetAsync(dCounter.ensure(bytes), 0, dCounter.capacity(), stream));
+		counterBytesZeroed = dCounter.capacity();
+	}
 }
 
 void BatchRun::uploadJobs(const rgl::BatchSchedule& s, cudaStream_t st)
@@ -139,9 +233,16 @@ void BatchRun::uploadJobs(const rgl::BatchSchedule& s, cudaStream_t st)
 		tasks += (b.p.nRays + per - 1) / per;
 	}
 	base[n] = (int32_t) tasks;
-	std::vector<uint8_t> bytes(sizeof(rgl::BatchJob) * n + sizeof(int32_t) * (n + 1));
+	for (int w = 0; w < waveCount(); ++w) {
+		const int lo = waveFirst[w], hi = waveFirst[w + 1];
+		for (int j = lo; j <= hi; ++j) {
+			base.push_back(base[j] - base[lo]);
+		}
+	}
+	const size_t nBase = base.size();
+	std::vector<uint8_t> bytes(sizeof(rgl::BatchJob) * n + sizeof(int32_t) * nBase);
 	std::memcpy(bytes.data(), jobs.data(), sizeof(rgl::BatchJob) * n);
-	std::memcpy(bytes.data() + sizeof(rgl::BatchJob) * n, base.data(), sizeof(int32_t) * (n + 1));
+	std::memcpy(bytes.data() + sizeof(rgl::BatchJob) * n, base.data(), sizeof(int32_t) * nBase);
 	if (bytes == uploaded) {
 		return;
 	}
@@ -149,18 +250,18 @@ void BatchRun::uploadJobs(const rgl::BatchSchedule& s, cudaStream_t st)
 	// the only reader of these buffers, has completed.
 	RGL_CHECK_CUDA(cudaMemcpyAsync(dJobs.ensure(sizeof(rgl::BatchJob) * std::max<size_t>(n, 1)), jobs.data(), sizeof(rgl::BatchJob) * n,
 	                               cudaMemcpyHostToDevice, st));
-	RGL_CHECK_CUDA(cudaMemcpyAsync(dTaskBase.ensure(sizeof(int32_t) * (n + 1)), base.data(), sizeof(int32_t) * (n + 1),
+	RGL_CHECK_CUDA(cudaMemcpyAsync(dTaskBase.ensure(sizeof(int32_t) * nBase), base.data(), sizeof(int32_t) * nBase,
 	                               cudaMemcpyHostToDevice, st));
 	RGL_CHECK_CUDA(cudaStreamSynchronize(st));
 	uploaded = std::move(bytes);
 }
 
-void BatchRun::enqueueMembers(bool preTrace, cudaStream_t s)
+void BatchRun::enqueueMembers(bool preTrace, size_t lo, size_t hi, cudaStream_t s)
 {
-	const int nb = (int) std::min<size_t>(branches.size(), members.size());
+	const int nb = (int) std::min<size_t>(branches.size(), hi - lo);
 	if (nb <= 1) {
-		for (auto& m : members) {
-			for (auto& node : preTrace ? m.pre : m.post) {
+		for (size_t j = lo; j < hi; ++j) {
+			for (auto& node : preTrace ? members[j].pre : members[j].post) {
 				node->enqueueImpl(s);
 			}
 		}
@@ -170,9 +271,9 @@ void BatchRun::enqueueMembers(bool preTrace, cudaStream_t s)
 	for (int b = 0; b < nb; ++b) {
 		RGL_CHECK_CUDA(cudaStreamWaitEvent(branches[b], forkEv, 0));
 	}
-	for (size_t j = 0; j < members.size(); ++j) {
+	for (size_t j = lo; j < hi; ++j) {
 		for (auto& node : preTrace ? members[j].pre : members[j].post) {
-			node->enqueueImpl(branches[j % nb]);
+			node->enqueueImpl(branches[(j - lo) % nb]);
 		}
 	}
 	for (int b = 0; b < nb; ++b) {
@@ -181,22 +282,38 @@ void BatchRun::enqueueMembers(bool preTrace, cudaStream_t s)
 	}
 }
 
-void BatchRun::enqueueTrace(const rgl::BatchSchedule& s, cudaStream_t st)
+// One traversal launch over wave `wave`'s sensors, with its own counter block. Every wave after the
+// first overlaps the tail of the launch before it on the stream.
+void BatchRun::enqueueTrace(const rgl::BatchSchedule& s, int wave, cudaStream_t st)
 {
-	rgl::launchTraceBatch(dJobs.as<rgl::BatchJob>(), dTaskBase.as<int32_t>(), (int) members.size(), maxSamples, shading, s,
-	                      dCounter.as<uint32_t>(), st);
+	const int n = (int) members.size(), lo = waveFirst[wave], hi = waveFirst[wave + 1];
+	rgl::launchTraceBatch(dJobs.as<rgl::BatchJob>() + lo, dTaskBase.as<int32_t>() + (n + 1) + lo + wave, hi - lo, maxSamples, shading, s,
+	                      dCounter.as<uint32_t>() + wave * (rgl::kTraceCounterBytes / sizeof(uint32_t)), st, wave > 0);
 }
 
+// The frame's device work. On `s`: refit, every graph's nodes before the traversal, the traversal
+// launches one after another; on the side stream: wave w's later nodes after its launch completes
+// (an ordinary edge from that launch alone; the next launch's edge to it is programmatic), then the
+// completion events of wave w's graphs. The side stream rejoins `s` at the end.
 void BatchRun::enqueueFrame(cudaStream_t s)
 {
 	for (Scene* sc : scenes) {
 		sc->enqueueRefit(s);
 	}
-	enqueueMembers(true, s);
+	enqueueMembers(true, 0, members.size(), s);
 	recordEvent(traceStart, s);
-	enqueueTrace(schedule, s);
+	for (int w = 0; w < waveCount(); ++w) {
+		enqueueTrace(schedule, w, s);
+		RGL_CHECK_CUDA(cudaEventRecord(waveTraced[w], s));
+		RGL_CHECK_CUDA(cudaStreamWaitEvent(postStream, waveTraced[w], 0));
+		enqueueMembers(false, waveFirst[w], waveFirst[w + 1], postStream);
+		for (int j = waveFirst[w]; j < waveFirst[w + 1]; ++j) {
+			members[j].ctx->recordBatchedDone(postStream);
+		}
+	}
 	recordEvent(traceStop, s);
-	enqueueMembers(false, s);
+	RGL_CHECK_CUDA(cudaEventRecord(postJoin, postStream));
+	RGL_CHECK_CUDA(cudaStreamWaitEvent(s, postJoin, 0));
 }
 
 // Sorts every sensor's beams by `order` (job index in the key's top bits keeps each sensor's beams
@@ -207,7 +324,7 @@ void BatchRun::computeOrder(int order, cudaStream_t st)
 		orderHeld = order;
 		return;
 	}
-	enqueueMembers(true, st);
+	enqueueMembers(true, 0, members.size(), st);
 	auto* keys = static_cast<uint32_t*>(dKeys.ensure(sizeof(uint32_t) * beams));
 	auto* vals = static_cast<uint32_t*>(dOrder.ensure(sizeof(uint32_t) * beams));
 	for (size_t j = 0; j < members.size(); ++j) {
@@ -226,20 +343,31 @@ void BatchRun::computeOrder(int order, cudaStream_t st)
 	int32_t e = 0;
 	RGL_CHECK_CUDA(cudaMemcpy(&e, dError.get(), sizeof(e), cudaMemcpyDeviceToHost));
 	if (e != 0) {
-		RGL_CHECK_CUDA(cudaMemset(dError.get(), 0, sizeof(int32_t)));
+		RGL_CHECK_CUDA(cudaMemsetAsync(dError.get(), 0, sizeof(int32_t), st));
 		throw std::runtime_error("batched beam ordering: radix sort look-back did not complete on the device");
 	}
 	orderHeld = order;
 }
 
+// Times the frame's traversal launches (one per wave, each overlapping the previous one's tail)
+// under schedule s.
 float BatchRun::timeTrace(const rgl::BatchSchedule& s, int reps)
 {
 	uploadJobs(s, stream);
-	enqueueTrace(s, stream); // warm-up
+	ensureWaveResources();
+	for (int w = 0; w < waveCount(); ++w) {
+		rgl::prepareTraceBatch(waveFirst[w + 1] - waveFirst[w], maxSamples, shading, s);
+	}
+	auto traceAll = [&]() {
+		for (int w = 0; w < waveCount(); ++w) {
+			enqueueTrace(s, w, stream);
+		}
+	};
+	traceAll(); // warm-up
 	float best = std::numeric_limits<float>::infinity();
 	for (int r = 0; r < reps; ++r) {
 		RGL_CHECK_CUDA(cudaEventRecord(traceStart, stream));
-		enqueueTrace(s, stream);
+		traceAll();
 		RGL_CHECK_CUDA(cudaEventRecord(traceStop, stream));
 		RGL_CHECK_CUDA(cudaEventSynchronize(traceStop));
 		float ms = 0.0f;
@@ -256,7 +384,7 @@ float BatchRun::timeTrace(const rgl::BatchSchedule& s, int reps)
 void BatchRun::tune()
 {
 	lastTuning.clear();
-	enqueueMembers(true, stream);
+	enqueueMembers(true, 0, members.size(), stream);
 	auto measure = [&](const rgl::BatchSchedule& s) {
 		const float probe = timeTrace(s, 1);
 		const int reps = std::max(2, std::min(10, (int) (20.0f / std::max(probe, 1e-3f))));
@@ -366,7 +494,10 @@ void BatchRun::run()
 		}
 		uploadJobs(schedule, stream);
 		// Launch configuration (occupancy, shared-memory limit) is resolved outside any capture.
-		rgl::prepareTraceBatch((int) members.size(), maxSamples, shading, schedule);
+		for (int w = 0; w < waveCount(); ++w) {
+			rgl::prepareTraceBatch(waveFirst[w + 1] - waveFirst[w], maxSamples, shading, schedule);
+		}
+		ensureWaveResources();
 
 		RGL_CHECK_CUDA(cudaEventRecord(frameStart, stream));
 		if (!cudaGraphsEnabled()) {
@@ -375,7 +506,7 @@ void BatchRun::run()
 		} else {
 			const bool stale = exec == nullptr || version > execVersion || execEpoch != rgl::allocationEpoch() ||
 			                   execScenes != sceneVersions || execSceneList != scenes || !sameSchedule(schedule, execSchedule) ||
-			                   ctxs != execCtxs;
+			                   ctxs != execCtxs || execWaveFirst != waveFirst;
 			if (stale) {
 				releaseExec();
 				const uint64_t launches0 = rgl::launchCount();
@@ -393,7 +524,10 @@ void BatchRun::run()
 				}
 				cudaGraph_t graph = nullptr;
 				RGL_CHECK_CUDA(cudaStreamEndCapture(stream, &graph));
-				const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+				cudaError_t inst = prioritizeNodeKernels(graph, priorityHigh);
+				if (inst == cudaSuccess) {
+					inst = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+				}
 				cudaGraphDestroy(graph);
 				RGL_CHECK_CUDA(inst);
 				execKernels = rgl::launchCount() - launches0;
@@ -403,6 +537,7 @@ void BatchRun::run()
 				execSceneList = scenes;
 				execSchedule = schedule;
 				execCtxs = ctxs;
+				execWaveFirst = waveFirst;
 				++captures;
 			} else {
 				++replays;
@@ -422,7 +557,7 @@ void BatchRun::run()
 		sc->recordReady(stream);
 	}
 	for (auto& m : members) {
-		m.ctx->markBatchedRun(stream);
+		m.ctx->markBatchedRun();
 	}
 	running = true;
 }

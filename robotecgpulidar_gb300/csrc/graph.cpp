@@ -1450,9 +1450,13 @@ void GraphRunCtx::prepareForBatch(cudaStream_t s)
 	}
 }
 
-void GraphRunCtx::markBatchedRun(cudaStream_t s)
+void GraphRunCtx::recordBatchedDone(cudaStream_t s)
 {
-	RGL_CHECK_CUDA(cudaEventRecord(done, s));
+	recordEvent(done, s);
+}
+
+void GraphRunCtx::markBatchedRun()
+{
 	running = true;
 	batchedLast = true;
 }

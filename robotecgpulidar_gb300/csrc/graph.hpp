@@ -625,11 +625,12 @@ struct GraphRunCtx : std::enable_shared_from_this<GraphRunCtx>
 	void invalidateOrder() { order.clear(); }
 
 	// Batched frames (batch.cpp) drive the graph themselves: they validate and prepare it, enqueue
-	// its nodes inside the frame's capture and then mark the graph as running on the frame's stream,
-	// so results are read through the usual calls.
+	// its nodes inside the frame's capture followed by the graph's completion event (an event node of
+	// the capture), and mark the graph as running, so results are read through the usual calls.
 	uint64_t validateForBatch(); // waits for the previous run; returns the largest parameter version
 	void prepareForBatch(cudaStream_t s);
-	void markBatchedRun(cudaStream_t s);
+	void recordBatchedDone(cudaStream_t s);
+	void markBatchedRun();
 	const std::vector<Node::Ptr>& executionOrder() const { return order; }
 
 	std::set<Node::Ptr> nodes;

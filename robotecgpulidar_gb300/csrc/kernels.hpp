@@ -136,13 +136,19 @@ int batchBeamsPerTask(int packing, int nSamples);
 // Resolves and caches the launch configuration (occupancy, shared-memory opt-in) of a schedule;
 // call it outside stream capture before the first captured launch of that schedule.
 void prepareTraceBatch(int nJobs, int maxSamples, bool shading, const BatchSchedule& s);
+// Whether `fn` (a kernel node's function) is one of the persistent traversal kernels.
+bool isTraceBatchKernel(const void* fn);
 // The traversal's counter block: task ticket and finished blocks, zeroed once when allocated; every
 // launch leaves it zero again.
 constexpr size_t kTraceCounterBytes = 2 * sizeof(uint32_t);
 // Persistent launch over `nJobs` sensors; dTaskBase holds nJobs + 1 prefix sums of tasks per sensor;
 // dCounter is a kTraceCounterBytes counter block (launches that share one must be stream-ordered).
+// With `overlapPrevious` the launch uses programmatic stream serialization: when the kernel before it
+// on the stream is a traversal launch (which triggers once all its tasks are handed out), its blocks
+// start as that launch's blocks exit. Only for launches that read nothing the previous one writes and
+// use their own counter block.
 void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs, int maxSamples, bool shading,
-                      const BatchSchedule& s, uint32_t* dCounter, cudaStream_t stream);
+                      const BatchSchedule& s, uint32_t* dCounter, cudaStream_t stream, bool overlapPrevious = false);
 // ---- segcompact.cu: compaction of many requests' points in three launches
 constexpr int kSegTile = 1024; // points per tile
 struct SegCompactJob

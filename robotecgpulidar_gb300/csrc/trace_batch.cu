@@ -187,6 +187,19 @@ LaunchShape batchLaunchShape(int nJobs, int maxSamples, bool shading, const Batc
 }
 } // namespace
 
+bool isTraceBatchKernel(const void* fn)
+{
+	for (int regs : {64, 80, 96, 128}) {
+		for (const void* k : {batchKernel<0, false>(regs), batchKernel<0, true>(regs), batchKernel<1, false>(regs), batchKernel<1, true>(regs),
+		                      batchKernel<2, false>(regs), batchKernel<2, true>(regs)}) {
+			if (k == fn) {
+				return true;
+			}
+		}
+	}
+	return false;
+}
+
 void prepareTraceBatch(int nJobs, int maxSamples, bool shading, const BatchSchedule& s)
 {
 	if (nJobs > 0) {
@@ -195,7 +208,7 @@ void prepareTraceBatch(int nJobs, int maxSamples, bool shading, const BatchSched
 }
 
 void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs, int maxSamples, bool shading, const BatchSchedule& s,
-                      uint32_t* dCounter, cudaStream_t stream)
+                      uint32_t* dCounter, cudaStream_t stream, bool overlapPrevious)
 {
 	if (nJobs <= 0) {
 		return;
@@ -203,7 +216,17 @@ void launchTraceBatch(const BatchJob* dJobs, const int32_t* dTaskBase, int nJobs
 	const LaunchShape ls = batchLaunchShape(nJobs, maxSamples, shading, s);
 	int chunk = s.chunk < 1 ? 1 : s.chunk;
 	void* args[] = {(void*) &dJobs, (void*) &dTaskBase, (void*) &nJobs, (void*) &dCounter, (void*) &chunk};
-	RGL_BATCH_CUDA_OK(cudaLaunchKernel(ls.fn, dim3(ls.grid), dim3(s.block), args, ls.smem, stream));
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(ls.grid);
+	cfg.blockDim = dim3(s.block);
+	cfg.dynamicSmemBytes = ls.smem;
+	cfg.stream = stream;
+	cudaLaunchAttribute attr[1] = {};
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = overlapPrevious ? 1 : 0;
+	RGL_BATCH_CUDA_OK(cudaLaunchKernelExC(&cfg, ls.fn, args));
 	countLaunch();
 }
 

@@ -170,6 +170,10 @@ __global__ void __maxnreg__(REGS) kTraceBatch(const BatchJob* __restrict__ jobs,
 			}
 		}
 	}
+	// Every task is handed out: a traversal launched after this one with programmatic stream
+	// serialization may start its blocks as this grid's blocks exit (the first warp of each block to
+	// get here triggers for the block). The next launch reads nothing this one writes.
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 	// The last block to finish re-arms both counters for the next launch, so no launch needs a memset
 	// first: every block has left the task loop when it counts itself finished.
 	__syncthreads();

@@ -201,6 +201,8 @@ def _proto(l):
         "rgl_gb300_batch_get_schedule": [vp, P(i32), P(i32), P(i32), P(i32), P(i32)],
         "rgl_gb300_batch_get_stats": [vp, P(f), P(f), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)],
         "rgl_gb300_batch_get_tuning": [vp, i32, P(i32), P(f), P(i32)],
+        "rgl_gb300_batch_configure_waves": [vp, i32],
+        "rgl_gb300_batch_get_waves": [vp, P(i32)],
         "rgl_gb300_configure_trace_schedule": [i32, i32, i32, i32],
         "rgl_gb300_scene_create": [P(vp)],
         "rgl_gb300_scene_destroy": [vp],
@@ -474,6 +476,18 @@ def batch_tuning(b) -> list:
     check(lib().rgl_gb300_batch_get_tuning(b, n.value, sch, ms, C.byref(n)))
     keys = ["block", "packing", "order", "chunk", "regs"]
     return [(dict(zip(keys, sch[5 * i:5 * i + 5])), ms[i]) for i in range(n.value)]
+
+
+def batch_configure_waves(b, waves: int = 0):
+    """Waves per frame (0: automatic)."""
+    check(lib().rgl_gb300_batch_configure_waves(b, waves))
+
+
+def batch_waves(b) -> int:
+    """Waves of the last frame (0 before the first)."""
+    n = C.c_int32()
+    check(lib().rgl_gb300_batch_get_waves(b, C.byref(n)))
+    return n.value
 
 
 def batch_stats(b) -> dict:

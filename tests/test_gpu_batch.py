@@ -178,6 +178,50 @@ def test_mixed_sample_counts_batch_equals_solo_runs(rgl, sched):
     rgl.batch_destroy(batch)
 
 
+@pytest.mark.parametrize("waves", [1, 2, 3, 6, 9])
+def test_waves_equal_solo_runs(rgl, waves):
+    """A frame cut into waves (one traversal launch and one set of later nodes per wave; each graph's
+    results readable when its wave ends) writes what the solo runs write, over re-posed frames; the
+    wave count is capped by the number of graphs."""
+    scene, ents, graphs, batch = build_batch(rgl)
+    rgl.batch_configure_schedule(batch, autotune=False, block=128, packing=0, order=1, chunk=1, regs=128)
+    rgl.batch_configure_waves(batch, waves)
+    assert rgl.batch_waves(batch) == 0
+    rng = np.random.default_rng(31)
+    captures = []
+    for frame in range(3):
+        if frame > 0:
+            for i, tf in scenes.repose(scene, 0.25, rng):
+                rgl.entity_set_transform(ents[i], tf)
+        reseed(rgl, graphs, frame)
+        rgl.batch_run(batch)
+        # Read in batch order right away: the first graphs' reads overlap the later waves.
+        batched = [collect(rgl, g) for g in graphs]
+        assert rgl.batch_waves(batch) == min(waves, len(graphs))
+        st = rgl.batch_stats(batch)
+        captures.append(st["captures"])
+        assert st["trace_ms"] > 0 and st["frame_ms"] >= st["trace_ms"]
+        assert_same(rgl, batched, solo_results(rgl, graphs, frame))
+    assert captures[2] == captures[1]  # re-posed frames replay the captured waves
+    rgl.batch_destroy(batch)
+
+
+def test_automatic_waves_follow_the_ray_count(rgl):
+    """0 waves: one wave per 4 Mi traced rays, at most 8; this batch traces far fewer rays."""
+    _, _, graphs, batch = build_batch(rgl)
+    rgl.batch_configure_schedule(batch, autotune=False)
+    rgl.batch_run(batch)
+    assert rgl.batch_waves(batch) == 1
+    rgl.batch_configure_waves(batch, 4)
+    reseed(rgl, graphs)
+    rgl.batch_run(batch)
+    assert rgl.batch_waves(batch) == 4
+    batched = [collect(rgl, g) for g in graphs]
+    assert rgl.batch_stats(batch)["captures"] == 2  # a new wave cut is a new capture
+    assert_same(rgl, batched, solo_results(rgl, graphs))
+    rgl.batch_destroy(batch)
+
+
 def test_repose_frames_equal_solo_runs(rgl):
     scene, ents, graphs, batch = build_batch(rgl)
     rng = np.random.default_rng(9)
@@ -258,5 +302,7 @@ def test_batch_api_argument_checks(rgl):
     assert lib.rgl_gb300_batch_create(C.byref(b), None, 1) == rgl.RGL_INVALID_ARGUMENT
     arr = (C.c_void_p * 1)(None)
     assert lib.rgl_gb300_batch_create(C.byref(b), arr, 1) == rgl.RGL_INVALID_ARGUMENT
+    assert lib.rgl_gb300_batch_configure_waves(C.c_void_p(0x1234), 2) == rgl.RGL_INVALID_API_OBJECT
+    assert lib.rgl_gb300_batch_configure_waves(None, 2) == rgl.RGL_INVALID_ARGUMENT
     assert lib.rgl_gb300_batch_run(C.c_void_p(0x1234)) == rgl.RGL_INVALID_API_OBJECT
     assert "Object does not exist: Batch" in rgl.last_error()
