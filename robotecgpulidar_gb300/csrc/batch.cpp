@@ -73,6 +73,11 @@ BatchRun::~BatchRun()
 	if (running) {
 		cudaEventSynchronize(frameStop);
 	}
+	for (auto& m : members) {
+		for (cudaEvent_t e : waveDone) {
+			m.ctx->forgetBatchEvent(e);
+		}
+	}
 	releaseExec();
 	for (size_t b = 0; b < branches.size(); ++b) {
 		cudaEventDestroy(joinEv[b]);
@@ -85,6 +90,9 @@ BatchRun::~BatchRun()
 	cudaEventDestroy(traceStop);
 	cudaEventDestroy(postJoin);
 	for (cudaEvent_t e : waveTraced) {
+		cudaEventDestroy(e);
+	}
+	for (cudaEvent_t e : waveDone) {
 		cudaEventDestroy(e);
 	}
 	cudaStreamDestroy(postStream);
@@ -208,9 +216,11 @@ void BatchRun::ensureWaveResources()
 		addBranch();
 	}
 	while ((int) waveTraced.size() < waveCount()) {
-		cudaEvent_t e = nullptr;
+		cudaEvent_t e = nullptr, d = nullptr;
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 		waveTraced.push_back(e);
+		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&d, cudaEventDisableTiming));
+		waveDone.push_back(d);
 	}
 	const size_t bytes = rgl::kTraceCounterBytes * waveCount();
 	if (bytes > counterBytesZeroed) {
@@ -293,8 +303,8 @@ void BatchRun::enqueueTrace(const rgl::BatchSchedule& s, int wave, cudaStream_t 
 
 // The frame's device work. On `s`: refit, every graph's nodes before the traversal, the traversal
 // launches one after another; on the side stream: wave w's later nodes after its launch completes
-// (an ordinary edge from that launch alone; the next launch's edge to it is programmatic), then the
-// completion events of wave w's graphs. The side stream rejoins `s` at the end.
+// (an ordinary edge from that launch alone; the next launch's edge to it is programmatic), then
+// wave w's completion event (an event node of the capture). The side stream rejoins `s` at the end.
 void BatchRun::enqueueFrame(cudaStream_t s)
 {
 	for (Scene* sc : scenes) {
@@ -307,9 +317,7 @@ void BatchRun::enqueueFrame(cudaStream_t s)
 		RGL_CHECK_CUDA(cudaEventRecord(waveTraced[w], s));
 		RGL_CHECK_CUDA(cudaStreamWaitEvent(postStream, waveTraced[w], 0));
 		enqueueMembers(false, waveFirst[w], waveFirst[w + 1], postStream);
-		for (int j = waveFirst[w]; j < waveFirst[w + 1]; ++j) {
-			members[j].ctx->recordBatchedDone(postStream);
-		}
+		recordEvent(waveDone[w], postStream);
 	}
 	recordEvent(traceStop, s);
 	RGL_CHECK_CUDA(cudaEventRecord(postJoin, postStream));
@@ -510,11 +518,16 @@ void BatchRun::run()
 			if (stale) {
 				releaseExec();
 				const uint64_t launches0 = rgl::launchCount();
+				// The graphs' parameter blocks are copied by one gather node ahead of the frame instead of
+				// one copy node each (a frame of many sensors would otherwise hold hundreds).
+				std::vector<rgl::ParamCopy> paramCopies;
 				RGL_CHECK_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+				rgl::deferredParamCopies = &paramCopies;
 				try {
 					enqueueFrame(stream);
 				}
 				catch (...) {
+					rgl::deferredParamCopies = nullptr;
 					cudaGraph_t partial = nullptr;
 					cudaStreamEndCapture(stream, &partial);
 					if (partial) {
@@ -522,9 +535,20 @@ void BatchRun::run()
 					}
 					throw;
 				}
+				rgl::deferredParamCopies = nullptr;
 				cudaGraph_t graph = nullptr;
 				RGL_CHECK_CUDA(cudaStreamEndCapture(stream, &graph));
-				cudaError_t inst = prioritizeNodeKernels(graph, priorityHigh);
+				cudaError_t inst = cudaSuccess;
+				if (!paramCopies.empty()) {
+					const size_t bytes = sizeof(rgl::ParamCopy) * paramCopies.size();
+					inst = cudaMemcpy(dParamTable.ensure(bytes), paramCopies.data(), bytes, cudaMemcpyHostToDevice);
+					if (inst == cudaSuccess) {
+						inst = rgl::addParamGatherNode(graph, dParamTable.as<rgl::ParamCopy>(), (int) paramCopies.size());
+					}
+				}
+				if (inst == cudaSuccess) {
+					inst = prioritizeNodeKernels(graph, priorityHigh);
+				}
 				if (inst == cudaSuccess) {
 					inst = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
 				}
@@ -556,8 +580,10 @@ void BatchRun::run()
 	for (Scene* sc : scenes) {
 		sc->recordReady(stream);
 	}
-	for (auto& m : members) {
-		m.ctx->markBatchedRun();
+	for (int w = 0; w < waveCount(); ++w) {
+		for (int j = waveFirst[w]; j < waveFirst[w + 1]; ++j) {
+			members[j].ctx->markBatchedRun(waveDone[w]);
+		}
 	}
 	running = true;
 }

@@ -11,7 +11,7 @@
 //    wave (trace_batch.cu), each launched with programmatic stream serialization after the previous
 //    one, so its blocks fill the SMs that the previous launch's tail leaves idle. A side stream runs
 //    each wave's later nodes (compaction, formatting) once its traversal completes and then records
-//    the completion events of the wave's graphs. Per-sensor node work is spread over a few forked
+//    the wave's completion event, which the wave's graphs wait on. Per-sensor node work is spread over a few forked
 //    streams, so it becomes parallel branches of the graph.
 // Results are read per graph with rgl_graph_get_result_size/_data, as after rgl_graph_run, and equal
 // what a run of that graph alone writes. A graph's results are ready when its wave's later nodes
@@ -88,7 +88,8 @@ private:
 	cudaStream_t postStream = nullptr; // later nodes of each wave
 	int priorityHigh = 0;             // the device's greatest stream priority: every kernel but the traversal's
 	cudaEvent_t frameStart = nullptr, frameStop = nullptr, traceStart = nullptr, traceStop = nullptr, postJoin = nullptr;
-	std::vector<cudaEvent_t> waveTraced; // per wave: its traversal launch completed
+	std::vector<cudaEvent_t> waveTraced; // per wave: its traversal launch completed (capture edges)
+	std::vector<cudaEvent_t> waveDone;   // per wave: its graphs' nodes completed (what their reads wait for)
 	bool running = false;
 
 	// Job table: host copy, device copy, task prefix sums for the current schedule (dTaskBase: the
@@ -104,6 +105,7 @@ private:
 	rgl::DeviceBuffer dJobs, dTaskBase, dCounter, dKeys, dOrder, dSortScratch, dError; // dCounter: one block per wave
 	size_t counterBytesZeroed = 0;
 	std::vector<uint8_t> uploaded; // bytes of the job table and task bases last uploaded
+	rgl::DeviceBuffer dParamTable{false}; // the captured frame's parameter copies (read by its gather node)
 
 	// Captured frame.
 	cudaGraphExec_t exec = nullptr;

@@ -8,6 +8,8 @@
 
 namespace rgl {
 
+thread_local std::vector<ParamCopy>* deferredParamCopies = nullptr;
+
 std::string format(const char* fmt, ...)
 {
 	va_list ap;

@@ -143,6 +143,20 @@ private:
 // Library-wide CUDA state: device selected lazily on the first API call.
 void ensureCudaInitialized();
 
+// One parameter block's host-to-device copy, made by a gather kernel (kernels.hpp) instead of a
+// copy node of its own.
+struct ParamCopy
+{
+	const void* src; // pinned host memory
+	void* dst;       // device memory
+	uint32_t bytes;
+	uint32_t pad;
+};
+// While non-null on this thread (during the capture of a batched frame), StagedParam::enqueue appends
+// its copy here instead of issuing it; the capturing code then makes all of them in one kernel node
+// placed before every other node of the graph.
+extern thread_local std::vector<ParamCopy>* deferredParamCopies;
+
 // A small parameter block (a transform, noise parameters) staged in pinned host memory before every
 // run and copied to device memory by the run itself, so a captured run replayed later reads the
 // current values. Call host() and device() in the prepare phase, enqueue() in the enqueue phase.
@@ -154,7 +168,11 @@ public:
 	const T* device() { return static_cast<const T*>(d_.ensure(sizeof(T))); }
 	const T* enqueue(cudaStream_t s)
 	{
-		RGL_CHECK_CUDA(cudaMemcpyAsync(d_.get(), h_.get(), sizeof(T), cudaMemcpyHostToDevice, s));
+		if (deferredParamCopies != nullptr) {
+			deferredParamCopies->push_back(ParamCopy{h_.get(), d_.get(), (uint32_t) sizeof(T), 0});
+		} else {
+			RGL_CHECK_CUDA(cudaMemcpyAsync(d_.get(), h_.get(), sizeof(T), cudaMemcpyHostToDevice, s));
+		}
 		return d_.as<T>();
 	}
 

@@ -1450,15 +1450,22 @@ void GraphRunCtx::prepareForBatch(cudaStream_t s)
 	}
 }
 
-void GraphRunCtx::recordBatchedDone(cudaStream_t s)
+void GraphRunCtx::markBatchedRun(cudaEvent_t frameDone)
 {
-	recordEvent(done, s);
-}
-
-void GraphRunCtx::markBatchedRun()
-{
+	batchDone = frameDone;
 	running = true;
 	batchedLast = true;
+}
+
+void GraphRunCtx::forgetBatchEvent(cudaEvent_t frameDone)
+{
+	if (batchDone == frameDone && frameDone != nullptr) {
+		cudaEventSynchronize(batchDone);
+		batchDone = nullptr;
+		if (batchedLast) {
+			running = false;
+		}
+	}
 }
 
 void GraphRunCtx::synchronize(bool refreshErrors)
@@ -1467,7 +1474,7 @@ void GraphRunCtx::synchronize(bool refreshErrors)
 		return;
 	}
 	running = false;
-	RGL_CHECK_CUDA(cudaEventSynchronize(done));
+	RGL_CHECK_CUDA(cudaEventSynchronize(batchedLast && batchDone ? batchDone : done));
 	RGL_CHECK_CUDA(cudaGetLastError());
 	if (refreshErrors) {
 		rgl::refreshErrorSlots();

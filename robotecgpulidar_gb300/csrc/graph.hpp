@@ -625,12 +625,13 @@ struct GraphRunCtx : std::enable_shared_from_this<GraphRunCtx>
 	void invalidateOrder() { order.clear(); }
 
 	// Batched frames (batch.cpp) drive the graph themselves: they validate and prepare it, enqueue
-	// its nodes inside the frame's capture followed by the graph's completion event (an event node of
-	// the capture), and mark the graph as running, so results are read through the usual calls.
+	// its nodes inside the frame, and mark the graph as running until `frameDone` (recorded by the
+	// frame once the graph's nodes are done, owned by the batch) completes, so results are read
+	// through the usual calls. forgetBatchEvent drops an event the batch is about to destroy.
 	uint64_t validateForBatch(); // waits for the previous run; returns the largest parameter version
 	void prepareForBatch(cudaStream_t s);
-	void recordBatchedDone(cudaStream_t s);
-	void markBatchedRun();
+	void markBatchedRun(cudaEvent_t frameDone);
+	void forgetBatchEvent(cudaEvent_t frameDone);
 	const std::vector<Node::Ptr>& executionOrder() const { return order; }
 
 	std::set<Node::Ptr> nodes;
@@ -644,6 +645,7 @@ private:
 	std::vector<Node::Ptr> order;
 	cudaStream_t stream_ = nullptr;
 	cudaEvent_t done = nullptr, runStart = nullptr, runStop = nullptr;
+	cudaEvent_t batchDone = nullptr; // completion of the graph's part of the last batched frame
 	bool running = false;
 	bool batchedLast = false; // the last run was part of a batched frame (no per-graph timing)
 	// Captured run: replayed while no node changed and no buffer moved.

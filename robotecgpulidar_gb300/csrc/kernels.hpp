@@ -11,6 +11,8 @@
 
 namespace rgl {
 
+struct ParamCopy; // common.hpp
+
 // Counts kernel launches issued by this library (reported by rgl_gb300_get_kernel_launch_count).
 void countLaunch(uint64_t n = 1);
 uint64_t launchCount();
@@ -136,6 +138,9 @@ int batchBeamsPerTask(int packing, int nSamples);
 // Resolves and caches the launch configuration (occupancy, shared-memory opt-in) of a schedule;
 // call it outside stream capture before the first captured launch of that schedule.
 void prepareTraceBatch(int nJobs, int maxSamples, bool shading, const BatchSchedule& s);
+// Adds to `graph` one kernel node that makes the n parameter copies listed in dTable (device memory,
+// kept while the graph lives) and makes it the predecessor of every node that had none.
+cudaError_t addParamGatherNode(cudaGraph_t graph, const ParamCopy* dTable, int n);
 // Whether `fn` (a kernel node's function) is one of the persistent traversal kernels.
 bool isTraceBatchKernel(const void* fn);
 // The traversal's counter block: task ticket and finished blocks, zeroed once when allocated; every

@@ -10,10 +10,66 @@
 
 #include <algorithm>
 
+#include "common.hpp"
 #include "kernels.hpp"
 #include "philox.hpp"
 
 namespace rgl {
+
+namespace {
+// One warp per parameter block: 4-byte words, then any tail bytes (pinned and device allocations
+// are at least 256-byte aligned).
+__global__ void kGatherParams(const ParamCopy* __restrict__ table, int n)
+{
+	const int warp = (int) ((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = (int) (threadIdx.x & 31);
+	if (warp >= n) {
+		return;
+	}
+	const ParamCopy c = table[warp];
+	const uint32_t words = c.bytes >> 2;
+	const uint32_t* src = static_cast<const uint32_t*>(c.src);
+	uint32_t* dst = static_cast<uint32_t*>(c.dst);
+	for (uint32_t i = lane; i < words; i += 32) {
+		dst[i] = src[i];
+	}
+	for (uint32_t i = (words << 2) + lane; i < c.bytes; i += 32) {
+		static_cast<uint8_t*>(c.dst)[i] = static_cast<const uint8_t*>(c.src)[i];
+	}
+}
+} // namespace
+
+cudaError_t addParamGatherNode(cudaGraph_t graph, const ParamCopy* dTable, int n)
+{
+	if (n <= 0) {
+		return cudaSuccess;
+	}
+	size_t nRoots = 0;
+	cudaError_t e = cudaGraphGetRootNodes(graph, nullptr, &nRoots);
+	std::vector<cudaGraphNode_t> roots(nRoots);
+	if (e == cudaSuccess && nRoots > 0) {
+		e = cudaGraphGetRootNodes(graph, roots.data(), &nRoots);
+	}
+	if (e != cudaSuccess) {
+		return e;
+	}
+	constexpr int kBlock = 128;
+	void* args[] = {(void*) &dTable, (void*) &n};
+	cudaKernelNodeParams p = {};
+	p.func = reinterpret_cast<void*>(&kGatherParams);
+	p.gridDim = dim3((unsigned) ((n * 32 + kBlock - 1) / kBlock));
+	p.blockDim = dim3(kBlock);
+	p.sharedMemBytes = 0;
+	p.kernelParams = args;
+	cudaGraphNode_t gather = nullptr;
+	e = cudaGraphAddKernelNode(&gather, graph, nullptr, 0, &p);
+	for (size_t i = 0; i < nRoots && e == cudaSuccess; ++i) {
+		e = cudaGraphAddDependencies(graph, &gather, &roots[i], nullptr, 1);
+	}
+	if (e == cudaSuccess) {
+		countLaunch();
+	}
+	return e;
+}
 
 namespace {
 
