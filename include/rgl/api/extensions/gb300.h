@@ -44,10 +44,18 @@ RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t*
  * Traversal schedule of graph runs (rgl_graph_run). Every raytrace runs on the persistent traversal
  * kernel of batched frames as a one-job launch; this sets its block size (64, 128, 256), packing
  * (0: a beam's sub-rays on adjacent lanes, walking the scene together; 1: one lane per beam), tasks
- * per fetch (1..64) and register budget (64, 80, 96, 128). The default is 128, 0, 1, 128. Changes speed
+ * per fetch (1..64) and register budget (64, 80, 96, 128). The default is 256, 0, 1, 128. Changes speed
  * only, never results.
  */
 RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs);
+
+/*
+ * Beam visiting order of graph runs: 0 as given, 1 sorted by octahedral direction key (the default),
+ * 2 by Morton key of a probe point along the ray. A run computes the order (one key kernel and one
+ * sort) when its ray count, ray buffer or this setting changed, and keeps it for later ray contents
+ * of the same count. Changes speed only, never results.
+ */
+RGL_API rgl_status_t rgl_gb300_configure_trace_order(int32_t order);
 
 /* Waits until the last run of the node's graph completed (rgl_graph_get_result_* also wait). */
 RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node);

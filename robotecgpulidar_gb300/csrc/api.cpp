@@ -1670,12 +1670,23 @@ RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t p
 		CHECK_ARG(chunk >= 1 && chunk <= 64);
 		CHECK_ARG(regs == 64 || regs == 80 || regs == 96 || regs == 128);
 		GraphRunCtx::synchronizeAll();
-		setTraceSchedule(rgl::BatchSchedule{block, packing, rgl::kOrderNatural, chunk, regs});
+		setTraceSchedule(rgl::BatchSchedule{block, packing, traceSchedule().order, chunk, regs});
 		// Captured runs baked the old schedule into their launches.
 		for (auto& kv : Nodes::map()) {
 			if (std::dynamic_pointer_cast<RaytraceNode>(kv.second)) {
 				kv.second->markParamsChanged();
 			}
 		}
+	});
+}
+
+RGL_API rgl_status_t rgl_gb300_configure_trace_order(int32_t order)
+{
+	return safeCall([&]() {
+		CHECK_ARG(order == rgl::kOrderNatural || order == rgl::kOrderOctahedral || order == rgl::kOrderMorton);
+		GraphRunCtx::synchronizeAll();
+		rgl::BatchSchedule sch = traceSchedule();
+		sch.order = order;
+		setTraceSchedule(sch);
 	});
 }

@@ -28,7 +28,7 @@ namespace {
 // Schedule of single-graph traversals (a batch of one job). The default is the fastest measured on
 // the 1M-triangle single-sensor scan: lane-group packing, 128-thread blocks, one task per fetch, 128
 // registers per thread (0.287 ms against 0.294 ms at 96 registers for the traversal of that scan).
-rgl::BatchSchedule gTraceSchedule{128, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 128};
+rgl::BatchSchedule gTraceSchedule{256, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 128};
 } // namespace
 rgl::BatchSchedule traceSchedule() { return gTraceSchedule; }
 void setTraceSchedule(const rgl::BatchSchedule& s) { gTraceSchedule = s; }
@@ -503,7 +503,7 @@ void RaytraceNode::prepareImpl(cudaStream_t s)
 		RGL_CHECK_CUDA(cudaEventCreate(&evStop));
 	}
 	scene->prepare(s);
-	stageJob();
+	stageJob(s);
 }
 
 rgl::TraceParams RaytraceNode::traceParams()
@@ -580,13 +580,46 @@ void RaytraceNode::fillJob(rgl::BatchJob& b)
 	}
 }
 
-void RaytraceNode::stageJob()
+void RaytraceNode::ensureOrder(const rgl::BatchJob& b, cudaStream_t s)
+{
+	const int n = b.p.nRays;
+	if (orderValid && orderCount == n && orderKind == schedule.order && orderRays == b.p.rays) {
+		return;
+	}
+	orderValid = false;
+	orderCount = n;
+	orderKind = schedule.order;
+	orderRays = b.p.rays;
+	constexpr int kKeyBits = 22; // one job: no job bits above the 22-bit direction or position key
+	const float lo[3] = {scene->worldLower()[0], scene->worldLower()[1], scene->worldLower()[2]};
+	const float hi[3] = {scene->worldUpper()[0], scene->worldUpper()[1], scene->worldUpper()[2]};
+	auto* keys = static_cast<uint32_t*>(orderKeys.ensure(sizeof(uint32_t) * n));
+	auto* vals = static_cast<uint32_t*>(orderVals.ensure(sizeof(uint32_t) * n));
+	auto* err = static_cast<int32_t*>(orderError.ensure(sizeof(int32_t)));
+	RGL_CHECK_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
+	rgl::launchBeamKeys(b.p.rays, b.hasRayTransform ? &b.rayTransform : nullptr, n, 0, schedule.order, lo, hi, keys, vals, s);
+	rgl::sortPairs(keys, vals, n, kKeyBits, orderScratch.ensure(rgl::sortPairsScratchBytes(n, kKeyBits)), err, s);
+	int32_t failed = 0;
+	RGL_CHECK_CUDA(cudaMemcpyAsync(&failed, err, sizeof(failed), cudaMemcpyDeviceToHost, s));
+	RGL_CHECK_CUDA(cudaStreamSynchronize(s));
+	// A sort whose look-back gave up leaves no permutation: cast in the given order instead.
+	orderValid = failed == 0;
+	if (!orderValid) {
+		rgl::logMessage(rgl::LogLevel::Warn, "RaytraceNode: beam ordering sort did not complete; casting beams in the given order");
+	}
+}
+
+void RaytraceNode::stageJob(cudaStream_t s)
 {
 	rgl::BatchJob& b = job.host().job;
+	schedule = traceSchedule();
 	fillJob(b);
+	if (schedule.order != rgl::kOrderNatural && b.p.nRays > 0) {
+		ensureOrder(b, s);
+		b.order = orderValid ? orderVals.as<uint32_t>() : nullptr;
+	}
 	const rgl::TraceParams& p = b.p;
 	(void) job.device();
-	schedule = traceSchedule();
 	const int per = rgl::batchBeamsPerTask(schedule.packing, p.nSamples);
 	rgl::TaskRange& tr = job.host().tasks;
 	tr.base[0] = 0;

@@ -328,7 +328,7 @@ struct RaytraceNode : PointsNode
 	// The node's job of a traversal launch (parameters, sub-ray table, lane-group width, a folded
 	// sensor transform); order and task bases are the launcher's.
 	void fillJob(rgl::BatchJob& b);
-	void stageJob();
+	void stageJob(cudaStream_t s);
 	const rgl::Mat34* sampleTableDev() const { return sampleTable.as<rgl::Mat34>(); }
 	Scene* scene = nullptr;
 
@@ -366,6 +366,15 @@ private:
 	rgl::DeviceBuffer counter;
 	rgl::BatchSchedule schedule{};
 	bool shading = false;
+	// Beam visiting order of the launch (schedule.order other than as given): the sorted beam indices,
+	// made when the ray count, the ray buffer or the order kind changes. Later ray contents of the same
+	// count keep it: any permutation gives the same results, only the speed depends on it. The job
+	// carries the pointer, staged every run, so the buffers may move without a new capture.
+	void ensureOrder(const rgl::BatchJob& b, cudaStream_t s);
+	rgl::DeviceBuffer orderKeys{false}, orderVals{false}, orderScratch{false}, orderError{false};
+	int32_t orderCount = -1, orderKind = rgl::kOrderNatural;
+	const void* orderRays = nullptr;
+	bool orderValid = false;
 };
 
 struct YieldPointsNode : PointsNodeSingleInput

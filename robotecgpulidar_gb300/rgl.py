@@ -204,6 +204,7 @@ def _proto(l):
         "rgl_gb300_batch_configure_waves": [vp, i32],
         "rgl_gb300_batch_get_waves": [vp, P(i32)],
         "rgl_gb300_configure_trace_schedule": [i32, i32, i32, i32],
+        "rgl_gb300_configure_trace_order": [i32],
         "rgl_gb300_scene_create": [P(vp)],
         "rgl_gb300_scene_destroy": [vp],
         "rgl_gb300_scene_get_stats_of": [vp, P(C.c_int64), P(C.c_int64), P(i32)],

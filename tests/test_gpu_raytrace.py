@@ -265,14 +265,49 @@ def test_union_and_single_ray_traversals_agree(rgl, layers, vertices):
     rgl.points_yield(n["out"], fields)
     rgl.chain(n["rays"], n["pose"], n["trace"], n["out"])
     got = {}
-    for packing, regs in ((0, 80), (1, 128), (0, 96), (1, 64)):
+    for packing, regs, order in ((0, 80, 0), (1, 128, 0), (0, 96, 1), (1, 64, 2), (0, 128, 1), (1, 128, 1)):
         rgl.check(lib.rgl_gb300_configure_trace_schedule(256, packing, 1, regs))
+        rgl.check(lib.rgl_gb300_configure_trace_order(order))
         rgl.graph_run(n["rays"])
-        got[(packing, regs)] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
-    rgl.check(lib.rgl_gb300_configure_trace_schedule(128, 0, 1, 96))  # back to the default
-    ref = got[(1, 128)]
+        got[(packing, regs, order)] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
+    rgl.check(lib.rgl_gb300_configure_trace_schedule(256, 0, 1, 128))  # back to the default
+    rgl.check(lib.rgl_gb300_configure_trace_order(1))
+    ref = got[(1, 128, 0)]
     for k, v in got.items():
-        assert v == ref, f"schedule {k} differs from single-ray traversal"
+        assert v == ref, f"schedule {k} differs from single-ray traversal in the given order"
+
+
+def test_kept_beam_order_after_new_ray_contents(rgl):
+    """A graph run keeps its beam order (sorted directions of the rays it first cast) when new rays of
+    the same count arrive: the order is then stale but still a permutation, and the points equal a run
+    in the given order."""
+    scene = scenes.million_scene(seed=3, instances=30, spheres=3, cells=128, extent=150.0)
+    rgl.spawn_scene(scene)
+    lib = rgl.lib()
+    n = {k: rgl.node() for k in ("rays", "pose", "trace", "out")}
+    first = scenes.lidar_rays(32, 360)
+    rgl.rays_from_mat3x4f(n["rays"], first)
+    rgl.rays_transform(n["pose"], scenes.translation(3.0, -2.0, 6.0))
+    rgl.raytrace(n["trace"])
+    rgl.check(lib.rgl_node_raytrace_configure_return_mode(n["trace"], rgl.RGL_RETURN_FIRST_LAST))
+    fields = [rgl.RGL_FIELD_XYZ_VEC3_F32, rgl.RGL_FIELD_DISTANCE_F32, rgl.RGL_FIELD_ENTITY_ID_I32, rgl.RGL_FIELD_IS_HIT_I32]
+    rgl.points_yield(n["out"], fields)
+    rgl.chain(n["rays"], n["pose"], n["trace"], n["out"])
+    rng = np.random.default_rng(12)
+    second = first[rng.permutation(first.shape[0])]  # same count, other beams at every index
+    got = {}
+    try:
+        for order in (1, 2, 0):
+            rgl.check(lib.rgl_gb300_configure_trace_order(order))
+            rgl.rays_from_mat3x4f(n["rays"], first)
+            rgl.graph_run(n["rays"])
+            rgl.rays_from_mat3x4f(n["rays"], second)
+            rgl.graph_run(n["rays"])
+            got[order] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
+    finally:
+        rgl.check(lib.rgl_gb300_configure_trace_order(1))
+    for order in (1, 2):
+        assert got[order] == got[0], f"order {order} kept over new ray contents differs from the given order"
 
 
 def _beam_field_graph(rgl, rays, pose, fields, ring_ids=None, offsets=None):
