@@ -50,8 +50,9 @@ RGL_API rgl_status_t rgl_gb300_graph_get_capture_stats(rgl_node_t node, int64_t*
 RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs);
 
 /*
- * Beam visiting order of graph runs: 0 as given, 1 sorted by octahedral direction key (the default),
- * 2 by Morton key of a probe point along the ray. A run computes the order (one key kernel and one
+ * Beam visiting order of graph runs: 0 as given, 1 sorted by octahedral direction key, 2 by Morton key
+ * of a probe point along the ray, 3 by elevation of the world direction, then azimuth (the rows of a
+ * scan; the default). A run computes the order (one key kernel and one
  * sort) when its ray count, ray buffer or this setting changed, and keeps it for later ray contents
  * of the same count. Changes speed only, never results.
  */
@@ -139,6 +140,7 @@ RGL_API rgl_status_t rgl_gb300_batch_destroy(rgl_gb300_batch_t batch);
  *   packing  0: a beam's sub-rays on adjacent lanes, walking the scene together; 1: one lane per
  *            beam, sub-rays in turn
  *   order    beam visiting order. 0: as given; 1: sorted by octahedral direction; 2: by Morton code
+ *            of a probe point; 3: by elevation, then azimuth (the rows of a scan)
  *   chunk    tasks (one warp's beams each) taken per fetch from the shared work counter, 1..64
  *   regs     registers per thread: 64, 80, 96 or 128 (fewer registers, more resident warps)
  * The schedule changes speed only, never results.

@@ -1359,7 +1359,7 @@ RGL_API rgl_status_t rgl_gb300_batch_configure_schedule(rgl_gb300_batch_t batch,
 		CHECK_ARG(batch != nullptr);
 		CHECK_ARG(block == 64 || block == 128 || block == 256);
 		CHECK_ARG(packing == rgl::kPackLaneGroup || packing == rgl::kPackSerial);
-		CHECK_ARG(order == rgl::kOrderNatural || order == rgl::kOrderOctahedral || order == rgl::kOrderMorton);
+		CHECK_ARG(order >= rgl::kOrderNatural && order <= rgl::kOrderElevation);
 		CHECK_ARG(chunk >= 1 && chunk <= 64);
 		CHECK_ARG(regs == 64 || regs == 80 || regs == 96 || regs == 128);
 		auto b = Batches::get(batch, "Batch");
@@ -1683,7 +1683,7 @@ RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t p
 RGL_API rgl_status_t rgl_gb300_configure_trace_order(int32_t order)
 {
 	return safeCall([&]() {
-		CHECK_ARG(order == rgl::kOrderNatural || order == rgl::kOrderOctahedral || order == rgl::kOrderMorton);
+		CHECK_ARG(order >= rgl::kOrderNatural && order <= rgl::kOrderElevation);
 		GraphRunCtx::synchronizeAll();
 		rgl::BatchSchedule sch = traceSchedule();
 		sch.order = order;

@@ -402,7 +402,7 @@ void BatchRun::tune()
 	};
 	rgl::BatchSchedule best = rgl::BatchSchedule{256, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 80};
 	float bestMs = std::numeric_limits<float>::infinity();
-	for (int order : {rgl::kOrderNatural, rgl::kOrderOctahedral, rgl::kOrderMorton}) {
+	for (int order : {rgl::kOrderNatural, rgl::kOrderOctahedral, rgl::kOrderMorton, rgl::kOrderElevation}) {
 		computeOrder(order, stream);
 		for (int packing : {rgl::kPackLaneGroup, rgl::kPackSerial}) {
 			rgl::BatchSchedule s{128, packing, order, 1, 128};

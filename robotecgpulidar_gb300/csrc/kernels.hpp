@@ -112,6 +112,7 @@ enum BeamOrder : int32_t
 	kOrderNatural = 0,    // beams in the order the client gave them
 	kOrderOctahedral = 1, // sorted by an octahedral encoding of the world direction
 	kOrderMorton = 2,     // sorted by the Morton code of a point a fixed distance along the ray
+	kOrderElevation = 3,  // sorted by the elevation of the world direction, then its azimuth (scan rows)
 };
 struct BatchSchedule
 {

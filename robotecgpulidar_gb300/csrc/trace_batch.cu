@@ -90,6 +90,13 @@ __global__ void kBeamKeys(const Mat34* __restrict__ rays, Mat34 tf, int hasTf, i
 			v = fv;
 		}
 		code = (spread2(quant(u * 0.5f + 0.5f, 2048u)) << 1) | spread2(quant(v * 0.5f + 0.5f, 2048u));
+	} else if (order == kOrderElevation) {
+		// Rows of a scan: the sine of the elevation above the world xy plane in the high 11 bits, a
+		// pseudo-angle of the azimuth (monotonic in atan2(y, x), in (-2, 2]) in the low 11 bits.
+		const float l1 = fabsf(d.x) + fabsf(d.y);
+		const float pa = l1 > 0.0f ? 1.0f - d.x / l1 : 0.0f;
+		const float az = d.y < 0.0f ? -pa : pa;
+		code = (quant(d.z * 0.5f + 0.5f, 2048u) << 11) | quant(az * 0.25f + 0.5f, 2048u);
 	} else {
 		const float px = (o.x + d.x * probe - lo.x) * inv.x;
 		const float py = (o.y + d.y * probe - lo.y) * inv.y;

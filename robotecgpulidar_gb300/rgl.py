@@ -439,7 +439,7 @@ def kernel_launch_count() -> int:
 # ---------------------------------------------------------------- batched multi-sensor frames
 
 PACK_LANE_GROUP, PACK_SERIAL = 0, 1
-ORDER_NATURAL, ORDER_OCTAHEDRAL, ORDER_MORTON = 0, 1, 2
+ORDER_NATURAL, ORDER_OCTAHEDRAL, ORDER_MORTON, ORDER_ELEVATION = 0, 1, 2, 3
 
 
 def batch_create(nodes) -> C.c_void_p:

@@ -126,6 +126,7 @@ SCHEDULES = [
     dict(autotune=False, block=256, packing=0, order=2, chunk=4, regs=96),
     dict(autotune=False, block=128, packing=0, order=0, chunk=8, regs=128),
     dict(autotune=False, block=128, packing=1, order=2, chunk=2, regs=96),
+    dict(autotune=False, block=256, packing=0, order=3, chunk=1, regs=128),
 ]
 
 
@@ -144,8 +145,8 @@ def test_batched_frame_equals_solo_runs(rgl, sched):
     if sched["autotune"]:
         assert st["tunings"] == 1
         # Every stage is recorded; the kept schedule is the fastest candidate tried.
-        assert len(tuning) >= 12 and all(ms > 0 for _, ms in tuning)
-        assert {(s["packing"], s["order"]) for s, _ in tuning[:6]} == {(p, o) for p in (0, 1) for o in (0, 1, 2)}
+        assert len(tuning) >= 14 and all(ms > 0 for _, ms in tuning)
+        assert {(s["packing"], s["order"]) for s, _ in tuning[:8]} == {(p, o) for p in (0, 1) for o in (0, 1, 2, 3)}
         assert rgl.batch_schedule(batch) == min(tuning, key=lambda c: c[1])[0]
     else:
         assert tuning == []
@@ -204,6 +205,31 @@ def test_waves_equal_solo_runs(rgl, waves):
         assert_same(rgl, batched, solo_results(rgl, graphs, frame))
     assert captures[2] == captures[1]  # re-posed frames replay the captured waves
     rgl.batch_destroy(batch)
+
+
+def test_waves_without_cuda_graphs_equal_solo_runs(rgl):
+    """With CUDA graphs off the frame's work is enqueued directly (waves, side stream, events as in the
+    captured frame) and writes the same points."""
+    lib = rgl.lib()
+    rgl.check(lib.rgl_gb300_configure_cuda_graphs(False))
+    try:
+        scene, ents, graphs, batch = build_batch(rgl)
+        rgl.batch_configure_schedule(batch, autotune=False, block=256, packing=1, order=2, chunk=1, regs=128)
+        rgl.batch_configure_waves(batch, 3)
+        rng = np.random.default_rng(5)
+        for frame in range(2):
+            if frame > 0:
+                for i, tf in scenes.repose(scene, 0.25, rng):
+                    rgl.entity_set_transform(ents[i], tf)
+            reseed(rgl, graphs, frame)
+            rgl.batch_run(batch)
+            batched = [collect(rgl, g) for g in graphs]
+            assert rgl.batch_waves(batch) == 3
+            assert_same(rgl, batched, solo_results(rgl, graphs, frame))
+        assert rgl.batch_stats(batch)["captures"] == 0
+        rgl.batch_destroy(batch)
+    finally:
+        rgl.check(lib.rgl_gb300_configure_cuda_graphs(True))
 
 
 def test_automatic_waves_follow_the_ray_count(rgl):

@@ -265,13 +265,13 @@ def test_union_and_single_ray_traversals_agree(rgl, layers, vertices):
     rgl.points_yield(n["out"], fields)
     rgl.chain(n["rays"], n["pose"], n["trace"], n["out"])
     got = {}
-    for packing, regs, order in ((0, 80, 0), (1, 128, 0), (0, 96, 1), (1, 64, 2), (0, 128, 1), (1, 128, 1)):
+    for packing, regs, order in ((0, 80, 0), (1, 128, 0), (0, 96, 1), (1, 64, 2), (0, 128, 1), (1, 128, 1), (0, 128, 3), (1, 96, 3)):
         rgl.check(lib.rgl_gb300_configure_trace_schedule(256, packing, 1, regs))
         rgl.check(lib.rgl_gb300_configure_trace_order(order))
         rgl.graph_run(n["rays"])
         got[(packing, regs, order)] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
     rgl.check(lib.rgl_gb300_configure_trace_schedule(256, 0, 1, 128))  # back to the default
-    rgl.check(lib.rgl_gb300_configure_trace_order(1))
+    rgl.check(lib.rgl_gb300_configure_trace_order(3))
     ref = got[(1, 128, 0)]
     for k, v in got.items():
         assert v == ref, f"schedule {k} differs from single-ray traversal in the given order"
@@ -297,7 +297,7 @@ def test_kept_beam_order_after_new_ray_contents(rgl):
     second = first[rng.permutation(first.shape[0])]  # same count, other beams at every index
     got = {}
     try:
-        for order in (1, 2, 0):
+        for order in (1, 2, 3, 0):
             rgl.check(lib.rgl_gb300_configure_trace_order(order))
             rgl.rays_from_mat3x4f(n["rays"], first)
             rgl.graph_run(n["rays"])
@@ -305,8 +305,8 @@ def test_kept_beam_order_after_new_ray_contents(rgl):
             rgl.graph_run(n["rays"])
             got[order] = {f: rgl.result_bytes(n["out"], f).tobytes() for f in fields}
     finally:
-        rgl.check(lib.rgl_gb300_configure_trace_order(1))
-    for order in (1, 2):
+        rgl.check(lib.rgl_gb300_configure_trace_order(3))
+    for order in (1, 2, 3):
         assert got[order] == got[0], f"order {order} kept over new ray contents differs from the given order"
 
 
