@@ -1637,7 +1637,7 @@ RGL_API rgl_status_t rgl_gb300_server_configure_schedule(rgl_gb300_server_t serv
 	return safeCall([&]() {
 		CHECK_ARG(server != nullptr);
 		CHECK_ARG(block == 64 || block == 128 || block == 256);
-		CHECK_ARG(order == rgl::kOrderNatural || order == rgl::kOrderOctahedral || order == rgl::kOrderMorton);
+		CHECK_ARG(order >= rgl::kOrderNatural && order <= rgl::kOrderElevation);
 		CHECK_ARG(chunk >= 1 && chunk <= 64);
 		CHECK_ARG(regs == 64 || regs == 80 || regs == 96 || regs == 128);
 		CHECK_ARG(max_batch_beams >= 1);

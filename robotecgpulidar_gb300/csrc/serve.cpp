@@ -185,6 +185,32 @@ uint32_t octahedralKey(const rgl::Mat34& m)
 	auto q = [](float c) { return (uint32_t) std::min(2047.0f, std::max(0.0f, (c * 0.5f + 0.5f) * 2048.0f)); };
 	return (spread2(q(u)) << 1) | spread2(q(v));
 }
+
+// 22-bit key of a sensor-local ray direction in scan-row order: the sine of its elevation above the
+// local xy plane in the high 11 bits, a pseudo-angle of its azimuth (monotonic in atan2(y, x), in
+// (-2, 2]) in the low 11 bits. Beams of one row travel similar distances, so a warp's lanes finish
+// together more often than in direction patches.
+uint32_t rowKey(const rgl::Mat34& m)
+{
+	const float x = m.m[0][2], y = m.m[1][2], z = m.m[2][2];
+	const float len = std::sqrt(x * x + y * y + z * z);
+	const float l1 = std::fabs(x) + std::fabs(y);
+	const float pa = l1 > 0.0f ? 1.0f - x / l1 : 0.0f;
+	const float az = y < 0.0f ? -pa : pa;
+	auto q = [](float c) { return (uint32_t) std::min(2047.0f, std::max(0.0f, c * 2048.0f)); };
+	return (q(len > 0.0f ? z / len * 0.5f + 0.5f : 0.5f) << 11) | q(az * 0.25f + 0.5f);
+}
+
+std::vector<uint32_t> sortedBy(const rgl::Mat34* mats, int32_t count, uint32_t (*key)(const rgl::Mat34&))
+{
+	std::vector<uint32_t> k(count), order(count);
+	for (int32_t i = 0; i < count; ++i) {
+		k[i] = key(mats[i]);
+		order[i] = (uint32_t) i;
+	}
+	std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return k[a] < k[b]; });
+	return order;
+}
 } // namespace
 
 int32_t Server::addPattern(const void* rays, int32_t count)
@@ -192,16 +218,14 @@ int32_t Server::addPattern(const void* rays, int32_t count)
 	auto p = std::make_unique<Pattern>();
 	RGL_CHECK_CUDA(cudaMemcpy(p->rays.ensure(sizeof(rgl::Mat34) * (size_t) count), rays, sizeof(rgl::Mat34) * (size_t) count,
 	                          cudaMemcpyHostToDevice));
-	// Visiting order: a warp casts 32 beams; sorted by direction, they form a compact patch of the
-	// pattern instead of, e.g., one column of channels. Results stay in beam order.
+	// Visiting orders: a warp casts 32 beams (or 6 beams of 5 sub-rays); sorted by direction they form
+	// a compact patch of the pattern, sorted by rows a stretch of one elevation, instead of, e.g., one
+	// column of channels. Results stay in beam order.
 	const auto* mats = static_cast<const rgl::Mat34*>(rays);
-	std::vector<uint32_t> key(count), order(count);
-	for (int32_t i = 0; i < count; ++i) {
-		key[i] = octahedralKey(mats[i]);
-		order[i] = (uint32_t) i;
-	}
-	std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
-	RGL_CHECK_CUDA(cudaMemcpy(p->order.ensure(sizeof(uint32_t) * (size_t) count), order.data(), sizeof(uint32_t) * (size_t) count,
+	const std::vector<uint32_t> byDirection = sortedBy(mats, count, octahedralKey), byRow = sortedBy(mats, count, rowKey);
+	RGL_CHECK_CUDA(cudaMemcpy(p->order.ensure(sizeof(uint32_t) * (size_t) count), byDirection.data(), sizeof(uint32_t) * (size_t) count,
+	                          cudaMemcpyHostToDevice));
+	RGL_CHECK_CUDA(cudaMemcpy(p->rowOrder.ensure(sizeof(uint32_t) * (size_t) count), byRow.data(), sizeof(uint32_t) * (size_t) count,
 	                          cudaMemcpyHostToDevice));
 	p->count = count;
 	std::lock_guard<std::mutex> g(m);
@@ -455,7 +479,9 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after)
 		b.p.out.isHit = flags + pointBase;
 		b.p.out.entityId = ent + pointBase;
 		b.samples = nullptr; // one sample per beam: never read
-		b.order = sched.order == rgl::kOrderNatural ? nullptr : patterns[r.pattern]->order.as<uint32_t>();
+		b.order = sched.order == rgl::kOrderNatural     ? nullptr
+		          : sched.order == rgl::kOrderElevation ? patterns[r.pattern]->rowOrder.as<uint32_t>()
+		                                                : patterns[r.pattern]->order.as<uint32_t>();
 		b.groupSize = 1;
 		b.hasRayTransform = 1;
 		b.rayTransform = r.pose;

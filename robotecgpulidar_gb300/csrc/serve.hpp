@@ -105,7 +105,8 @@ private:
 	struct Pattern
 	{
 		rgl::DeviceBuffer rays{false};
-		rgl::DeviceBuffer order{false}; // beams sorted by octahedral direction: warps get compact patches
+		rgl::DeviceBuffer order{false};    // beams sorted by octahedral direction: warps get compact patches
+		rgl::DeviceBuffer rowOrder{false}; // beams sorted by elevation, then azimuth: warps get stretches of a row
 		int32_t count = 0;
 	};
 	// One in-flight batch slot: device and pinned buffers reused by every batch launched from it.
@@ -164,7 +165,7 @@ private:
 
 	int64_t budget;
 	int maxInFlight;
-	rgl::BatchSchedule schedule{128, rgl::kPackLaneGroup, rgl::kOrderOctahedral, 1, 128}; // guarded by m
+	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderElevation, 1, 128}; // guarded by m
 	int64_t maxBatchBeams = 8 << 20;                                                       // guarded by m
 	cudaStream_t stream = nullptr;
 	std::vector<std::unique_ptr<Pattern>> patterns;

@@ -236,8 +236,8 @@ def test_batches_of_varying_size_complete_and_host_results_match(rgl):
 
 
 def test_server_schedule_changes_speed_only(rgl):
-    """Natural and octahedral beam order, other block/register shapes and batches capped at a few
-    thousand beams (every request its own batch) give byte-identical results."""
+    """Scan-row, natural and octahedral beam order, other block/register shapes and batches capped at
+    a few thousand beams (every request its own batch) give byte-identical results."""
     (sa, _), (sb, _) = two_scenes(rgl)
     srv = rgl.Server(8 << 30, 2)
     try:
@@ -245,7 +245,8 @@ def test_server_schedule_changes_speed_only(rgl):
         specs = [(sa if k % 2 else sb, pats[k % len(pats)], pose(300 + k), rgl.RGL_RETURN_FIRST_LAST if k % 3 else rgl.RGL_RETURN_FIRST)
                  for k in range(16)]
         runs = []
-        for sched in (dict(), dict(order=0), dict(block=128, regs=64, chunk=4), dict(order=2, regs=128, max_batch_beams=4096)):
+        for sched in (dict(), dict(order=0), dict(block=128, regs=64, chunk=4), dict(order=2, regs=128, max_batch_beams=4096),
+                      dict(order=1, block=128)):
             srv.configure_schedule(**sched)
             reqs = [srv.submit(sc, p, tf, mode, 0.1, 90.0) for sc, p, tf, mode in specs]
             for r in reqs:
