@@ -75,8 +75,11 @@ rgl_status_t updateState(rgl_status_t s, std::optional<std::string> msg = std::n
 	return s;
 }
 
+// Calls that cannot change what a graph's validation finds (runs, result reads, poses, statistics)
+// use safeCallKeepingValidation; every other call counts as a possible graph edit (noteGraphEdit), so
+// a batched frame re-validates its graphs only after some other call.
 template<class Fn>
-rgl_status_t safeCall(Fn&& fn)
+rgl_status_t safeCallKeepingValidation(Fn&& fn)
 {
 	static bool initTried = false;
 	if (!initTried) {
@@ -119,6 +122,13 @@ rgl_status_t safeCall(Fn&& fn)
 		return updateState(RGL_INTERNAL_EXCEPTION, std::string("exceptional exception"));
 	}
 	return updateState(RGL_SUCCESS);
+}
+
+template<class Fn>
+rgl_status_t safeCall(Fn&& fn)
+{
+	noteGraphEdit();
+	return safeCallKeepingValidation(std::forward<Fn>(fn));
 }
 
 #define CHECK_ARG(expr)                                                                                                        \
@@ -439,7 +449,7 @@ RGL_API rgl_status_t rgl_entity_destroy(rgl_entity_t entity)
 
 RGL_API rgl_status_t rgl_entity_set_transform(rgl_entity_t entity, const rgl_mat3x4f* transform)
 {
-	const rgl_status_t status = safeCall([&]() {
+	const rgl_status_t status = safeCallKeepingValidation([&]() {
 		CHECK_ARG(entity != nullptr);
 		CHECK_ARG(transform != nullptr);
 		GraphRunCtx::synchronizeAll();
@@ -576,7 +586,7 @@ RGL_API rgl_status_t rgl_scene_set_time(rgl_scene_t scene, uint64_t nanoseconds)
 
 RGL_API rgl_status_t rgl_graph_run(rgl_node_t raw_node)
 {
-	const rgl_status_t status = safeCall([&]() {
+	const rgl_status_t status = safeCallKeepingValidation([&]() {
 		CHECK_ARG(raw_node != nullptr);
 		auto node = getNode(raw_node);
 		if (!node->ctx) {
@@ -600,7 +610,7 @@ RGL_API rgl_status_t rgl_graph_destroy(rgl_node_t raw_node)
 
 RGL_API rgl_status_t rgl_graph_get_result_size(rgl_node_t node, rgl_field_t field, int32_t* out_count, int32_t* out_size_of)
 {
-	const rgl_status_t status = safeCall([&]() {
+	const rgl_status_t status = safeCallKeepingValidation([&]() {
 		CHECK_ARG(node != nullptr);
 		auto pn = getNodeAs<PointsNode>(node, "IPointsNode");
 		if (pn->dirty || !pn->ctx) {
@@ -622,7 +632,7 @@ RGL_API rgl_status_t rgl_graph_get_result_size(rgl_node_t node, rgl_field_t fiel
 
 RGL_API rgl_status_t rgl_graph_get_result_data(rgl_node_t node, rgl_field_t field, void* dst)
 {
-	const rgl_status_t status = safeCall([&]() {
+	const rgl_status_t status = safeCallKeepingValidation([&]() {
 		CHECK_ARG(node != nullptr);
 		CHECK_ARG(dst != nullptr);
 		auto pn = getNodeAs<PointsNode>(node, "IPointsNode");
@@ -1175,7 +1185,7 @@ RGL_API rgl_status_t rgl_gb300_configure_timing(bool enable)
 
 RGL_API rgl_status_t rgl_gb300_graph_get_timing(rgl_node_t node, float* out_run_ms, float* out_trace_ms)
 {
-	return safeCall([&]() {
+	return safeCallKeepingValidation([&]() {
 		CHECK_ARG(node != nullptr);
 		auto n = getNode(node);
 		if (!n->ctx) {
@@ -1193,7 +1203,7 @@ RGL_API rgl_status_t rgl_gb300_graph_get_timing(rgl_node_t node, float* out_run_
 
 RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node)
 {
-	return safeCall([&]() {
+	return safeCallKeepingValidation([&]() {
 		CHECK_ARG(node != nullptr);
 		auto n = getNode(node);
 		if (n->ctx) {
@@ -1204,7 +1214,7 @@ RGL_API rgl_status_t rgl_gb300_graph_sync(rgl_node_t node)
 
 RGL_API rgl_status_t rgl_gb300_get_kernel_launch_count(uint64_t* out_count)
 {
-	return safeCall([&]() {
+	return safeCallKeepingValidation([&]() {
 		CHECK_ARG(out_count != nullptr);
 		*out_count = launchCount();
 	});
@@ -1337,7 +1347,7 @@ RGL_API rgl_status_t rgl_gb300_batch_create(rgl_gb300_batch_t* out_batch, const 
 
 RGL_API rgl_status_t rgl_gb300_batch_run(rgl_gb300_batch_t batch)
 {
-	return safeCall([&]() {
+	return safeCallKeepingValidation([&]() {
 		CHECK_ARG(batch != nullptr);
 		Batches::get(batch, "Batch")->run();
 	});
@@ -1436,7 +1446,7 @@ RGL_API rgl_status_t rgl_gb300_batch_get_tuning(rgl_gb300_batch_t batch, int32_t
 RGL_API rgl_status_t rgl_gb300_batch_get_stats(rgl_gb300_batch_t batch, float* out_frame_ms, float* out_trace_ms, int64_t* out_beams,
                                                int64_t* out_rays, int64_t* out_captures, int64_t* out_replays, int64_t* out_tunings)
 {
-	return safeCall([&]() {
+	return safeCallKeepingValidation([&]() {
 		CHECK_ARG(batch != nullptr);
 		auto b = Batches::get(batch, "Batch");
 		b->synchronize();

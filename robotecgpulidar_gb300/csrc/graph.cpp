@@ -37,6 +37,12 @@ void setTraceSchedule(const rgl::BatchSchedule& s) { gTraceSchedule = s; }
 bool timingEnabled() { return gTiming; }
 void setTimingEnabled(bool on) { gTiming = on; }
 bool cudaGraphsEnabled() { return gCudaGraphs; }
+
+namespace {
+std::atomic<uint64_t> gGraphEdits{1};
+} // namespace
+void noteGraphEdit() { gGraphEdits.fetch_add(1, std::memory_order_relaxed); }
+uint64_t graphEditEpoch() { return gGraphEdits.load(std::memory_order_relaxed); }
 void setCudaGraphsEnabled(bool on) { gCudaGraphs = on; }
 
 void recordEvent(cudaEvent_t ev, cudaStream_t s)
@@ -1461,19 +1467,29 @@ void GraphRunCtx::run()
 	RGL_CHECK_CUDA(cudaEventRecord(done, stream_));
 }
 
+// As run() but without the nodes' validation when no API call that may change a graph came since
+// this graph's last successful validation (a frame after frame of re-posed entities).
 uint64_t GraphRunCtx::validateForBatch()
 {
 	synchronize();
 	if (order.empty()) {
 		order = findExecutionOrder(nodes);
 		releaseGraph();
+		validated = false;
 	}
+	const uint64_t epoch = graphEditEpoch();
+	const bool fresh = validated && validatedEpoch == epoch;
+	validated = false;
 	uint64_t version = 0;
 	for (auto& n : order) {
-		n->validateImpl();
+		if (!fresh) {
+			n->validateImpl();
+		}
 		n->dirty = false;
 		version = std::max(version, n->paramVersion);
 	}
+	validated = true;
+	validatedEpoch = epoch;
 	return version;
 }
 

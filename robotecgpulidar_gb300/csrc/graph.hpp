@@ -655,6 +655,8 @@ private:
 	cudaStream_t stream_ = nullptr;
 	cudaEvent_t done = nullptr, runStart = nullptr, runStop = nullptr;
 	cudaEvent_t batchDone = nullptr; // completion of the graph's part of the last batched frame
+	uint64_t validatedEpoch = 0;     // graphEditEpoch() of the last successful batch validation
+	bool validated = false;
 	bool running = false;
 	bool batchedLast = false; // the last run was part of a batched frame (no per-graph timing)
 	// Captured run: replayed while no node changed and no buffer moved.
@@ -674,3 +676,7 @@ bool cudaGraphsEnabled();
 void setCudaGraphsEnabled(bool on);
 // Records `ev` on `s`; inside a stream capture the record becomes a node of the captured graph.
 void recordEvent(cudaEvent_t ev, cudaStream_t s);
+// Counter of API calls that may have changed a graph (nodes, parameters, links, scene time): a
+// graph validated at the current value needs no validation again.
+void noteGraphEdit();
+uint64_t graphEditEpoch();

@@ -289,6 +289,33 @@ def test_repose_reaches_traversal_without_recapture(rgl, oracle):
     rgl.batch_destroy(batch)
 
 
+def test_batch_validation_follows_graph_edits(rgl):
+    """Frames that only re-pose entities keep the graphs' last validation; any other API call may edit
+    a graph, so the next frame validates again and reports what the edit broke."""
+    scene, ents, graphs, batch = build_batch(rgl)
+    rgl.batch_configure_schedule(batch, autotune=False)
+    reseed(rgl, graphs)
+    rgl.batch_run(batch)
+    rng = np.random.default_rng(21)
+    for i, tf in scenes.repose(scene, 0.25, rng):
+        rgl.entity_set_transform(ents[i], tf)
+    rgl.batch_run(batch)  # nothing but poses changed since the last frame (the noise frame advanced to 1)
+    batched = [collect(rgl, g) for g in graphs]
+    assert_same(rgl, batched, solo_results(rgl, graphs, frame=1))
+    # Two ranges for a pattern of many rays: the graph no longer validates.
+    rgl.rays_set_range(graphs[1]["range"], [[0.1, 90.0], [0.1, 90.0]])
+    with pytest.raises(rgl.RGLError) as e:
+        rgl.batch_run(batch)
+    assert e.value.status == rgl.RGL_INVALID_PIPELINE
+    assert "doesn't match number of rays" in str(e.value)
+    rgl.rays_set_range(graphs[1]["range"], [[0.1, 90.0]])
+    reseed(rgl, graphs)
+    rgl.batch_run(batch)
+    batched = [collect(rgl, g) for g in graphs]
+    assert_same(rgl, batched, solo_results(rgl, graphs))
+    rgl.batch_destroy(batch)
+
+
 def test_batch_recaptures_on_structure_change(rgl):
     scene, ents, graphs, batch = build_batch(rgl)
     rgl.batch_configure_schedule(batch, autotune=False)
