@@ -174,6 +174,11 @@ __global__ void __maxnreg__(REGS) kTraceBatch(const BatchJob* __restrict__ jobs,
 	// serialization may start its blocks as this grid's blocks exit (the first warp of each block to
 	// get here triggers for the block). The next launch reads nothing this one writes.
 	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+	// Launched that way itself, a launch ends only after the launch before it has completed: later work
+	// on the stream, which waits for this launch, then also follows every earlier one, and each
+	// launch's counter block is re-armed before the stream reaches the next launch that uses it. A
+	// launch without a programmatic predecessor passes this at once.
+	asm volatile("griddepcontrol.wait;" ::: "memory");
 	// The last block to finish re-arms both counters for the next launch, so no launch needs a memset
 	// first: every block has left the task loop when it counts itself finished.
 	__syncthreads();
