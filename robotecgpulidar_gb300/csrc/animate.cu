@@ -35,7 +35,7 @@ __global__ void kSkin(int n, const float* __restrict__ rest, const BoneWeights* 
 		const int b = w.bone[k];
 		if (b < 0 || b >= nBones) {
 			if (w.weight[k] != 0.0f) {
-				atomicExch(errorFlag, 1); // a weighted bone outside the pose: reported, not read
+				*(volatile int32_t*) errorFlag = 1; // a weighted bone outside the pose: reported, not read
 			}
 			continue;
 		}

@@ -230,9 +230,9 @@ namespace {
 constexpr int kSlotsPerChunk = 4096;
 struct SlotChunk
 {
-	int32_t* dev = nullptr;
-	int32_t* host = nullptr;
-	int highWater = 0; // slots ever handed out; the refresh copies this many
+	int32_t* dev = nullptr;           // device address of `host` (mapped pinned memory)
+	volatile int32_t* host = nullptr;
+	int highWater = 0; // slots ever handed out
 	std::vector<int> freeList;
 };
 std::mutex slotMutex;
@@ -272,16 +272,18 @@ int32_t* ErrorSlot::device()
 		}
 		if (c < 0) {
 			SlotChunk n;
-			RGL_CHECK_CUDA(cudaMalloc(&n.dev, sizeof(int32_t) * kSlotsPerChunk));
-			RGL_CHECK_CUDA(cudaMemset(n.dev, 0, sizeof(int32_t) * kSlotsPerChunk));
-			RGL_CHECK_CUDA(cudaMallocHost(&n.host, sizeof(int32_t) * kSlotsPerChunk));
-			std::memset(n.host, 0, sizeof(int32_t) * kSlotsPerChunk);
+			void* h = nullptr;
+			RGL_CHECK_CUDA(cudaHostAlloc(&h, sizeof(int32_t) * kSlotsPerChunk, cudaHostAllocMapped | cudaHostAllocPortable));
+			std::memset(h, 0, sizeof(int32_t) * kSlotsPerChunk);
+			void* d = nullptr;
+			RGL_CHECK_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+			n.host = static_cast<volatile int32_t*>(h);
+			n.dev = static_cast<int32_t*>(d);
 			n.highWater = 1;
 			chunks.push_back(std::move(n));
 			c = (int) chunks.size() - 1;
 			i = 0;
 		}
-		RGL_CHECK_CUDA(cudaMemset(chunks[c].dev + i, 0, sizeof(int32_t)));
 		chunks[c].host[i] = 0;
 		chunk_ = c;
 		index_ = i;
@@ -304,19 +306,14 @@ void ErrorSlot::clear()
 		return;
 	}
 	std::lock_guard<std::mutex> g(slotMutex);
-	auto& c = slotChunks()[chunk_];
-	RGL_CHECK_CUDA(cudaMemset(c.dev + index_, 0, sizeof(int32_t)));
-	c.host[index_] = 0;
+	slotChunks()[chunk_].host[index_] = 0;
 }
 
 void refreshErrorSlots()
 {
-	std::lock_guard<std::mutex> g(slotMutex);
-	for (auto& c : slotChunks()) {
-		if (c.highWater > 0) {
-			RGL_CHECK_CUDA(cudaMemcpy(c.host, c.dev, sizeof(int32_t) * c.highWater, cudaMemcpyDeviceToHost));
-		}
-	}
+	// The kernels' stores to mapped memory are visible once their completion has been observed (an
+	// event or stream synchronisation); the fence keeps the compiler and CPU from reading earlier.
+	std::atomic_thread_fence(std::memory_order_acquire);
 }
 
 void ensureCudaInitialized()

@@ -100,9 +100,10 @@ private:
 	bool tracked_ = true;
 };
 
-// Device-side error flag of a kernel (stack overflow, look-back timeout, ...). The flags of all
-// nodes live in shared chunks of int32 slots, so a completed run checks every flag with one
-// device-to-host copy per chunk (refreshErrorSlots) instead of one blocking copy per node.
+// Error flag of a kernel (stack overflow, look-back timeout, ...). The flags of all nodes live in
+// shared chunks of int32 slots in mapped pinned host memory: a kernel raises one with a plain store of
+// 1 through the device address, and a completed run checks its flags by reading host memory, with no
+// copy (result reads would otherwise pay one blocking device-to-host copy each).
 class ErrorSlot
 {
 public:
@@ -112,16 +113,17 @@ public:
 	~ErrorSlot();
 	// Device address of the flag (zero when first handed out). Allocates: call outside stream capture.
 	int32_t* device();
-	// Value of the flag at the last refreshErrorSlots().
+	// Value of the flag; valid once the work that may raise it has completed.
 	bool raised() const;
-	// Resets the flag on the device and in the host copy.
+	// Resets the flag (no work that may raise it may be running).
 	void clear();
 
 private:
 	int chunk_ = -1;
 	int index_ = -1;
 };
-// Copies every flag to the host. Call after the work that may raise them has completed.
+// Orders the host's later reads of the flags after the completion it has just observed. Call after
+// the work that may raise them has completed.
 void refreshErrorSlots();
 
 // Grow-only pinned host allocation.

@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(kBlock) kCompact(const int32_t* __restrict__ f
 	}
 	if (tid == 0) {
 		if (lbFail) {
-			atomicExch(errorFlag, 1);
+			*(volatile int32_t*) errorFlag = 1; // an error slot in mapped host memory (or a device word)
 		}
 		const uint32_t run = tileKept;
 		if (tile > 0) {

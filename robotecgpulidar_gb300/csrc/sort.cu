@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kThreads) kOnesweep(const uint32_t* __restrict
 				uint32_t flag = s & ~kValueMask;
 				if (flag == 0u) {
 					if (++spins > kSpinLimit) {
-						atomicExch(errorFlag, 1);
+						*(volatile int32_t*) errorFlag = 1;
 						break;
 					}
 					continue;

@@ -163,7 +163,7 @@ __global__ void __maxnreg__(REGS) kTraceBatch(const BatchJob* __restrict__ jobs,
 			}
 			if (st.overflow) {
 				if (job->p.errorFlag) {
-					atomicExch(job->p.errorFlag, 1);
+					*(volatile int32_t*) job->p.errorFlag = 1; // an error slot in mapped host memory
 				}
 				st.overflow = false;
 				st.sp = 0;
