@@ -122,6 +122,28 @@ def test_skeleton_animation_matches_oracle(rgl, oracle):
     assert rel.max() <= 1e-5
 
 
+def test_bone_outside_the_pose_raises_the_kernel_flag(rgl):
+    """A weighted bone index beyond the pose is found by the skinning kernel, which raises its error
+    flag (a slot in mapped host memory); the call fails with the reference's kind of error, and once
+    the weights are fixed the same pose applies."""
+    lib = rgl.lib()
+    g = grid_mesh()
+    m = rgl.mesh_create(g.vertices, g.indices)
+    e = rgl.entity_create(m)
+    w, restposes = skin_setup(rgl, g)
+    w["b"][::7, 1] = 5  # bone 5 of a two-bone pose
+    w["w"][::7, 0] = 0.5
+    w["w"][::7, 1] = 0.5
+    rgl.check(lib.rgl_mesh_set_bone_weights(m, rgl.ptr(w), len(w)))
+    rgl.check(lib.rgl_mesh_set_restposes(m, rgl.ptr(restposes), 2))
+    pose = np.stack([scenes.translation(0, 0, 0), scenes.trs((0.0, 0.0, 0.8), (0.0, -0.3, 0.0))]).astype(np.float32)
+    st = lib.rgl_entity_set_pose_world(e, rgl.ptr(pose), 2)
+    assert st == rgl.RGL_INVALID_ARGUMENT and "outside the pose" in rgl.last_error()
+    w_ok, _ = skin_setup(rgl, g)
+    rgl.check(lib.rgl_mesh_set_bone_weights(m, rgl.ptr(w_ok), len(w_ok)))
+    rgl.check(lib.rgl_entity_set_pose_world(e, rgl.ptr(pose), 2))
+
+
 def test_hit_velocity_of_animated_vertices(rgl, oracle):
     lib = rgl.lib()
     g = grid_mesh()
