@@ -713,6 +713,8 @@ def run_serving(args):
 
     # ---- served
     srv = rgl.Server(SERVE_BUDGET, 2)
+    if args.max_batch_beams:
+        srv.configure_schedule(max_batch_beams=args.max_batch_beams)
     pats = [srv.add_pattern(r) for r in rays_of]
     warm = [srv.submit(handles[fleet[k].scene], pats[k], fleet[k].pose, modes[k % 2], *RANGE) for k in range(SERVE_ROBOTS)]
     srv.drain()
@@ -902,6 +904,7 @@ def main():
     ap.add_argument("--waves", type=int, default=0, help="multi_sensor: waves per batched frame (0: automatic)")
     ap.add_argument("--trace-seconds", type=float, default=30.0, help="serving: length of each arrival trace")
     ap.add_argument("--max-lag", type=float, default=5.0, help="serving: stop a trace once the loop lags arrivals by this much (s)")
+    ap.add_argument("--max-batch-beams", type=int, default=0, help="serving: most beams per batch (0: the library's default)")
     ap.add_argument("--capacity-requests", type=int, default=2000, help="serving: requests of the all-at-once capacity run")
     ap.add_argument("--blas-builder", choices=list(BLAS_BUILDERS), default="device_sah",
                     help="mesh BLAS builder: binned SAH on the device (default), the same tree built on the host, or the device LBVH")

@@ -249,7 +249,7 @@ RGL_API rgl_status_t rgl_gb300_server_drain(rgl_gb300_server_t server);
  * rgl_gb300_batch_configure_schedule; order 0 casts a pattern's beams in the given order, 1 and 2 in
  * its octahedral direction order, 3 in its scan-row order: elevation, then azimuth) and the most beams
  * coalesced into one batch (>= 1; a single larger request still forms a batch of its own). Applies to
- * batches launched afterwards; changes speed only, never results. Defaults: 256, 3, 1, 128 and 8 Mi
+ * batches launched afterwards; changes speed only, never results. Defaults: 256, 3, 1, 128 and 4 Mi
  * beams.
  */
 RGL_API rgl_status_t rgl_gb300_server_configure_schedule(rgl_gb300_server_t server, int32_t block, int32_t order, int32_t chunk,

@@ -166,7 +166,7 @@ private:
 	int64_t budget;
 	int maxInFlight;
 	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderElevation, 1, 128}; // guarded by m
-	int64_t maxBatchBeams = 8 << 20;                                                       // guarded by m
+	int64_t maxBatchBeams = 4 << 20;                                                       // guarded by m
 	cudaStream_t stream = nullptr;
 	std::vector<std::unique_ptr<Pattern>> patterns;
 	std::vector<std::unique_ptr<Slot>> slots;

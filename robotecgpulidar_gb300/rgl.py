@@ -598,7 +598,7 @@ class Server:
     def drain(self):
         check(lib().rgl_gb300_server_drain(self.h))
 
-    def configure_schedule(self, block=256, order=3, chunk=1, regs=128, max_batch_beams=8 << 20):
+    def configure_schedule(self, block=256, order=3, chunk=1, regs=128, max_batch_beams=4 << 20):
         check(lib().rgl_gb300_server_configure_schedule(self.h, block, order, chunk, regs, max_batch_beams))
 
     def stats(self) -> dict:
