@@ -728,6 +728,7 @@ def run_serving(args):
     for rate in args.rates:
         arr, robots, mode, poses = make_trace(rate, int(rate))
         st0 = srv.stats()
+        srv.batch_times(reset=True)
         lat, rays_done, t_last, i, saturated = [], 0, 0.0, 0, False
         outstanding = {}
         t0 = time.perf_counter()
@@ -762,6 +763,7 @@ def run_serving(args):
         res["batches"] = st1["batches"] - st0["batches"]
         res["mean_requests_per_batch"] = (st1["requests_in_batches"] - st0["requests_in_batches"]) / max(1, res["batches"])
         res["offered_mrays_s"] = sum(fleet[int(k)].rays for k in robots) / args.trace_seconds / 1e6
+        res["batch_phases"] = srv.batch_times(reset=True)
         served[str(int(rate))] = res
     # Capacity: the same request mix submitted at once, results read as requests complete (three
     # times, to show the spread; the best run is reported).

@@ -259,3 +259,12 @@ RGL_API rgl_status_t rgl_gb300_server_configure_schedule(rgl_gb300_server_t serv
 RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64_t* out_submitted, int64_t* out_completed,
                                                 int64_t* out_failed, int64_t* out_batches, int64_t* out_requests_in_batches,
                                                 int64_t* out_peak_reserved_bytes, int64_t* out_device_us);
+
+/*
+ * Phases of the batches retired since the last call with `reset` (or since creation), on the device's
+ * clock, three entries each: traversal and compaction (launch to kept counts published), the server's
+ * reaction (counts published to the first result copy enqueued), the result copies. out_max_ms gets
+ * the longest of each phase, out_over_5ms how many batches spent more than 5 ms in it.
+ */
+RGL_API rgl_status_t rgl_gb300_server_get_batch_times(rgl_gb300_server_t server, bool reset, float* out_max_ms, int64_t* out_over_5ms,
+                                                      int64_t* out_batches);

@@ -1672,6 +1672,20 @@ RGL_API rgl_status_t rgl_gb300_server_get_stats(rgl_gb300_server_t server, int64
 	});
 }
 
+RGL_API rgl_status_t rgl_gb300_server_get_batch_times(rgl_gb300_server_t server, bool reset, float* out_max_ms, int64_t* out_over_5ms,
+                                                      int64_t* out_batches)
+{
+	return safeCallKeepingValidation([&]() {
+		CHECK_ARG(server != nullptr);
+		const Server::BatchTimes t = Servers::get(server, "Server")->batchTimes(reset);
+		for (int k = 0; k < 3; ++k) {
+			if (out_max_ms) out_max_ms[k] = t.maxMs[k];
+			if (out_over_5ms) out_over_5ms[k] = t.over5ms[k];
+		}
+		if (out_batches) *out_batches = t.batches;
+	});
+}
+
 RGL_API rgl_status_t rgl_gb300_configure_trace_schedule(int32_t block, int32_t packing, int32_t chunk, int32_t regs)
 {
 	return safeCall([&]() {

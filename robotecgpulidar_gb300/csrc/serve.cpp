@@ -66,6 +66,8 @@ Server::Server(int64_t hbmBudgetBytes, int32_t maxInFlightBatches) : budget(hbmB
 		RGL_CHECK_CUDA(cudaEventCreateWithFlags(&s->counted, cudaEventDisableTiming));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t0));
 		RGL_CHECK_CUDA(cudaEventCreate(&s->t1));
+		RGL_CHECK_CUDA(cudaEventCreate(&s->tCounted));
+		RGL_CHECK_CUDA(cudaEventCreate(&s->tCopy));
 		RGL_CHECK_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
 		RGL_CHECK_CUDA(cudaMemset(s->counter.ensure(rgl::kTraceCounterBytes), 0, rgl::kTraceCounterBytes));
 		slots.push_back(std::move(s));
@@ -110,6 +112,8 @@ Server::~Server()
 		cudaEventDestroy(s->counted);
 		cudaEventDestroy(s->t0);
 		cudaEventDestroy(s->t1);
+		cudaEventDestroy(s->tCounted);
+		cudaEventDestroy(s->tCopy);
 		cudaStreamDestroy(s->stream);
 	}
 	cudaStreamDestroy(stream);
@@ -212,6 +216,16 @@ std::vector<uint32_t> sortedBy(const rgl::Mat34* mats, int32_t count, uint32_t (
 	return order;
 }
 } // namespace
+
+Server::BatchTimes Server::batchTimes(bool reset)
+{
+	std::lock_guard<std::mutex> g(m);
+	const BatchTimes out = bt;
+	if (reset) {
+		bt = BatchTimes{};
+	}
+	return out;
+}
 
 int32_t Server::addPattern(const void* rays, int32_t count)
 {
@@ -526,6 +540,7 @@ void Server::launch(Slot& slot, const rgl::BatchSchedule& sched, Slot* after)
 	// the other slot's result copies on the copy engine, and this batch's successor waits for it.
 	rgl::launchPublishWords(dResults, slot.hResultsDev, 2 * n, slot.stream);
 	RGL_CHECK_CUDA(cudaEventRecord(slot.counted, slot.stream));
+	RGL_CHECK_CUDA(cudaEventRecord(slot.tCounted, slot.stream));
 	slot.phase = Phase::Tracing;
 	RGL_CHECK_CUDA(cudaLaunchHostFunc(slot.stream, &Server::batchDone, this));
 }
@@ -538,6 +553,7 @@ void Server::copyOut(Slot& slot)
 	const auto* hCounts = static_cast<const volatile int32_t*>(slot.hResults.get());
 	const size_t n = slot.reqs.size();
 	const auto* staged = slot.staged.as<float>();
+	RGL_CHECK_CUDA(cudaEventRecord(slot.tCopy, slot.stream));
 	for (size_t j = 0; j < n; ++j) {
 		const Request& r = *slot.reqs[j];
 		const int64_t kept = hCounts[j];
@@ -571,10 +587,20 @@ void Server::retire(Slot& slot)
 	const auto* hCounts = static_cast<const int32_t*>(slot.hResults.get());
 	const size_t n = slot.reqs.size();
 	const auto now = Clock::now();
-	float ms = 0.0f;
+	float ms = 0.0f, phase[3] = {0.0f, 0.0f, 0.0f};
 	cudaEventElapsedTime(&ms, slot.t0, slot.t1);
+	const bool timed = cudaEventElapsedTime(&phase[0], slot.t0, slot.tCounted) == cudaSuccess &&
+	                   cudaEventElapsedTime(&phase[1], slot.tCounted, slot.tCopy) == cudaSuccess &&
+	                   cudaEventElapsedTime(&phase[2], slot.tCopy, slot.t1) == cudaSuccess;
 	std::lock_guard<std::mutex> g(m);
 	st.deviceSeconds += ms * 1e-3;
+	if (timed) {
+		for (int k = 0; k < 3; ++k) {
+			bt.maxMs[k] = std::max(bt.maxMs[k], phase[k]);
+			bt.over5ms[k] += phase[k] > 5.0f ? 1 : 0;
+		}
+		++bt.batches;
+	}
 	for (size_t j = 0; j < n; ++j) {
 		Request& r = *slot.reqs[j];
 		const bool failed = hCounts[n + j] != 0;

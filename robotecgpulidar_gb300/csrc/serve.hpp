@@ -74,6 +74,18 @@ struct Server
 	};
 	Stats stats();
 
+	// Phases of the batches retired since the last reset, on the device's clock: traversal and
+	// compaction (launch to counts published), the host's reaction (counts published to the first
+	// result copy enqueued: the scheduler's wake-up), the result copies. Per phase the longest and the
+	// number above 5 ms.
+	struct BatchTimes
+	{
+		float maxMs[3] = {0.0f, 0.0f, 0.0f};
+		int64_t over5ms[3] = {0, 0, 0};
+		int64_t batches = 0;
+	};
+	BatchTimes batchTimes(bool reset);
+
 private:
 	enum class State
 	{
@@ -126,6 +138,7 @@ private:
 		cudaStream_t stream = nullptr;  // slots run on their own streams: one batch's tail overlaps the next
 		cudaEvent_t counted = nullptr, done = nullptr;
 		cudaEvent_t t0 = nullptr, t1 = nullptr; // device time of the batch
+		cudaEvent_t tCounted = nullptr, tCopy = nullptr; // counts published; first result copy enqueued
 		rgl::DeviceBuffer tables{false}, tileCounts{false}, tileOffsets{false}, results{false}, counter{false};
 		rgl::DeviceBuffer rawFlags{false}, rawXyz{false}, rawDist{false}, rawEnt{false};
 		rgl::DeviceBuffer staged{false}; // compacted results: per request one block, xyz | distance | entity id
@@ -182,6 +195,7 @@ private:
 	int64_t nextId = 1;
 	int64_t reserved = 0;
 	Stats st;
+	BatchTimes bt; // guarded by m
 	bool stop = false;
 	uint64_t wakeups = 0; // bumped (under m) by submissions, releases and finished batches
 	std::thread worker;

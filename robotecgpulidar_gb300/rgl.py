@@ -222,6 +222,7 @@ def _proto(l):
         "rgl_gb300_server_release": [vp, C.c_int64],
         "rgl_gb300_server_drain": [vp],
         "rgl_gb300_server_configure_schedule": [vp, i32, i32, i32, i32, C.c_int64],
+        "rgl_gb300_server_get_batch_times": [vp, C.c_bool, P(f), P(C.c_int64), P(C.c_int64)],
         "rgl_gb300_server_get_stats": [vp] + [P(C.c_int64)] * 7,
     }
     for name, args in sigs.items():
@@ -600,6 +601,16 @@ class Server:
 
     def configure_schedule(self, block=256, order=3, chunk=1, regs=128, max_batch_beams=4 << 20):
         check(lib().rgl_gb300_server_configure_schedule(self.h, block, order, chunk, regs, max_batch_beams))
+
+    def batch_times(self, reset=True) -> dict:
+        """Longest phase times (ms) and batches above 5 ms per phase since the last reset: traversal and
+        compaction, the server's reaction to the counts, the result copies."""
+        mx = (C.c_float * 3)()
+        over = (C.c_int64 * 3)()
+        n = C.c_int64()
+        check(lib().rgl_gb300_server_get_batch_times(self.h, reset, mx, over, C.byref(n)))
+        names = ("trace", "reaction", "copies")
+        return {"batches": n.value, "max_ms": dict(zip(names, [round(x, 3) for x in mx])), "over_5ms": dict(zip(names, list(over)))}
 
     def stats(self) -> dict:
         v = [C.c_int64() for _ in range(7)]

@@ -231,6 +231,12 @@ def test_batches_of_varying_size_complete_and_host_results_match(rgl):
             for r in reqs:
                 srv.release(r)
         assert srv.stats()["failed"] == 0
+        # Every retired batch was timed in its three phases on the device's clock.
+        srv.drain()
+        bt = srv.batch_times(reset=True)
+        assert bt["batches"] == srv.stats()["batches"]
+        assert bt["max_ms"]["trace"] > 0 and bt["max_ms"]["copies"] >= 0
+        assert srv.batch_times()["batches"] == 0
     finally:
         srv.destroy()
 
