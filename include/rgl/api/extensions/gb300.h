@@ -155,8 +155,8 @@ RGL_API rgl_status_t rgl_gb300_batch_get_schedule(rgl_gb300_batch_t batch, int32
  * about equal traced rays, each traced by its own persistent launch (which starts while the previous
  * one drains) and followed by its graphs' later nodes; a graph's results are ready, and
  * rgl_graph_get_result_* returns, once its wave's later nodes end, so reads of the first graphs
- * overlap the device work of the rest. 0 (the default) picks one wave per 4 Mi traced rays, at most
- * 8; the count never exceeds the number of graphs. get_waves gives the count of the last frame (0
+ * overlap the device work of the rest. 0 (the default) picks one wave per 2 Mi traced rays, at most
+ * 16; the count never exceeds the number of graphs. get_waves gives the count of the last frame (0
  * before the first). Changes speed and result latency only, never results.
  */
 RGL_API rgl_status_t rgl_gb300_batch_configure_waves(rgl_gb300_batch_t batch, int32_t waves);

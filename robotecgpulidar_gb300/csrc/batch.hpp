@@ -41,8 +41,8 @@ struct BatchRun
 	rgl::BatchSchedule schedule{256, rgl::kPackLaneGroup, rgl::kOrderNatural, 1, 80};
 	// Waves per frame: 0 picks one wave per kRaysPerWave traced rays (at most kAutoWaves).
 	int wavesWanted = 0;
-	static constexpr int kAutoWaves = 8;
-	static constexpr int64_t kRaysPerWave = int64_t{4} << 20;
+	static constexpr int kAutoWaves = 16;
+	static constexpr int64_t kRaysPerWave = int64_t{2} << 20;
 	int waveCount() const { return (int) waveFirst.size() - 1; }
 
 	// Statistics of the last frame and of the batch's lifetime.

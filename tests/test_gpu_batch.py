@@ -233,7 +233,7 @@ def test_waves_without_cuda_graphs_equal_solo_runs(rgl):
 
 
 def test_automatic_waves_follow_the_ray_count(rgl):
-    """0 waves: one wave per 4 Mi traced rays, at most 8; this batch traces far fewer rays."""
+    """0 waves: one wave per 2 Mi traced rays, at most 16; this batch traces far fewer rays."""
     _, _, graphs, batch = build_batch(rgl)
     rgl.batch_configure_schedule(batch, autotune=False)
     rgl.batch_run(batch)
