@@ -236,6 +236,8 @@ struct HostStack
 };
 
 int gNodeVisits = 0;
+int gRayTris = 0;                             // triangle tests of the current ray
+std::vector<int> gVisitsPerRay, gTrisPerRay; // per ray of the last harness_cast (single-ray mode)
 long gTriTests = 0, gBinLoads = 0, gInstLoads = 0, gTlasVisits = 0;
 const WideNode* gTlasBase = nullptr;
 
@@ -255,6 +257,7 @@ struct HostLoader
 	TriRecord tri(const TriRecord* base, int32_t i) const
 	{
 		++gTriTests;
+		++gRayTris;
 		return base[i];
 	}
 	const InstanceRec& instance(const InstanceRec* base, int32_t i) const
@@ -617,6 +620,8 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	gTriTests = gBinLoads = gInstLoads = gTlasVisits = 0;
 	gMaxStackDepth = 0;
 	gDeepPushes = gDeepPops = 0;
+	gVisitsPerRay.assign(nRays, 0);
+	gTrisPerRay.assign(nRays, 0);
 	if (gPacketGroup > 0) {
 		gNodeVisits = 0;
 		std::vector<HitRec> hits(nRays);
@@ -635,11 +640,14 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 		const float* p = rays + 7 * r;
 		HostStack st;
 		gNodeVisits = 0;
+		gRayTris = 0;
 		HitRec h = traceClosest(sv, v3(p[0], p[1], p[2]), v3(p[3], p[4], p[5]), p[6], st, ld);
 		overflow = overflow || st.overflow;
 		gMaxStackDepth = std::max(gMaxStackDepth, st.maxDepth);
 		gMaxNodeVisits = std::max(gMaxNodeVisits, gNodeVisits);
 		gTotalNodeVisits += gNodeVisits;
+		gVisitsPerRay[r] = gNodeVisits;
+		gTrisPerRay[r] = gRayTris;
 		outT[r] = h.t;
 		outInst[r] = h.inst;
 		outPrim[r] = h.inst >= 0 ? inst[h.inst].tris[h.tri].primId : -1;
@@ -647,6 +655,15 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	if (overflow)
 		return -1;
 	return nMeshes > 0 ? (int) blas[0].wide.size() : 0;
+}
+
+// Node visits and triangle tests of each ray of the last harness_cast (single-ray mode).
+void harness_ray_work(int* visits, int* tris, int n)
+{
+	for (int i = 0; i < n && i < (int) gVisitsPerRay.size(); ++i) {
+		visits[i] = gVisitsPerRay[i];
+		tris[i] = gTrisPerRay[i];
+	}
 }
 
 } // extern "C"

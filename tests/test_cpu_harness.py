@@ -3,6 +3,7 @@ host/device functions the CUDA kernels wrap (LBVH, 8-wide collapse with verified
 two-level watertight closest-hit traversal) serially on the host; results must agree with the FP64
 oracle (hit/miss and entity exact off the oracle's ambiguity band, distance within 1e-5 relative)."""
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -163,3 +164,51 @@ def test_packets_resolve_ties_like_single_rays(harness):
     packet = cast_world(harness, scene, o, d, 100.0, group=group)
     assert np.array_equal(single[0].view(np.uint32), packet[0].view(np.uint32))
     assert np.array_equal(single[1], packet[1]) and np.array_equal(single[2], packet[2])
+
+
+def warp_lane_use(work_per_beam, order, beams_per_warp=6, lanes=32):
+    """Share of a warp's lane slots doing work when `beams_per_warp` beams of `work_per_beam.shape[1]`
+    sub-rays (one lane each) run until the warp's longest ray ends, beams taken in `order`."""
+    w = work_per_beam[order]
+    m = (len(w) // beams_per_warp) * beams_per_warp
+    g = w[:m].reshape(-1, beams_per_warp * w.shape[1])
+    return g.sum() / (lanes * g.max(axis=1)).sum()
+
+
+def test_scan_row_order_groups_similar_work(harness):
+    """Beams of one elevation at neighbouring azimuths do similar traversal work, so the scan-row
+    visiting order (elevation, then azimuth: the graph runs' default) keeps more of a warp's lanes busy
+    than a spinning lidar's given order (one azimuth's channels from the ground to the sky). Work per
+    ray is the host traversal's node visits plus triangle tests; 5 sub-rays per beam on a ring of
+    0.1 degrees, 6 beams per warp, as the device runs them."""
+    scene = scenes.million_scene()
+    pose = scenes.translation(0, 0, 6.0)
+    world = np.einsum("ij,njk->nik", pose[:, :3].astype(np.float64), scenes.lidar_rays(64, 512).astype(np.float64))
+    world[:, :, 3] += pose[:, 3]
+    o = world[:, :, 3]
+    d = world[:, :, 2] / np.linalg.norm(world[:, :, 2], axis=1, keepdims=True)
+    a = np.where(np.abs(d[:, 2:3]) < 0.9, np.array([[0.0, 0.0, 1.0]]), np.array([[1.0, 0.0, 0.0]]))
+    u = np.cross(d, a)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    v = np.cross(d, u)
+    half = math.radians(0.1)
+    subs = [d] + [d + half * (math.cos(2 * math.pi * k / 4) * u + math.sin(2 * math.pi * k / 4) * v) for k in range(4)]
+    n = len(d)
+    rays = np.zeros((n * 5, 3, 4), np.float32)
+    rays[:, :, 3] = np.repeat(o, 5, axis=0)
+    rays[:, :, 2] = np.stack(subs, axis=1).reshape(-1, 3)
+    cast(harness, scene, rays, 100.0)
+    visits = np.zeros(n * 5, np.int32)
+    tris = np.zeros(n * 5, np.int32)
+    harness.harness_ray_work(visits.ctypes.data_as(C.c_void_p), tris.ctypes.data_as(C.c_void_p), n * 5)
+    work = (visits + tris).reshape(n, 5)
+    assert work.min() > 0
+    # Scan-row key: sine of the elevation (11 bits), then a pseudo-angle of the azimuth (11 bits).
+    l1 = np.abs(d[:, 0]) + np.abs(d[:, 1])
+    pa = np.where(l1 > 0, 1.0 - d[:, 0] / np.maximum(l1, 1e-30), 0.0)
+    az = np.where(d[:, 1] < 0, -pa, pa)
+    q = lambda c: np.clip((c * 2048).astype(np.int64), 0, 2047)
+    key = (q(d[:, 2] * 0.5 + 0.5) << 11) | q(az * 0.25 + 0.5)
+    given = warp_lane_use(work, np.arange(n))
+    rows = warp_lane_use(work, np.argsort(key, kind="stable"))
+    assert rows > given + 0.03, (given, rows)
