@@ -6,6 +6,7 @@
 #include <set>
 
 #include "scene.hpp"
+#include "wave_split.hpp"
 
 using rgl::format;
 using rgl::InvalidPipeline;
@@ -171,25 +172,15 @@ void BatchRun::buildJobs()
 	shape.push_back(waveCount());
 }
 
-// Cuts the members, in batch order, into waves of about equal traced rays: wave w ends at the first
-// member whose running ray total reaches (w + 1) / W of the frame's. No wave is empty.
+// Cuts the members, in batch order, into waves of about equal traced rays (wave_split.hpp).
 void BatchRun::splitWaves()
 {
-	const int n = (int) members.size();
-	int W = wavesWanted > 0 ? wavesWanted : (int) std::min<int64_t>(kAutoWaves, std::max<int64_t>(1, rays / kRaysPerWave));
-	W = std::max(1, std::min(W, n));
-	waveFirst.assign(1, 0);
-	int64_t acc = 0;
-	for (int j = 0; j < n; ++j) {
-		acc += (int64_t) jobs[j].p.nRays * jobs[j].p.nSamples;
-		const int w = waveCount();
-		const bool last = w == W - 1;
-		// Close wave w after member j if it reached its share, leaving a member for each later wave.
-		if (!last && j + 1 < n && n - (j + 1) >= W - (w + 1) && (acc * W >= rays * (w + 1) || n - (j + 1) == W - (w + 1))) {
-			waveFirst.push_back(j + 1);
-		}
+	std::vector<int64_t> memberRays(members.size());
+	for (size_t j = 0; j < members.size(); ++j) {
+		memberRays[j] = (int64_t) jobs[j].p.nRays * jobs[j].p.nSamples;
 	}
-	waveFirst.push_back(n);
+	const int W = wavesWanted > 0 ? wavesWanted : (int) std::min<int64_t>(kAutoWaves, std::max<int64_t>(1, rays / kRaysPerWave));
+	waveFirst = rgl::splitIntoWaves(memberRays, W);
 }
 
 // A forked stream at the greatest priority, so that the graphs' node kernels on it start before

@@ -9,6 +9,7 @@
 #include "bvh_core.hpp"
 #include "sah_build.hpp"
 #include "trace_core.hpp"
+#include "wave_split.hpp"
 
 using namespace rgl;
 
@@ -655,6 +656,15 @@ int harness_cast(int nMeshes, const float* const* verts, const int* nVerts, cons
 	if (overflow)
 		return -1;
 	return nMeshes > 0 ? (int) blas[0].wide.size() : 0;
+}
+
+// The wave cut of a batched frame (wave_split.hpp): first member of each wave, then n, into outFirst
+// (room for n + 2 entries); returns the number of waves.
+int harness_split_waves(const int64_t* rays, int n, int waves, int* outFirst)
+{
+	const std::vector<int> first = rgl::splitIntoWaves(std::vector<int64_t>(rays, rays + n), waves);
+	std::copy(first.begin(), first.end(), outFirst);
+	return (int) first.size() - 1;
 }
 
 // Node visits and triangle tests of each ray of the last harness_cast (single-ray mode).

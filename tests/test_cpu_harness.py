@@ -22,7 +22,7 @@ def load_harness():
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(
         os.path.getmtime(p) for p in [SRC] + [os.path.join(ROOT, "robotecgpulidar_gb300", "csrc", f)
-                                            for f in ("bvh_core.hpp", "trace_core.hpp", "rgl_math.hpp", "device_types.hpp")]
+                                            for f in ("bvh_core.hpp", "trace_core.hpp", "rgl_math.hpp", "device_types.hpp", "wave_split.hpp")]
     ):
         cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
         subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
@@ -212,3 +212,35 @@ def test_scan_row_order_groups_similar_work(harness):
     given = warp_lane_use(work, np.arange(n))
     rows = warp_lane_use(work, np.argsort(key, kind="stable"))
     assert rows > given + 0.03, (given, rows)
+
+
+def split_waves(h, rays, waves):
+    r = np.ascontiguousarray(rays, np.int64)
+    out = np.zeros(len(r) + 2, np.int32)
+    w = h.harness_split_waves(r.ctypes.data_as(C.c_void_p), len(r), waves, out.ctypes.data_as(C.c_void_p))
+    return [int(x) for x in out[:w + 1]]
+
+
+def test_wave_cut_of_batched_frames(harness):
+    """Batched frames cut their sensors, in order, into contiguous waves of about equal rays; never more
+    waves than sensors, none empty, and a heavy sensor closes its wave early."""
+    assert split_waves(harness, [100] * 8, 4) == [0, 2, 4, 6, 8]
+    assert split_waves(harness, [100] * 8, 1) == [0, 8]
+    assert split_waves(harness, [100] * 3, 9) == [0, 1, 2, 3]  # capped at the sensor count
+    assert split_waves(harness, [1000, 1, 1, 1, 1, 1], 3) == [0, 1, 2, 6]  # the heavy first sensor alone
+    assert split_waves(harness, [1, 1, 1, 1, 1, 1000], 3) == [0, 4, 5, 6]  # later waves keep a sensor each
+    assert split_waves(harness, [0, 0, 0, 0], 2) == [0, 1, 4]
+    rng = np.random.default_rng(4)
+    for _ in range(200):
+        n = int(rng.integers(1, 40))
+        rays = rng.integers(1, 1 << 20, size=n)
+        W = int(rng.integers(1, 20))
+        first = split_waves(harness, rays, W)
+        waves = min(W, n)
+        assert first[0] == 0 and first[-1] == n and len(first) - 1 == waves
+        assert all(b > a for a, b in zip(first, first[1:]))
+        # Each wave but the last ends once its running total reaches its share, or when exactly one
+        # sensor is left for each later wave.
+        cum = np.cumsum(rays)
+        for w, end in enumerate(first[1:-1]):
+            assert cum[end - 1] * waves >= cum[-1] * (w + 1) or n - end == waves - (w + 1)
