@@ -333,10 +333,23 @@ def run_ours(args):
     peak, peak_src = 6785.9, "fallback"
     if os.path.exists(peaks_path):
         peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
-    traffic = None
+    traffic, warp_insts = None, None
     tpath = os.path.join(ROOT, "profiles", "trace_kernel_traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("dram_bytes_per_launch")
+        prof = json.load(open(tpath))
+        traffic = prof.get("dram_bytes_per_launch")
+        warp_insts = prof.get("warp_instructions_per_launch")
+    # The traversal is bound by instruction issue, not by bytes: its warp instructions per launch (ncu)
+    # over the event-timed launch, against one warp instruction per clock on each of the SMs' 4
+    # schedulers at the clock sampled during the run.
+    issue = None
+    if warp_insts:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+        issue_peak = sms * 4 * mhz * 1e6
+        issue_achieved = warp_insts / (trace_mean_ms / 1e3)
+        issue = {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s", "frac": issue_achieved / issue_peak,
+                 "warp_instructions_per_launch": int(warp_insts), "sm_mhz": mhz}
 
     line = None
     if rank == 0:
@@ -352,7 +365,7 @@ def run_ours(args):
                     "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "kernel": "kTraceBatch", "algorithmic_bytes_per_launch": int(algo_bytes),
-                         "kernel_ms": trace_mean_ms, "peak_source": peak_src},
+                         "kernel_ms": trace_mean_ms, "peak_source": peak_src, "issue": issue},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
