@@ -388,8 +388,8 @@ REPOSE_FRACTION = 0.2
 
 def run_multi_sensor(args):
     """64 uneven sensors on the 1M-triangle scene, 20 % of the entities re-posed every frame. Times
-    the batched frame (rgl_gb300_batch_run: the refit, then per wave of sensors one CUDA graph with
-    their nodes and one persistent traversal launch) against the plain loop of one rgl_graph_run per
+    the batched frame (rgl_gb300_batch_run: one CUDA graph with the refit, every sensor's nodes and one
+    persistent traversal launch per wave of sensors) against the plain loop of one rgl_graph_run per
     sensor graph, both over the same graphs and poses. Besides the device-only frame, both are timed
     end to end: run, then read every graph's XYZ, distance and entity id into pinned host buffers."""
     from robotecgpulidar_gb300 import build as b
